@@ -1,0 +1,224 @@
+#ifndef GG_RUNTIME_H
+#define GG_RUNTIME_H
+
+/*
+ * gg_runtime: the thin C ABI between the CSR algorithm entry points and the
+ * GB300 kernels.  It replaces the reference's CAPI offload layer
+ * (02_capi_graph/include/capi_utils/capienv.h:146-166,
+ *  02_capi_graph/src/capi_utils/capienv.c):
+ *
+ *   reference (capienv.c)                      here
+ *   -----------------------------------------  -----------------------------
+ *   mapGraphCSRToWED      :396-438             gg_graph_map
+ *   setupAFUGraphCSR      :30-55               gg_device_init (+ gg_graph_map)
+ *   startAFU / startCU    :58-109              gg_pagerank / gg_bfs / gg_spmv
+ *   waitAFU (unbounded)   :111-172             bounded wait inside each call,
+ *                                              GG_ETIMEDOUT after the limit
+ *   readCmdResponseStats  :174-201             per-call result structs
+ *                                              (kernel time, launches)
+ *   releaseAFU            :299-303             gg_graph_unmap
+ *
+ * All entry points are plain C: host pointers, sizes, an opaque graph handle
+ * and an optional CUDA stream passed as `void *` (NULL = the library's own
+ * stream).  Every call returns a gg_status; gg_last_error() gives a message.
+ * Calls on one gg_graph must not overlap; different graphs may be used from
+ * different host threads.
+ */
+
+#include <stdint.h>
+#include <stddef.h>
+
+#include "graphCSR.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gg_status
+{
+    GG_OK = 0,
+    GG_ERR_INVALID = 1,    /* bad argument (size, source, mode, missing array) */
+    GG_ERR_NO_DEVICE = 2,  /* no CUDA device / driver */
+    GG_ERR_CUDA = 3,       /* CUDA runtime error */
+    GG_ERR_NOMEM = 4,      /* device or host allocation failed */
+    GG_ETIMEDOUT = 5,      /* device work did not finish within the wait limit */
+    GG_ERR_KERNEL = 6      /* a kernel reported an error through its status word */
+} gg_status;
+
+typedef struct gg_graph gg_graph;
+
+/* Arrays a mapping must carry (bit mask). */
+#define GG_MAP_OUT    0x1u   /* out-CSR: edges_idx, out_degree, edges_array_dest */
+#define GG_MAP_IN     0x2u   /* in-CSR (CSC): inverse edges_idx, in-degree, in-neighbours; out_degree */
+#define GG_MAP_OUT_W  0x4u   /* out-edge weights (constant 0.0001f when the graph has none) */
+#define GG_MAP_IN_W   0x8u   /* in-edge weights */
+#define GG_MAP_ALL    0xFu
+
+/* Storage type of the gathered vertex values (PageRank contributions, SpMV
+ * x) and of SpMV edge weights.  Accumulation is always FP32. */
+typedef enum gg_storage
+{
+    GG_STORE_F32 = 0,
+    GG_STORE_BF16 = 1,
+    GG_STORE_F16 = 2
+} gg_storage;
+
+/* ---- device and graph ----------------------------------------------------- */
+
+gg_status gg_device_init(int device);
+const char *gg_last_error(void);
+/* Upper bound, in milliseconds, of every host wait on device work
+ * (default 120000, env GG_WAIT_TIMEOUT_MS). */
+void gg_set_wait_timeout_ms(uint32_t ms);
+
+/* Copy the arrays selected by `what` to HBM.  Offsets are padded so that
+ * every array starts on a 256-byte boundary.  The host graph is only read. */
+gg_status gg_graph_map(const struct GraphCSR *graph, uint32_t what, void *stream, gg_graph **out);
+/* Upload any arrays in `what` that the mapping does not carry yet. */
+gg_status gg_graph_extend(gg_graph *g, const struct GraphCSR *graph, uint32_t what, void *stream);
+gg_status gg_graph_unmap(gg_graph *g);
+/* Bytes of device memory held by the mapping (graph + work buffers). */
+size_t gg_graph_device_bytes(const gg_graph *g);
+
+/* ---- PageRank --------------------------------------------------------------- */
+
+/* Modes use the reference's pushpull codes (pageRank.c:879-935). */
+typedef enum gg_pr_mode
+{
+    GG_PR_PULL = 0, GG_PR_PUSH = 1, GG_PR_PULL_FX64 = 2, GG_PR_PUSH_FX64 = 3,
+    GG_PR_PULL_Q32 = 4, GG_PR_PUSH_Q = 5, GG_PR_DD_PULL = 6, GG_PR_DD_PUSH = 7,
+    GG_PR_DD_PULLPUSH = 8, GG_PR_PULL_FX32 = 9, GG_PR_PULL_FX16 = 10,
+    GG_PR_PULL_FX8 = 11, GG_PR_PULL_Q16 = 12, GG_PR_PULL_Q8 = 13
+} gg_pr_mode;
+
+typedef struct gg_pr_params
+{
+    uint32_t mode;            /* gg_pr_mode */
+    uint32_t storage;         /* gg_storage of the gathered contributions (pull/push FP modes) */
+    uint32_t max_iterations;
+    uint32_t init_one_over_n; /* 0: reference (start 0.15, divide by V at the end); 1: start 1/V, rank = 0.15/V + 0.85*sum, no final division */
+    double epsilon;
+    float damp;               /* 0.85f in the reference */
+    uint32_t profile;         /* 1: time every gather launch with CUDA events */
+} gg_pr_params;
+
+typedef struct gg_pr_result
+{
+    uint32_t iterations;      /* reference convention (see pageRank.h) */
+    uint32_t active;          /* active vertices in the last iteration run */
+    double error_total;       /* last iteration's sum |delta| / V */
+    double rank_sum;          /* sum of the returned ranks */
+    float gather_ms;          /* profile: summed device time of the gather launches */
+    uint32_t gather_launches; /* gather launches timed */
+    uint32_t launches;        /* kernels launched by the call */
+} gg_pr_result;
+
+/* Run PageRank on a mapping that carries GG_MAP_IN (pull) or GG_MAP_OUT (push).
+ * `ranks` (host, V floats) receives the final ranks when not NULL. */
+gg_status gg_pagerank(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_result *r, void *stream);
+/* Device pointer to the last run's final ranks (V floats), valid until the
+ * next call on `g`. */
+const float *gg_pagerank_device_ranks(const gg_graph *g);
+
+/* ---- BFS -------------------------------------------------------------------- */
+
+typedef enum gg_bfs_mode
+{
+    GG_BFS_PULL = 0, GG_BFS_PUSH = 1, GG_BFS_DO = 2, GG_BFS_PUSH_BITMAP = 3, GG_BFS_DO_BITMAP = 4
+} gg_bfs_mode;
+
+typedef struct gg_bfs_params
+{
+    uint32_t mode;            /* gg_bfs_mode */
+    uint32_t source;          /* internal vertex id (already relabelled) */
+    uint32_t alpha;           /* 15 in the reference (BFS.c:564) */
+    uint32_t beta;            /* 18 in the reference (BFS.c:565) */
+    uint32_t profile;
+} gg_bfs_params;
+
+typedef struct gg_bfs_result
+{
+    uint32_t processed_nodes; /* vertices discovered after the source */
+    uint32_t levels;          /* frontier steps run */
+    uint32_t top_down_steps;
+    uint32_t bottom_up_steps;
+    uint64_t edges_examined;  /* adjacency entries read by all steps */
+    float step_ms;            /* profile: summed device time of the step kernels */
+    uint32_t launches;
+} gg_bfs_result;
+
+/* Needs GG_MAP_OUT for top-down steps and GG_MAP_IN for bottom-up steps.
+ * `parents` (int32, V) and `distances` (uint32, V) are host outputs (may be NULL). */
+gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parents, uint32_t *distances,
+                 gg_bfs_result *r, void *stream);
+
+/* One frontier step on host state, for the reference's step functions.
+ * direction 0: top-down from `frontier` (a queue of `frontier_len` ids when
+ * `frontier_is_bitmap` is 0, else a bitmap of ceil(V/32) words);
+ * direction 1: bottom-up from the bitmap `frontier`.
+ * parents/distances are read and updated in place; the next frontier is
+ * written as a queue (`next_queue`, may be NULL) and/or a bitmap
+ * (`next_bitmap`, may be NULL); *next_len receives its size and *counter
+ * receives mf (top-down) or nf (bottom-up). */
+gg_status gg_bfs_step_host(gg_graph *g, int direction, const uint32_t *frontier, uint32_t frontier_len,
+                           int frontier_is_bitmap, int32_t *parents, uint32_t *distances,
+                           uint32_t *next_queue, uint32_t *next_bitmap, uint32_t *next_len,
+                           uint32_t *counter, void *stream);
+
+/* ---- SpMV ------------------------------------------------------------------- */
+
+typedef enum gg_spmv_mode
+{
+    GG_SPMV_PULL = 0, GG_SPMV_PUSH = 1, GG_SPMV_PULL_FX = 2, GG_SPMV_PUSH_FX = 3
+} gg_spmv_mode;
+
+typedef struct gg_spmv_params
+{
+    uint32_t mode;            /* gg_spmv_mode */
+    uint32_t storage;         /* gg_storage of x and of the edge weights (pull/push FP modes) */
+    uint32_t iterations;
+    uint32_t profile;
+} gg_spmv_params;
+
+typedef struct gg_spmv_result
+{
+    double checksum;          /* sum of round2(y[v]) as the reference prints (SPMV.c:727-730) */
+    float spmv_ms;            /* profile: summed device time of the product launches */
+    uint32_t spmv_launches;
+    uint32_t launches;
+} gg_spmv_result;
+
+/* Pull needs GG_MAP_IN|GG_MAP_IN_W, push GG_MAP_OUT|GG_MAP_OUT_W.
+ * `x` (host, V) is the input vector, or NULL for the reference's
+ * x[v] = 1/outdeg(v) (0.001 when 0); `x_out` receives the x used; `y`
+ * receives the result.  Any of them may be NULL. */
+gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *x, float *x_out, float *y,
+                  gg_spmv_result *r, void *stream);
+
+/* ---- drop-in side options ---------------------------------------------------- */
+
+/*
+ * GPU-only knobs for the reference-compatible entry points, kept out of
+ * `struct Arguments` so its layout stays the reference's.  Defaults:
+ * storage FP32, device 0, graph re-uploaded on every call.
+ */
+typedef struct GraphGpuOptions
+{
+    uint32_t storage;         /* gg_storage for PageRank/SpMV gathers */
+    int device;
+    uint32_t keep_resident;   /* 1: keep each GraphCSR's device copy between calls (graphGpuRelease frees it) */
+    uint32_t verbose;         /* 1: print the reference's iteration tables */
+} GraphGpuOptions;
+
+void graphGpuSetOptions(const GraphGpuOptions *opts);
+void graphGpuGetOptions(GraphGpuOptions *opts);
+/* Status of the last failed drop-in call (GG_OK if none). */
+gg_status graphGpuLastError(void);
+/* Drop the resident device copy of `graph`, if any. */
+void graphGpuRelease(struct GraphCSR *graph);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

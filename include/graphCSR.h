@@ -1,0 +1,126 @@
+#ifndef GRAPHCSR_H
+#define GRAPHCSR_H
+
+/*
+ * CSR graph as the CSR traversal hot path consumes it.
+ *
+ * The reference takes `struct GraphCSR` from its OpenGraph submodule, which is
+ * empty in the reference snapshot (.gitmodules:1-3).  The fields below are
+ * exactly the ones the hot path touches, reconstructed from their uses:
+ *   - graph->num_vertices / num_edges           (pageRank.c:1026, BFS.c:555)
+ *   - graph->vertices->{out_degree,in_degree,edges_idx}
+ *                                               (BFS.c:711-713, capienv.c:409-411)
+ *   - graph->inverse_vertices->{...}            (pageRank.c:968, capienv.c:424-426)
+ *   - graph->sorted_edges_array->{edges_array_src,edges_array_dest,
+ *       edges_array_weight,label_array,inverse_label_array}
+ *                                               (BFS.c:301, SPMV.c:790-806, capienv.c:413-419)
+ *   - graph->inverse_sorted_edges_array->{...}  (pageRank.c:969, capienv.c:428-434)
+ * This makes the drop-in source/API compatible with the reference's
+ * algorithm files; binary layout compatibility with OpenGraph cannot be
+ * checked because that source is absent.
+ *
+ * Storage: uint32 vertex ids and uint32 edge offsets (E < 2^32), the layout
+ * the GPU kernels read.  `vertices->edges_idx[v]` is the first edge of v in
+ * `sorted_edges_array`; `inverse_vertices->edges_idx[v]` is the first in-edge
+ * of v in `inverse_sorted_edges_array`, whose `edges_array_dest` holds the
+ * in-neighbour (the edge's source).  Adjacency lists are sorted by neighbour
+ * id (count sort by source, stable by destination), so every traversal order
+ * is deterministic.
+ */
+
+#include <stdint.h>
+#include "graphConfig.h"
+
+struct Vertex
+{
+    uint32_t *out_degree;
+    uint32_t *in_degree;
+    uint32_t *edges_idx;
+};
+
+struct EdgeList
+{
+    uint32_t num_edges;
+    uint32_t num_vertices;
+    float max_weight;
+    uint32_t *edges_array_src;
+    uint32_t *edges_array_dest;
+    float *edges_array_weight;      /* NULL: unweighted graph */
+    uint32_t *label_array;          /* original id -> internal id (identity unless relabelled) */
+    uint32_t *inverse_label_array;  /* internal id -> original id */
+};
+
+struct GraphCSR
+{
+    uint32_t num_edges;
+    uint32_t num_vertices;
+    float max_weight;
+    uint32_t avg_degree;
+    struct Vertex *vertices;
+    struct Vertex *inverse_vertices;
+    struct EdgeList *sorted_edges_array;
+    struct EdgeList *inverse_sorted_edges_array;
+};
+
+/*
+ * The reference masks two "heat" bits off neighbour ids when its mask mode
+ * (-M) is on (EXTRACT_VALUE, OpenGraph; cf. VERTEX_CACHE_MASK_U32 in
+ * cu_PageRank/CSR/PULL/FixedPoint/pkg/globals_cu_pkg.sv:90).  The GPU path
+ * runs with mask mode 0, where the macro is the identity.
+ */
+#define EXTRACT_VALUE(x) (x)
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- edge lists ---------------------------------------------------------- */
+
+struct EdgeList *newEdgeList(uint32_t num_edges, uint32_t num_vertices, int weighted);
+void freeEdgeList(struct EdgeList *edgeList);
+
+/*
+ * Load the reference's binary edge-list formats (04_test_graphs/TEST/...):
+ *   .bin  : little-endian uint32 pairs  (src, dst)
+ *   .wbin : little-endian uint32 triples (src, dst, weight); the weight word
+ *           is read as an integer and stored as float (the fixture files hold
+ *           integer weights).
+ * Returns NULL on I/O error (message on stderr).  num_vertices = max id + 1.
+ */
+struct EdgeList *readEdgeListsbin(const char *fname, int weighted);
+/* Text form: one "src dst" or "src dst weight" line per edge. */
+struct EdgeList *readEdgeListsText(const char *fname, int weighted);
+
+/*
+ * Seeded R-MAT edge list (Chakrabarti, Zhan, Faloutsos, SDM 2004): 2^scale
+ * vertices, edge_factor * 2^scale directed edges; each edge picks a quadrant
+ * per level with probabilities (a, b, c, 1-a-b-c).  Randomness is counter
+ * based: draw l of edge i is splitmix64(seed + (i*scale + l + 1) * phi) with
+ * phi = 0x9E3779B97F4A7C15, turned into a 53-bit uniform.  Self-loops and
+ * duplicates are kept; there is no label permutation.  With `weighted`,
+ * edge i gets float weight (splitmix64(weight_seed + (i+1)*phi) >> 40) * 2^-24
+ * in [0,1).  `symmetric` appends the reverse of every edge (2E edges).
+ */
+struct EdgeList *generateRMATEdgeList(uint32_t scale, uint32_t edge_factor,
+                                      double a, double b, double c,
+                                      uint64_t seed, int weighted, uint64_t weight_seed,
+                                      int symmetric);
+
+/* ---- CSR ------------------------------------------------------------------ */
+
+/*
+ * Build CSR and inverse CSR (CSC) from an edge list with counting sorts:
+ * stable by destination, then stable by source (CSR, lists sorted by
+ * destination), then stable by destination (CSC, lists sorted by source).
+ * The edge list is not modified and may be freed afterwards.  label arrays
+ * are the identity.  Host arrays are page-locked for fast upload when a CUDA
+ * device is present (graphCSRFree undoes that).
+ */
+struct GraphCSR *graphCSRFromEdgeList(const struct EdgeList *edgeList);
+void graphCSRFree(struct GraphCSR *graph);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
