@@ -1,0 +1,476 @@
+"""accelgraph_express_gb300: GB300-native CSR traversal (PageRank, SpMV, BFS).
+
+The product is ``libaccelgraph_gb300.so``: the reference-compatible C entry
+points (``pageRank*GraphCSR``, ``breadthFirstSearch*GraphCSR``,
+``SPMV*GraphCSR``), the graph builder, and the ``gg_*`` GPU runtime, declared
+in ``include/*.h``.  This module binds it with ctypes for Python callers,
+tests and the benchmark; it adds no compute of its own and raises if the
+library is missing or no GPU is present when a GPU call is made.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libaccelgraph_gb300.so")
+
+_LIB = None
+
+
+def build(jobs: int | None = None) -> str:
+    """Compile libaccelgraph_gb300.so for sm_103a (make in csrc/)."""
+    jobs = jobs or max(1, min(16, os.cpu_count() or 1))
+    subprocess.check_call(["make", "-s", "-j", str(jobs), "-C", os.path.join(HERE, "csrc")])
+    return LIB_PATH
+
+
+# ---------------------------------------------------------------------------
+# C structures (include/*.h)
+# ---------------------------------------------------------------------------
+
+class Mt19937State(C.Structure):
+    _fields_ = [("mt", C.c_uint32 * 624), ("mti", C.c_int)]
+
+
+class Arguments(C.Structure):
+    """struct Arguments (include/graphConfig.h, reference graphConfig.h:11-52)."""
+    _fields_ = [("wflag", C.c_int), ("xflag", C.c_int), ("sflag", C.c_int), ("Sflag", C.c_int),
+                ("dflag", C.c_int), ("binSize", C.c_uint32), ("verbosity", C.c_uint32),
+                ("iterations", C.c_uint32), ("trials", C.c_uint32), ("epsilon", C.c_double),
+                ("source", C.c_int), ("algorithm", C.c_uint32), ("datastructure", C.c_uint32),
+                ("pushpull", C.c_uint32), ("sort", C.c_uint32), ("lmode", C.c_uint32),
+                ("lmode_l2", C.c_uint32), ("lmode_l3", C.c_uint32), ("mmode", C.c_uint32),
+                ("symmetric", C.c_uint32), ("weighted", C.c_uint32), ("delta", C.c_uint32),
+                ("pre_numThreads", C.c_int), ("algo_numThreads", C.c_int), ("ker_numThreads", C.c_int),
+                ("fnameb", C.c_char_p), ("fnamel", C.c_char_p), ("fnameb_format", C.c_uint32),
+                ("convert_format", C.c_uint32), ("mt19937var", Mt19937State), ("cache_size", C.c_uint32),
+                ("afu_config", C.c_uint64), ("afu_config_2", C.c_uint64), ("cu_config", C.c_uint64),
+                ("cu_config_2", C.c_uint64), ("cu_config_3", C.c_uint64), ("cu_config_4", C.c_uint64)]
+
+
+class Vertex(C.Structure):
+    _fields_ = [("out_degree", C.POINTER(C.c_uint32)), ("in_degree", C.POINTER(C.c_uint32)),
+                ("edges_idx", C.POINTER(C.c_uint32))]
+
+
+class EdgeList(C.Structure):
+    _fields_ = [("num_edges", C.c_uint32), ("num_vertices", C.c_uint32), ("max_weight", C.c_float),
+                ("edges_array_src", C.POINTER(C.c_uint32)), ("edges_array_dest", C.POINTER(C.c_uint32)),
+                ("edges_array_weight", C.POINTER(C.c_float)), ("label_array", C.POINTER(C.c_uint32)),
+                ("inverse_label_array", C.POINTER(C.c_uint32))]
+
+
+class GraphCSR(C.Structure):
+    _fields_ = [("num_edges", C.c_uint32), ("num_vertices", C.c_uint32), ("max_weight", C.c_float),
+                ("avg_degree", C.c_uint32), ("vertices", C.POINTER(Vertex)),
+                ("inverse_vertices", C.POINTER(Vertex)), ("sorted_edges_array", C.POINTER(EdgeList)),
+                ("inverse_sorted_edges_array", C.POINTER(EdgeList))]
+
+
+class PageRankStats(C.Structure):
+    _fields_ = [("damp", C.c_float), ("base_pr", C.c_float), ("iterations", C.c_uint32),
+                ("num_vertices", C.c_uint32), ("activeVertices", C.c_uint32),
+                ("realRanks", C.POINTER(C.c_uint32)), ("pageRanks", C.POINTER(C.c_float)),
+                ("time_total", C.c_double), ("error_total", C.c_double)]
+
+
+class BFSStats(C.Structure):
+    _fields_ = [("distances", C.POINTER(C.c_uint32)), ("parents", C.POINTER(C.c_int)),
+                ("distances_DualOrder", C.POINTER(C.c_uint32)), ("parents_DualOrder", C.POINTER(C.c_int)),
+                ("processed_nodes", C.c_uint32), ("num_vertices", C.c_uint32), ("iteration", C.c_uint32),
+                ("time_total", C.c_double)]
+
+
+class SPMVStats(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("arguments", C.POINTER(Arguments)),
+                ("num_vertices", C.c_uint32), ("vector_output", C.POINTER(C.c_float)),
+                ("vector_input", C.POINTER(C.c_float)), ("time_total", C.c_double)]
+
+
+class Bitmap(C.Structure):
+    _fields_ = [("size", C.c_uint32), ("numSetBits", C.c_uint32), ("bitarray", C.POINTER(C.c_uint32))]
+
+
+class ArrayQueue(C.Structure):
+    _fields_ = [("head", C.c_uint32), ("tail", C.c_uint32), ("tail_next", C.c_uint32), ("size", C.c_uint32),
+                ("queue", C.POINTER(C.c_uint32)), ("q_bitmap", C.POINTER(Bitmap)),
+                ("q_bitmap_next", C.POINTER(Bitmap))]
+
+
+class PrParams(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("storage", C.c_uint32), ("max_iterations", C.c_uint32),
+                ("init_one_over_n", C.c_uint32), ("epsilon", C.c_double), ("damp", C.c_float),
+                ("profile", C.c_uint32)]
+
+
+class PrResult(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("active", C.c_uint32), ("error_total", C.c_double),
+                ("rank_sum", C.c_double), ("gather_ms", C.c_float), ("gather_launches", C.c_uint32),
+                ("launches", C.c_uint32)]
+
+
+class BfsParams(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("source", C.c_uint32), ("alpha", C.c_uint32), ("beta", C.c_uint32),
+                ("profile", C.c_uint32)]
+
+
+class BfsResult(C.Structure):
+    _fields_ = [("processed_nodes", C.c_uint32), ("levels", C.c_uint32), ("top_down_steps", C.c_uint32),
+                ("bottom_up_steps", C.c_uint32), ("edges_examined", C.c_uint64), ("step_ms", C.c_float),
+                ("launches", C.c_uint32)]
+
+
+class SpmvParams(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("storage", C.c_uint32), ("iterations", C.c_uint32),
+                ("profile", C.c_uint32)]
+
+
+class SpmvResult(C.Structure):
+    _fields_ = [("checksum", C.c_double), ("spmv_ms", C.c_float), ("spmv_launches", C.c_uint32),
+                ("launches", C.c_uint32)]
+
+
+class GraphGpuOptions(C.Structure):
+    _fields_ = [("storage", C.c_uint32), ("device", C.c_int), ("keep_resident", C.c_uint32),
+                ("verbose", C.c_uint32)]
+
+
+MAP_OUT, MAP_IN, MAP_OUT_W, MAP_IN_W, MAP_ALL = 0x1, 0x2, 0x4, 0x8, 0xF
+STORE = {"f32": 0, "bf16": 1, "f16": 2}
+PR_MODES = {"pull": 0, "push": 1, "pull_fx64": 2, "push_fx64": 3, "pull_q32": 4, "push_q": 5, "dd_pull": 6,
+            "dd_push": 7, "dd_pullpush": 8, "pull_fx32": 9, "pull_fx16": 10, "pull_fx8": 11,
+            "pull_q16": 12, "pull_q8": 13}
+BFS_MODES = {"pull": 0, "push": 1, "do": 2, "push_bitmap": 3, "do_bitmap": 4}
+SPMV_MODES = {"pull": 0, "push": 1, "pull_fx": 2, "push_fx": 3}
+
+
+class GgError(RuntimeError):
+    pass
+
+
+def lib() -> C.CDLL:
+    """The product library.  Raises if it has not been built."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise GgError(f"{LIB_PATH} is missing: run accelgraph_express_gb300.build() first")
+        L = C.CDLL(LIB_PATH)
+        P = C.POINTER
+        L.gg_last_error.restype = C.c_char_p
+        L.gg_device_init.argtypes = [C.c_int]
+        L.gg_graph_map.argtypes = [P(GraphCSR), C.c_uint32, C.c_void_p, P(C.c_void_p)]
+        L.gg_graph_extend.argtypes = [C.c_void_p, P(GraphCSR), C.c_uint32, C.c_void_p]
+        L.gg_graph_unmap.argtypes = [C.c_void_p]
+        L.gg_graph_device_bytes.argtypes = [C.c_void_p]
+        L.gg_graph_device_bytes.restype = C.c_size_t
+        L.gg_pagerank.argtypes = [C.c_void_p, P(PrParams), C.c_void_p, P(PrResult), C.c_void_p]
+        L.gg_pagerank_device_ranks.argtypes = [C.c_void_p]
+        L.gg_pagerank_device_ranks.restype = C.c_void_p
+        L.gg_bfs.argtypes = [C.c_void_p, P(BfsParams), C.c_void_p, C.c_void_p, P(BfsResult), C.c_void_p]
+        L.gg_spmv.argtypes = [C.c_void_p, P(SpmvParams), C.c_void_p, C.c_void_p, C.c_void_p, P(SpmvResult),
+                              C.c_void_p]
+        L.gg_set_wait_timeout_ms.argtypes = [C.c_uint32]
+        L.newEdgeList.argtypes = [C.c_uint32, C.c_uint32, C.c_int]
+        L.newEdgeList.restype = P(EdgeList)
+        L.freeEdgeList.argtypes = [P(EdgeList)]
+        L.readEdgeListsbin.argtypes = [C.c_char_p, C.c_int]
+        L.readEdgeListsbin.restype = P(EdgeList)
+        L.readEdgeListsText.argtypes = [C.c_char_p, C.c_int]
+        L.readEdgeListsText.restype = P(EdgeList)
+        L.generateRMATEdgeList.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                           C.c_uint64, C.c_int, C.c_uint64, C.c_int]
+        L.generateRMATEdgeList.restype = P(EdgeList)
+        L.graphCSRFromEdgeList.argtypes = [P(EdgeList)]
+        L.graphCSRFromEdgeList.restype = P(GraphCSR)
+        L.graphCSRFree.argtypes = [P(GraphCSR)]
+        L.argumentsSetDefaults.argtypes = [P(Arguments)]
+        for name in ["pageRankGraphCSR", "pageRankPullGraphCSR", "pageRankPushGraphCSR",
+                     "pageRankPullFixedPoint64BitGraphCSR", "pageRankPullFixedPoint32BitGraphCSR",
+                     "pageRankPullFixedPoint16BitGraphCSR", "pageRankPullFixedPoint8BitGraphCSR",
+                     "pageRankPushFixedPointGraphCSR", "pageRankPullQuant32BitGraphCSR",
+                     "pageRankPullQuant16BitGraphCSR", "pageRankPullQuant8BitGraphCSR",
+                     "pageRankPushQuantGraphCSR", "pageRankDataDrivenPullGraphCSR",
+                     "pageRankDataDrivenPushGraphCSR", "pageRankDataDrivenPullPushGraphCSR"]:
+            getattr(L, name).argtypes = [P(Arguments), P(GraphCSR)]
+            getattr(L, name).restype = P(PageRankStats)
+        for name in ["breadthFirstSearchGraphCSR", "breadthFirstSearchPullGraphCSR",
+                     "breadthFirstSearchPushGraphCSR", "breadthFirstSearchDirectionOptimizedGraphCSR",
+                     "breadthFirstSearchPushBitmapGraphCSR",
+                     "breadthFirstSearchPushDirectionOptimizedBitmapGraphCSR"]:
+            getattr(L, name).argtypes = [P(Arguments), P(GraphCSR)]
+            getattr(L, name).restype = P(BFSStats)
+        for name in ["SPMVGraphCSR", "SPMVPullGraphCSR", "SPMVPushGraphCSR", "SPMVPullFixedPointGraphCSR",
+                     "SPMVPushFixedPointGraphCSR"]:
+            getattr(L, name).argtypes = [P(Arguments), P(GraphCSR)]
+            getattr(L, name).restype = P(SPMVStats)
+        L.freePageRankStats.argtypes = [P(PageRankStats)]
+        L.freeBFSStats.argtypes = [P(BFSStats)]
+        L.freeSPMVStats.argtypes = [P(SPMVStats)]
+        L.newBFSStatsGraphCSR.argtypes = [P(GraphCSR)]
+        L.newBFSStatsGraphCSR.restype = P(BFSStats)
+        L.topDownStepGraphCSR.argtypes = [P(GraphCSR), P(ArrayQueue), C.c_void_p, P(BFSStats)]
+        L.topDownStepGraphCSR.restype = C.c_uint32
+        L.bottomUpStepGraphCSR.argtypes = [P(GraphCSR), P(Bitmap), P(Bitmap), P(BFSStats)]
+        L.bottomUpStepGraphCSR.restype = C.c_uint32
+        L.topDownStepUsingBitmapsGraphCSR.argtypes = [P(GraphCSR), P(ArrayQueue), P(BFSStats)]
+        L.topDownStepUsingBitmapsGraphCSR.restype = C.c_uint32
+        L.newArrayQueue.argtypes = [C.c_uint32]
+        L.newArrayQueue.restype = P(ArrayQueue)
+        L.freeArrayQueue.argtypes = [P(ArrayQueue)]
+        L.enArrayQueue.argtypes = [P(ArrayQueue), C.c_uint32]
+        L.slideWindowArrayQueue.argtypes = [P(ArrayQueue)]
+        L.newBitmap.argtypes = [C.c_uint32]
+        L.newBitmap.restype = P(Bitmap)
+        L.freeBitmap.argtypes = [P(Bitmap)]
+        L.setBit.argtypes = [P(Bitmap), C.c_uint32]
+        L.getNumOfSetBits.argtypes = [P(Bitmap)]
+        L.getNumOfSetBits.restype = C.c_uint32
+        L.graphGpuSetOptions.argtypes = [P(GraphGpuOptions)]
+        L.graphGpuGetOptions.argtypes = [P(GraphGpuOptions)]
+        L.graphGpuLastError.restype = C.c_int
+        L.graphGpuRelease.argtypes = [P(GraphCSR)]
+        _LIB = L
+    return _LIB
+
+
+def _check(st, what):
+    if st != 0:
+        msg = lib().gg_last_error().decode(errors="replace")
+        raise GgError(f"{what}: status {st}: {msg}")
+
+
+def device_init(device: int = 0):
+    _check(lib().gg_device_init(device), "gg_device_init")
+
+
+def _np(ptr, n, dtype):
+    if n == 0 or not ptr:
+        return np.zeros(0, dtype)
+    ctype = {np.uint32: C.c_uint32, np.int32: C.c_int, np.float32: C.c_float}[dtype]
+    return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ctype)), shape=(n,)).copy()
+
+
+# ---------------------------------------------------------------------------
+# host graphs
+# ---------------------------------------------------------------------------
+
+class Graph:
+    """A GraphCSR built by the library (CSR + inverse CSR, uint32)."""
+
+    def __init__(self, ptr):
+        if not ptr:
+            raise GgError("graph construction failed")
+        self.ptr = ptr
+
+    @classmethod
+    def from_edges(cls, src, dst, weights=None, num_vertices=None):
+        src = np.ascontiguousarray(src, np.uint32)
+        dst = np.ascontiguousarray(dst, np.uint32)
+        E = len(src)
+        V = int(num_vertices) if num_vertices is not None else (int(max(src.max(), dst.max())) + 1 if E else 0)
+        L = lib()
+        el = L.newEdgeList(E, V, 1 if weights is not None else 0)
+        if not el:
+            raise GgError("newEdgeList failed")
+        try:
+            if E:
+                C.memmove(el.contents.edges_array_src, src.ctypes.data, E * 4)
+                C.memmove(el.contents.edges_array_dest, dst.ctypes.data, E * 4)
+                if weights is not None:
+                    w = np.ascontiguousarray(weights, np.float32)
+                    C.memmove(el.contents.edges_array_weight, w.ctypes.data, E * 4)
+                    el.contents.max_weight = float(w.max())
+            el.contents.num_vertices = V
+            return cls(L.graphCSRFromEdgeList(el))
+        finally:
+            L.freeEdgeList(el)
+
+    @classmethod
+    def rmat(cls, scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=27491095, weighted=False,
+             weight_seed=27491095 + 2, symmetric=False):
+        L = lib()
+        el = L.generateRMATEdgeList(scale, edge_factor, a, b, c, seed, int(weighted), weight_seed, int(symmetric))
+        if not el:
+            raise GgError("generateRMATEdgeList failed")
+        try:
+            return cls(L.graphCSRFromEdgeList(el))
+        finally:
+            L.freeEdgeList(el)
+
+    @classmethod
+    def from_file(cls, path, weighted=False):
+        L = lib()
+        fn = L.readEdgeListsbin if path.endswith("bin") else L.readEdgeListsText
+        el = fn(path.encode(), int(weighted))
+        if not el:
+            raise GgError(f"cannot read {path}")
+        try:
+            return cls(L.graphCSRFromEdgeList(el))
+        finally:
+            L.freeEdgeList(el)
+
+    @property
+    def V(self):
+        return int(self.ptr.contents.num_vertices)
+
+    @property
+    def E(self):
+        return int(self.ptr.contents.num_edges)
+
+    def arrays(self):
+        """Copies of the CSR / CSC arrays: out_off (V+1), out_adj, in_off, in_adj,
+        out_w, in_w (None when unweighted), out_degree, in_degree."""
+        g = self.ptr.contents
+        V, E = self.V, self.E
+        ov, iv = g.vertices.contents, g.inverse_vertices.contents
+        oe, ie = g.sorted_edges_array.contents, g.inverse_sorted_edges_array.contents
+        out_off = np.append(_np(ov.edges_idx, V, np.uint32), np.uint32(E)).astype(np.uint32)
+        in_off = np.append(_np(iv.edges_idx, V, np.uint32), np.uint32(E)).astype(np.uint32)
+        d = dict(out_off=out_off, out_adj=_np(oe.edges_array_dest, E, np.uint32), in_off=in_off,
+                 in_adj=_np(ie.edges_array_dest, E, np.uint32), out_degree=_np(ov.out_degree, V, np.uint32),
+                 in_degree=_np(iv.out_degree, V, np.uint32), out_w=None, in_w=None)
+        if oe.edges_array_weight:
+            d["out_w"] = _np(oe.edges_array_weight, E, np.float32)
+            d["in_w"] = _np(ie.edges_array_weight, E, np.float32)
+        return d
+
+    def free(self):
+        if self.ptr:
+            lib().graphGpuRelease(self.ptr)
+            lib().graphCSRFree(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# device graphs (gg_runtime)
+# ---------------------------------------------------------------------------
+
+class DeviceGraph:
+    """A gg_graph mapping of a Graph (arrays resident in HBM)."""
+
+    def __init__(self, graph: Graph, what=MAP_ALL, stream=None):
+        self.graph = graph
+        self.h = C.c_void_p()
+        _check(lib().gg_graph_map(graph.ptr, what, stream, C.byref(self.h)), "gg_graph_map")
+
+    def extend(self, what, stream=None):
+        _check(lib().gg_graph_extend(self.h, self.graph.ptr, what, stream), "gg_graph_extend")
+
+    def device_bytes(self):
+        return int(lib().gg_graph_device_bytes(self.h))
+
+    def pagerank(self, mode="pull", storage="f32", iterations=20, epsilon=1e-4, init_one_over_n=False,
+                 damp=0.85, profile=False, copy_out=True, stream=None):
+        p = PrParams(PR_MODES[mode] if isinstance(mode, str) else mode, STORE[storage], iterations,
+                     int(init_one_over_n), epsilon, damp, int(profile))
+        r = PrResult()
+        ranks = np.empty(self.graph.V, np.float32) if copy_out else None
+        _check(lib().gg_pagerank(self.h, C.byref(p), None if ranks is None else ranks.ctypes.data, C.byref(r),
+                                 stream), "gg_pagerank")
+        return ranks, {k: getattr(r, k) for k, _ in PrResult._fields_}
+
+    def bfs(self, source, mode="do", profile=False, copy_out=True, stream=None):
+        p = BfsParams(BFS_MODES[mode] if isinstance(mode, str) else mode, source, 15, 18, int(profile))
+        r = BfsResult()
+        V = self.graph.V
+        parents = np.empty(V, np.int32) if copy_out else None
+        dist = np.empty(V, np.uint32) if copy_out else None
+        _check(lib().gg_bfs(self.h, C.byref(p), None if parents is None else parents.ctypes.data,
+                            None if dist is None else dist.ctypes.data, C.byref(r), stream), "gg_bfs")
+        return parents, dist, {k: getattr(r, k) for k, _ in BfsResult._fields_}
+
+    def spmv(self, mode="pull", storage="f32", iterations=1, x=None, profile=False, copy_out=True, stream=None):
+        p = SpmvParams(SPMV_MODES[mode] if isinstance(mode, str) else mode, STORE[storage], iterations,
+                       int(profile))
+        r = SpmvResult()
+        V = self.graph.V
+        xin = None if x is None else np.ascontiguousarray(x, np.float32)
+        xo = np.empty(V, np.float32) if copy_out else None
+        y = np.empty(V, np.float32) if copy_out else None
+        _check(lib().gg_spmv(self.h, C.byref(p), None if xin is None else xin.ctypes.data,
+                             None if xo is None else xo.ctypes.data, None if y is None else y.ctypes.data,
+                             C.byref(r), stream), "gg_spmv")
+        return xo, y, {k: getattr(r, k) for k, _ in SpmvResult._fields_}
+
+    def free(self):
+        if self.h:
+            lib().gg_graph_unmap(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# the reference-compatible entry points
+# ---------------------------------------------------------------------------
+
+def default_arguments(**kw) -> Arguments:
+    a = Arguments()
+    lib().argumentsSetDefaults(C.byref(a))
+    for k, v in kw.items():
+        setattr(a, k, v)
+    return a
+
+
+def set_gpu_options(storage="f32", device=0, keep_resident=False, verbose=False):
+    o = GraphGpuOptions(STORE[storage], device, int(keep_resident), int(verbose))
+    lib().graphGpuSetOptions(C.byref(o))
+
+
+def pagerank_csr(graph: Graph, args: Arguments, fn="pageRankGraphCSR"):
+    """Call a pageRank*GraphCSR entry point; returns (ranks, stats dict)."""
+    L = lib()
+    s = getattr(L, fn)(C.byref(args), graph.ptr)
+    if not s:
+        raise GgError(f"{fn} failed: status {L.graphGpuLastError()}: {L.gg_last_error().decode()}")
+    try:
+        st = s.contents
+        ranks = _np(st.pageRanks, graph.V, np.float32)
+        return ranks, {"iterations": st.iterations, "error_total": st.error_total, "time_total": st.time_total,
+                       "activeVertices": st.activeVertices, "damp": st.damp, "base_pr": st.base_pr,
+                       "realRanks": _np(st.realRanks, graph.V, np.uint32)}
+    finally:
+        L.freePageRankStats(s)
+
+
+def bfs_csr(graph: Graph, args: Arguments, fn="breadthFirstSearchGraphCSR"):
+    """Call a breadthFirstSearch*GraphCSR entry point; returns (parents, distances, stats dict)."""
+    L = lib()
+    s = getattr(L, fn)(C.byref(args), graph.ptr)
+    if not s:
+        raise GgError(f"{fn} failed: status {L.graphGpuLastError()}: {L.gg_last_error().decode()}")
+    try:
+        st = s.contents
+        return (_np(st.parents, graph.V, np.int32), _np(st.distances, graph.V, np.uint32),
+                {"processed_nodes": st.processed_nodes, "iteration": st.iteration, "time_total": st.time_total,
+                 "source": args.source})
+    finally:
+        L.freeBFSStats(s)
+
+
+def spmv_csr(graph: Graph, args: Arguments, fn="SPMVGraphCSR"):
+    """Call an SPMV*GraphCSR entry point; returns (x, y, stats dict)."""
+    L = lib()
+    s = getattr(L, fn)(C.byref(args), graph.ptr)
+    if not s:
+        raise GgError(f"{fn} failed: status {L.graphGpuLastError()}: {L.gg_last_error().decode()}")
+    try:
+        st = s.contents
+        return (_np(st.vector_input, graph.V, np.float32), _np(st.vector_output, graph.V, np.float32),
+                {"iterations": st.iterations, "time_total": st.time_total})
+    finally:
+        L.freeSPMVStats(s)

@@ -1,0 +1,111 @@
+/*
+ * Internal declarations shared by the gg_runtime translation units.
+ * Not part of the public ABI (include/gg_runtime.h is).
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+
+#include "gg_runtime.h"
+
+/* Threads and items per thread of the merge-path tile kernels.  One CTA
+ * consumes TILE_ITEMS = NT*IPT merge items (row ends + edges).  IPT is odd so
+ * that the per-thread reads of the staged values hit distinct shared-memory
+ * banks. */
+#define GG_TILE_NT 256
+#define GG_TILE_IPT 7
+#define GG_TILE_ITEMS (GG_TILE_NT * GG_TILE_IPT)
+
+/* Slack after every edge array so 16-byte vector loads of the last group
+ * stay inside the allocation. */
+#define GG_EDGE_PAD 16
+
+struct gg_tiles
+{
+    uint32_t ntiles = 0;
+    uint2 *coord = nullptr;   /* ntiles+1 merge-path coordinates (row, edge) */
+    void *acc = nullptr;      /* ntiles cross-tile partial sums (8 bytes each) */
+    uint32_t *cnt = nullptr;  /* ntiles arrival counters */
+};
+
+/* Growable device scratch owned by a mapping. */
+struct gg_buf
+{
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct gg_graph
+{
+    uint32_t V = 0, E = 0;
+    uint32_t what = 0;
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+
+    /* out-CSR */
+    uint32_t *out_off = nullptr;
+    uint32_t *out_adj = nullptr;
+    float *out_w = nullptr;
+    /* in-CSR (CSC) */
+    uint32_t *in_off = nullptr;
+    uint32_t *in_adj = nullptr;
+    float *in_w = nullptr;
+    uint32_t *out_deg = nullptr;
+
+    gg_tiles in_tiles;   /* tiles over the CSC (pull) */
+    gg_tiles out_tiles;  /* tiles over the CSR (push) */
+
+    /* bf16/f16 copies of the edge weights, made on first use */
+    void *in_w16[3] = {nullptr, nullptr, nullptr};
+    void *out_w16[3] = {nullptr, nullptr, nullptr};
+
+    /* work buffers, grown on demand */
+    gg_buf work[16];
+
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    /* timing events reused across calls (profile mode) */
+    cudaEvent_t *ev_pool = nullptr;
+    uint32_t ev_count = 0;
+    size_t device_bytes = 0;
+    const float *last_ranks = nullptr;
+};
+
+/* error state */
+gg_status gg_fail(gg_status s, const std::string &msg);
+gg_status gg_cuda_fail(cudaError_t e, const char *what);
+#define GG_CUDA(call)                                                   \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return gg_cuda_fail(e_, #call);          \
+    } while (0)
+#define GG_CHECK(expr)                                                  \
+    do {                                                                \
+        gg_status s_ = (expr);                                          \
+        if (s_ != GG_OK) return s_;                                     \
+    } while (0)
+
+/* device memory helpers (account into g->device_bytes) */
+gg_status gg_dev_alloc(gg_graph *g, void **p, size_t bytes);
+void gg_dev_free(gg_graph *g, void *p, size_t bytes);
+/* work buffer slot `slot`, at least `bytes` long (contents undefined) */
+gg_status gg_work(gg_graph *g, int slot, size_t bytes, void **out);
+cudaStream_t gg_stream(gg_graph *g, void *user_stream);
+/* host wait on all work queued on `s`, bounded by the wait limit */
+gg_status gg_wait(cudaStream_t s);
+/* tiles of the CSC (in = 1) or CSR (in = 0), computed on first use */
+gg_status gg_tiles_get(gg_graph *g, int in, cudaStream_t s, gg_tiles **out);
+/* bf16 (storage 1) / f16 (storage 2) copy of the in- or out-edge weights */
+gg_status gg_weights16(gg_graph *g, int in, int storage, cudaStream_t s, const void **out);
+/* the i-th pooled timing event of g, created on first use */
+gg_status gg_event_at(gg_graph *g, uint32_t i, cudaEvent_t *out);
+/* elapsed ms between two events recorded on s (after a wait) */
+float gg_event_ms(cudaEvent_t a, cudaEvent_t b);
+
+/* launch helpers implemented in the kernel translation units */
+gg_status gg_launch_tile_coords(const uint32_t *off, uint32_t V, uint32_t E, uint32_t ntiles,
+                                uint2 *coord, cudaStream_t s);
+gg_status gg_launch_to_half(const float *src, void *dst, size_t n, int storage, cudaStream_t s);
+int gg_sm_count();

@@ -1,0 +1,429 @@
+/*
+ * gg_runtime core: device context, graph mapping, work buffers, bounded
+ * waits.  This is the GPU replacement of the reference's CAPI layer
+ * (02_capi_graph/src/capi_utils/capienv.c): mapGraphCSRToWED (:396-438)
+ * becomes gg_graph_map, setupAFUGraphCSR (:30-55) gg_device_init, the
+ * unbounded waitAFU poll (:111-172) a wait with a time limit, releaseAFU
+ * (:299-303) gg_graph_unmap.
+ */
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+
+#include "gg_internal.h"
+
+namespace {
+
+thread_local std::string t_last_error;
+std::atomic<uint32_t> g_wait_timeout_ms{0};
+int g_sm_count = 0;
+
+uint32_t wait_timeout_ms()
+{
+    uint32_t v = g_wait_timeout_ms.load();
+    if (v == 0)
+    {
+        const char *env = getenv("GG_WAIT_TIMEOUT_MS");
+        v = env ? (uint32_t)strtoul(env, nullptr, 10) : 0;
+        if (v == 0) v = 120000;
+        g_wait_timeout_ms.store(v);
+    }
+    return v;
+}
+
+size_t align_up(size_t n, size_t a) { return (n + a - 1) / a * a; }
+
+} // namespace
+
+gg_status gg_fail(gg_status s, const std::string &msg)
+{
+    t_last_error = msg;
+    return s;
+}
+
+gg_status gg_cuda_fail(cudaError_t e, const char *what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation)
+        return gg_fail(GG_ERR_NOMEM, m);
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+        return gg_fail(GG_ERR_NO_DEVICE, m);
+    return gg_fail(GG_ERR_CUDA, m);
+}
+
+extern "C" const char *gg_last_error(void) { return t_last_error.c_str(); }
+
+extern "C" void gg_set_wait_timeout_ms(uint32_t ms) { g_wait_timeout_ms.store(ms ? ms : 120000); }
+
+int gg_sm_count() { return g_sm_count > 0 ? g_sm_count : 152; }
+
+extern "C" gg_status gg_device_init(int device)
+{
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return gg_fail(GG_ERR_NO_DEVICE, std::string("no CUDA device: ") +
+                                             (e != cudaSuccess ? cudaGetErrorString(e) : "count is 0"));
+    if (device < 0 || device >= n)
+        return gg_fail(GG_ERR_INVALID, "device index out of range");
+    GG_CUDA(cudaSetDevice(device));
+    GG_CUDA(cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, device));
+    return GG_OK;
+}
+
+gg_status gg_dev_alloc(gg_graph *g, void **p, size_t bytes)
+{
+    *p = nullptr;
+    if (bytes == 0) bytes = 256;
+    cudaError_t e = cudaMalloc(p, align_up(bytes, 256));
+    if (e != cudaSuccess)
+    {
+        *p = nullptr;
+        return gg_cuda_fail(e, "cudaMalloc");
+    }
+    g->device_bytes += align_up(bytes, 256);
+    return GG_OK;
+}
+
+void gg_dev_free(gg_graph *g, void *p, size_t bytes)
+{
+    if (!p) return;
+    cudaFree(p);
+    size_t b = align_up(bytes ? bytes : 256, 256);
+    g->device_bytes = g->device_bytes >= b ? g->device_bytes - b : 0;
+}
+
+gg_status gg_work(gg_graph *g, int slot, size_t bytes, void **out)
+{
+    gg_buf &b = g->work[slot];
+    if (b.bytes < bytes)
+    {
+        if (b.ptr) gg_dev_free(g, b.ptr, b.bytes);
+        b.ptr = nullptr;
+        b.bytes = 0;
+        GG_CHECK(gg_dev_alloc(g, &b.ptr, bytes));
+        b.bytes = bytes;
+    }
+    *out = b.ptr;
+    return GG_OK;
+}
+
+cudaStream_t gg_stream(gg_graph *g, void *user_stream)
+{
+    return user_stream ? (cudaStream_t)user_stream : g->own_stream;
+}
+
+gg_status gg_wait(cudaStream_t s)
+{
+    /* Bounded host wait: poll an event instead of blocking forever like the
+     * reference's waitAFU loop. */
+    cudaEvent_t ev;
+    GG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ev, s);
+    if (e != cudaSuccess)
+    {
+        cudaEventDestroy(ev);
+        return gg_cuda_fail(e, "cudaEventRecord");
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    const uint32_t limit = wait_timeout_ms();
+    uint32_t spins = 0;
+    for (;;)
+    {
+        e = cudaEventQuery(ev);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady)
+        {
+            cudaEventDestroy(ev);
+            return gg_cuda_fail(e, "device work");
+        }
+        auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+        if ((uint64_t)ms > limit)
+        {
+            cudaEventDestroy(ev);
+            return gg_fail(GG_ETIMEDOUT, "device work did not finish within the wait limit");
+        }
+        if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+    cudaEventDestroy(ev);
+    return GG_OK;
+}
+
+gg_status gg_event_at(gg_graph *g, uint32_t i, cudaEvent_t *out)
+{
+    if (i >= g->ev_count)
+    {
+        uint32_t n = g->ev_count ? g->ev_count : 64;
+        while (n <= i) n *= 2;
+        cudaEvent_t *p = (cudaEvent_t *)realloc(g->ev_pool, n * sizeof(cudaEvent_t));
+        if (!p) return gg_fail(GG_ERR_NOMEM, "event pool");
+        for (uint32_t k = g->ev_count; k < n; k++) GG_CUDA(cudaEventCreate(&p[k]));
+        g->ev_pool = p;
+        g->ev_count = n;
+    }
+    *out = g->ev_pool[i];
+    return GG_OK;
+}
+
+float gg_event_ms(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) return 0.0f;
+    return ms;
+}
+
+/* ---- mapping ---------------------------------------------------------------- */
+
+static gg_status upload(gg_graph *g, void **dst, const void *src, size_t bytes, size_t alloc_bytes,
+                        cudaStream_t s)
+{
+    GG_CHECK(gg_dev_alloc(g, dst, alloc_bytes));
+    if (bytes)
+        GG_CUDA(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, s));
+    if (alloc_bytes > bytes)
+        GG_CUDA(cudaMemsetAsync((char *)*dst + bytes, 0, alloc_bytes - bytes, s));
+    return GG_OK;
+}
+
+static gg_status fill_constant_weights(gg_graph *g, float **dst, uint32_t E, cudaStream_t s);
+
+static gg_status map_arrays(gg_graph *g, const struct GraphCSR *graph, uint32_t what, cudaStream_t s)
+{
+    const uint32_t V = g->V, E = g->E;
+    const size_t off_bytes = ((size_t)V + 1) * 4;
+    const size_t edge_bytes = (size_t)E * 4, edge_alloc = ((size_t)E + GG_EDGE_PAD) * 4;
+    if ((what & (GG_MAP_OUT | GG_MAP_IN)) && !g->out_deg)
+    {
+        if (!graph->vertices || !graph->vertices->out_degree)
+            return gg_fail(GG_ERR_INVALID, "graph has no out_degree array");
+        GG_CHECK(upload(g, (void **)&g->out_deg, graph->vertices->out_degree, (size_t)V * 4, (size_t)V * 4 + 16, s));
+    }
+    if ((what & GG_MAP_OUT) && !g->out_off)
+    {
+        if (!graph->vertices->edges_idx || !graph->sorted_edges_array || (E && !graph->sorted_edges_array->edges_array_dest))
+            return gg_fail(GG_ERR_INVALID, "graph has no out-CSR arrays");
+        /* offsets: edges_idx[0..V-1] plus the total E */
+        GG_CHECK(upload(g, (void **)&g->out_off, graph->vertices->edges_idx, (size_t)V * 4, off_bytes, s));
+        GG_CUDA(cudaMemcpyAsync(g->out_off + V, &g->E, 4, cudaMemcpyHostToDevice, s));
+        GG_CHECK(upload(g, (void **)&g->out_adj, graph->sorted_edges_array->edges_array_dest, edge_bytes, edge_alloc, s));
+    }
+    if ((what & GG_MAP_IN) && !g->in_off)
+    {
+        if (!graph->inverse_vertices || !graph->inverse_vertices->edges_idx || !graph->inverse_sorted_edges_array ||
+            (E && !graph->inverse_sorted_edges_array->edges_array_dest))
+            return gg_fail(GG_ERR_INVALID, "graph has no inverse (CSC) arrays");
+        GG_CHECK(upload(g, (void **)&g->in_off, graph->inverse_vertices->edges_idx, (size_t)V * 4, off_bytes, s));
+        GG_CUDA(cudaMemcpyAsync(g->in_off + V, &g->E, 4, cudaMemcpyHostToDevice, s));
+        GG_CHECK(upload(g, (void **)&g->in_adj, graph->inverse_sorted_edges_array->edges_array_dest, edge_bytes, edge_alloc, s));
+    }
+    if ((what & GG_MAP_OUT_W) && !g->out_w)
+    {
+        const float *w = graph->sorted_edges_array ? graph->sorted_edges_array->edges_array_weight : nullptr;
+        if (w)
+            GG_CHECK(upload(g, (void **)&g->out_w, w, edge_bytes, edge_alloc, s));
+        else
+            GG_CHECK(fill_constant_weights(g, &g->out_w, E, s));
+    }
+    if ((what & GG_MAP_IN_W) && !g->in_w)
+    {
+        const float *w = graph->inverse_sorted_edges_array ? graph->inverse_sorted_edges_array->edges_array_weight : nullptr;
+        if (w)
+            GG_CHECK(upload(g, (void **)&g->in_w, w, edge_bytes, edge_alloc, s));
+        else
+            GG_CHECK(fill_constant_weights(g, &g->in_w, E, s));
+    }
+    g->what |= what;
+    /* the copies read pageable host memory; make them complete before the
+     * caller may free or change it */
+    return gg_wait(s);
+}
+
+__global__ void k_fill(float *p, size_t n, float v)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+static gg_status fill_constant_weights(gg_graph *g, float **dst, uint32_t E, cudaStream_t s)
+{
+    /* the reference's unweighted build multiplies by 0.0001f (SPMV.c:804) */
+    GG_CHECK(gg_dev_alloc(g, (void **)dst, ((size_t)E + GG_EDGE_PAD) * 4));
+    k_fill<<<gg_sm_count() * 4, 256, 0, s>>>(*dst, (size_t)E + GG_EDGE_PAD, 0.0001f);
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+}
+
+extern "C" gg_status gg_graph_map(const struct GraphCSR *graph, uint32_t what, void *stream, gg_graph **out)
+{
+    if (!out) return gg_fail(GG_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!graph) return gg_fail(GG_ERR_INVALID, "graph is NULL");
+    int dev = 0;
+    GG_CUDA(cudaGetDevice(&dev));
+    gg_graph *g = new gg_graph();
+    g->V = graph->num_vertices;
+    g->E = graph->num_edges;
+    g->device = dev;
+    cudaError_t e = cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess)
+    {
+        delete g;
+        return gg_cuda_fail(e, "cudaStreamCreate");
+    }
+    cudaEventCreate(&g->ev_begin);
+    cudaEventCreate(&g->ev_end);
+    gg_status st = map_arrays(g, graph, what, gg_stream(g, stream));
+    if (st != GG_OK)
+    {
+        std::string keep = t_last_error;
+        gg_graph_unmap(g);
+        t_last_error = keep;
+        return st;
+    }
+    *out = g;
+    return GG_OK;
+}
+
+extern "C" gg_status gg_graph_extend(gg_graph *g, const struct GraphCSR *graph, uint32_t what, void *stream)
+{
+    if (!g || !graph) return gg_fail(GG_ERR_INVALID, "NULL argument");
+    if (graph->num_vertices != g->V || graph->num_edges != g->E)
+        return gg_fail(GG_ERR_INVALID, "graph size differs from the mapping");
+    return map_arrays(g, graph, what, gg_stream(g, stream));
+}
+
+static void free_tiles(gg_graph *g, gg_tiles &t)
+{
+    gg_dev_free(g, t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2));
+    gg_dev_free(g, t.acc, (size_t)t.ntiles * 8 + 8);
+    gg_dev_free(g, t.cnt, (size_t)t.ntiles * 4 + 4);
+    t = gg_tiles();
+}
+
+extern "C" gg_status gg_graph_unmap(gg_graph *g)
+{
+    if (!g) return GG_OK;
+    if (g->own_stream) cudaStreamSynchronize(g->own_stream);
+    const size_t off_bytes = ((size_t)g->V + 1) * 4, edge_alloc = ((size_t)g->E + GG_EDGE_PAD) * 4;
+    gg_dev_free(g, g->out_off, off_bytes);
+    gg_dev_free(g, g->out_adj, edge_alloc);
+    gg_dev_free(g, g->out_w, edge_alloc);
+    gg_dev_free(g, g->in_off, off_bytes);
+    gg_dev_free(g, g->in_adj, edge_alloc);
+    gg_dev_free(g, g->in_w, edge_alloc);
+    gg_dev_free(g, g->out_deg, (size_t)g->V * 4 + 16);
+    for (int i = 0; i < 3; i++)
+    {
+        gg_dev_free(g, g->in_w16[i], edge_alloc);
+        gg_dev_free(g, g->out_w16[i], edge_alloc);
+    }
+    free_tiles(g, g->in_tiles);
+    free_tiles(g, g->out_tiles);
+    for (auto &b : g->work) gg_dev_free(g, b.ptr, b.bytes);
+    for (uint32_t i = 0; i < g->ev_count; i++) cudaEventDestroy(g->ev_pool[i]);
+    free(g->ev_pool);
+    if (g->ev_begin) cudaEventDestroy(g->ev_begin);
+    if (g->ev_end) cudaEventDestroy(g->ev_end);
+    if (g->own_stream) cudaStreamDestroy(g->own_stream);
+    delete g;
+    return GG_OK;
+}
+
+extern "C" size_t gg_graph_device_bytes(const gg_graph *g) { return g ? g->device_bytes : 0; }
+
+gg_status gg_tiles_get(gg_graph *g, int in, cudaStream_t s, gg_tiles **out)
+{
+    gg_tiles &t = in ? g->in_tiles : g->out_tiles;
+    const uint32_t *off = in ? g->in_off : g->out_off;
+    if (!off) return gg_fail(GG_ERR_INVALID, in ? "mapping has no CSC arrays" : "mapping has no CSR arrays");
+    if (!t.coord)
+    {
+        const uint64_t items = (uint64_t)g->V + g->E;
+        const uint64_t nt = (items + GG_TILE_ITEMS - 1) / GG_TILE_ITEMS;
+        if (nt >= 0xffffffffull) return gg_fail(GG_ERR_INVALID, "graph too large for 32-bit tile ids");
+        t.ntiles = (uint32_t)(nt ? nt : 1);
+        GG_CHECK(gg_dev_alloc(g, (void **)&t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2)));
+        GG_CHECK(gg_dev_alloc(g, &t.acc, (size_t)t.ntiles * 8 + 8));
+        GG_CHECK(gg_dev_alloc(g, (void **)&t.cnt, (size_t)t.ntiles * 4 + 4));
+        GG_CUDA(cudaMemsetAsync(t.acc, 0, (size_t)t.ntiles * 8 + 8, s));
+        GG_CUDA(cudaMemsetAsync(t.cnt, 0, (size_t)t.ntiles * 4 + 4, s));
+        GG_CHECK(gg_launch_tile_coords(off, g->V, g->E, t.ntiles, t.coord, s));
+    }
+    *out = &t;
+    return GG_OK;
+}
+
+gg_status gg_weights16(gg_graph *g, int in, int storage, cudaStream_t s, const void **out)
+{
+    if (storage != GG_STORE_BF16 && storage != GG_STORE_F16)
+        return gg_fail(GG_ERR_INVALID, "not a 16-bit storage");
+    void *&slot = in ? g->in_w16[storage] : g->out_w16[storage];
+    const float *w = in ? g->in_w : g->out_w;
+    if (!w) return gg_fail(GG_ERR_INVALID, "mapping has no edge weights");
+    if (!slot)
+    {
+        GG_CHECK(gg_dev_alloc(g, &slot, ((size_t)g->E + GG_EDGE_PAD) * 4));
+        GG_CHECK(gg_launch_to_half(w, slot, (size_t)g->E + GG_EDGE_PAD, storage, s));
+    }
+    *out = slot;
+    return GG_OK;
+}
+
+/* ---- small kernels used by the runtime ------------------------------------------- */
+
+__global__ void k_tile_coords(const uint32_t *__restrict__ off, uint32_t V, uint32_t E, uint32_t ntiles,
+                              uint2 *__restrict__ coord)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > ntiles) return;
+    const uint64_t items = (uint64_t)V + E;
+    uint64_t d = (uint64_t)t * GG_TILE_ITEMS;
+    if (d > items) d = items;
+    /* rows ended before diagonal d: largest i with off[i] + (i-1) < d over row ends off[1..V] */
+    uint64_t lo = d > E ? d - E : 0, hi = d < V ? d : V;
+    while (lo < hi)
+    {
+        uint64_t mid = (lo + hi) >> 1;
+        if ((uint64_t)off[mid + 1] + mid < d)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    coord[t] = make_uint2((uint32_t)lo, (uint32_t)(d - lo));
+}
+
+gg_status gg_launch_tile_coords(const uint32_t *off, uint32_t V, uint32_t E, uint32_t ntiles, uint2 *coord,
+                                cudaStream_t s)
+{
+    const uint32_t n = ntiles + 1;
+    k_tile_coords<<<(n + 255) / 256, 256, 0, s>>>(off, V, E, ntiles, coord);
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+}
+
+__global__ void k_to_half(const float *__restrict__ src, void *__restrict__ dst, size_t n, int storage)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    {
+        if (storage == GG_STORE_BF16)
+            ((__nv_bfloat16 *)dst)[i] = __float2bfloat16_rn(src[i]);
+        else
+            ((__half *)dst)[i] = __float2half_rn(src[i]);
+    }
+}
+
+gg_status gg_launch_to_half(const float *src, void *dst, size_t n, int storage, cudaStream_t s)
+{
+    k_to_half<<<gg_sm_count() * 4, 256, 0, s>>>(src, dst, n, storage);
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+}

@@ -1,0 +1,458 @@
+/*
+ * Host graph construction for the CSR traversal path: edge-list loaders,
+ * the seeded R-MAT generator, and the CSR + inverse-CSR (CSC) build.
+ *
+ * The reference gets these from its OpenGraph submodule (edge-list loading,
+ * radix/count sort by source with the -o flag, accel-graph.c:71-73), which is
+ * absent from the snapshot; this is the project's own implementation of the
+ * same contract (graphCSR.h).  The build is a parallel LSD radix sort of
+ * 64-bit (key << 32 | other) words in 11-bit digits: stable, so every
+ * adjacency list ends up sorted by neighbour id and the result is
+ * deterministic for any thread count.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <errno.h>
+#include <omp.h>
+
+#include "graphCSR.h"
+#include "gg_host.h"
+
+#define PHI 0x9E3779B97F4A7C15ULL
+
+static uint64_t mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+static void *xmalloc(size_t n)
+{
+    void *p = NULL;
+    if (posix_memalign(&p, 64, n ? n : 64) != 0)
+        return NULL;
+    return p;
+}
+
+/* ---- edge lists -------------------------------------------------------------- */
+
+struct EdgeList *newEdgeList(uint32_t num_edges, uint32_t num_vertices, int weighted)
+{
+    struct EdgeList *e = (struct EdgeList *)calloc(1, sizeof(struct EdgeList));
+    if (!e)
+        return NULL;
+    e->num_edges = num_edges;
+    e->num_vertices = num_vertices;
+    e->edges_array_src = (uint32_t *)xmalloc((size_t)num_edges * 4 + 64);
+    e->edges_array_dest = (uint32_t *)xmalloc((size_t)num_edges * 4 + 64);
+    if (weighted)
+        e->edges_array_weight = (float *)xmalloc((size_t)num_edges * 4 + 64);
+    if (!e->edges_array_src || !e->edges_array_dest || (weighted && !e->edges_array_weight))
+    {
+        freeEdgeList(e);
+        return NULL;
+    }
+    return e;
+}
+
+void freeEdgeList(struct EdgeList *e)
+{
+    if (!e)
+        return;
+    free(e->edges_array_src);
+    free(e->edges_array_dest);
+    free(e->edges_array_weight);
+    free(e->label_array);
+    free(e->inverse_label_array);
+    free(e);
+}
+
+static void finish_edge_list(struct EdgeList *e)
+{
+    uint32_t vmax = 0;
+    float wmax = 0.0f;
+    for (uint32_t i = 0; i < e->num_edges; i++)
+    {
+        if (e->edges_array_src[i] > vmax) vmax = e->edges_array_src[i];
+        if (e->edges_array_dest[i] > vmax) vmax = e->edges_array_dest[i];
+        if (e->edges_array_weight && e->edges_array_weight[i] > wmax) wmax = e->edges_array_weight[i];
+    }
+    e->num_vertices = e->num_edges ? vmax + 1 : 0;
+    e->max_weight = wmax;
+}
+
+struct EdgeList *readEdgeListsbin(const char *fname, int weighted)
+{
+    FILE *f = fopen(fname, "rb");
+    if (!f)
+    {
+        fprintf(stderr, "readEdgeListsbin: cannot open %s: %s\n", fname, strerror(errno));
+        return NULL;
+    }
+    fseek(f, 0, SEEK_END);
+    long bytes = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    const size_t rec = weighted ? 12 : 8;
+    if (bytes < 0 || (size_t)bytes % rec != 0)
+    {
+        fprintf(stderr, "readEdgeListsbin: %s: size %ld is not a multiple of %zu\n", fname, bytes, rec);
+        fclose(f);
+        return NULL;
+    }
+    uint32_t n = (uint32_t)((size_t)bytes / rec);
+    struct EdgeList *e = newEdgeList(n, 0, weighted);
+    uint32_t *buf = (uint32_t *)xmalloc((size_t)bytes + 16);
+    if (!e || !buf || fread(buf, 1, (size_t)bytes, f) != (size_t)bytes)
+    {
+        fprintf(stderr, "readEdgeListsbin: %s: read failed\n", fname);
+        free(buf);
+        freeEdgeList(e);
+        fclose(f);
+        return NULL;
+    }
+    fclose(f);
+    const uint32_t k = weighted ? 3 : 2;
+    for (uint32_t i = 0; i < n; i++)
+    {
+        e->edges_array_src[i] = buf[(size_t)i * k];
+        e->edges_array_dest[i] = buf[(size_t)i * k + 1];
+        if (weighted)
+            e->edges_array_weight[i] = (float)buf[(size_t)i * k + 2];
+    }
+    free(buf);
+    finish_edge_list(e);
+    return e;
+}
+
+struct EdgeList *readEdgeListsText(const char *fname, int weighted)
+{
+    FILE *f = fopen(fname, "r");
+    if (!f)
+    {
+        fprintf(stderr, "readEdgeListsText: cannot open %s: %s\n", fname, strerror(errno));
+        return NULL;
+    }
+    uint32_t cap = 1024, n = 0;
+    uint32_t *s = (uint32_t *)malloc(cap * 4), *d = (uint32_t *)malloc(cap * 4);
+    float *w = weighted ? (float *)malloc(cap * 4) : NULL;
+    char line[512];
+    while (fgets(line, sizeof line, f))
+    {
+        unsigned long a, b;
+        double c = 1.0;
+        int got = sscanf(line, "%lu %lu %lf", &a, &b, &c);
+        if (got < 2)
+            continue;
+        if (n == cap)
+        {
+            cap *= 2;
+            s = (uint32_t *)realloc(s, cap * 4);
+            d = (uint32_t *)realloc(d, cap * 4);
+            if (w) w = (float *)realloc(w, cap * 4);
+        }
+        s[n] = (uint32_t)a;
+        d[n] = (uint32_t)b;
+        if (w) w[n] = (float)(got >= 3 ? c : 1.0);
+        n++;
+    }
+    fclose(f);
+    struct EdgeList *e = newEdgeList(n, 0, weighted);
+    if (e)
+    {
+        memcpy(e->edges_array_src, s, (size_t)n * 4);
+        memcpy(e->edges_array_dest, d, (size_t)n * 4);
+        if (w) memcpy(e->edges_array_weight, w, (size_t)n * 4);
+        finish_edge_list(e);
+    }
+    free(s);
+    free(d);
+    free(w);
+    return e;
+}
+
+struct EdgeList *generateRMATEdgeList(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                                      uint64_t seed, int weighted, uint64_t weight_seed, int symmetric)
+{
+    if (scale == 0 || scale > 31)
+        return NULL;
+    const uint64_t V = 1ull << scale;
+    const uint64_t E0 = V * edge_factor;
+    const uint64_t E = symmetric ? 2 * E0 : E0;
+    if (E >= 0xffffffffull)
+    {
+        fprintf(stderr, "generateRMATEdgeList: %llu edges do not fit 32-bit offsets\n", (unsigned long long)E);
+        return NULL;
+    }
+    struct EdgeList *e = newEdgeList((uint32_t)E, (uint32_t)V, weighted);
+    if (!e)
+        return NULL;
+    const double t1 = a, t2 = a + b, t3 = a + b + c;
+    uint32_t *src = e->edges_array_src, *dst = e->edges_array_dest;
+    float *w = e->edges_array_weight;
+#pragma omp parallel for schedule(static)
+    for (uint64_t i = 0; i < E0; i++)
+    {
+        uint32_t s = 0, d = 0;
+        for (uint32_t l = 0; l < scale; l++)
+        {
+            const uint64_t r = mix64(seed + (i * scale + l + 1) * PHI);
+            const double u = (double)(r >> 11) * (1.0 / 9007199254740992.0);
+            const uint32_t bit = 1u << (scale - 1 - l);
+            if (u < t1) { }
+            else if (u < t2) d |= bit;
+            else if (u < t3) s |= bit;
+            else { s |= bit; d |= bit; }
+        }
+        src[i] = s;
+        dst[i] = d;
+        if (symmetric)
+        {
+            src[E0 + i] = d;
+            dst[E0 + i] = s;
+        }
+        if (w)
+        {
+            const uint64_t r = mix64(weight_seed + (i + 1) * PHI);
+            const float wv = (float)((double)(r >> 40) * (1.0 / 16777216.0));
+            w[i] = wv;
+            if (symmetric) w[E0 + i] = wv;
+        }
+    }
+    e->num_vertices = (uint32_t)V;
+    float wmax = 0.0f;
+    if (w)
+        for (uint64_t i = 0; i < E; i++)
+            if (w[i] > wmax) wmax = w[i];
+    e->max_weight = wmax;
+    return e;
+}
+
+/* ---- parallel stable LSD radix sort of 64-bit words with a float payload ----- */
+
+#define RDX_BITS 11
+#define RDX_SIZE (1u << RDX_BITS)
+
+static void radix_sort64(uint64_t *keys, uint64_t *tmp, float *pay, float *ptmp, size_t n, int key_bits)
+{
+    const int passes = (key_bits + RDX_BITS - 1) / RDX_BITS;
+    int T = omp_get_max_threads();
+    if (T < 1) T = 1;
+    if ((size_t)T > n / 4096 + 1) T = (int)(n / 4096 + 1);
+    size_t *hist = (size_t *)calloc((size_t)T * RDX_SIZE, sizeof(size_t));
+    for (int p = 0; p < passes; p++)
+    {
+        const int shift = p * RDX_BITS;
+        memset(hist, 0, (size_t)T * RDX_SIZE * sizeof(size_t));
+#pragma omp parallel num_threads(T)
+        {
+            const int t = omp_get_thread_num();
+            const size_t lo = n * (size_t)t / (size_t)T, hi = n * (size_t)(t + 1) / (size_t)T;
+            size_t *h = hist + (size_t)t * RDX_SIZE;
+            for (size_t i = lo; i < hi; i++)
+                h[(keys[i] >> shift) & (RDX_SIZE - 1)]++;
+#pragma omp barrier
+#pragma omp single
+            {
+                size_t run = 0;
+                for (uint32_t d = 0; d < RDX_SIZE; d++)
+                    for (int tt = 0; tt < T; tt++)
+                    {
+                        size_t c = hist[(size_t)tt * RDX_SIZE + d];
+                        hist[(size_t)tt * RDX_SIZE + d] = run;
+                        run += c;
+                    }
+            }
+            for (size_t i = lo; i < hi; i++)
+            {
+                const size_t at = h[(keys[i] >> shift) & (RDX_SIZE - 1)]++;
+                tmp[at] = keys[i];
+                if (pay)
+                    ptmp[at] = pay[i];
+            }
+        }
+        uint64_t *k2 = keys; keys = tmp; tmp = k2;
+        float *p2 = pay; pay = ptmp; ptmp = p2;
+    }
+    if (passes & 1)
+    {
+        /* result is in the scratch buffers: copy back */
+#pragma omp parallel for schedule(static)
+        for (size_t i = 0; i < n; i++)
+        {
+            tmp[i] = keys[i];
+            if (pay)
+                ptmp[i] = pay[i];
+        }
+    }
+    free(hist);
+}
+
+static int bits_for(uint32_t V)
+{
+    int b = 1;
+    while (b < 32 && (1ull << b) < V)
+        b++;
+    return b;
+}
+
+/* One direction: CSR keyed by `key` (lists sorted by `other`). */
+static int build_direction(uint32_t V, uint32_t E, const uint32_t *key, const uint32_t *other, const float *w,
+                           struct Vertex *vx, struct EdgeList *el)
+{
+    uint64_t *k = (uint64_t *)xmalloc((size_t)E * 8 + 64), *t = (uint64_t *)xmalloc((size_t)E * 8 + 64);
+    float *pw = NULL, *pt = NULL;
+    if (w)
+    {
+        pw = (float *)xmalloc((size_t)E * 4 + 64);
+        pt = (float *)xmalloc((size_t)E * 4 + 64);
+    }
+    if (!k || !t || (w && (!pw || !pt)))
+    {
+        free(k); free(t); free(pw); free(pt);
+        return -1;
+    }
+    /* word = key in the high b bits, other in the low b bits: the radix
+     * digits cover 2b bits, low (other) digits first, so the sort is by key
+     * and then by other */
+    const int b = bits_for(V);
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < E; i++)
+    {
+        k[i] = ((uint64_t)key[i] << b) | other[i];
+        if (w) pw[i] = w[i];
+    }
+    radix_sort64(k, t, pw, pt, E, 2 * b);
+    const uint64_t lowmask = (1ull << b) - 1;
+    /* edges_idx[v] = first position whose key is >= v (binary search) */
+#pragma omp parallel for schedule(static)
+    for (uint32_t v = 0; v < V; v++)
+    {
+        size_t lo = 0, hi = E;
+        while (lo < hi)
+        {
+            size_t mid = (lo + hi) >> 1;
+            if ((k[mid] >> b) < v) lo = mid + 1; else hi = mid;
+        }
+        vx->edges_idx[v] = (uint32_t)lo;
+    }
+#pragma omp parallel for schedule(static)
+    for (uint32_t v = 0; v < V; v++)
+        vx->out_degree[v] = (v + 1 < V ? vx->edges_idx[v + 1] : E) - vx->edges_idx[v];
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < E; i++)
+    {
+        el->edges_array_src[i] = (uint32_t)(k[i] >> b);
+        el->edges_array_dest[i] = (uint32_t)(k[i] & lowmask);
+        if (w) el->edges_array_weight[i] = pw[i];
+    }
+    free(k); free(t); free(pw); free(pt);
+    return 0;
+}
+
+static struct Vertex *new_vertex(uint32_t V)
+{
+    struct Vertex *v = (struct Vertex *)calloc(1, sizeof(struct Vertex));
+    if (!v) return NULL;
+    v->out_degree = (uint32_t *)xmalloc((size_t)V * 4 + 64);
+    v->in_degree = (uint32_t *)xmalloc((size_t)V * 4 + 64);
+    v->edges_idx = (uint32_t *)xmalloc((size_t)V * 4 + 64);
+    return v;
+}
+
+static void free_vertex(struct Vertex *v)
+{
+    if (!v) return;
+    gg_host_unpin(v->out_degree);
+    gg_host_unpin(v->in_degree);
+    gg_host_unpin(v->edges_idx);
+    free(v->out_degree);
+    free(v->in_degree);
+    free(v->edges_idx);
+    free(v);
+}
+
+static void free_edges(struct EdgeList *e)
+{
+    if (!e) return;
+    gg_host_unpin(e->edges_array_src);
+    gg_host_unpin(e->edges_array_dest);
+    gg_host_unpin(e->edges_array_weight);
+    freeEdgeList(e);
+}
+
+struct GraphCSR *graphCSRFromEdgeList(const struct EdgeList *in)
+{
+    if (!in)
+        return NULL;
+    const uint32_t V = in->num_vertices, E = in->num_edges;
+    struct GraphCSR *g = (struct GraphCSR *)calloc(1, sizeof(struct GraphCSR));
+    if (!g)
+        return NULL;
+    g->num_vertices = V;
+    g->num_edges = E;
+    g->max_weight = in->max_weight;
+    g->avg_degree = V ? E / V : 0;
+    g->vertices = new_vertex(V);
+    g->inverse_vertices = new_vertex(V);
+    const int weighted = in->edges_array_weight != NULL;
+    g->sorted_edges_array = newEdgeList(E, V, weighted);
+    g->inverse_sorted_edges_array = newEdgeList(E, V, weighted);
+    if (!g->vertices || !g->inverse_vertices || !g->sorted_edges_array || !g->inverse_sorted_edges_array)
+    {
+        graphCSRFree(g);
+        return NULL;
+    }
+    if (build_direction(V, E, in->edges_array_src, in->edges_array_dest, in->edges_array_weight, g->vertices,
+                        g->sorted_edges_array) != 0 ||
+        build_direction(V, E, in->edges_array_dest, in->edges_array_src, in->edges_array_weight,
+                        g->inverse_vertices, g->inverse_sorted_edges_array) != 0)
+    {
+        graphCSRFree(g);
+        return NULL;
+    }
+    /* the inverse direction stores (dst, src): edges_array_src holds the
+     * destination and edges_array_dest the in-neighbour, as the reference's
+     * inverse_sorted_edges_array does */
+    memcpy(g->vertices->in_degree, g->inverse_vertices->out_degree, (size_t)V * 4);
+    memcpy(g->inverse_vertices->in_degree, g->vertices->out_degree, (size_t)V * 4);
+    for (int d = 0; d < 2; d++)
+    {
+        struct EdgeList *el = d ? g->inverse_sorted_edges_array : g->sorted_edges_array;
+        el->num_vertices = V;
+        el->max_weight = in->max_weight;
+        el->label_array = (uint32_t *)xmalloc((size_t)V * 4 + 64);
+        el->inverse_label_array = (uint32_t *)xmalloc((size_t)V * 4 + 64);
+        if (!el->label_array || !el->inverse_label_array)
+        {
+            graphCSRFree(g);
+            return NULL;
+        }
+        for (uint32_t v = 0; v < V; v++)
+            el->label_array[v] = el->inverse_label_array[v] = v;
+    }
+    /* page-lock the arrays the GPU path uploads (no-op without a device) */
+    gg_host_pin(g->vertices->out_degree, (size_t)V * 4);
+    gg_host_pin(g->vertices->edges_idx, (size_t)V * 4);
+    gg_host_pin(g->inverse_vertices->edges_idx, (size_t)V * 4);
+    gg_host_pin(g->sorted_edges_array->edges_array_dest, (size_t)E * 4);
+    gg_host_pin(g->inverse_sorted_edges_array->edges_array_dest, (size_t)E * 4);
+    if (weighted)
+    {
+        gg_host_pin(g->sorted_edges_array->edges_array_weight, (size_t)E * 4);
+        gg_host_pin(g->inverse_sorted_edges_array->edges_array_weight, (size_t)E * 4);
+    }
+    return g;
+}
+
+void graphCSRFree(struct GraphCSR *g)
+{
+    if (!g)
+        return;
+    free_vertex(g->vertices);
+    free_vertex(g->inverse_vertices);
+    free_edges(g->sorted_edges_array);
+    free_edges(g->inverse_sorted_edges_array);
+    free(g);
+}

@@ -1,0 +1,360 @@
+/*
+ * SpMV on CSR (02_capi_graph/src/algorithms/capi/SPMV.c:594-1135) on one GPU.
+ *
+ *   pull  (mode 0): y[v] = sum over in-edges (u,v) of w(u,v)*x[u]; the
+ *                   merge-path tile gather over the CSC, recomputed every
+ *                   iteration like the FPGA CU run per iteration (:712-718)
+ *   push  (mode 1): y[dst] += w*x[src] over out-edges with FP32 atomics,
+ *                   accumulating across iterations (:795-820)
+ *   pull fixed (2): Q16.16 operands, (x*w) >> 16 summed in 64 bits
+ *                   (cu_SPMV/CSR/PULL/FixedPoint/cu/cu_sum_kernel_control.sv:155-184)
+ *   push fixed (3): Q32.32, y64 += (w*x) >> 32 (:1080-1093)
+ * x and the weights may be stored as BF16/FP16 (FP32 products and sums).
+ */
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <cstring>
+#include <vector>
+
+#include "gg_device.cuh"
+
+namespace {
+
+using namespace gg;
+
+template <class T> struct Vec4;
+template <> struct Vec4<float>
+{
+    static __device__ __forceinline__ void load(const float *p, float o[4])
+    {
+        float4 v = *reinterpret_cast<const float4 *>(p);
+        o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+    }
+};
+template <> struct Vec4<__nv_bfloat16>
+{
+    static __device__ __forceinline__ void load(const __nv_bfloat16 *p, float o[4])
+    {
+        uint2 v = *reinterpret_cast<const uint2 *>(p);
+        __nv_bfloat162 a = *reinterpret_cast<__nv_bfloat162 *>(&v.x), b = *reinterpret_cast<__nv_bfloat162 *>(&v.y);
+        float2 fa = __bfloat1622float2(a), fb = __bfloat1622float2(b);
+        o[0] = fa.x; o[1] = fa.y; o[2] = fb.x; o[3] = fb.y;
+    }
+};
+template <> struct Vec4<__half>
+{
+    static __device__ __forceinline__ void load(const __half *p, float o[4])
+    {
+        uint2 v = *reinterpret_cast<const uint2 *>(p);
+        __half2 a = *reinterpret_cast<__half2 *>(&v.x), b = *reinterpret_cast<__half2 *>(&v.y);
+        float2 fa = __half22float2(a), fb = __half22float2(b);
+        o[0] = fa.x; o[1] = fa.y; o[2] = fb.x; o[3] = fb.y;
+    }
+};
+
+template <class T>
+struct SpmvPullOp
+{
+    typedef float Acc;
+    const T *w;
+    const T *x;
+    float *y;
+    __device__ __forceinline__ bool skip() const { return false; }
+    __device__ __forceinline__ void load4(uint32_t e4, uint4 q, float v[4]) const
+    {
+        float wv[4];
+        Vec4<T>::load(w + e4, wv);
+        v[0] = __fmul_rn(wv[0], to_f32(x[q.x]));
+        v[1] = __fmul_rn(wv[1], to_f32(x[q.y]));
+        v[2] = __fmul_rn(wv[2], to_f32(x[q.z]));
+        v[3] = __fmul_rn(wv[3], to_f32(x[q.w]));
+    }
+    __device__ __forceinline__ void finish(uint32_t r, float sum, double &, uint32_t &) { y[r] = sum; }
+    __device__ __forceinline__ void block_end() {}
+    __device__ __forceinline__ void reduce(double, uint32_t) const {}
+};
+
+template <class T>
+__global__ void __launch_bounds__(GG_TILE_NT) k_spmv_pull(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                                          const uint2 *__restrict__ coord, uint32_t V, float *g_acc,
+                                                          uint32_t *g_cnt, SpmvPullOp<T> op)
+{
+    tile_pull<GG_TILE_NT, GG_TILE_IPT>(off, adj, V, coord, g_acc, g_cnt, op, blockIdx.x);
+}
+
+struct SpmvPullFxOp
+{
+    typedef unsigned long long Acc;
+    const float *w;
+    const uint32_t *x32;
+    float *y;
+    __device__ __forceinline__ bool skip() const { return false; }
+    __device__ __forceinline__ void load4(uint32_t e4, uint4 q, unsigned long long v[4]) const
+    {
+        float4 wv = *reinterpret_cast<const float4 *>(w + e4);
+        v[0] = ((unsigned long long)x32[q.x] * fx_from_float(wv.x, 65536.0, 0xffffffffu)) >> 16;
+        v[1] = ((unsigned long long)x32[q.y] * fx_from_float(wv.y, 65536.0, 0xffffffffu)) >> 16;
+        v[2] = ((unsigned long long)x32[q.z] * fx_from_float(wv.z, 65536.0, 0xffffffffu)) >> 16;
+        v[3] = ((unsigned long long)x32[q.w] * fx_from_float(wv.w, 65536.0, 0xffffffffu)) >> 16;
+    }
+    __device__ __forceinline__ void finish(uint32_t r, unsigned long long sum, double &, uint32_t &)
+    {
+        y[r] = fx_to_float(sum, 1.0 / 65536.0);
+    }
+    __device__ __forceinline__ void block_end() {}
+    __device__ __forceinline__ void reduce(double, uint32_t) const {}
+};
+
+__global__ void __launch_bounds__(GG_TILE_NT) k_spmv_pull_fx(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                                             const uint2 *__restrict__ coord, uint32_t V,
+                                                             unsigned long long *g_acc, uint32_t *g_cnt, SpmvPullFxOp op)
+{
+    tile_pull<GG_TILE_NT, GG_TILE_IPT>(off, adj, V, coord, g_acc, g_cnt, op, blockIdx.x);
+}
+
+template <class T>
+__global__ void __launch_bounds__(GG_TILE_NT) k_spmv_push(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                                          const uint2 *__restrict__ coord, uint32_t V, const T *w,
+                                                          const T *x, float *y)
+{
+    struct Op
+    {
+        typedef float RowVal;
+        const T *w;
+        const T *x;
+        float *y;
+        __device__ __forceinline__ float row_value(uint32_t r) const { return to_f32(x[r]); }
+        __device__ __forceinline__ void scatter(float xv, uint32_t e, uint32_t dst) const
+        {
+            atomicAdd(&y[dst], __fmul_rn(to_f32(w[e]), xv));
+        }
+    } op{w, x, y};
+    tile_push<GG_TILE_NT, GG_TILE_IPT>(off, adj, V, coord, op, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(GG_TILE_NT) k_spmv_push_fx(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                                             const uint2 *__restrict__ coord, uint32_t V, const float *w,
+                                                             const unsigned long long *x64, unsigned long long *y64)
+{
+    struct Op
+    {
+        typedef unsigned long long RowVal;
+        const float *w;
+        const unsigned long long *x64;
+        unsigned long long *y64;
+        __device__ __forceinline__ unsigned long long row_value(uint32_t r) const { return x64[r]; }
+        __device__ __forceinline__ void scatter(unsigned long long xv, uint32_t e, uint32_t dst) const
+        {
+            atomicAdd(&y64[dst], fx64_mul(fx64_from_double((double)w[e]), xv));
+        }
+    } op{w, x64, y64};
+    tile_push<GG_TILE_NT, GG_TILE_IPT>(off, adj, V, coord, op, blockIdx.x);
+}
+
+/* x[v] = 1/outdeg(v), or 0.001 when 0 (SPMV.c:696-701), unless given; the
+ * stored copy in the chosen storage and the fixed-point copies */
+template <class T>
+__global__ void k_spmv_x(const uint32_t *__restrict__ outdeg, const float *xin, float *xf, T *xs, uint32_t *x32,
+                         unsigned long long *x64, float *y, uint32_t V)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    {
+        float xv;
+        if (xin)
+            xv = xin[v];
+        else
+        {
+            uint32_t d = outdeg[v];
+            xv = d ? __fdiv_rn(1.0f, __uint2float_rn(d)) : 0.001f;
+        }
+        xf[v] = xv;
+        if (xs) xs[v] = from_f32<T>(xv);
+        if (x32) x32[v] = fx_from_float(xv, 65536.0, 0xffffffffu);
+        if (x64) x64[v] = fx64_from_double((double)xv);
+        y[v] = 0.0f;
+    }
+}
+
+__global__ void k_spmv_fx64_out(const unsigned long long *y64, float *y, uint32_t V)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+        y[v] = __double2float_rn(fx64_to_double(y64[v]));
+}
+
+/* sum of round2(y) as the reference prints it (SPMV.c:727-730) */
+__global__ void k_spmv_checksum(const float *y, uint32_t V, double *out)
+{
+    double s = 0.0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    {
+        double t = __dadd_rn((double)__fmul_rn(y[v], 100.0f), 0.5);
+        s += (double)(int)t / 100.0;
+    }
+    uint32_t dummy = 0;
+    block_sum2<256>(s, dummy);
+    if (threadIdx.x == 0 && s != 0.0) atomicAdd(out, s);
+}
+
+int grid_v(uint32_t V) { int b = (int)((V + 255) / 256); int cap = gg_sm_count() * 8; return b < 1 ? 1 : (b > cap ? cap : b); }
+
+template <class T>
+gg_status spmv_fp(gg_graph *g, const gg_spmv_params *p, const float *x_dev, float *xf, float *y, cudaStream_t s,
+                  uint32_t &launches, uint32_t &timed, std::vector<cudaEvent_t> &evs)
+{
+    const uint32_t V = g->V;
+    const bool pull = p->mode == GG_SPMV_PULL;
+    gg_tiles *t;
+    GG_CHECK(gg_tiles_get(g, pull ? 1 : 0, s, &t));
+    void *xs = nullptr;
+    const T *w;
+    if constexpr (sizeof(T) == 4)
+    {
+        w = (const T *)(pull ? g->in_w : g->out_w);
+    }
+    else
+    {
+        const void *w16;
+        GG_CHECK(gg_weights16(g, pull ? 1 : 0, p->storage, s, &w16));
+        w = (const T *)w16;
+        GG_CHECK(gg_work(g, 12, ((size_t)V + 16) * sizeof(T), &xs));
+    }
+    k_spmv_x<T><<<grid_v(V), 256, 0, s>>>(g->out_deg, x_dev, xf, (T *)xs, nullptr, nullptr, y, V);
+    launches++;
+    const T *xv = sizeof(T) == 4 ? (const T *)xf : (const T *)xs;
+    for (uint32_t it = 0; it < p->iterations; it++)
+    {
+        if (p->profile)
+        {
+            cudaEvent_t e;
+            GG_CHECK(gg_event_at(g, (uint32_t)evs.size(), &e));
+            GG_CUDA(cudaEventRecord(e, s));
+            evs.push_back(e);
+        }
+        if (pull)
+        {
+            SpmvPullOp<T> op{w, xv, y};
+            k_spmv_pull<T><<<t->ntiles, GG_TILE_NT, 0, s>>>(g->in_off, g->in_adj, t->coord, V, (float *)t->acc, t->cnt, op);
+        }
+        else
+            k_spmv_push<T><<<t->ntiles, GG_TILE_NT, 0, s>>>(g->out_off, g->out_adj, t->coord, V, w, xv, y);
+        if (p->profile)
+        {
+            cudaEvent_t e;
+            GG_CHECK(gg_event_at(g, (uint32_t)evs.size(), &e));
+            GG_CUDA(cudaEventRecord(e, s));
+            evs.push_back(e);
+        }
+        launches++;
+        timed++;
+    }
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+}
+
+} // namespace
+
+extern "C" gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *x, float *x_out, float *y,
+                             gg_spmv_result *r, void *stream)
+{
+    if (!g || !p) return gg_fail(GG_ERR_INVALID, "NULL argument");
+    if (p->mode > 3) return gg_fail(GG_ERR_INVALID, "unknown SpMV mode");
+    if (p->storage > 2) return gg_fail(GG_ERR_INVALID, "unknown storage");
+    const bool pull = p->mode == GG_SPMV_PULL || p->mode == GG_SPMV_PULL_FX;
+    if (pull && (!g->in_off || !g->in_w)) return gg_fail(GG_ERR_INVALID, "pull SpMV needs GG_MAP_IN|GG_MAP_IN_W");
+    if (!pull && (!g->out_off || !g->out_w)) return gg_fail(GG_ERR_INVALID, "push SpMV needs GG_MAP_OUT|GG_MAP_OUT_W");
+    if (!g->out_deg) return gg_fail(GG_ERR_INVALID, "mapping has no out-degrees");
+    cudaStream_t s = gg_stream(g, stream);
+    const uint32_t V = g->V;
+    gg_spmv_result res;
+    memset(&res, 0, sizeof(res));
+    void *xf, *yv, *xin = nullptr, *chk;
+    GG_CHECK(gg_work(g, 0, ((size_t)V + 16) * 4, &xf));
+    GG_CHECK(gg_work(g, 11, ((size_t)V + 16) * 4, &yv));
+    GG_CHECK(gg_work(g, 10, 64, &chk));
+    GG_CUDA(cudaMemsetAsync(chk, 0, 64, s));
+    if (x)
+    {
+        GG_CHECK(gg_work(g, 13, ((size_t)V + 16) * 4, &xin));
+        GG_CUDA(cudaMemcpyAsync(xin, x, (size_t)V * 4, cudaMemcpyHostToDevice, s));
+    }
+    std::vector<cudaEvent_t> evs;
+    uint32_t launches = 0, timed = 0;
+    if (V > 0)
+    {
+        if (p->mode == GG_SPMV_PULL || p->mode == GG_SPMV_PUSH)
+        {
+            gg_status st = p->storage == GG_STORE_BF16
+                               ? spmv_fp<__nv_bfloat16>(g, p, (const float *)xin, (float *)xf, (float *)yv, s, launches, timed, evs)
+                           : p->storage == GG_STORE_F16
+                               ? spmv_fp<__half>(g, p, (const float *)xin, (float *)xf, (float *)yv, s, launches, timed, evs)
+                               : spmv_fp<float>(g, p, (const float *)xin, (float *)xf, (float *)yv, s, launches, timed, evs);
+            if (st != GG_OK) return st;
+        }
+        else
+        {
+            gg_tiles *t;
+            GG_CHECK(gg_tiles_get(g, pull ? 1 : 0, s, &t));
+            void *xq, *y64 = nullptr;
+            GG_CHECK(gg_work(g, 12, ((size_t)V + 16) * 8, &xq));
+            if (!pull)
+            {
+                GG_CHECK(gg_work(g, 14, ((size_t)V + 16) * 8, &y64));
+                GG_CUDA(cudaMemsetAsync(y64, 0, ((size_t)V + 16) * 8, s));
+            }
+            k_spmv_x<float><<<grid_v(V), 256, 0, s>>>(g->out_deg, (const float *)xin, (float *)xf, nullptr,
+                                                      pull ? (uint32_t *)xq : nullptr,
+                                                      pull ? nullptr : (unsigned long long *)xq, (float *)yv, V);
+            launches++;
+            for (uint32_t it = 0; it < p->iterations; it++)
+            {
+                if (p->profile)
+                {
+                    cudaEvent_t e;
+                    GG_CHECK(gg_event_at(g, (uint32_t)evs.size(), &e));
+                    GG_CUDA(cudaEventRecord(e, s));
+                    evs.push_back(e);
+                }
+                if (pull)
+                {
+                    SpmvPullFxOp op{g->in_w, (const uint32_t *)xq, (float *)yv};
+                    k_spmv_pull_fx<<<t->ntiles, GG_TILE_NT, 0, s>>>(g->in_off, g->in_adj, t->coord, V,
+                                                                    (unsigned long long *)t->acc, t->cnt, op);
+                }
+                else
+                    k_spmv_push_fx<<<t->ntiles, GG_TILE_NT, 0, s>>>(g->out_off, g->out_adj, t->coord, V, g->out_w,
+                                                                    (const unsigned long long *)xq, (unsigned long long *)y64);
+                if (p->profile)
+                {
+                    cudaEvent_t e;
+                    GG_CHECK(gg_event_at(g, (uint32_t)evs.size(), &e));
+                    GG_CUDA(cudaEventRecord(e, s));
+                    evs.push_back(e);
+                }
+                launches++;
+                timed++;
+            }
+            if (!pull)
+            {
+                k_spmv_fx64_out<<<grid_v(V), 256, 0, s>>>((const unsigned long long *)y64, (float *)yv, V);
+                launches++;
+            }
+        }
+        k_spmv_checksum<<<grid_v(V), 256, 0, s>>>((const float *)yv, V, (double *)chk);
+        launches++;
+        GG_CUDA(cudaGetLastError());
+    }
+    double checksum = 0.0;
+    GG_CUDA(cudaMemcpyAsync(&checksum, chk, 8, cudaMemcpyDeviceToHost, s));
+    if (y && V) GG_CUDA(cudaMemcpyAsync(y, yv, (size_t)V * 4, cudaMemcpyDeviceToHost, s));
+    if (x_out && V) GG_CUDA(cudaMemcpyAsync(x_out, xf, (size_t)V * 4, cudaMemcpyDeviceToHost, s));
+    GG_CHECK(gg_wait(s));
+    res.checksum = checksum;
+    res.launches = launches;
+    res.spmv_launches = timed;
+    if (p->profile)
+        for (size_t i = 0; i + 1 < evs.size(); i += 2) res.spmv_ms += gg_event_ms(evs[i], evs[i + 1]);
+    if (r) *r = res;
+    return GG_OK;
+}

@@ -1,0 +1,99 @@
+"""Generate the golden vectors under tests/golden/ from the reference itself.
+
+Run in a tree where the reference snapshot is mounted (default
+/root/reference, or $ACCELGRAPH_REFERENCE):
+
+    python tests/golden/make_golden.py
+
+It writes
+  fixtures.npz  the reference's fixture graphs (04_test_graphs/TEST/*), as
+                uint32 edge arrays (weights from the .wbin files), and
+  golden_*.npz  outputs of the reference's own pageRank.c / BFS.c / SPMV.c,
+                compiled from the reference sources by oracle/build_ref.sh
+                (FPGA-offloaded loops replaced by the compute-unit emulation
+                in oracle/ref_shim/ref_capi_emu.c), on those fixtures and on
+                small seeded R-MAT graphs, run with one OpenMP thread.
+The GPU machine has no reference tree; the tests read these files there.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle_ctypes as O  # noqa: E402
+
+REF = os.environ.get("ACCELGRAPH_REFERENCE", "/root/reference")
+TEST = os.path.join(REF, "04_test_graphs", "TEST")
+
+FIXTURES = {
+    "graphbrew": ("graphbrew/graph.bin", False),
+    "test": ("test/graph.wbin", True),
+    "v51_e1021": ("v51_e1021/graph.wbin", True),
+    "v300_e2730": ("v300_e2730/graph.wbin", True),
+}
+RMAT = {"rmat8": (8, 8), "rmat10": (10, 16), "rmat12u": (12, 8)}
+PR_ITERS, PR_EPS = 20, 1e-4
+SPMV_ITERS = 3
+
+
+def load(rel, weighted):
+    a = np.fromfile(os.path.join(TEST, rel), dtype=np.uint32)
+    k = 3 if weighted else 2
+    a = a.reshape(-1, k)
+    w = a[:, 2].astype(np.float32) if weighted else None
+    return a[:, 0].copy(), a[:, 1].copy(), w
+
+
+def sources(V):
+    return sorted({0, 1, V // 2, V - 1})
+
+
+def main():
+    if O.ref_lib() is None:
+        sys.exit("the reference could not be built (is the reference tree mounted?)")
+    fx = {}
+    graphs = {}
+    for name, (rel, weighted) in FIXTURES.items():
+        s, d, w = load(rel, weighted)
+        fx[name + "_src"], fx[name + "_dst"] = s, d
+        if w is not None:
+            fx[name + "_w"] = w
+        V = int(max(s.max(), d.max())) + 1
+        graphs[name] = O.Csr(V, s, d, w)
+    np.savez_compressed(os.path.join(HERE, "fixtures.npz"), **fx)
+    for name, (scale, ef) in RMAT.items():
+        graphs[name] = O.rmat_csr(scale, ef, weighted=True, symmetric=name.endswith("u"))
+
+    for name, g in graphs.items():
+        out = {"V": np.uint32(g.V), "E": np.uint32(g.E)}
+        for mode in range(14):
+            r, info = O.ref_pagerank(g, mode, PR_ITERS, PR_EPS)
+            out[f"pr{mode}_ranks"] = r
+            out[f"pr{mode}_iters"] = np.uint32(info["iterations"])
+            out[f"pr{mode}_err"] = np.float64(info["error_total"])
+        srcs = sources(g.V)
+        out["bfs_sources"] = np.array(srcs, np.int32)
+        for mode in range(5):
+            for s in srcs:
+                p, d, info = O.ref_bfs(g, mode, s)
+                out[f"bfs{mode}_{s}_parents"] = p
+                out[f"bfs{mode}_{s}_dist"] = d
+                out[f"bfs{mode}_{s}_processed"] = np.uint32(info["processed_nodes"])
+                out[f"bfs{mode}_{s}_iteration"] = np.uint32(info["iteration"])
+        # the reference is built WEIGHTED 0 (graphConfig.h:7): its SpMV uses
+        # the constant weight 0.0001f, so its golden runs on the unweighted view
+        gu = O.Csr.from_arrays(g.V, g.E, g.out_off, g.out_adj, g.in_off, g.in_adj)
+        for mode in range(4):
+            x, y = O.ref_spmv(gu, mode, SPMV_ITERS)
+            out[f"spmv{mode}_x"] = x
+            out[f"spmv{mode}_y"] = y
+        np.savez_compressed(os.path.join(HERE, f"golden_{name}.npz"), **out)
+        print("wrote", name, g.V, g.E)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,164 @@
+"""Host-side pieces of the product on CPU: the C-ABI library loads and
+exports every function include/*.h declares; the graph builder, R-MAT
+generator and edge-list loaders agree with the oracle's independent ones;
+host utilities behave like the reference's OpenGraph helpers.  No GPU
+compute is called."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from graphs import fixture_edges
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_functions():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b([A-Za-z_]\w*)\s*\(([^;{]*)\)\s*;", text, flags=re.M):
+            if m.group(0).lstrip().startswith(("typedef", "#", "return")):
+                continue
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_function(gg):
+    names = _declared_functions()
+    assert len(names) > 80
+    L = gg.lib()
+    missing = [n for n in sorted(names) if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_struct_sizes_match_c_layout(gg, tmp_path):
+    """The ctypes mirror has the C compiler's layout of every drop-in struct."""
+    structs = {"Arguments": gg.Arguments, "GraphCSR": gg.GraphCSR, "EdgeList": gg.EdgeList,
+               "Vertex": gg.Vertex, "PageRankStats": gg.PageRankStats, "BFSStats": gg.BFSStats,
+               "SPMVStats": gg.SPMVStats, "Bitmap": gg.Bitmap, "ArrayQueue": gg.ArrayQueue}
+    typedefs = {"gg_pr_params": gg.PrParams, "gg_pr_result": gg.PrResult, "gg_bfs_params": gg.BfsParams,
+                "gg_bfs_result": gg.BfsResult, "gg_spmv_params": gg.SpmvParams, "gg_spmv_result": gg.SpmvResult,
+                "GraphGpuOptions": gg.GraphGpuOptions}
+    src = ['#include <stdio.h>', '#include "pageRank.h"', '#include "BFS.h"', '#include "SPMV.h"',
+           '#include "gg_runtime.h"', "int main(void){"]
+    for n in structs:
+        src.append(f'printf("{n} %zu\\n", sizeof(struct {n}));')
+    for n in typedefs:
+        src.append(f'printf("{n} %zu\\n", sizeof({n}));')
+    src.append("return 0;}")
+    (tmp_path / "sz.c").write_text("\n".join(src))
+    import subprocess
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(tmp_path / "sz.c"), "-o",
+                           str(tmp_path / "sz")])
+    out = subprocess.check_output([str(tmp_path / "sz")]).decode().split("\n")
+    sizes = dict(line.split() for line in out if line)
+    for n, t in {**structs, **typedefs}.items():
+        assert int(sizes[n]) == C.sizeof(t), n
+    a = gg.default_arguments()
+    assert a.iterations == 20 and abs(a.epsilon - 1e-4) < 1e-15 and a.binSize == 512
+    assert a.mt19937var.mt[0] == 27491095 and a.cu_config == 1
+
+
+def test_mt19937_known_answer(gg):
+    # first outputs of MT19937 seeded with 5489 (the generator's published test value)
+    st = gg.Mt19937State()
+    gg.lib().initializeMersenneState(C.byref(st), 5489)
+    gg.lib().generateRandInt.restype = C.c_uint32
+    outs = [gg.lib().generateRandInt(C.byref(st)) for _ in range(3)]
+    assert outs == [3499211612, 581869302, 3890346734]
+
+
+@pytest.mark.parametrize("scale,ef,weighted,sym", [(6, 4, False, False), (10, 16, True, False), (12, 8, True, True)])
+def test_builder_matches_oracle(gg, orc, scale, ef, weighted, sym):
+    g = gg.Graph.rmat(scale, ef, weighted=weighted, symmetric=sym)
+    a = g.arrays()
+    src, dst, w = orc.rmat_edges(scale, ef, weighted=weighted, symmetric=sym)
+    o = orc.Csr(1 << scale, src, dst, w)
+    for k in ["out_off", "out_adj", "in_off", "in_adj"]:
+        np.testing.assert_array_equal(a[k], getattr(o, k), err_msg=k)
+    np.testing.assert_array_equal(a["out_degree"], np.diff(o.out_off))
+    np.testing.assert_array_equal(a["in_degree"], np.diff(o.in_off))
+    if weighted:
+        np.testing.assert_array_equal(a["out_w"], o.out_w)
+        np.testing.assert_array_equal(a["in_w"], o.in_w)
+    assert g.E == len(src) and g.V == 1 << scale
+
+
+def test_rmat_statistics(orc):
+    """Quadrant frequencies follow (a, b, c, d) = (0.57, 0.19, 0.19, 0.05) at the top level."""
+    src, dst, _ = orc.rmat_edges(14, 16)
+    top_s, top_d = src >> 13, dst >> 13
+    q = np.bincount(top_s * 2 + top_d, minlength=4) / len(src)
+    np.testing.assert_allclose(q, [0.57, 0.19, 0.19, 0.05], atol=0.005)
+
+
+def test_builder_on_reference_fixtures(gg, orc):
+    for name, (s, d, w) in fixture_edges().items():
+        g = gg.Graph.from_edges(s, d, w)
+        a = g.arrays()
+        o = orc.Csr(g.V, s, d, w)
+        np.testing.assert_array_equal(a["in_adj"][:g.E], o.in_adj[:g.E])
+        np.testing.assert_array_equal(a["out_off"], o.out_off)
+
+
+def test_loaders_read_reference_formats(gg, tmp_path):
+    src = np.array([1, 2, 3, 0], np.uint32)
+    dst = np.array([2, 3, 0, 1], np.uint32)
+    np.stack([src, dst], 1).astype(np.uint32).tofile(tmp_path / "g.bin")
+    np.stack([src, dst, np.array([5, 6, 7, 8])], 1).astype(np.uint32).tofile(tmp_path / "g.wbin")
+    (tmp_path / "g.txt").write_text("1 2\n2 3\n3 0\n0 1\n")
+    for f, w in [("g.bin", False), ("g.wbin", True), ("g.txt", False)]:
+        g = gg.Graph.from_file(str(tmp_path / f), weighted=w)
+        a = g.arrays()
+        assert g.V == 4 and g.E == 4
+        np.testing.assert_array_equal(a["out_adj"], [1, 2, 3, 0])
+        if w:
+            np.testing.assert_array_equal(a["out_w"], [8, 5, 6, 7])
+    assert not gg.lib().readEdgeListsbin(str(tmp_path / "missing.bin").encode(), 0)
+
+
+def test_empty_and_tiny_graphs(gg):
+    g = gg.Graph.from_edges(np.zeros(0, np.uint32), np.zeros(0, np.uint32), num_vertices=3)
+    a = g.arrays()
+    assert g.E == 0 and list(a["out_off"]) == [0, 0, 0, 0]
+    g = gg.Graph.from_edges([0, 0, 0], [0, 0, 1])  # self loops and duplicates kept
+    a = g.arrays()
+    assert list(a["out_adj"]) == [0, 0, 1] and list(a["in_off"]) == [0, 2, 3]
+
+
+def test_bitmap_and_queue_helpers(gg):
+    L = gg.lib()
+    b = L.newBitmap(100)
+    for v in (0, 31, 32, 99):
+        L.setBit(b, v)
+    assert L.getNumOfSetBits(b) == 4
+    L.freeBitmap(b)
+    q = L.newArrayQueue(10)
+    L.enArrayQueue(q, 4)
+    L.enArrayQueue(q, 7)
+    assert q.contents.tail - q.contents.head == 2
+    L.freeArrayQueue(q)
+
+
+def test_gpu_calls_fail_loudly_without_device(gg):
+    """On a machine without a GPU the runtime reports an error instead of
+    computing on the CPU."""
+    n = C.c_int(0)
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    st = gg.lib().gg_device_init(0)
+    assert st != 0
+    g = gg.Graph.rmat(6, 4)
+    assert not gg.lib().pageRankGraphCSR(C.byref(gg.default_arguments()), g.ptr)
+    assert gg.lib().graphGpuLastError() != 0

@@ -1,0 +1,105 @@
+"""The oracle, pinned: against the golden vectors made by the reference's own
+code (tests/golden), and -- where the reference tree is mounted -- against
+that code live.  Runs on CPU."""
+import os
+
+import numpy as np
+import pytest
+
+from graphs import GOLDEN, fixture_edges
+
+NAMES = ["graphbrew", "test", "v51_e1021", "v300_e2730", "rmat8", "rmat10", "rmat12u"]
+RMAT = {"rmat8": (8, 8, False), "rmat10": (10, 16, False), "rmat12u": (12, 8, True)}
+
+
+def _graph(orc, name, weighted=True):
+    if name in RMAT:
+        s, e, sym = RMAT[name]
+        src, dst, w = orc.rmat_edges(s, e, weighted=weighted, symmetric=sym)
+        return orc.Csr(1 << s, src, dst, w)
+    src, dst, w = fixture_edges()[name]
+    V = int(max(src.max(), dst.max())) + 1
+    return orc.Csr(V, src, dst, w if weighted else None)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_pagerank_matches_reference_golden(orc, name):
+    z = np.load(os.path.join(GOLDEN, f"golden_{name}.npz"))
+    g = _graph(orc, name)
+    for mode in range(14):
+        r, info = orc.pagerank(g, mode, 20, 1e-4)
+        np.testing.assert_array_equal(r.view(np.uint32), z[f"pr{mode}_ranks"].view(np.uint32),
+                                      err_msg=f"{name} mode {mode}")
+        assert info["iterations"] == int(z[f"pr{mode}_iters"])
+        assert info["error_total"] == float(z[f"pr{mode}_err"])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_bfs_matches_reference_golden(orc, name):
+    z = np.load(os.path.join(GOLDEN, f"golden_{name}.npz"))
+    g = _graph(orc, name)
+    for mode in range(5):
+        for s in z["bfs_sources"]:
+            s = int(s)
+            p, d, info = orc.bfs(g, mode, s)
+            np.testing.assert_array_equal(p, z[f"bfs{mode}_{s}_parents"])
+            np.testing.assert_array_equal(d, z[f"bfs{mode}_{s}_dist"])
+            assert info["processed_nodes"] == int(z[f"bfs{mode}_{s}_processed"])
+            assert info["iteration"] == int(z[f"bfs{mode}_{s}_iteration"])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_spmv_matches_reference_golden(orc, name):
+    z = np.load(os.path.join(GOLDEN, f"golden_{name}.npz"))
+    g = _graph(orc, name, weighted=False)
+    for mode in (0, 1, 3):
+        x, y, _ = orc.spmv(g, mode, 3)
+        np.testing.assert_array_equal(x, z[f"spmv{mode}_x"])
+        np.testing.assert_array_equal(y.view(np.uint32), z[f"spmv{mode}_y"].view(np.uint32))
+    # the reference's pull fixed-point variant returns zeros (SPMV.c:980-983)
+    assert not z["spmv2_y"].any()
+
+
+def test_oracle_vs_reference_live(orc):
+    """Fresh random graphs through the reference's compiled code."""
+    if orc.ref_lib() is None:
+        pytest.skip("reference tree not mounted here")
+    rng = np.random.default_rng(11)
+    for trial in range(4):
+        V = int(rng.integers(20, 400))
+        E = int(rng.integers(0, 6 * V))
+        src = rng.integers(0, V, E).astype(np.uint32)
+        dst = rng.integers(0, V, E).astype(np.uint32)
+        g = orc.Csr(V, src, dst)
+        for mode in range(14):
+            a, ia = orc.pagerank(g, mode, 15, 1e-4)
+            b, ib = orc.ref_pagerank(g, mode, 15, 1e-4)
+            np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+            assert ia["iterations"] == ib["iterations"]
+        for mode in range(5):
+            s = int(rng.integers(0, V))
+            p, d, i1 = orc.bfs(g, mode, s)
+            rp, rd, i2 = orc.ref_bfs(g, mode, s)
+            np.testing.assert_array_equal(d, rd)
+            np.testing.assert_array_equal(p, rp)
+            assert i1["processed_nodes"] == i2["processed_nodes"] and i1["iteration"] == i2["iteration"]
+
+
+def test_oracle_fp64_close_to_fp32(orc):
+    g = orc.rmat_csr(12, 16)
+    r32, info = orc.pagerank(g, 0, 30, 0.0)
+    r64 = orc.pagerank_f64(g, info["executed"])
+    assert np.abs(r32 - r64).sum() / np.abs(r64).sum() < 1e-5
+    assert info["executed"] == 30
+
+
+def test_oracle_planted_error_is_caught(orc):
+    """A corrupted oracle input must change the compared output (the checks
+    above are not vacuous)."""
+    g = orc.rmat_csr(10, 16)
+    r, _ = orc.pagerank(g, 2, 10, 1e-4)
+    bad_adj = g.in_adj.copy()
+    bad_adj[0] = (bad_adj[0] + 1) % g.V
+    gb = orc.Csr.from_arrays(g.V, g.E, g.out_off, g.out_adj, g.in_off, bad_adj)
+    rb, _ = orc.pagerank(gb, 2, 10, 1e-4)
+    assert not np.array_equal(r, rb)

@@ -1,0 +1,145 @@
+"""PageRank on the GPU vs the oracle and the reference's golden vectors.
+
+Tolerances (stated here, used below):
+  * integer-summed modes (fixed point 2, 3, 9, 10, 11; quantised 4, 12, 13):
+    ranks bit-exact, iteration counts exact -- their sums are order-free;
+  * FP32 modes (0 pull, 1 push, 5 push-quant, 6 data-driven pull): the GPU
+    sums in a different order than the sequential reference, so ranks agree
+    to |d| <= 4e-6 * max|rank| and iteration counts agree exactly;
+  * data-driven push / pull-push (7, 8) are racy in the reference itself;
+    GPU ranks are compared to the FP64 fixed point with L1 <= 5e-2 relative;
+  * BF16 / FP16 contribution storage vs the FP64 oracle: L1 relative error
+    <= 2e-2 (BF16) and <= 3e-3 (FP16), reported as measured in the bench.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from graphs import GOLDEN, fixture_edges, pair, special_edges
+
+pytestmark = pytest.mark.gpu
+
+INT_MODES = {2, 3, 4, 9, 10, 11, 12, 13}
+FP_MODES = {0, 1, 5, 6}
+FP_TOL = 4e-6
+
+
+@pytest.fixture(scope="module")
+def graphs(gpu, orc):
+    out = {}
+    for name, (s, d, w) in fixture_edges().items():
+        out[name] = pair(gpu, orc, gpu.Graph.from_edges(s, d, w))
+    for name, (s, d, w, V) in special_edges().items():
+        out[name] = pair(gpu, orc, gpu.Graph.from_edges(s, d, w, num_vertices=V))
+    out["rmat8"] = pair(gpu, orc, gpu.Graph.rmat(8, 8, weighted=True))
+    out["rmat10"] = pair(gpu, orc, gpu.Graph.rmat(10, 16, weighted=True))
+    out["rmat12u"] = pair(gpu, orc, gpu.Graph.rmat(12, 8, weighted=True, symmetric=True))
+    out["rmat16"] = pair(gpu, orc, gpu.Graph.rmat(16, 16))
+    return out
+
+
+@pytest.fixture(scope="module")
+def dgs(gpu, graphs):
+    return {k: gpu.DeviceGraph(g, gpu.MAP_ALL) for k, (g, _) in graphs.items()}
+
+
+def _cmp(mode, ranks, res, ref, info):
+    if mode in INT_MODES:
+        assert res["iterations"] == info["iterations"]
+        np.testing.assert_array_equal(ranks.view(np.uint32), ref.view(np.uint32))
+    elif mode in FP_MODES:
+        assert res["iterations"] == info["iterations"]
+        scale = max(float(np.abs(ref).max()), 1e-30)
+        assert float(np.abs(ranks.astype(np.float64) - ref).max()) <= FP_TOL * scale
+
+
+@pytest.mark.parametrize("mode", list(range(14)))
+def test_pagerank_modes_vs_oracle(graphs, dgs, orc, mode):
+    for name, (g, o) in graphs.items():
+        ranks, res = dgs[name].pagerank(mode, iterations=20, epsilon=1e-4)
+        ref, info = orc.pagerank(o, mode, 20, 1e-4)
+        if mode in (7, 8):
+            ex = orc.pagerank_f64(o, 60)
+            l1 = np.abs(ranks - ex).sum() / max(np.abs(ex).sum(), 1e-30)
+            assert l1 <= 5e-2, (name, l1)
+            continue
+        try:
+            _cmp(mode, ranks, res, ref, info)
+        except AssertionError as e:
+            raise AssertionError(f"graph {name} mode {mode}: {e}") from None
+        if mode in INT_MODES or mode in FP_MODES:
+            assert abs(res["error_total"] - info["error_total"]) <= 1e-6 * max(info["error_total"], 1e-12) + 1e-12
+
+
+@pytest.mark.parametrize("name", ["graphbrew", "test", "v51_e1021", "v300_e2730", "rmat8", "rmat10", "rmat12u"])
+def test_pagerank_vs_reference_golden(graphs, dgs, name):
+    """Against outputs of the reference's own pageRank.c (tests/golden)."""
+    z = np.load(os.path.join(GOLDEN, f"golden_{name}.npz"))
+    g, o = graphs[name]
+    assert int(z["V"]) == g.V and int(z["E"]) == g.E
+    for mode in range(14):
+        if mode in (7, 8):
+            continue
+        ranks, res = dgs[name].pagerank(mode, iterations=20, epsilon=1e-4)
+        ref = z[f"pr{mode}_ranks"]
+        info = {"iterations": int(z[f"pr{mode}_iters"]), "error_total": float(z[f"pr{mode}_err"])}
+        try:
+            _cmp(mode, ranks, res, ref, info)
+        except AssertionError as e:
+            raise AssertionError(f"graph {name} mode {mode}: {e}") from None
+
+
+@pytest.mark.parametrize("storage,tol", [("bf16", 2e-2), ("f16", 3e-3)])
+@pytest.mark.parametrize("mode", ["pull", "push"])
+def test_pagerank_low_precision_storage(graphs, dgs, orc, storage, tol, mode):
+    for name in ["rmat10", "rmat16", "hubs"]:
+        g, o = graphs[name]
+        ranks, res = dgs[name].pagerank(mode, storage=storage, iterations=30, epsilon=0.0)
+        ex = orc.pagerank_f64(o, 30)
+        l1 = np.abs(ranks - ex).sum() / np.abs(ex).sum()
+        assert l1 <= tol, (name, storage, l1)
+        assert res["iterations"] == 30
+
+
+def test_pagerank_one_over_n_formulation(graphs, dgs, orc):
+    g, o = graphs["rmat16"]
+    ranks, res = dgs["rmat16"].pagerank("pull", iterations=20, epsilon=0.0, init_one_over_n=True)
+    ex = orc.pagerank_f64(o, 20, init_one_over_n=True)
+    assert np.abs(ranks - ex).sum() <= 1e-5 * np.abs(ex).sum()
+    ref, info = orc.pagerank(o, 0, 20, 0.0, init_one_over_n=True)
+    assert float(np.abs(ranks - ref).max()) <= FP_TOL * float(ref.max())
+
+
+def test_pagerank_fp32_vs_fp64(graphs, dgs, orc):
+    """Plain FP32 pull stays within FP32 rounding of the FP64 oracle."""
+    for name in ["rmat16", "hubs", "star_in"]:
+        g, o = graphs[name]
+        ranks, res = dgs[name].pagerank("pull", iterations=30, epsilon=0.0)
+        ex = orc.pagerank_f64(o, 30)
+        assert np.abs(ranks - ex).sum() / np.abs(ex).sum() <= 1e-5, name
+
+
+def test_pagerank_repeat_is_stable(graphs, dgs):
+    """Integer modes are deterministic run to run; FP32 pull within tolerance."""
+    d = dgs["rmat16"]
+    a, _ = d.pagerank("pull_fx64", iterations=10)
+    b, _ = d.pagerank("pull_fx64", iterations=10)
+    np.testing.assert_array_equal(a, b)
+    a, _ = d.pagerank("pull", iterations=10)
+    b, _ = d.pagerank("pull", iterations=10)
+    assert float(np.abs(a - b).max()) <= FP_TOL * float(a.max())
+
+
+def test_pagerank_edge_cases(gpu, orc):
+    # one vertex, no edges
+    g = gpu.Graph.from_edges(np.zeros(0, np.uint32), np.zeros(0, np.uint32), num_vertices=1)
+    d = gpu.DeviceGraph(g, gpu.MAP_ALL)
+    r, res = d.pagerank("pull", iterations=5)
+    assert r.shape == (1,) and abs(r[0] - 0.15) < 1e-7 and res["iterations"] == 1
+    # zero iterations leaves the initial ranks divided by V
+    g2 = gpu.Graph.rmat(6, 4)
+    d2 = gpu.DeviceGraph(g2, gpu.MAP_ALL)
+    r2, res2 = d2.pagerank("pull", iterations=0)
+    assert res2["iterations"] == 0
+    np.testing.assert_allclose(r2, np.float32(0.15) / np.float32(64))
