@@ -338,6 +338,27 @@ class Graph:
             d["in_w"] = _np(ie.edges_array_weight, E, np.float32)
         return d
 
+    def views(self):
+        """Zero-copy numpy views of the adjacency and degree arrays (valid
+        while the graph lives): out_adj, in_adj, out_degree, in_degree,
+        out_edges_idx, in_edges_idx, out_w, in_w."""
+        g = self.ptr.contents
+        V, E = self.V, self.E
+        ov, iv = g.vertices.contents, g.inverse_vertices.contents
+        oe, ie = g.sorted_edges_array.contents, g.inverse_sorted_edges_array.contents
+
+        def view(p, n, ct):
+            return np.ctypeslib.as_array(C.cast(p, C.POINTER(ct)), shape=(max(n, 1),))[:n]
+
+        d = dict(out_adj=view(oe.edges_array_dest, E, C.c_uint32), in_adj=view(ie.edges_array_dest, E, C.c_uint32),
+                 out_degree=view(ov.out_degree, V, C.c_uint32), in_degree=view(iv.out_degree, V, C.c_uint32),
+                 out_edges_idx=view(ov.edges_idx, V, C.c_uint32), in_edges_idx=view(iv.edges_idx, V, C.c_uint32),
+                 out_w=None, in_w=None)
+        if oe.edges_array_weight:
+            d["out_w"] = view(oe.edges_array_weight, E, C.c_float)
+            d["in_w"] = view(ie.edges_array_weight, E, C.c_float)
+        return d
+
     def free(self):
         if self.ptr:
             lib().graphGpuRelease(self.ptr)

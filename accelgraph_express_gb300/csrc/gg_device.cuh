@@ -94,232 +94,341 @@ __device__ __forceinline__ unsigned long long atomic_take(unsigned long long *p)
  *
  * A CSR with V rows and E edges is the merge of two lists: the V row-end
  * offsets and the E edge slots.  Cutting that merge into tiles of
- * TILE_ITEMS items balances work whatever the degree distribution
+ * GG_TILE_ITEMS items balances work whatever the degree distribution
  * (Merrill & Garland, "Merge-based parallel sparse matrix-vector
  * multiplication", SC'16).  coord[t] = (rows ended, edges consumed) at
- * diagonal t*TILE_ITEMS.
+ * diagonal t*GG_TILE_ITEMS.  Each tile is consumed by one warp.
  *
  * A row whose items fall in more than one tile is finished by the last tile
  * to arrive: every participating tile adds its partial into acc[first tile
  * of the row] and bumps cnt[first tile]; the tile that brings the count to
  * the number of participants takes the total (resetting both) and runs the
- * row epilogue.  No tile waits for another.
+ * row epilogue.  No tile waits for another.  A row lying wholly in one tile
+ * is finished by that tile alone (the tile before it also lists it, as its
+ * partial last row, when it ends exactly at the row's first edge).
  */
 
-__device__ __forceinline__ uint2 merge_path_search(uint64_t diag, const uint32_t *row_end, uint32_t nrows,
+__device__ __forceinline__ uint2 merge_path_search(uint32_t diag, const uint32_t *row_end, uint32_t nrows,
                                                    uint32_t nedges, uint32_t edge_base)
 {
-    /* row_end[i] is the (absolute) end offset of row i; edges are numbered
-     * from edge_base.  Returns (rows consumed, edges consumed). */
-    uint64_t lo = diag > nedges ? diag - nedges : 0;
-    uint64_t hi = diag < nrows ? diag : nrows;
+    /* row_end[i] is the (absolute) end offset of local row i; edges are
+     * numbered from edge_base.  Returns (rows consumed, edges consumed). */
+    uint32_t lo = diag > nedges ? diag - nedges : 0;
+    uint32_t hi = diag < nrows ? diag : nrows;
     while (lo < hi)
     {
-        uint64_t mid = (lo + hi) >> 1;
-        if ((uint64_t)(row_end[mid] - edge_base) + mid < diag)
+        uint32_t mid = (lo + hi) >> 1;
+        if ((row_end[mid] - edge_base) + mid < diag)
             lo = mid + 1;
         else
             hi = mid;
     }
-    return make_uint2((uint32_t)lo, (uint32_t)(diag - lo));
+    return make_uint2(lo, diag - lo);
 }
 
+/* Per-warp tile geometry shared by the pull and push engines. */
+struct TileGeom
+{
+    uint32_t i0, j0, i1, j1, nrows, nedges, nitems;
+    __device__ __forceinline__ void load(const uint2 *coord, uint32_t tile, uint32_t V)
+    {
+        const uint2 c0 = coord[tile], c1 = coord[tile + 1];
+        i0 = c0.x; j0 = c0.y; i1 = c1.x; j1 = c1.y;
+        /* rows touched: i0 .. last_row; row i1 (if < V) may have edges here
+         * but its end item lies in a later tile */
+        const uint32_t last_row = i1 < V ? i1 : V - 1;
+        nrows = (i1 < V || i0 < V) ? last_row - i0 + 1 : 0;
+        nedges = j1 - j0;
+        nitems = (i1 - i0) + nedges;
+    }
+};
+
 /*
- * The tile engine.  Op supplies:
- *   typedef Acc;                             float or unsigned long long
- *   bool skip() const;                       whole launch is a no-op
- *   void load4(uint32_t e4, uint4 idx, Acc v[4]) const;
- *                                            values of edges e4..e4+3 with
- *                                            neighbour ids idx (pull gather)
- *   void finish(uint32_t row, Acc sum, double &err, uint32_t &act);
- *                                            row epilogue
- *   void block_end();                        called by every thread after
- *                                            the epilogue (block reductions)
- *   void reduce(double err, uint32_t act);   block totals (thread 0)
+ * The pull engine (persistent warps).  Op supplies:
+ *   typedef Acc;                        float or unsigned long long
+ *   typedef RowPre;                     per-row data the epilogue needs
+ *   Acc load1(uint32_t e, uint32_t u) const;
+ *                                       value of edge e with neighbour u
+ *                                       (the gather)
+ *   RowPre prefetch(uint32_t row) const;
+ *   void finish(uint32_t row, Acc sum, const RowPre &pre, double &err, uint32_t &act);
+ *                                       row epilogue
+ *   void warp_end(double err, uint32_t act);
+ *                                       called by every lane at the end
+ *                                       (warp reductions and atomics)
+ * Per tile every load is issued up front, together: the neighbour ids (one
+ * warp instruction covering 32 consecutive edges), the tile's row offsets,
+ * the first 32 rows' epilogue data, and the next tile's coordinates; then
+ * the neighbour values.  With the value gather saturating L2 sector
+ * requests, each extra dependent round trip per tile would cost a full
+ * queueing latency.  The values are staged in shared memory and consumed
+ * along the merge path (GG_TILE_IPT items per lane).  A row ended inside a
+ * lane is stored directly; the partial sum of the row open at the end of
+ * each lane is combined across lanes by a warp-shuffle segmented scan, so no
+ * shared-memory atomics are needed.  Rows whose items span tiles add their
+ * in-tile partial to acc[first tile of the row] with a fire-and-forget
+ * reduction and are finished by warp_pull_fixup after the launch.  Only
+ * __syncwarp orders the phases.
  */
-template <int NT, int IPT, class Op>
-__device__ __forceinline__ void tile_pull(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                          uint32_t V, const uint2 *__restrict__ coord,
-                                          typename Op::Acc *g_acc, uint32_t *g_cnt, Op &op, uint32_t tile)
+template <int IPT, int WARPS, class Op>
+__device__ __forceinline__ void warp_pull(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                          uint32_t V, const uint2 *__restrict__ coord, uint32_t ntiles,
+                                          typename Op::Acc *g_acc, Op &op)
 {
     typedef typename Op::Acc Acc;
-    constexpr int TI = NT * IPT;
-    __shared__ uint32_t s_off[TI + 2];
-    __shared__ Acc s_val[TI];
-    __shared__ Acc s_row[TI + 1];
-
-    const uint2 c0 = coord[tile], c1 = coord[tile + 1];
-    const uint32_t i0 = c0.x, j0 = c0.y, i1 = c1.x, j1 = c1.y;
-    /* rows touched: i0 .. last_row; row i1 (if < V) may have edges here but
-     * its end item lies in a later tile */
-    const uint32_t last_row = i1 < V ? i1 : V - 1;
-    const uint32_t nrows = (i1 < V || i0 < V) ? last_row - i0 + 1 : 0;
-    const uint32_t nedges = j1 - j0;
-    const uint32_t nitems = (i1 - i0) + nedges;
-
-    /* s_off[k] = off[i0 + k], k = 0 .. nrows (start of each touched row and
-     * the end of the last one) */
-    for (uint32_t k = threadIdx.x; k <= nrows; k += NT)
-        s_off[k] = off[i0 + k];
-    for (uint32_t k = threadIdx.x; k < nrows + 1; k += NT)
-        s_row[k] = Acc(0);
-
-    /* gather: coalesced 16-byte index loads, independent value loads */
+    typedef typename Op::RowPre RowPre;
+    constexpr uint32_t TW = 32 * IPT;
+    __shared__ uint32_t sm_off[WARPS][TW + 2];
+    __shared__ Acc sm_val[WARPS][TW];
+    __shared__ Acc sm_row[WARPS][TW + 1];
+    const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t *s_off = sm_off[w];
+    Acc *s_val = sm_val[w];
+    Acc *s_row = sm_row[w];
+    double err = 0.0;
+    uint32_t act = 0;
+    const uint32_t nw = gridDim.x * WARPS;
+    uint32_t tile = blockIdx.x * WARPS + w;
+    uint2 c0 = make_uint2(0, 0), c1 = make_uint2(0, 0);
+    if (tile < ntiles)
     {
-        const uint32_t e_begin = j0 & ~3u;
-        for (uint32_t e4 = e_begin + 4u * threadIdx.x; e4 < j1; e4 += 4u * NT)
+        c0 = coord[tile];
+        c1 = coord[tile + 1];
+    }
+    for (; tile < ntiles; tile += nw)
+    {
+        TileGeom t;
+        t.i0 = c0.x; t.j0 = c0.y; t.i1 = c1.x; t.j1 = c1.y;
         {
-            const uint4 q = *reinterpret_cast<const uint4 *>(adj + e4);
-            Acc v[4];
-            op.load4(e4, q, v);
+            const uint32_t last_row = t.i1 < V ? t.i1 : V - 1;
+            t.nrows = (t.i1 < V || t.i0 < V) ? last_row - t.i0 + 1 : 0;
+            t.nedges = t.j1 - t.j0;
+            t.nitems = (t.i1 - t.i0) + t.nedges;
+        }
+        /* every load of this tile in flight together (nedges <= TW,
+         * nrows <= TW + 1) */
+        uint32_t id[IPT];
 #pragma unroll
-            for (int c = 0; c < 4; c++)
+        for (int g = 0; g < IPT; g++)
+        {
+            const uint32_t e = t.j0 + lane + 32u * g;
+            if (e < t.j1) id[g] = __ldg(adj + e);
+        }
+        for (uint32_t k = lane; k <= t.nrows; k += 32)
+            s_off[k] = off[t.i0 + k];
+        RowPre pre0{};
+        if (lane < t.nrows) pre0 = op.prefetch(t.i0 + lane);
+        {
+            const uint32_t nt = tile + nw;
+            if (nt < ntiles)
             {
-                uint32_t e = e4 + c;
-                if (e >= j0 && e < j1) s_val[e - j0] = v[c];
+                c0 = coord[nt];
+                c1 = coord[nt + 1];
             }
         }
-    }
-    __syncthreads();
-
-    /* merge-path consumption: IPT items per thread */
-    {
-        const uint32_t d = threadIdx.x * IPT;
-        if (d < nitems)
+#pragma unroll
+        for (int g = 0; g < IPT; g++)
         {
-            /* rows of this tile whose end item is in this tile: i0 .. i1-1,
-             * their ends are s_off[1 .. i1-i0] */
-            uint2 p = merge_path_search(d, s_off + 1, i1 - i0, nedges, j0);
+            const uint32_t e = t.j0 + lane + 32u * g;
+            if (e < t.j1) s_val[e - t.j0] = op.load1(e, id[g]);
+        }
+        __syncwarp();
+
+        /* merge-path consumption; the first row a lane ends may have begun
+         * in earlier lanes, so its sum waits for the carry scan */
+        const uint32_t nend = t.i1 - t.i0; /* local rows whose end is in this tile */
+        const uint32_t d = lane * IPT;
+        uint32_t first_row = 0xffffffffu, key = 0xffffffffu;
+        Acc first_sum = Acc(0), carry = Acc(0);
+        bool first_done = false;
+        if (d < t.nitems)
+        {
+            uint2 p = merge_path_search(d, s_off + 1, nend, t.nedges, t.j0);
             uint32_t ri = p.x, ej = p.y;
+            first_row = ri;
+            uint32_t rend = ri < nend ? s_off[ri + 1] - t.j0 : 0xffffffffu;
             Acc sum = Acc(0);
-            bool has = false;
-            const uint32_t dend = min(d + IPT, nitems);
+            const uint32_t dend = min(d + IPT, t.nitems);
             for (uint32_t k = d; k < dend; k++)
             {
-                /* end of local row ri relative to j0; the partial last row
-                 * (ri == i1 - i0) never ends inside the tile */
-                uint32_t rend = ri < i1 - i0 ? s_off[ri + 1] - j0 : 0xffffffffu;
                 if (ej < rend)
                 {
                     sum += s_val[ej];
                     ej++;
-                    has = true;
                 }
                 else
                 {
-                    if (has) atomicAdd(&s_row[ri], sum);
+                    if (!first_done)
+                    {
+                        first_sum = sum;
+                        first_done = true;
+                    }
+                    else
+                        s_row[ri] = sum;
                     sum = Acc(0);
-                    has = false;
                     ri++;
+                    rend = ri < nend ? s_off[ri + 1] - t.j0 : 0xffffffffu;
                 }
             }
-            if (has) atomicAdd(&s_row[ri], sum);
+            key = ri;
+            carry = sum;
         }
-    }
-    __syncthreads();
-
-    /* row epilogue */
-    double err = 0.0;
-    uint32_t act = 0;
-    const uint64_t tlo = (uint64_t)tile * TI, thi = tlo + TI;
-    for (uint32_t k = threadIdx.x; k < nrows; k += NT)
-    {
-        const uint32_t r = i0 + k;
-        const uint64_t first = (uint64_t)r + s_off[k];
-        const uint64_t last = (uint64_t)r + s_off[k + 1]; /* the row's end item */
-        const uint32_t t_first = (uint32_t)(first / TI), t_last = (uint32_t)(last / TI);
-        if (t_first == t_last)
-        {
-            op.finish(r, s_row[k], err, act);
-        }
-        else
-        {
-            /* the row spans tiles: take part only if this tile holds some of
-             * its items */
-            const uint64_t a = first > tlo ? first : tlo;
-            const uint64_t b = (last + 1) < thi ? (last + 1) : thi;
-            if (a < b)
-            {
-                atomic_add_acc(&g_acc[t_first], s_row[k]);
-                __threadfence();
-                uint32_t prev = atomicAdd(&g_cnt[t_first], 1u);
-                if (prev == t_last - t_first)
-                {
-                    __threadfence();
-                    Acc total = atomic_take(&g_acc[t_first]);
-                    g_cnt[t_first] = 0u;
-                    op.finish(r, total, err, act);
-                }
-            }
-        }
-    }
-    op.block_end();
-    block_sum2<NT>(err, act);
-    if (threadIdx.x == 0) op.reduce(err, act);
-}
-
-/*
- * Push counterpart: the same tiles over the out-CSR; every edge (row -> dst)
- * applies op.scatter(row, e, dst).  Per-row data is fetched once per thread
- * segment through op.row_value(row).
- */
-template <int NT, int IPT, class Op>
-__device__ __forceinline__ void tile_push(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                          uint32_t V, const uint2 *__restrict__ coord, Op &op, uint32_t tile)
-{
-    constexpr int TI = NT * IPT;
-    __shared__ uint32_t s_off[TI + 2];
-    __shared__ uint32_t s_adj[TI];
-
-    const uint2 c0 = coord[tile], c1 = coord[tile + 1];
-    const uint32_t i0 = c0.x, j0 = c0.y, i1 = c1.x, j1 = c1.y;
-    const uint32_t last_row = i1 < V ? i1 : V - 1;
-    const uint32_t nrows = (i1 < V || i0 < V) ? last_row - i0 + 1 : 0;
-    const uint32_t nedges = j1 - j0;
-    const uint32_t nitems = (i1 - i0) + nedges;
-
-    for (uint32_t k = threadIdx.x; k <= nrows; k += NT)
-        s_off[k] = off[i0 + k];
-    {
-        const uint32_t e_begin = j0 & ~3u;
-        for (uint32_t e4 = e_begin + 4u * threadIdx.x; e4 < j1; e4 += 4u * NT)
-        {
-            const uint4 q = *reinterpret_cast<const uint4 *>(adj + e4);
-            const uint32_t qa[4] = {q.x, q.y, q.z, q.w};
+        /* segmented inclusive scan of the open-row partials, keyed by row
+         * (keys are non-decreasing across lanes) */
 #pragma unroll
-            for (int c = 0; c < 4; c++)
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t k2 = __shfl_up_sync(0xffffffffu, key, o);
+            const Acc v2 = __shfl_up_sync(0xffffffffu, carry, o);
+            if (lane >= (uint32_t)o && k2 == key) carry += v2;
+        }
+        {
+            const uint32_t kp = __shfl_up_sync(0xffffffffu, key, 1);
+            const Acc vp = __shfl_up_sync(0xffffffffu, carry, 1);
+            if (first_done) s_row[first_row] = first_sum + ((lane > 0 && kp == first_row) ? vp : Acc(0));
+            /* the row left open at the end of the tile (row i1) */
+            if (t.i1 < V)
             {
-                uint32_t e = e4 + c;
-                if (e >= j0 && e < j1) s_adj[e - j0] = qa[c];
+                const uint32_t m = __ballot_sync(0xffffffffu, key == nend);
+                const Acc tot = m ? __shfl_sync(0xffffffffu, carry, 31 - __clz((int)m)) : Acc(0);
+                if (lane == 0) s_row[nend] = tot;
             }
         }
-    }
-    __syncthreads();
+        __syncwarp();
 
-    const uint32_t d = threadIdx.x * IPT;
-    if (d < nitems)
-    {
-        uint2 p = merge_path_search(d, s_off + 1, i1 - i0, nedges, j0);
-        uint32_t ri = p.x, ej = p.y;
-        const uint32_t dend = min(d + IPT, nitems);
-        bool have = false;
-        typename Op::RowVal rv{};
-        for (uint32_t k = d; k < dend; k++)
+        /* row epilogue: rows wholly inside the tile are finished here; rows
+         * spanning tiles send their partial to the fix-up pass */
+        const uint64_t tlo = (uint64_t)tile * TW, thi = tlo + TW;
+        for (uint32_t k = lane; k < t.nrows; k += 32)
         {
-            uint32_t rend = ri < i1 - i0 ? s_off[ri + 1] - j0 : 0xffffffffu;
-            if (ej < rend)
+            const uint32_t r = t.i0 + k;
+            const uint64_t first = (uint64_t)r + s_off[k];
+            const uint64_t last = (uint64_t)r + s_off[k + 1]; /* the row's end item */
+            const uint32_t t_first = (uint32_t)(first / TW), t_last = (uint32_t)(last / TW);
+            if (t_first == t_last)
             {
-                if (!have) { rv = op.row_value(i0 + ri); have = true; }
-                op.scatter(rv, j0 + ej, s_adj[ej]);
-                ej++;
+                if (t_first == tile) op.finish(r, s_row[k], k == lane ? pre0 : op.prefetch(r), err, act);
             }
             else
             {
-                ri++;
-                have = false;
+                const uint64_t a = first > tlo ? first : tlo;
+                const uint64_t b = (last + 1) < thi ? (last + 1) : thi;
+                if (a < b) atomic_add_acc(&g_acc[t_first], s_row[k]);
             }
         }
+        __syncwarp();
     }
+    op.warp_end(err, act);
+}
+
+/*
+ * After warp_pull: finish every row whose items span tiles.  Such a row
+ * starts in tile t and is left open at t's end, i.e. it is row coord[t+1].x
+ * with at least one edge before coord[t+1].y and its first item inside t.
+ * acc[t] holds the sum of all its tiles' partials (the launch boundary
+ * orders them); it is reset for the next launch.  One thread per tile.
+ */
+template <class Op>
+__device__ __forceinline__ void warp_pull_fixup(const uint32_t *__restrict__ off, uint32_t V,
+                                                const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t tw,
+                                                typename Op::Acc *g_acc, Op &op)
+{
+    typedef typename Op::Acc Acc;
+    double err = 0.0;
+    uint32_t act = 0;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x)
+    {
+        const uint2 c1 = coord[t + 1];
+        const uint32_t r = c1.x;
+        if (r >= V) continue;
+        const uint32_t o = off[r];
+        if (o < c1.y && (uint64_t)r + o >= (uint64_t)t * tw)
+        {
+            const Acc total = g_acc[t];
+            g_acc[t] = Acc(0);
+            op.finish(r, total, op.prefetch(r), err, act);
+        }
+    }
+    op.warp_end(err, act);
+}
+
+/*
+ * The push engine: the same warp tiles over the out-CSR; every edge
+ * (row -> dst) applies op.scatter(row value, edge, dst).  Per-row data is
+ * fetched once per lane segment through op.row_value(row).
+ */
+template <int IPT, int WARPS, class Op>
+__device__ __forceinline__ void warp_push(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                          uint32_t V, const uint2 *__restrict__ coord, uint32_t ntiles, Op &op)
+{
+    constexpr uint32_t TW = 32 * IPT;
+    __shared__ uint32_t sm_off[WARPS][TW + 2];
+    __shared__ uint32_t sm_adj[WARPS][TW];
+    const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t *s_off = sm_off[w];
+    uint32_t *s_adj = sm_adj[w];
+    const uint32_t nw = gridDim.x * WARPS;
+    for (uint32_t tile = blockIdx.x * WARPS + w; tile < ntiles; tile += nw)
+    {
+        TileGeom t;
+        t.load(coord, tile, V);
+#pragma unroll
+        for (int g = 0; g < IPT; g++)
+        {
+            const uint32_t e = t.j0 + lane + 32u * g;
+            if (e < t.j1) s_adj[e - t.j0] = __ldg(adj + e);
+        }
+        for (uint32_t k = lane; k <= t.nrows; k += 32)
+            s_off[k] = off[t.i0 + k];
+        __syncwarp();
+        const uint32_t d = lane * IPT;
+        if (d < t.nitems)
+        {
+            const uint32_t nend = t.i1 - t.i0;
+            uint2 p = merge_path_search(d, s_off + 1, nend, t.nedges, t.j0);
+            uint32_t ri = p.x, ej = p.y;
+            const uint32_t *ids = s_adj;
+            uint32_t rend = ri < nend ? s_off[ri + 1] - t.j0 : 0xffffffffu;
+            const uint32_t dend = min(d + IPT, t.nitems);
+            bool have = false;
+            typename Op::RowVal rv{};
+            for (uint32_t k = d; k < dend; k++)
+            {
+                if (ej < rend)
+                {
+                    if (!have) { rv = op.row_value(t.i0 + ri); have = true; }
+                    op.scatter(rv, t.j0 + ej, ids[ej]);
+                    ej++;
+                }
+                else
+                {
+                    ri++;
+                    have = false;
+                    rend = ri < nend ? s_off[ri + 1] - t.j0 : 0xffffffffu;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+/* warp sums of the per-lane residual terms, then one atomic per warp */
+__device__ __forceinline__ void warp_reduce_to(double err, uint32_t act, double *err_dst, uint32_t *act_dst)
+{
+    err = warp_sum(err);
+    act = warp_sum(act);
+    if ((threadIdx.x & 31) == 0)
+    {
+        if (err != 0.0) atomicAdd(err_dst, err);
+        if (act) atomicAdd(act_dst, act);
+    }
+}
+
+__device__ __forceinline__ void warp_max_to(uint32_t v, uint32_t *dst)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_down_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && v) atomicMax(dst, v);
 }
 
 } // namespace gg

@@ -11,13 +11,15 @@
 
 #include "gg_runtime.h"
 
-/* Threads and items per thread of the merge-path tile kernels.  One CTA
- * consumes TILE_ITEMS = NT*IPT merge items (row ends + edges).  IPT is odd so
- * that the per-thread reads of the staged values hit distinct shared-memory
- * banks. */
-#define GG_TILE_NT 256
-#define GG_TILE_IPT 7
-#define GG_TILE_ITEMS (GG_TILE_NT * GG_TILE_IPT)
+/* Merge-path tiles are consumed by single warps: one warp takes a tile of
+ * GG_TILE_ITEMS = 32 * GG_TILE_IPT merge items (row ends + edges), so no
+ * CTA-wide barrier sits on the hot path.  IPT is odd so that the lanes'
+ * reads of the staged values hit distinct shared-memory banks.  Kernels run
+ * persistent CTAs of GG_TILE_WARPS warps that stride over the tiles. */
+#define GG_TILE_IPT 11
+#define GG_TILE_ITEMS (32 * GG_TILE_IPT)
+#define GG_TILE_WARPS 8
+#define GG_TILE_NT (32 * GG_TILE_WARPS)
 
 /* Slack after every edge array so 16-byte vector loads of the last group
  * stay inside the allocation. */
@@ -27,8 +29,7 @@ struct gg_tiles
 {
     uint32_t ntiles = 0;
     uint2 *coord = nullptr;   /* ntiles+1 merge-path coordinates (row, edge) */
-    void *acc = nullptr;      /* ntiles cross-tile partial sums (8 bytes each) */
-    uint32_t *cnt = nullptr;  /* ntiles arrival counters */
+    void *acc = nullptr;      /* ntiles cross-tile partial sums (8 bytes each), zero between launches */
 };
 
 /* Growable device scratch owned by a mapping. */
@@ -109,3 +110,9 @@ gg_status gg_launch_tile_coords(const uint32_t *off, uint32_t V, uint32_t E, uin
                                 uint2 *coord, cudaStream_t s);
 gg_status gg_launch_to_half(const float *src, void *dst, size_t n, int storage, cudaStream_t s);
 int gg_sm_count();
+/* persistent grid for a tile kernel: one CTA per resident slot, no more
+ * CTAs than tiles need */
+int gg_persistent_grid(const void *kernel, uint32_t ntiles);
+/* smallest float f with (double)f >= x, and largest float f with (double)f <= x */
+float gg_float_ceil(double x);
+float gg_float_floor(double x);

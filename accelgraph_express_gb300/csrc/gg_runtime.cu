@@ -11,6 +11,7 @@
 #include <cuda_fp16.h>
 
 #include <atomic>
+#include <cmath>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -65,6 +66,58 @@ extern "C" const char *gg_last_error(void) { return t_last_error.c_str(); }
 extern "C" void gg_set_wait_timeout_ms(uint32_t ms) { g_wait_timeout_ms.store(ms ? ms : 120000); }
 
 int gg_sm_count() { return g_sm_count > 0 ? g_sm_count : 152; }
+
+int gg_persistent_grid(const void *kernel, uint32_t ntiles)
+{
+    static std::mutex mu;
+    static const void *keys[64];
+    static int vals[64];
+    static int n = 0;
+    int bps = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (int i = 0; i < n; i++)
+            if (keys[i] == kernel) bps = vals[i];
+        if (!bps)
+        {
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, GG_TILE_NT, 0);
+            if (e != cudaSuccess || bps < 1)
+            {
+                cudaGetLastError();
+                bps = 1;
+            }
+            if (getenv("GG_DEBUG"))
+                fprintf(stderr, "gg: kernel %p: %d CTAs of %d threads per SM (%s)\n", kernel, bps, GG_TILE_NT,
+                        cudaGetErrorString(e));
+            if (n < 64)
+            {
+                keys[n] = kernel;
+                vals[n] = bps;
+                n++;
+            }
+        }
+    }
+    const uint64_t need = ((uint64_t)ntiles + GG_TILE_WARPS - 1) / GG_TILE_WARPS;
+    const uint64_t cap = (uint64_t)gg_sm_count() * (uint64_t)bps;
+    const uint64_t g = need < cap ? need : cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+float gg_float_ceil(double x)
+{
+    if (x != x) return (float)x;
+    float f = (float)x;
+    if ((double)f < x) f = nextafterf(f, INFINITY);
+    return f;
+}
+
+float gg_float_floor(double x)
+{
+    if (x != x) return (float)x;
+    float f = (float)x;
+    if ((double)f > x) f = nextafterf(f, -INFINITY);
+    return f;
+}
 
 extern "C" gg_status gg_device_init(int device)
 {
@@ -305,7 +358,6 @@ static void free_tiles(gg_graph *g, gg_tiles &t)
 {
     gg_dev_free(g, t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2));
     gg_dev_free(g, t.acc, (size_t)t.ntiles * 8 + 8);
-    gg_dev_free(g, t.cnt, (size_t)t.ntiles * 4 + 4);
     t = gg_tiles();
 }
 
@@ -353,9 +405,7 @@ gg_status gg_tiles_get(gg_graph *g, int in, cudaStream_t s, gg_tiles **out)
         t.ntiles = (uint32_t)(nt ? nt : 1);
         GG_CHECK(gg_dev_alloc(g, (void **)&t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2)));
         GG_CHECK(gg_dev_alloc(g, &t.acc, (size_t)t.ntiles * 8 + 8));
-        GG_CHECK(gg_dev_alloc(g, (void **)&t.cnt, (size_t)t.ntiles * 4 + 4));
         GG_CUDA(cudaMemsetAsync(t.acc, 0, (size_t)t.ntiles * 8 + 8, s));
-        GG_CUDA(cudaMemsetAsync(t.cnt, 0, (size_t)t.ntiles * 4 + 4, s));
         GG_CHECK(gg_launch_tile_coords(off, g->V, g->E, t.ntiles, t.coord, s));
     }
     *out = &t;

@@ -166,22 +166,39 @@ struct PrCommon
     const uint32_t *outdeg;
     uint32_t V;
     float base, damp;
-    double epsilon;
+    float eps_f;       /* smallest float e with (double)e >= epsilon */
+    float eps_fl;      /* largest float e with (double)e <= epsilon */
     IterRec *rec;      /* records of this run */
     uint32_t it;       /* iteration index of this launch */
     __device__ __forceinline__ bool skip() const { return it > 0 && rec[it - 1].active == 0u; }
+    /* pageRank.c:1057-1067: |rank' - rank| is a float difference, exact in
+     * FP64; the FP64 sum of the differences is divided by V once on the host
+     * (the reference divides each term), and `error >= epsilon` is the same
+     * test as e >= eps_f in FP32, so no FP64 division or compare runs per
+     * vertex (FP64 is 1/64 of the FP32 rate here) */
     __device__ __forceinline__ void update(uint32_t r, float nr, double &err, uint32_t &act) const
     {
         float pr = rank[r];
         rank[r] = nr;
-        double e = fabs((double)__fsub_rn(nr, pr));
-        err += e / (double)V;
-        if (e >= epsilon) act++;
+        float e = fabsf(__fsub_rn(nr, pr));
+        err += (double)e;
+        if (e >= eps_f) act++;
+    }
+    __device__ __forceinline__ void update_pre(uint32_t r, float nr, float pr, double &err, uint32_t &act) const
+    {
+        rank[r] = nr;
+        float e = fabsf(__fsub_rn(nr, pr));
+        err += (double)e;
+        if (e >= eps_f) act++;
     }
     __device__ __forceinline__ void reduce(double err, uint32_t act) const
     {
         if (err != 0.0) atomicAdd(&rec[it].err, err);
         if (act) atomicAdd(&rec[it].active, act);
+    }
+    __device__ __forceinline__ void warp_reduce(double err, uint32_t act) const
+    {
+        warp_reduce_to(err, act, &rec[it].err, &rec[it].active);
     }
 };
 
@@ -197,20 +214,16 @@ struct PullOp : PrCommon
     float *cf;         /* float contributions (quantised modes) */
     uint32_t tmax = 0; /* this thread's largest new contribution (quantised modes) */
 
-    __device__ __forceinline__ void load4(uint32_t, uint4 q, Acc v[4]) const
-    {
-        v[0] = decode<K>(cin[q.x]);
-        v[1] = decode<K>(cin[q.y]);
-        v[2] = decode<K>(cin[q.z]);
-        v[3] = decode<K>(cin[q.w]);
-    }
-    __device__ __forceinline__ void finish(uint32_t r, Acc sum, double &err, uint32_t &act)
+    struct RowPre { float rank; uint32_t deg; };
+    __device__ __forceinline__ Acc load1(uint32_t, uint32_t u) const { return decode<K>(cin[u]); }
+    __device__ __forceinline__ RowPre prefetch(uint32_t r) const { return RowPre{rank[r], outdeg[r]}; }
+    __device__ __forceinline__ void finish(uint32_t r, Acc sum, const RowPre &pre, double &err, uint32_t &act)
     {
         float qscale = 0.0f;
         if constexpr (Fmt<K>::quant) qscale = quant_scale(rec[it].maxbits, Fmt<K>::bits);
         float nr = next_rank<K>(base, damp, sum, qscale);
-        update(r, nr, err, act);
-        uint32_t d = outdeg[r];
+        update_pre(r, nr, pre.rank, err, act);
+        const uint32_t d = pre.deg;
         float c = contrib_of(nr, d);
         if constexpr (Fmt<K>::quant)
         {
@@ -220,19 +233,28 @@ struct PullOp : PrCommon
         else
             cout[r] = encode<K>(c, d);
     }
-    __device__ __forceinline__ void block_end()
+    __device__ __forceinline__ void warp_end(double err, uint32_t act)
     {
-        if constexpr (Fmt<K>::quant) block_max_bits<GG_TILE_NT>(tmax, &rec[it + 1].maxbits);
+        warp_reduce(err, act);
+        if constexpr (Fmt<K>::quant) warp_max_to(tmax, &rec[it + 1].maxbits);
     }
 };
 
 template <int K>
 __global__ void __launch_bounds__(GG_TILE_NT) k_pr_pull(const uint32_t *__restrict__ off,
                                                         const uint32_t *__restrict__ adj, const uint2 *__restrict__ coord,
-                                                        typename Fmt<K>::Acc *g_acc, uint32_t *g_cnt, PullOp<K> op)
+                                                        uint32_t ntiles, typename Fmt<K>::Acc *g_acc, PullOp<K> op)
 {
     if (op.skip()) return;
-    tile_pull<GG_TILE_NT, GG_TILE_IPT>(off, adj, op.V, coord, g_acc, g_cnt, op, blockIdx.x);
+    warp_pull<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, op.V, coord, ntiles, g_acc, op);
+}
+
+template <int K>
+__global__ void __launch_bounds__(256) k_pr_pull_fixup(const uint32_t *__restrict__ off, const uint2 *__restrict__ coord,
+                                                       uint32_t ntiles, typename Fmt<K>::Acc *g_acc, PullOp<K> op)
+{
+    if (op.skip()) return;
+    warp_pull_fixup(off, op.V, coord, ntiles, GG_TILE_ITEMS, g_acc, op);
 }
 
 /* ---- init, quantise, finalise --------------------------------------------------- */
@@ -297,7 +319,7 @@ __global__ void k_pr_finalize(float *__restrict__ rank, uint32_t V, int divide, 
 
 template <int K>
 __global__ void __launch_bounds__(GG_TILE_NT) k_pr_push_f(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                                          const uint2 *__restrict__ coord, uint32_t V,
+                                                          const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t V,
                                                           const typename Fmt<K>::CT *cin, float *next,
                                                           IterRec *rec, uint32_t it)
 {
@@ -310,11 +332,11 @@ __global__ void __launch_bounds__(GG_TILE_NT) k_pr_push_f(const uint32_t *__rest
         __device__ __forceinline__ float row_value(uint32_t r) const { return to_f32(cin[r]); }
         __device__ __forceinline__ void scatter(float rv, uint32_t, uint32_t dst) const { atomicAdd(&next[dst], rv); }
     } op{cin, next};
-    tile_push<GG_TILE_NT, GG_TILE_IPT>(off, adj, V, coord, op, blockIdx.x);
+    warp_push<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, op);
 }
 
 __global__ void __launch_bounds__(GG_TILE_NT) k_pr_push_fx64(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                                             const uint2 *__restrict__ coord, uint32_t V,
+                                                             const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t V,
                                                              const unsigned long long *cin, unsigned long long *next,
                                                              IterRec *rec, uint32_t it)
 {
@@ -330,11 +352,11 @@ __global__ void __launch_bounds__(GG_TILE_NT) k_pr_push_fx64(const uint32_t *__r
             atomicAdd(&next[dst], rv);
         }
     } op{cin, next};
-    tile_push<GG_TILE_NT, GG_TILE_IPT>(off, adj, V, coord, op, blockIdx.x);
+    warp_push<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, op);
 }
 
 __global__ void __launch_bounds__(GG_TILE_NT) k_pr_push_q(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                                          const uint2 *__restrict__ coord, uint32_t V,
+                                                          const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t V,
                                                           const uint8_t *q, const uint32_t *zeros, float *next,
                                                           IterRec *rec, uint32_t it)
 {
@@ -353,7 +375,7 @@ __global__ void __launch_bounds__(GG_TILE_NT) k_pr_push_q(const uint32_t *__rest
         }
         __device__ __forceinline__ void scatter(float rv, uint32_t, uint32_t dst) const { atomicAdd(&next[dst], rv); }
     } op{q, quant_scale(rec[it].maxbits, 8), zeros[it], next};
-    tile_push<GG_TILE_NT, GG_TILE_IPT>(off, adj, V, coord, op, blockIdx.x);
+    warp_push<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, op);
 }
 
 /* vertex update after a push (pageRank.c:2067-2081) */
@@ -407,33 +429,39 @@ struct DdPullOp : PrCommon
     const uint8_t *wl_curr;
     uint8_t *wl_next;
     const uint32_t *out_off, *out_adj;
-    __device__ __forceinline__ void load4(uint32_t, uint4 q, float v[4]) const
+    struct RowPre { float rank; uint32_t on; };
+    __device__ __forceinline__ float load1(uint32_t, uint32_t u) const { return cf[u]; }
+    __device__ __forceinline__ RowPre prefetch(uint32_t r) const { return RowPre{rank[r], wl_curr[r]}; }
+    __device__ __forceinline__ void finish(uint32_t r, float sum, const RowPre &pre, double &err, uint32_t &act)
     {
-        v[0] = cf[q.x]; v[1] = cf[q.y]; v[2] = cf[q.z]; v[3] = cf[q.w];
-    }
-    __device__ __forceinline__ void finish(uint32_t r, float sum, double &err, uint32_t &act)
-    {
-        if (!wl_curr[r]) return;
+        if (!pre.on) return;
         float nr = __fadd_rn(base, __fmul_rn(damp, sum));
-        float pr = rank[r];
-        double e = fabs((double)__fsub_rn(nr, pr));
-        err += e / (double)V;
-        if (e >= epsilon)
+        float pr = pre.rank;
+        float e = fabsf(__fsub_rn(nr, pr));
+        err += (double)e;
+        if (e >= eps_f)
         {
             rank[r] = nr;
             for (uint32_t j = out_off[r]; j < out_off[r + 1]; j++) wl_next[out_adj[j]] = 1;
             act++;
         }
     }
-    __device__ __forceinline__ void block_end() {}
+    __device__ __forceinline__ void warp_end(double err, uint32_t act) { warp_reduce(err, act); }
 };
 
 __global__ void __launch_bounds__(GG_TILE_NT) k_dd_pull(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                                        const uint2 *__restrict__ coord, float *g_acc, uint32_t *g_cnt,
+                                                        const uint2 *__restrict__ coord, uint32_t ntiles, float *g_acc,
                                                         DdPullOp op)
 {
     if (op.skip()) return;
-    tile_pull<GG_TILE_NT, GG_TILE_IPT>(off, adj, op.V, coord, g_acc, g_cnt, op, blockIdx.x);
+    warp_pull<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, op.V, coord, ntiles, g_acc, op);
+}
+
+__global__ void __launch_bounds__(256) k_dd_pull_fixup(const uint32_t *__restrict__ off, const uint2 *__restrict__ coord,
+                                                       uint32_t ntiles, float *g_acc, DdPullOp op)
+{
+    if (op.skip()) return;
+    warp_pull_fixup(off, op.V, coord, ntiles, GG_TILE_ITEMS, g_acc, op);
 }
 
 /* data-driven push (mode 7) and pull-push (mode 8): one warp per worklist
@@ -510,7 +538,7 @@ __global__ void k_dd_push(PrCommon c, int pullpush, const uint32_t *__restrict__
         {
             uint32_t u = out_adj[j];
             float prev = atomicAdd(&resid[u], delta);
-            if (fabs((double)__fadd_rn(prev, delta)) >= c.epsilon && (double)prev <= c.epsilon)
+            if (fabsf(__fadd_rn(prev, delta)) >= c.eps_f && prev <= c.eps_fl)
             {
                 act++;
                 if (pullpush) atomicAdd(&resid[u], delta);
@@ -535,6 +563,7 @@ struct Run
     gg_graph *g;
     cudaStream_t s;
     const gg_pr_params *p;
+    float eps_f = 0.0f, eps_fl = 0.0f;
     uint32_t launches = 0;
     uint32_t gather_launches = 0;
     float gather_ms = 0.0f;
@@ -542,6 +571,7 @@ struct Run
 };
 
 int grid_v(uint32_t V) { int b = (int)((V + 255) / 256); int cap = gg_sm_count() * 8; return b < 1 ? 1 : (b > cap ? cap : b); }
+int fixup_grid(uint32_t ntiles) { return grid_v(ntiles); }
 
 gg_status timed_begin(Run &R)
 {
@@ -581,14 +611,16 @@ gg_status run_pull(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
         }
         PullOp<K> op;
         op.rank = rank; op.outdeg = g->out_deg; op.V = V; op.base = base; op.damp = R.p->damp;
-        op.epsilon = R.p->epsilon; op.rec = rec; op.it = it;
+        op.eps_f = R.eps_f; op.eps_fl = R.eps_fl; op.rec = rec; op.it = it;
         op.cin = Fmt<K>::quant ? cb[0] : cb[it & 1];
         op.cout = cb[(it + 1) & 1];
         op.cf = (float *)cf;
         GG_CHECK(timed_begin(R));
-        k_pr_pull<K><<<t->ntiles, GG_TILE_NT, 0, R.s>>>(g->in_off, g->in_adj, t->coord, (Acc *)t->acc, t->cnt, op);
+        k_pr_pull<K><<<gg_persistent_grid((const void *)k_pr_pull<K>, t->ntiles), GG_TILE_NT, 0, R.s>>>(
+            g->in_off, g->in_adj, t->coord, t->ntiles, (Acc *)t->acc, op);
+        k_pr_pull_fixup<K><<<fixup_grid(t->ntiles), 256, 0, R.s>>>(g->in_off, t->coord, t->ntiles, (Acc *)t->acc, op);
         GG_CHECK(timed_end(R));
-        R.launches++;
+        R.launches += 2;
         R.gather_launches++;
     }
     GG_CUDA(cudaGetLastError());
@@ -626,19 +658,22 @@ gg_status run_push(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
         {
             k_quantize<uint8_t><<<grid_v(V), 256, 0, R.s>>>((const float *)cf, (uint8_t *)c0, V, 8, 1, rec, it,
                                                            (uint32_t *)zeros);
-            k_pr_push_q<<<t->ntiles, GG_TILE_NT, 0, R.s>>>(g->out_off, g->out_adj, t->coord, V, (const uint8_t *)c0,
+            k_pr_push_q<<<gg_persistent_grid((const void *)k_pr_push_q, t->ntiles), GG_TILE_NT, 0, R.s>>>(
+                g->out_off, g->out_adj, t->coord, t->ntiles, V, (const uint8_t *)c0,
                                                            (const uint32_t *)zeros, (float *)nx, rec, it);
             R.launches += 2;
         }
         else if constexpr (K == K_FX64)
         {
-            k_pr_push_fx64<<<t->ntiles, GG_TILE_NT, 0, R.s>>>(g->out_off, g->out_adj, t->coord, V,
+            k_pr_push_fx64<<<gg_persistent_grid((const void *)k_pr_push_fx64, t->ntiles), GG_TILE_NT, 0, R.s>>>(
+                g->out_off, g->out_adj, t->coord, t->ntiles, V,
                                                               (const unsigned long long *)c0, (unsigned long long *)nx, rec, it);
             R.launches++;
         }
         else
         {
-            k_pr_push_f<K><<<t->ntiles, GG_TILE_NT, 0, R.s>>>(g->out_off, g->out_adj, t->coord, V, (const CT *)c0,
+            k_pr_push_f<K><<<gg_persistent_grid((const void *)k_pr_push_f<K>, t->ntiles), GG_TILE_NT, 0, R.s>>>(
+                g->out_off, g->out_adj, t->coord, t->ntiles, V, (const CT *)c0,
                                                               (float *)nx, rec, it);
             R.launches++;
         }
@@ -646,7 +681,7 @@ gg_status run_push(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
         R.gather_launches++;
         PrCommon c;
         c.rank = rank; c.outdeg = g->out_deg; c.V = V; c.base = base; c.damp = R.p->damp;
-        c.epsilon = R.p->epsilon; c.rec = rec; c.it = it;
+        c.eps_f = R.eps_f; c.eps_fl = R.eps_fl; c.rec = rec; c.it = it;
         if constexpr (K == K_FX64)
             k_pr_push_update<K_FX64><<<grid_v(V), 256, 0, R.s>>>(c, (unsigned long long *)nx, (unsigned long long *)c0, nullptr);
         else if constexpr (K == K_Q8Z)
@@ -684,14 +719,16 @@ gg_status run_dd(Run &R, int mode, IterRec *rec, float *rank, uint32_t iters, fl
             k_dd_contrib<<<grid_v(V), 256, 0, R.s>>>(rank, g->out_deg, (float *)cf, V, rec, it);
             DdPullOp op;
             op.rank = rank; op.outdeg = g->out_deg; op.V = V; op.base = base; op.damp = R.p->damp;
-            op.epsilon = R.p->epsilon; op.rec = rec; op.it = it;
+            op.eps_f = R.eps_f; op.eps_fl = R.eps_fl; op.rec = rec; op.it = it;
             op.cf = (const float *)cf; op.wl_curr = wl[it & 1]; op.wl_next = wl[(it + 1) & 1];
             op.out_off = g->out_off; op.out_adj = g->out_adj;
             GG_CHECK(timed_begin(R));
-            k_dd_pull<<<t->ntiles, GG_TILE_NT, 0, R.s>>>(g->in_off, g->in_adj, t->coord, (float *)t->acc, t->cnt, op);
+            k_dd_pull<<<gg_persistent_grid((const void *)k_dd_pull, t->ntiles), GG_TILE_NT, 0, R.s>>>(
+                g->in_off, g->in_adj, t->coord, t->ntiles, (float *)t->acc, op);
+            k_dd_pull_fixup<<<fixup_grid(t->ntiles), 256, 0, R.s>>>(g->in_off, t->coord, t->ntiles, (float *)t->acc, op);
             GG_CHECK(timed_end(R));
             k_clear_bytes<<<grid_v(V), 256, 0, R.s>>>(wl[it & 1], V, rec, it);
-            R.launches += 3;
+            R.launches += 4;
             R.gather_launches++;
         }
     }
@@ -705,7 +742,7 @@ gg_status run_dd(Run &R, int mode, IterRec *rec, float *rank, uint32_t iters, fl
         {
             PrCommon c;
             c.rank = rank; c.outdeg = g->out_deg; c.V = V; c.base = base; c.damp = R.p->damp;
-            c.epsilon = R.p->epsilon; c.rec = rec; c.it = it;
+            c.eps_f = R.eps_f; c.eps_fl = R.eps_fl; c.rec = rec; c.it = it;
             GG_CHECK(timed_begin(R));
             k_dd_push<<<gg_sm_count() * 8, 256, 0, R.s>>>(c, mode == GG_PR_DD_PULLPUSH, g->in_off, g->in_adj, g->out_off,
                                                           g->out_adj, (float *)resid, wl[it & 1], wl[(it + 1) & 1]);
@@ -736,6 +773,8 @@ extern "C" gg_status gg_pagerank(gg_graph *g, const gg_pr_params *p, float *rank
     R.g = g;
     R.s = gg_stream(g, stream);
     R.p = p;
+    R.eps_f = gg_float_ceil(p->epsilon);
+    R.eps_fl = gg_float_floor(p->epsilon);
     const uint32_t V = g->V, iters = p->max_iterations;
     gg_pr_result res;
     memset(&res, 0, sizeof(res));
@@ -801,7 +840,10 @@ extern "C" gg_status gg_pagerank(gg_graph *g, const gg_pr_params *p, float *rank
     res.iterations = k;
     const uint32_t last = k < iters ? k : (iters ? iters - 1 : 0);
     res.active = iters ? h[last].active : 0;
-    res.error_total = iters ? h[last].err : 0.0;
+    /* the kernels sum |delta|; the data-driven push variants add terms
+     * already divided by V (pageRank.c:3049) */
+    const bool pre_scaled = p->mode == GG_PR_DD_PUSH || p->mode == GG_PR_DD_PULLPUSH;
+    res.error_total = iters ? (pre_scaled ? h[last].err : h[last].err / (double)V) : 0.0;
     res.rank_sum = sum;
     res.launches = R.launches;
     res.gather_launches = R.gather_launches;

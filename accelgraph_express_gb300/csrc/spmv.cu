@@ -24,36 +24,6 @@ namespace {
 
 using namespace gg;
 
-template <class T> struct Vec4;
-template <> struct Vec4<float>
-{
-    static __device__ __forceinline__ void load(const float *p, float o[4])
-    {
-        float4 v = *reinterpret_cast<const float4 *>(p);
-        o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
-    }
-};
-template <> struct Vec4<__nv_bfloat16>
-{
-    static __device__ __forceinline__ void load(const __nv_bfloat16 *p, float o[4])
-    {
-        uint2 v = *reinterpret_cast<const uint2 *>(p);
-        __nv_bfloat162 a = *reinterpret_cast<__nv_bfloat162 *>(&v.x), b = *reinterpret_cast<__nv_bfloat162 *>(&v.y);
-        float2 fa = __bfloat1622float2(a), fb = __bfloat1622float2(b);
-        o[0] = fa.x; o[1] = fa.y; o[2] = fb.x; o[3] = fb.y;
-    }
-};
-template <> struct Vec4<__half>
-{
-    static __device__ __forceinline__ void load(const __half *p, float o[4])
-    {
-        uint2 v = *reinterpret_cast<const uint2 *>(p);
-        __half2 a = *reinterpret_cast<__half2 *>(&v.x), b = *reinterpret_cast<__half2 *>(&v.y);
-        float2 fa = __half22float2(a), fb = __half22float2(b);
-        o[0] = fa.x; o[1] = fa.y; o[2] = fb.x; o[3] = fb.y;
-    }
-};
-
 template <class T>
 struct SpmvPullOp
 {
@@ -61,27 +31,29 @@ struct SpmvPullOp
     const T *w;
     const T *x;
     float *y;
-    __device__ __forceinline__ bool skip() const { return false; }
-    __device__ __forceinline__ void load4(uint32_t e4, uint4 q, float v[4]) const
+    struct RowPre {};
+    __device__ __forceinline__ float load1(uint32_t e, uint32_t u) const
     {
-        float wv[4];
-        Vec4<T>::load(w + e4, wv);
-        v[0] = __fmul_rn(wv[0], to_f32(x[q.x]));
-        v[1] = __fmul_rn(wv[1], to_f32(x[q.y]));
-        v[2] = __fmul_rn(wv[2], to_f32(x[q.z]));
-        v[3] = __fmul_rn(wv[3], to_f32(x[q.w]));
+        return __fmul_rn(to_f32(w[e]), to_f32(x[u]));
     }
-    __device__ __forceinline__ void finish(uint32_t r, float sum, double &, uint32_t &) { y[r] = sum; }
-    __device__ __forceinline__ void block_end() {}
-    __device__ __forceinline__ void reduce(double, uint32_t) const {}
+    __device__ __forceinline__ RowPre prefetch(uint32_t) const { return RowPre{}; }
+    __device__ __forceinline__ void finish(uint32_t r, float sum, const RowPre &, double &, uint32_t &) { y[r] = sum; }
+    __device__ __forceinline__ void warp_end(double, uint32_t) const {}
 };
 
 template <class T>
 __global__ void __launch_bounds__(GG_TILE_NT) k_spmv_pull(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                                          const uint2 *__restrict__ coord, uint32_t V, float *g_acc,
-                                                          uint32_t *g_cnt, SpmvPullOp<T> op)
+                                                          const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t V,
+                                                          float *g_acc, SpmvPullOp<T> op)
 {
-    tile_pull<GG_TILE_NT, GG_TILE_IPT>(off, adj, V, coord, g_acc, g_cnt, op, blockIdx.x);
+    warp_pull<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, g_acc, op);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_spmv_pull_fixup(const uint32_t *__restrict__ off, const uint2 *__restrict__ coord,
+                                                         uint32_t ntiles, uint32_t V, float *g_acc, SpmvPullOp<T> op)
+{
+    warp_pull_fixup(off, V, coord, ntiles, GG_TILE_ITEMS, g_acc, op);
 }
 
 struct SpmvPullFxOp
@@ -90,34 +62,37 @@ struct SpmvPullFxOp
     const float *w;
     const uint32_t *x32;
     float *y;
-    __device__ __forceinline__ bool skip() const { return false; }
-    __device__ __forceinline__ void load4(uint32_t e4, uint4 q, unsigned long long v[4]) const
+    struct RowPre {};
+    __device__ __forceinline__ unsigned long long load1(uint32_t e, uint32_t u) const
     {
-        float4 wv = *reinterpret_cast<const float4 *>(w + e4);
-        v[0] = ((unsigned long long)x32[q.x] * fx_from_float(wv.x, 65536.0, 0xffffffffu)) >> 16;
-        v[1] = ((unsigned long long)x32[q.y] * fx_from_float(wv.y, 65536.0, 0xffffffffu)) >> 16;
-        v[2] = ((unsigned long long)x32[q.z] * fx_from_float(wv.z, 65536.0, 0xffffffffu)) >> 16;
-        v[3] = ((unsigned long long)x32[q.w] * fx_from_float(wv.w, 65536.0, 0xffffffffu)) >> 16;
+        return ((unsigned long long)x32[u] * fx_from_float(w[e], 65536.0, 0xffffffffu)) >> 16;
     }
-    __device__ __forceinline__ void finish(uint32_t r, unsigned long long sum, double &, uint32_t &)
+    __device__ __forceinline__ RowPre prefetch(uint32_t) const { return RowPre{}; }
+    __device__ __forceinline__ void finish(uint32_t r, unsigned long long sum, const RowPre &, double &, uint32_t &)
     {
         y[r] = fx_to_float(sum, 1.0 / 65536.0);
     }
-    __device__ __forceinline__ void block_end() {}
-    __device__ __forceinline__ void reduce(double, uint32_t) const {}
+    __device__ __forceinline__ void warp_end(double, uint32_t) const {}
 };
 
 __global__ void __launch_bounds__(GG_TILE_NT) k_spmv_pull_fx(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                                             const uint2 *__restrict__ coord, uint32_t V,
-                                                             unsigned long long *g_acc, uint32_t *g_cnt, SpmvPullFxOp op)
+                                                             const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t V,
+                                                             unsigned long long *g_acc, SpmvPullFxOp op)
 {
-    tile_pull<GG_TILE_NT, GG_TILE_IPT>(off, adj, V, coord, g_acc, g_cnt, op, blockIdx.x);
+    warp_pull<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, g_acc, op);
+}
+
+__global__ void __launch_bounds__(256) k_spmv_pull_fx_fixup(const uint32_t *__restrict__ off, const uint2 *__restrict__ coord,
+                                                            uint32_t ntiles, uint32_t V, unsigned long long *g_acc,
+                                                            SpmvPullFxOp op)
+{
+    warp_pull_fixup(off, V, coord, ntiles, GG_TILE_ITEMS, g_acc, op);
 }
 
 template <class T>
 __global__ void __launch_bounds__(GG_TILE_NT) k_spmv_push(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                                          const uint2 *__restrict__ coord, uint32_t V, const T *w,
-                                                          const T *x, float *y)
+                                                          const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t V,
+                                                          const T *w, const T *x, float *y)
 {
     struct Op
     {
@@ -131,12 +106,13 @@ __global__ void __launch_bounds__(GG_TILE_NT) k_spmv_push(const uint32_t *__rest
             atomicAdd(&y[dst], __fmul_rn(to_f32(w[e]), xv));
         }
     } op{w, x, y};
-    tile_push<GG_TILE_NT, GG_TILE_IPT>(off, adj, V, coord, op, blockIdx.x);
+    warp_push<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, op);
 }
 
 __global__ void __launch_bounds__(GG_TILE_NT) k_spmv_push_fx(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                                             const uint2 *__restrict__ coord, uint32_t V, const float *w,
-                                                             const unsigned long long *x64, unsigned long long *y64)
+                                                             const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t V,
+                                                             const float *w, const unsigned long long *x64,
+                                                             unsigned long long *y64)
 {
     struct Op
     {
@@ -150,7 +126,7 @@ __global__ void __launch_bounds__(GG_TILE_NT) k_spmv_push_fx(const uint32_t *__r
             atomicAdd(&y64[dst], fx64_mul(fx64_from_double((double)w[e]), xv));
         }
     } op{w, x64, y64};
-    tile_push<GG_TILE_NT, GG_TILE_IPT>(off, adj, V, coord, op, blockIdx.x);
+    warp_push<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, op);
 }
 
 /* x[v] = 1/outdeg(v), or 0.001 when 0 (SPMV.c:696-701), unless given; the
@@ -235,10 +211,14 @@ gg_status spmv_fp(gg_graph *g, const gg_spmv_params *p, const float *x_dev, floa
         if (pull)
         {
             SpmvPullOp<T> op{w, xv, y};
-            k_spmv_pull<T><<<t->ntiles, GG_TILE_NT, 0, s>>>(g->in_off, g->in_adj, t->coord, V, (float *)t->acc, t->cnt, op);
+            k_spmv_pull<T><<<gg_persistent_grid((const void *)k_spmv_pull<T>, t->ntiles), GG_TILE_NT, 0, s>>>(
+                g->in_off, g->in_adj, t->coord, t->ntiles, V, (float *)t->acc, op);
+            k_spmv_pull_fixup<T><<<grid_v(t->ntiles), 256, 0, s>>>(g->in_off, t->coord, t->ntiles, V, (float *)t->acc, op);
+            launches++;
         }
         else
-            k_spmv_push<T><<<t->ntiles, GG_TILE_NT, 0, s>>>(g->out_off, g->out_adj, t->coord, V, w, xv, y);
+            k_spmv_push<T><<<gg_persistent_grid((const void *)k_spmv_push<T>, t->ntiles), GG_TILE_NT, 0, s>>>(
+                g->out_off, g->out_adj, t->coord, t->ntiles, V, w, xv, y);
         if (p->profile)
         {
             cudaEvent_t e;
@@ -319,12 +299,16 @@ extern "C" gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *
                 if (pull)
                 {
                     SpmvPullFxOp op{g->in_w, (const uint32_t *)xq, (float *)yv};
-                    k_spmv_pull_fx<<<t->ntiles, GG_TILE_NT, 0, s>>>(g->in_off, g->in_adj, t->coord, V,
-                                                                    (unsigned long long *)t->acc, t->cnt, op);
+                    k_spmv_pull_fx<<<gg_persistent_grid((const void *)k_spmv_pull_fx, t->ntiles), GG_TILE_NT, 0, s>>>(
+                        g->in_off, g->in_adj, t->coord, t->ntiles, V, (unsigned long long *)t->acc, op);
+                    k_spmv_pull_fx_fixup<<<grid_v(t->ntiles), 256, 0, s>>>(g->in_off, t->coord, t->ntiles, V,
+                                                                          (unsigned long long *)t->acc, op);
+                    launches++;
                 }
                 else
-                    k_spmv_push_fx<<<t->ntiles, GG_TILE_NT, 0, s>>>(g->out_off, g->out_adj, t->coord, V, g->out_w,
-                                                                    (const unsigned long long *)xq, (unsigned long long *)y64);
+                    k_spmv_push_fx<<<gg_persistent_grid((const void *)k_spmv_push_fx, t->ntiles), GG_TILE_NT, 0, s>>>(
+                        g->out_off, g->out_adj, t->coord, t->ntiles, V, g->out_w, (const unsigned long long *)xq,
+                        (unsigned long long *)y64);
                 if (p->profile)
                 {
                     cudaEvent_t e;

@@ -1,0 +1,344 @@
+#!/usr/bin/env python3
+"""Benchmark: PageRank pull on a directed R-MAT scale-24 graph (16.7M vertices,
+268M edges, a,b,c,d = 0.57/0.19/0.19/0.05, seed 27491095), FP32, 30
+iterations per step, in GTEPS (edges x iterations / second).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+value      GTEPS with the graph resident in HBM, device time (CUDA events on
+           the launching stream) over exactly K steps, max over ranks.
+e2e        the same metric through the drop-in pageRankGraphCSR call on host
+           arrays: every step uploads the CSC (offsets, neighbour ids) and
+           out-degrees and reads the ranks back.
+roofline   the gather kernel (k_pr_pull): algorithmic bytes per launch
+           4E + 4(V+1) + (12 + 2s)V with s = 4 bytes of FP32 contribution
+           (CSC ids, CSC offsets, out-degree, rank read+write, contribution
+           written and gathered once), / its mean CUDA-event duration, vs the
+           measured HBM copy bandwidth.
+cpu_baseline  the oracle's OpenMP restatement of the reference's pull loop
+           (pageRank.c:1026-1085 with the gather as at :2890-2906) on all host
+           cores, on a bounded number of iterations of the same graph.
+--impl reference  times that CPU implementation alone, one iteration per
+           step (the reference's own code needs its absent OpenGraph library,
+           so the restatement stands in for it).
+With N > 1 GPUs every rank runs an independent replica (no collective on the
+data path); value sums all ranks' edges over the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 27491095
+ITERS = 30
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--scale", type=int, default=24)
+    p.add_argument("--edge-factor", type=int, default=16)
+    p.add_argument("--no-extras", action="store_true", help="skip the BF16/BFS/SpMV side measurements")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples (200 ms) while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join("/tmp", f"bench_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic(kernel):
+    """dram bytes per launch of `kernel` from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
+            d = json.load(f)
+        return d.get(kernel, {}).get("dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+def pr_bytes(V, E, s):
+    return 4 * E + 4 * (V + 1) + (12 + 2 * s) * V
+
+
+def cpu_pagerank(graph, O, iters, threads):
+    """The oracle's OpenMP pull on the product's graph arrays (zero copy)."""
+    v = graph.views()
+    V, E = graph.V, graph.E
+    import numpy as np
+    out_off = np.append(v["out_edges_idx"], np.uint32(E))
+    in_off = np.append(v["in_edges_idx"], np.uint32(E))
+    o = O.Csr.from_arrays(V, E, out_off, v["out_adj"], in_off, v["in_adj"])
+    t0 = time.perf_counter()
+    ranks, info = O.pagerank(o, 0, iters, 0.0, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return ranks, info, dt, o
+
+
+def run_reference(a, world, rank):
+    """The reference arm: the CPU implementation of the path on host cores."""
+    if rank != 0:
+        return
+    import accelgraph_express_gb300 as gg
+    from oracle import oracle_ctypes as O
+
+    threads = os.cpu_count() or 1
+    graph = gg.Graph.rmat(a.scale, a.edge_factor, seed=SEED)
+    V, E = graph.V, graph.E
+    times = []
+    for i in range(a.warmup + a.steps):
+        _, _, dt, _ = cpu_pagerank(graph, O, 1, threads)
+        if i >= a.warmup:
+            times.append(dt)
+    t = sum(times)
+    value = E * len(times) / t / 1e9
+    line = {
+        "impl": "reference", "metric": f"PageRank pull GTEPS, R-MAT-{a.scale} FP32", "value": value,
+        "unit": "GTEPS", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": 1e3 * t / len(times), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": f"synthetic R-MAT scale {a.scale}, edge factor {a.edge_factor}, seed {SEED}",
+        "config": {"workload": f"pagerank_pull_rmat{a.scale}", "vertices": V, "edges": E,
+                   "iterations_per_step": 1, "threads": threads},
+        "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
+                         "sample": f"1 PageRank pull iteration over R-MAT-{a.scale} per step"},
+        "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    world, rank, local = dist_env()
+    if a.impl == "reference":
+        run_reference(a, world, rank)
+        return
+
+    import numpy as np
+    import torch
+
+    import accelgraph_express_gb300 as gg
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    gg.device_init(local)
+    t_build = time.perf_counter()
+    graph = gg.Graph.rmat(a.scale, a.edge_factor, seed=SEED)
+    t_build = time.perf_counter() - t_build
+    V, E = graph.V, graph.E
+    dg = gg.DeviceGraph(graph, gg.MAP_IN)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    def step(profile=True):
+        _, r = dg.pagerank("pull", iterations=ITERS, epsilon=0.0, copy_out=False, profile=profile, stream=sptr)
+        return r
+
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    clocks = Clocks(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    gather_ms, gather_n, launches = 0.0, 0, 0
+    for _ in range(a.steps):
+        r = step()
+        gather_ms += r["gather_ms"]
+        gather_n += r["gather_launches"]
+        launches += r["launches"]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    elapsed_ms = max_over_ranks(ev0.elapsed_time(ev1))
+    value = world * E * ITERS * a.steps / (elapsed_ms / 1e3) / 1e9
+
+    # roofline of the gather kernel
+    peak, peak_kind = load_peaks()
+    per_launch_ms = gather_ms / max(gather_n, 1)
+    alg = pr_bytes(V, E, 4)
+    achieved = alg / (per_launch_ms / 1e3) / 1e9
+    traffic = load_traffic("k_pr_pull")
+
+    # e2e through the drop-in entry point on host arrays
+    gg.set_gpu_options(storage="f32", device=local, keep_resident=False, verbose=False)
+    args = gg.default_arguments(iterations=ITERS, epsilon=0.0)
+    gg.pagerank_csr(graph, args)
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(3, min(a.steps, 20))
+    for _ in range(e2e_steps):
+        gg.pagerank_csr(graph, args)
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = world * E * ITERS * e2e_steps / e2e_s / 1e9
+    h2d = 4 * V + 4 + 4 * E + 4 * V  # CSC edges_idx (+ E sentinel), CSC neighbour ids, out-degree
+    d2h = 4 * V + (ITERS + 2) * 16 + 8  # ranks, per-iteration records, rank sum
+
+    line = {
+        "metric": f"PageRank pull GTEPS, R-MAT-{a.scale} FP32", "value": value, "unit": "GTEPS",
+        "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": elapsed_ms / a.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": f"synthetic R-MAT scale {a.scale}, edge factor {a.edge_factor}, seed {SEED}, no label permutation",
+        "config": {"workload": f"pagerank_pull_rmat{a.scale}", "vertices": V, "edges": E,
+                   "iterations_per_step": ITERS, "epsilon": 0.0, "storage": "f32",
+                   "l2": "inputs larger than L2 (4E = %.2f GB CSC ids per iteration)" % (4 * E / 1e9),
+                   "parallelism": f"replicas x{world}", "graph_build_s": round(t_build, 2)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "k_pr_pull", "alg_bytes_per_launch": alg,
+                     "launch_ms": per_launch_ms, "peak_source": peak_kind},
+        "e2e": {"value": e2e_value, "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "steps": e2e_steps, "call": "pageRankGraphCSR"},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+
+    if rank == 0 and world == 1 and not a.no_cpu:
+        from oracle import oracle_ctypes as O
+        threads = os.cpu_count() or 1
+        _, _, dt1, _ = cpu_pagerank(graph, O, 1, threads)
+        n = int(max(1, min(ITERS, 12.0 / max(dt1, 1e-3))))
+        _, _, dt, _ = cpu_pagerank(graph, O, n, threads)
+        line["cpu_baseline"] = {"value": E * n / dt / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
+                                "sample": f"{n} PageRank pull iterations over the same R-MAT-{a.scale} graph"}
+
+    if rank == 0 and not a.no_extras:
+        line["extras"] = extras(gg, graph, dg, V, E, sptr, torch, peak)
+
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dg.free()
+    if dist:
+        dist.destroy_process_group()
+
+
+def extras(gg, graph, dg, V, E, sptr, torch, peak):
+    """Side measurements on the same box: BF16 / FP16 storage GTEPS with L1
+    and L-inf error vs the FP64 oracle."""
+    import numpy as np
+    from oracle import oracle_ctypes as O
+
+    out = {}
+    v = graph.views()
+    out_off = np.append(v["out_edges_idx"], np.uint32(E))
+    in_off = np.append(v["in_edges_idx"], np.uint32(E))
+    o = O.Csr.from_arrays(V, E, out_off, v["out_adj"], in_off, v["in_adj"])
+    t0 = time.perf_counter()
+    exact = O.pagerank_f64(o, ITERS)
+    f64_s = time.perf_counter() - t0
+    for storage, s in [("f32", 4), ("bf16", 2), ("f16", 2)]:
+        for _ in range(2):
+            dg.pagerank("pull", storage=storage, iterations=ITERS, epsilon=0.0, copy_out=False, stream=sptr)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 10
+        e0.record()
+        gms = 0.0
+        for _ in range(reps):
+            _, r = dg.pagerank("pull", storage=storage, iterations=ITERS, epsilon=0.0, copy_out=False,
+                               profile=True, stream=sptr)
+            gms += r["gather_ms"] / max(r["gather_launches"], 1)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        ranks, _ = dg.pagerank("pull", storage=storage, iterations=ITERS, epsilon=0.0, stream=sptr)
+        l1 = float(np.abs(ranks - exact).sum())
+        linf = float(np.abs(ranks - exact).max())
+        launch_ms = gms / reps
+        out[f"pr_pull_{storage}"] = {
+            "gteps": E * ITERS / (ms / 1e3) / 1e9, "ms_per_run": ms, "launch_ms": launch_ms,
+            "hbm_frac": pr_bytes(V, E, s) / (launch_ms / 1e3) / 1e9 / peak,
+            "l1_vs_fp64": l1, "linf_vs_fp64": linf, "l1_relative": l1 / float(np.abs(exact).sum())}
+    out["fp64_oracle_s"] = round(f64_s, 2)
+    return out
+
+
+if __name__ == "__main__":
+    main()

@@ -362,6 +362,7 @@ int orc_pagerank(const orc_csr *g, int mode, uint32_t iterations, double epsilon
             }
             else
             {
+#pragma omp parallel for schedule(static) num_threads(nthreads)
                 for (uint32_t v = 0; v < V; v++)
                 {
                     uint32_t d = out_degree(g, v);
@@ -488,13 +489,16 @@ void orc_pagerank_f64(const orc_csr *g, uint32_t executed, int init_one_over_n, 
     double *contrib = (double *)malloc(((size_t)V + 1) * sizeof(double));
     for (uint32_t v = 0; v < V; v++)
         ranks[v] = init_one_over_n ? 1.0 / V : 0.15;
+    /* per-vertex sums run in CSC order whatever the thread count */
     for (uint32_t it = 0; it < executed; it++)
     {
+#pragma omp parallel for schedule(static)
         for (uint32_t v = 0; v < V; v++)
         {
             uint32_t d = out_degree(g, v);
             contrib[v] = d ? ranks[v] / d : 0.0;
         }
+#pragma omp parallel for schedule(dynamic, 1024)
         for (uint32_t v = 0; v < V; v++)
         {
             double s = 0.0;
