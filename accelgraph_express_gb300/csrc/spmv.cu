@@ -16,6 +16,8 @@
 #include <cuda_fp16.h>
 
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "gg_device.cuh"
@@ -340,5 +342,92 @@ extern "C" gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *
     if (p->profile)
         for (size_t i = 0; i + 1 < evs.size(); i += 2) res.spmv_ms += gg_event_ms(evs[i], evs[i + 1]);
     if (r) *r = res;
+    return GG_OK;
+}
+
+/* ---- allocation-free SpMV pull -------------------------------------------------
+ *
+ * For callers that must not allocate GPU memory: code running inside an
+ * allocator-free section (a host memory manager or plugin host that owns
+ * every device allocation and forbids cudaMalloc/cudaFree from plugins, a
+ * real-time loop where an allocation could block or fragment, or a process
+ * whose device memory is fully reserved up front).  gg_spmv needs a
+ * gg_graph mapping and work buffers that the runtime allocates; this entry
+ * point instead takes the caller's device arrays and keeps its scratch (the
+ * merge-path tile coordinates and the cross-tile partial sums) in the
+ * file-scope array below, which exists on every GPU that loads the library
+ * until the process exits.
+ */
+#define GG_NOALLOC_SCRATCH_BYTES (4u << 20)
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[GG_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[kMaxDevices];
+
+size_t noalloc_coord_bytes(uint32_t ntiles) { return (((size_t)ntiles + 1) * sizeof(uint2) + 255) / 256 * 256; }
+
+} // namespace
+
+extern "C" uint64_t gg_spmv_pull_noalloc_max_items(void)
+{
+    /* the largest V + E whose tile scratch fits: (ntiles+1) coordinates of
+     * 8 bytes (rounded to 256) and ntiles partial sums of 4 bytes */
+    uint64_t lo = 0, hi = (uint64_t)GG_NOALLOC_SCRATCH_BYTES / 4 * GG_TILE_ITEMS;
+    while (lo < hi)
+    {
+        const uint64_t mid = (lo + hi + 1) / 2;
+        const uint64_t nt = (mid + GG_TILE_ITEMS - 1) / GG_TILE_ITEMS;
+        if (noalloc_coord_bytes((uint32_t)nt) + nt * 4 <= GG_NOALLOC_SCRATCH_BYTES)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+extern "C" gg_status gg_spmv_pull_noalloc(uint32_t V, uint32_t E, const uint32_t *in_off, const uint32_t *in_src,
+                                          const float *w, const float *x, float *y, void *stream)
+{
+    if (V == 0) return GG_OK;
+    if (!in_off || !x || !y || !w || (E && !in_src)) return gg_fail(GG_ERR_INVALID, "NULL device array");
+    const uint64_t items = (uint64_t)V + E;
+    const uint64_t max_items = gg_spmv_pull_noalloc_max_items();
+    if (items > max_items)
+        return gg_fail(GG_ERR_INVALID, "gg_spmv_pull_noalloc: V + E = " + std::to_string(items) +
+                                           " exceeds the scratch limit of " + std::to_string(max_items) +
+                                           " (4 MiB of tile scratch); use gg_spmv");
+    int dev = 0;
+    GG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return gg_fail(GG_ERR_INVALID, "device index beyond the scratch table");
+    void *base = nullptr;
+    {
+        /* once per device, with that device current: the host-side name of
+         * the array is not a device address, so ask the runtime for it */
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev])
+        {
+            void *p = nullptr;
+            GG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+            g_noalloc_addr[dev] = p;
+        }
+        base = g_noalloc_addr[dev];
+    }
+    const uint32_t ntiles = (uint32_t)((items + GG_TILE_ITEMS - 1) / GG_TILE_ITEMS);
+    uint2 *coord = (uint2 *)base;
+    float *acc = (float *)((unsigned char *)base + noalloc_coord_bytes(ntiles));
+    cudaStream_t s = (cudaStream_t)stream;
+    /* the array keeps the previous call's contents: the partial sums must
+     * start at zero, the coordinates are rewritten */
+    GG_CUDA(cudaMemsetAsync(acc, 0, (size_t)ntiles * sizeof(float), s));
+    GG_CHECK(gg_launch_tile_coords(in_off, V, E, ntiles, coord, s));
+    SpmvPullOp<float> op{w, x, y};
+    k_spmv_pull<float><<<gg_persistent_grid((const void *)k_spmv_pull<float>, ntiles), GG_TILE_NT, 0, s>>>(
+        in_off, in_src, coord, ntiles, V, acc, op);
+    k_spmv_pull_fixup<float><<<grid_v(ntiles), 256, 0, s>>>(in_off, coord, ntiles, V, acc, op);
+    GG_CUDA(cudaGetLastError());
     return GG_OK;
 }

@@ -195,6 +195,27 @@ typedef struct gg_spmv_result
 gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *x, float *x_out, float *y,
                   gg_spmv_result *r, void *stream);
 
+/*
+ * Allocation-free SpMV pull, y = A^T x, for callers that must not allocate
+ * GPU memory (no counterpart in the reference): a plugin whose host owns
+ * every device allocation, a real-time loop where cudaMalloc could block,
+ * or a process whose device memory is reserved up front.  All arrays are the
+ * caller's DEVICE pointers: in_off (V+1 offsets of the inverse CSR, with
+ * in_off[V] = E), in_src (E in-neighbours), w (E FP32 weights), x (V), y (V,
+ * overwritten).  The call allocates nothing: its scratch is a 4 MiB array
+ * inside the library that every GPU loading the library holds until the
+ * process exits, so V + E must not exceed gg_spmv_pull_noalloc_max_items()
+ * (GG_ERR_INVALID otherwise).  The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.
+ * Calls share the one array: calls whose work overlaps on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller.
+ * Work is queued on `stream` and not waited for.
+ */
+gg_status gg_spmv_pull_noalloc(uint32_t V, uint32_t E, const uint32_t *in_off, const uint32_t *in_src,
+                               const float *w, const float *x, float *y, void *stream);
+/* Largest V + E that gg_spmv_pull_noalloc accepts. */
+uint64_t gg_spmv_pull_noalloc_max_items(void);
+
 /* ---- drop-in side options ---------------------------------------------------- */
 
 /*
