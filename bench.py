@@ -207,7 +207,8 @@ def main():
 
     gg.device_init(local)
     t_build = time.perf_counter()
-    graph = gg.Graph.rmat(a.scale, a.edge_factor, seed=SEED)
+    # one weighted graph serves PageRank (weights unused) and SpMV
+    graph = gg.Graph.rmat(a.scale, a.edge_factor, seed=SEED, weighted=not a.no_extras, weight_seed=SEED + 2)
     t_build = time.perf_counter() - t_build
     V, E = graph.V, graph.E
     dg = gg.DeviceGraph(graph, gg.MAP_IN)
@@ -294,14 +295,121 @@ def main():
 
     if rank == 0:
         print(json.dumps(line), flush=True)
-    dg.free()
+    if dg.h:
+        dg.free()
     if dist:
         dist.destroy_process_group()
 
 
+def splitmix_sources(V, deg, n, seed):
+    """n distinct vertices of nonzero degree drawn from SplitMix64(seed)."""
+    out, i = [], 0
+    mask = (1 << 64) - 1
+    while len(out) < n:
+        z = (seed + (i + 1) * 0x9E3779B97F4A7C15) & mask
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & mask
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & mask
+        z ^= z >> 31
+        v = z % V
+        if deg[v] and v not in out:
+            out.append(int(v))
+        i += 1
+    return out
+
+
+def bfs_extras(gg, torch, peak, scale=22):
+    """BFS direction-optimising on an undirected R-MAT graph (each generated
+    edge inserted both ways), 64 sources of nonzero degree; TEPS by the
+    Graph500 convention (sum of the reached vertices' degrees / 2 per search),
+    harmonic mean over sources."""
+    import numpy as np
+    from oracle import oracle_ctypes as O
+
+    g = gg.Graph.rmat(scale, 16, seed=SEED, symmetric=True)
+    V, E = g.V, g.E
+    dg = gg.DeviceGraph(g, gg.MAP_IN | gg.MAP_OUT)
+    deg = g.views()["out_degree"]
+    srcs = splitmix_sources(V, deg, 64, SEED + 1)
+    for s in srcs[:3]:
+        dg.bfs(s, "do")
+    teps, ms_all, bytes_all, bu = [], [], [], 0
+    for s in srcs:
+        t0 = time.perf_counter()
+        parents, dist, r = dg.bfs(s, "do", copy_out=True)
+        dt = time.perf_counter() - t0
+        reached = (dist > 0) | (np.arange(V) == s)
+        edges = float(deg[reached].astype(np.int64).sum()) / 2.0
+        teps.append(edges / dt)
+        ms_all.append(dt * 1e3)
+        # ids + frontier/parent probes per examined edge, parent + level per
+        # reached vertex, visited + next bitmaps per bottom-up step
+        bytes_all.append(8.0 * r["edges_examined"] + 8.0 * int(reached.sum()) + r["bottom_up_steps"] * V / 4.0)
+        bu += r["bottom_up_steps"]
+    # levels of one search against the oracle (bit-exact)
+    v = g.views()
+    out_off = np.append(v["out_edges_idx"], np.uint32(E))
+    in_off = np.append(v["in_edges_idx"], np.uint32(E))
+    o = O.Csr.from_arrays(V, E, out_off, v["out_adj"], in_off, v["in_adj"])
+    t0 = time.perf_counter()
+    _, rd, info = O.bfs(o, 2, srcs[0], nthreads=os.cpu_count() or 1)
+    cpu_s = time.perf_counter() - t0
+    _, dist0, _ = dg.bfs(srcs[0], "do")
+    hm = len(teps) / sum(1.0 / t for t in teps)
+    out = {"graph": f"R-MAT-{scale} undirected, V={V}, E={E} directed", "sources": len(srcs),
+           "gteps_harmonic": hm / 1e9, "ms_mean": float(np.mean(ms_all)),
+           "alg_gbs_mean": float(np.mean([b / (m / 1e3) for b, m in zip(bytes_all, ms_all)]) / 1e9),
+           "hbm_frac_mean": float(np.mean([b / (m / 1e3) for b, m in zip(bytes_all, ms_all)]) / 1e9 / peak),
+           "bottom_up_steps_mean": bu / len(srcs),
+           "levels_match_oracle": bool(np.array_equal(dist0, rd)),
+           "cpu_baseline_gteps": float(deg[(rd > 0) | (np.arange(V) == srcs[0])].astype(np.int64).sum()) / 2.0 / cpu_s / 1e9}
+    dg.free()
+    g.free()
+    return out
+
+
+def spmv_extras(gg, graph, V, E, sptr, torch, peak):
+    """SpMV pull over the weighted R-MAT graph, FP32 and BF16 storage of x and
+    the weights (FP32 products and sums), 30 products per run; L1 / L-inf vs
+    the FP64 oracle."""
+    import numpy as np
+    from oracle import oracle_ctypes as O
+
+    dg = gg.DeviceGraph(graph, gg.MAP_IN | gg.MAP_IN_W)
+    v = graph.views()
+    out_off = np.append(v["out_edges_idx"], np.uint32(E))
+    in_off = np.append(v["in_edges_idx"], np.uint32(E))
+    o = O.Csr.from_arrays(V, E, out_off, v["out_adj"], in_off, v["in_adj"], v["out_w"], v["in_w"])
+    out = {}
+    x0 = None
+    for storage, s in [("f32", 4), ("bf16", 2)]:
+        dg.spmv("pull", storage=storage, iterations=2, copy_out=False, stream=sptr)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        reps, kms = 5, 0.0
+        for _ in range(reps):
+            _, _, r = dg.spmv("pull", storage=storage, iterations=ITERS, copy_out=False, profile=True, stream=sptr)
+            kms += r["spmv_ms"] / max(r["spmv_launches"], 1)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        x, y, _ = dg.spmv("pull", storage=storage, iterations=1, stream=sptr)
+        if x0 is None:
+            x0 = x
+            exact = O.spmv_f64(o, x)
+        alg = 4 * E + s * E + 4 * (V + 1) + s * V + 4 * V
+        out[f"spmv_pull_{storage}"] = {
+            "gteps": E * ITERS / (ms / 1e3) / 1e9, "launch_ms": kms / reps,
+            "hbm_frac": alg / (kms / reps / 1e3) / 1e9 / peak,
+            "l1_relative": float(np.abs(y - exact).sum() / np.abs(exact).sum()),
+            "linf_relative": float(np.abs(y - exact).max() / np.abs(exact).max())}
+    dg.free()
+    return out
+
+
 def extras(gg, graph, dg, V, E, sptr, torch, peak):
     """Side measurements on the same box: BF16 / FP16 storage GTEPS with L1
-    and L-inf error vs the FP64 oracle."""
+    and L-inf error vs the FP64 oracle, SpMV pull, BFS."""
     import numpy as np
     from oracle import oracle_ctypes as O
 
@@ -337,6 +445,9 @@ def extras(gg, graph, dg, V, E, sptr, torch, peak):
             "hbm_frac": pr_bytes(V, E, s) / (launch_ms / 1e3) / 1e9 / peak,
             "l1_vs_fp64": l1, "linf_vs_fp64": linf, "l1_relative": l1 / float(np.abs(exact).sum())}
     out["fp64_oracle_s"] = round(f64_s, 2)
+    out.update(spmv_extras(gg, graph, V, E, sptr, torch, peak))
+    dg.free()
+    out["bfs_do"] = bfs_extras(gg, torch, peak)
     return out
 
 
