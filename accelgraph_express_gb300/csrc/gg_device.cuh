@@ -85,6 +85,58 @@ __device__ __forceinline__ void block_sum2(double &a, uint32_t &b)
     }
 }
 
+/* Asynchronous 4-byte global -> shared copy (cp.async, cached in L1): the
+ * issuing thread holds no register for it and does not stall until
+ * cp_async_wait_all.  Both addresses must be 4-byte aligned. */
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+/* Asynchronous 16-byte copy through L2 only (cp.async.cg), so staged
+ * streams do not displace the L1-resident gather data.  Both addresses must
+ * be 16-byte aligned. */
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+/* Wait for this thread's cp.async copies; a __syncwarp after it makes every
+ * lane's copies visible to the whole warp. */
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+/* Streaming 4-byte load that does not allocate in L1 (the neighbour ids are
+ * read once per launch). */
+__device__ __forceinline__ uint32_t ldg_stream(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
+/*
+ * One warp copies src[i0 .. i0+n) into shared memory asynchronously, word
+ * i0+k landing at dst[(i0 & 3) + k]; dst must be 16-byte aligned with room
+ * for n + 3 words.  From a 16-byte-aligned src the body moves in 16-byte
+ * chunks starting at the aligned word at or below i0 (words before i0 are
+ * copied too, never words at or past i0+n); the last 1-3 words and any
+ * unaligned src go word by word.  Returns i0 & 3.
+ */
+__device__ __forceinline__ uint32_t stage_words(uint32_t *dst, const uint32_t *src, uint32_t i0, uint32_t n,
+                                                uint32_t lane)
+{
+    const uint32_t first = i0 & 3u;
+    if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0)
+    {
+        const uint32_t base = i0 - first, total = first + n, full = total >> 2;
+        for (uint32_t c = lane; c < full; c += 32) cp_async16(dst + 4u * c, src + base + 4u * c);
+        if (lane < (total & 3u)) cp_async4(dst + 4u * full + lane, src + base + 4u * full + lane);
+    }
+    else
+        for (uint32_t k = lane; k < n; k += 32) cp_async4(dst + first + k, src + i0 + k);
+    return first;
+}
+
 __device__ __forceinline__ void atomic_add_acc(float *p, float v) { atomicAdd(p, v); }
 __device__ __forceinline__ void atomic_add_acc(unsigned long long *p, unsigned long long v) { atomicAdd(p, v); }
 __device__ __forceinline__ float atomic_take(float *p) { return atomicExch(p, 0.0f); }
@@ -99,12 +151,11 @@ __device__ __forceinline__ unsigned long long atomic_take(unsigned long long *p)
  * multiplication", SC'16).  coord[t] = (rows ended, edges consumed) at
  * diagonal t*GG_TILE_ITEMS.  Each tile is consumed by one warp.
  *
- * A row whose items fall in more than one tile is finished by the last tile
- * to arrive: every participating tile adds its partial into acc[first tile
- * of the row] and bumps cnt[first tile]; the tile that brings the count to
- * the number of participants takes the total (resetting both) and runs the
- * row epilogue.  No tile waits for another.  A row lying wholly in one tile
- * is finished by that tile alone (the tile before it also lists it, as its
+ * A row whose items fall in more than one tile is finished after the launch:
+ * every participating tile adds its partial into acc[first tile of the row]
+ * and warp_pull_fixup, a separate launch, runs the row epilogue on the
+ * total.  No tile waits for another.  A row lying wholly in one tile is
+ * finished by that tile alone (the tile before it also lists it, as its
  * partial last row, when it ends exactly at the row's first edge).
  */
 
@@ -151,17 +202,29 @@ struct TileGeom
  *                                       value of edge e with neighbour u
  *                                       (the gather)
  *   RowPre prefetch(uint32_t row) const;
+ *                                       per-row data, loaded directly
+ *   static constexpr uint32_t PRE_WORDS;
+ *   void stage(uint32_t i0, uint32_t n, uint32_t lane, uint32_t *s, uint32_t stride) const;
+ *                                       the same data for rows i0..i0+n-1
+ *                                       as PRE_WORDS planes of 32-bit words
+ *                                       (plane p at s + p*stride), each
+ *                                       copied with stage_words
+ *   RowPre unstage(uint32_t row, const uint32_t *s, uint32_t j, uint32_t stride) const;
+ *                                       row's data from index j of the planes
  *   void finish(uint32_t row, Acc sum, const RowPre &pre, double &err, uint32_t &act);
  *                                       row epilogue
  *   void warp_end(double err, uint32_t act);
  *                                       called by every lane at the end
  *                                       (warp reductions and atomics)
  * Per tile every load is issued up front, together: the neighbour ids (one
- * warp instruction covering 32 consecutive edges), the tile's row offsets,
- * the first 32 rows' epilogue data, and the next tile's coordinates; then
- * the neighbour values.  With the value gather saturating L2 sector
- * requests, each extra dependent round trip per tile would cost a full
- * queueing latency.  The values are staged in shared memory and consumed
+ * warp instruction covering 32 consecutive edges), the next tile's
+ * coordinates, and, as asynchronous copies into shared memory, the tile's
+ * row offsets and every row's epilogue data; then the neighbour values.  A
+ * tile holds up to GG_TILE_ITEMS + 1 rows (R-MAT graphs have long runs of
+ * in-degree-0 and -1 vertices), and the copies keep their loads from forming
+ * one dependent round trip per 32 rows.  With the value gather saturating L2
+ * sector requests, each extra dependent round trip per tile would cost a
+ * full queueing latency.  The values are staged in shared memory and consumed
  * along the merge path (GG_TILE_IPT items per lane).  A row ended inside a
  * lane is stored directly; the partial sum of the row open at the end of
  * each lane is combined across lanes by a warp-shuffle segmented scan, so no
@@ -176,15 +239,21 @@ __device__ __forceinline__ void warp_pull(const uint32_t *__restrict__ off, cons
                                           typename Op::Acc *g_acc, Op &op)
 {
     typedef typename Op::Acc Acc;
-    typedef typename Op::RowPre RowPre;
     constexpr uint32_t TW = 32 * IPT;
-    __shared__ uint32_t sm_off[WARPS][TW + 2];
+    /* staged planes hold up to 3 words before the tile's first row
+     * (stage_words) and stay 16-byte aligned; an Op without per-row data
+     * keeps a token 4-word array */
+    constexpr uint32_t OFFW = TW + 8, PREW = TW + 4;
+    constexpr uint32_t PRE_ALL = Op::PRE_WORDS > 0 ? Op::PRE_WORDS * PREW : 4;
+    __shared__ __align__(16) uint32_t sm_off[WARPS][OFFW];
+    __shared__ __align__(16) uint32_t sm_pre[WARPS][PRE_ALL];
     __shared__ Acc sm_val[WARPS][TW];
     __shared__ Acc sm_row[WARPS][TW + 1];
     const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t *s_off = sm_off[w];
+    uint32_t *const s_offb = sm_off[w];
     Acc *s_val = sm_val[w];
     Acc *s_row = sm_row[w];
+    uint32_t *const s_pre = sm_pre[w];
     double err = 0.0;
     uint32_t act = 0;
     const uint32_t nw = gridDim.x * WARPS;
@@ -212,12 +281,12 @@ __device__ __forceinline__ void warp_pull(const uint32_t *__restrict__ off, cons
         for (int g = 0; g < IPT; g++)
         {
             const uint32_t e = t.j0 + lane + 32u * g;
-            if (e < t.j1) id[g] = __ldg(adj + e);
+            if (e < t.j1) id[g] = ldg_stream(adj + e);
         }
-        for (uint32_t k = lane; k <= t.nrows; k += 32)
-            s_off[k] = off[t.i0 + k];
-        RowPre pre0{};
-        if (lane < t.nrows) pre0 = op.prefetch(t.i0 + lane);
+        /* row i0+k of every staged plane sits at index shift+k */
+        const uint32_t shift = stage_words(s_offb, off, t.i0, t.nrows + 1, lane);
+        const uint32_t *s_off = s_offb + shift;
+        if constexpr (Op::PRE_WORDS > 0) op.stage(t.i0, t.nrows, lane, s_pre, PREW);
         {
             const uint32_t nt = tile + nw;
             if (nt < ntiles)
@@ -232,6 +301,7 @@ __device__ __forceinline__ void warp_pull(const uint32_t *__restrict__ off, cons
             const uint32_t e = t.j0 + lane + 32u * g;
             if (e < t.j1) s_val[e - t.j0] = op.load1(e, id[g]);
         }
+        cp_async_wait_all();
         __syncwarp();
 
         /* merge-path consumption; the first row a lane ends may have begun
@@ -307,7 +377,7 @@ __device__ __forceinline__ void warp_pull(const uint32_t *__restrict__ off, cons
             const uint32_t t_first = (uint32_t)(first / TW), t_last = (uint32_t)(last / TW);
             if (t_first == t_last)
             {
-                if (t_first == tile) op.finish(r, s_row[k], k == lane ? pre0 : op.prefetch(r), err, act);
+                if (t_first == tile) op.finish(r, s_row[k], op.unstage(r, s_pre, shift + k, PREW), err, act);
             }
             else
             {
@@ -362,24 +432,18 @@ __device__ __forceinline__ void warp_push(const uint32_t *__restrict__ off, cons
                                           uint32_t V, const uint2 *__restrict__ coord, uint32_t ntiles, Op &op)
 {
     constexpr uint32_t TW = 32 * IPT;
-    __shared__ uint32_t sm_off[WARPS][TW + 2];
-    __shared__ uint32_t sm_adj[WARPS][TW];
+    __shared__ __align__(16) uint32_t sm_off[WARPS][TW + 8];
+    __shared__ __align__(16) uint32_t sm_adj[WARPS][TW + 4];
     const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t *s_off = sm_off[w];
-    uint32_t *s_adj = sm_adj[w];
     const uint32_t nw = gridDim.x * WARPS;
     for (uint32_t tile = blockIdx.x * WARPS + w; tile < ntiles; tile += nw)
     {
         TileGeom t;
         t.load(coord, tile, V);
-#pragma unroll
-        for (int g = 0; g < IPT; g++)
-        {
-            const uint32_t e = t.j0 + lane + 32u * g;
-            if (e < t.j1) s_adj[e - t.j0] = __ldg(adj + e);
-        }
-        for (uint32_t k = lane; k <= t.nrows; k += 32)
-            s_off[k] = off[t.i0 + k];
+        /* edge j0+i at s_adj[i], row i0+k's offset at s_off[k] */
+        const uint32_t *s_adj = sm_adj[w] + stage_words(sm_adj[w], adj, t.j0, t.nedges, lane);
+        const uint32_t *s_off = sm_off[w] + stage_words(sm_off[w], off, t.i0, t.nrows + 1, lane);
+        cp_async_wait_all();
         __syncwarp();
         const uint32_t d = lane * IPT;
         if (d < t.nitems)

@@ -15,10 +15,12 @@
  * GG_TILE_ITEMS = 32 * GG_TILE_IPT merge items (row ends + edges), so no
  * CTA-wide barrier sits on the hot path.  IPT is odd so that the lanes'
  * reads of the staged values hit distinct shared-memory banks.  Kernels run
- * persistent CTAs of GG_TILE_WARPS warps that stride over the tiles. */
+ * persistent CTAs of GG_TILE_WARPS warps that stride over the tiles; small
+ * CTAs keep each one's static shared staging (offsets, values, row sums and
+ * per-row epilogue words for every warp) under 48 KB. */
 #define GG_TILE_IPT 11
 #define GG_TILE_ITEMS (32 * GG_TILE_IPT)
-#define GG_TILE_WARPS 8
+#define GG_TILE_WARPS 4
 #define GG_TILE_NT (32 * GG_TILE_WARPS)
 
 /* Slack after every edge array so 16-byte vector loads of the last group
@@ -111,8 +113,16 @@ gg_status gg_launch_tile_coords(const uint32_t *off, uint32_t V, uint32_t E, uin
 gg_status gg_launch_to_half(const float *src, void *dst, size_t n, int storage, cudaStream_t s);
 int gg_sm_count();
 /* persistent grid for a tile kernel: one CTA per resident slot, no more
- * CTAs than tiles need */
-int gg_persistent_grid(const void *kernel, uint32_t ntiles);
+ * CTAs than tiles need.  ctas_per_sm > 0 caps the resident CTAs per SM and
+ * sets the kernel's shared-memory carve-out to just hold them, so the rest
+ * of each SM's combined L1/shared array caches the gathered values. */
+int gg_persistent_grid(const void *kernel, uint32_t ntiles, int ctas_per_sm = 0);
+
+/* Resident CTAs per SM of the pull gathers.  Measured on GB300 for R-MAT
+ * scale 22-24 PageRank and SpMV pulls: fewer CTAs leave more L1 for the hot
+ * in-neighbours' values (skewed graphs concentrate most gathers on a few
+ * thousand sectors); more hide more latency. */
+#define GG_PULL_CTAS_PER_SM 5
 /* smallest float f with (double)f >= x, and largest float f with (double)f <= x */
 float gg_float_ceil(double x);
 float gg_float_floor(double x);

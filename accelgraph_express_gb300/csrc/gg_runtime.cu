@@ -67,7 +67,7 @@ extern "C" void gg_set_wait_timeout_ms(uint32_t ms) { g_wait_timeout_ms.store(ms
 
 int gg_sm_count() { return g_sm_count > 0 ? g_sm_count : 152; }
 
-int gg_persistent_grid(const void *kernel, uint32_t ntiles)
+int gg_persistent_grid(const void *kernel, uint32_t ntiles, int ctas_per_sm)
 {
     static std::mutex mu;
     static const void *keys[64];
@@ -80,12 +80,31 @@ int gg_persistent_grid(const void *kernel, uint32_t ntiles)
             if (keys[i] == kernel) bps = vals[i];
         if (!bps)
         {
-            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, GG_TILE_NT, 0);
+            cudaError_t e = cudaSuccess;
+            if (ctas_per_sm > 0)
+            {
+                /* carve-out: the smallest share of the SM's shared-memory
+                 * capacity that holds ctas_per_sm CTAs (1 KB reserved each) */
+                cudaFuncAttributes fa;
+                int dev = 0, smem_sm = 0;
+                e = cudaFuncGetAttributes(&fa, kernel);
+                if (e == cudaSuccess) e = cudaGetDevice(&dev);
+                if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+                if (e == cudaSuccess && smem_sm > 0)
+                {
+                    const double need = (double)ctas_per_sm * (double)(fa.sharedSizeBytes + 1024);
+                    int pct = (int)ceil(100.0 * need / (double)smem_sm);
+                    pct = pct < 1 ? 1 : (pct > 100 ? 100 : pct);
+                    e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+                }
+            }
+            if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, GG_TILE_NT, 0);
             if (e != cudaSuccess || bps < 1)
             {
                 cudaGetLastError();
                 bps = 1;
             }
+            if (ctas_per_sm > 0 && bps > ctas_per_sm) bps = ctas_per_sm;
             if (getenv("GG_DEBUG"))
                 fprintf(stderr, "gg: kernel %p: %d CTAs of %d threads per SM (%s)\n", kernel, bps, GG_TILE_NT,
                         cudaGetErrorString(e));

@@ -215,8 +215,18 @@ struct PullOp : PrCommon
     uint32_t tmax = 0; /* this thread's largest new contribution (quantised modes) */
 
     struct RowPre { float rank; uint32_t deg; };
+    static constexpr uint32_t PRE_WORDS = 2;
     __device__ __forceinline__ Acc load1(uint32_t, uint32_t u) const { return decode<K>(cin[u]); }
     __device__ __forceinline__ RowPre prefetch(uint32_t r) const { return RowPre{rank[r], outdeg[r]}; }
+    __device__ __forceinline__ void stage(uint32_t i0, uint32_t n, uint32_t lane, uint32_t *s, uint32_t stride) const
+    {
+        stage_words(s, reinterpret_cast<const uint32_t *>(rank), i0, n, lane);
+        stage_words(s + stride, outdeg, i0, n, lane);
+    }
+    __device__ __forceinline__ RowPre unstage(uint32_t, const uint32_t *s, uint32_t j, uint32_t stride) const
+    {
+        return RowPre{__uint_as_float(s[j]), s[stride + j]};
+    }
     __device__ __forceinline__ void finish(uint32_t r, Acc sum, const RowPre &pre, double &err, uint32_t &act)
     {
         float qscale = 0.0f;
@@ -430,8 +440,22 @@ struct DdPullOp : PrCommon
     uint8_t *wl_next;
     const uint32_t *out_off, *out_adj;
     struct RowPre { float rank; uint32_t on; };
+    static constexpr uint32_t PRE_WORDS = 2;
     __device__ __forceinline__ float load1(uint32_t, uint32_t u) const { return cf[u]; }
     __device__ __forceinline__ RowPre prefetch(uint32_t r) const { return RowPre{rank[r], wl_curr[r]}; }
+    /* the flag bytes travel as the aligned 4-byte words holding them: word
+     * c of the second plane holds rows (i0 & ~3) + 4c .. +3 (the worklists
+     * are allocated with 16 bytes of slack past V) */
+    __device__ __forceinline__ void stage(uint32_t i0, uint32_t n, uint32_t lane, uint32_t *s, uint32_t stride) const
+    {
+        stage_words(s, reinterpret_cast<const uint32_t *>(rank), i0, n, lane);
+        const uint32_t base = i0 & ~3u, nw = ((i0 & 3u) + n + 3u) >> 2;
+        for (uint32_t c = lane; c < nw; c += 32) cp_async4(s + stride + c, wl_curr + base + 4u * c);
+    }
+    __device__ __forceinline__ RowPre unstage(uint32_t, const uint32_t *s, uint32_t j, uint32_t stride) const
+    {
+        return RowPre{__uint_as_float(s[j]), (s[stride + (j >> 2)] >> (8u * (j & 3u))) & 0xffu};
+    }
     __device__ __forceinline__ void finish(uint32_t r, float sum, const RowPre &pre, double &err, uint32_t &act)
     {
         if (!pre.on) return;
@@ -616,7 +640,7 @@ gg_status run_pull(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
         op.cout = cb[(it + 1) & 1];
         op.cf = (float *)cf;
         GG_CHECK(timed_begin(R));
-        k_pr_pull<K><<<gg_persistent_grid((const void *)k_pr_pull<K>, t->ntiles), GG_TILE_NT, 0, R.s>>>(
+        k_pr_pull<K><<<gg_persistent_grid((const void *)k_pr_pull<K>, t->ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0, R.s>>>(
             g->in_off, g->in_adj, t->coord, t->ntiles, (Acc *)t->acc, op);
         k_pr_pull_fixup<K><<<fixup_grid(t->ntiles), 256, 0, R.s>>>(g->in_off, t->coord, t->ntiles, (Acc *)t->acc, op);
         GG_CHECK(timed_end(R));
@@ -723,7 +747,7 @@ gg_status run_dd(Run &R, int mode, IterRec *rec, float *rank, uint32_t iters, fl
             op.cf = (const float *)cf; op.wl_curr = wl[it & 1]; op.wl_next = wl[(it + 1) & 1];
             op.out_off = g->out_off; op.out_adj = g->out_adj;
             GG_CHECK(timed_begin(R));
-            k_dd_pull<<<gg_persistent_grid((const void *)k_dd_pull, t->ntiles), GG_TILE_NT, 0, R.s>>>(
+            k_dd_pull<<<gg_persistent_grid((const void *)k_dd_pull, t->ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0, R.s>>>(
                 g->in_off, g->in_adj, t->coord, t->ntiles, (float *)t->acc, op);
             k_dd_pull_fixup<<<fixup_grid(t->ntiles), 256, 0, R.s>>>(g->in_off, t->coord, t->ntiles, (float *)t->acc, op);
             GG_CHECK(timed_end(R));

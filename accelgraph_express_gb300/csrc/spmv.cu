@@ -34,6 +34,8 @@ struct SpmvPullOp
     const T *x;
     float *y;
     struct RowPre {};
+    static constexpr uint32_t PRE_WORDS = 0;
+    __device__ __forceinline__ RowPre unstage(uint32_t, const uint32_t *, uint32_t, uint32_t) const { return RowPre{}; }
     __device__ __forceinline__ float load1(uint32_t e, uint32_t u) const
     {
         return __fmul_rn(to_f32(w[e]), to_f32(x[u]));
@@ -65,6 +67,8 @@ struct SpmvPullFxOp
     const uint32_t *x32;
     float *y;
     struct RowPre {};
+    static constexpr uint32_t PRE_WORDS = 0;
+    __device__ __forceinline__ RowPre unstage(uint32_t, const uint32_t *, uint32_t, uint32_t) const { return RowPre{}; }
     __device__ __forceinline__ unsigned long long load1(uint32_t e, uint32_t u) const
     {
         return ((unsigned long long)x32[u] * fx_from_float(w[e], 65536.0, 0xffffffffu)) >> 16;
@@ -213,7 +217,7 @@ gg_status spmv_fp(gg_graph *g, const gg_spmv_params *p, const float *x_dev, floa
         if (pull)
         {
             SpmvPullOp<T> op{w, xv, y};
-            k_spmv_pull<T><<<gg_persistent_grid((const void *)k_spmv_pull<T>, t->ntiles), GG_TILE_NT, 0, s>>>(
+            k_spmv_pull<T><<<gg_persistent_grid((const void *)k_spmv_pull<T>, t->ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0, s>>>(
                 g->in_off, g->in_adj, t->coord, t->ntiles, V, (float *)t->acc, op);
             k_spmv_pull_fixup<T><<<grid_v(t->ntiles), 256, 0, s>>>(g->in_off, t->coord, t->ntiles, V, (float *)t->acc, op);
             launches++;
@@ -301,7 +305,7 @@ extern "C" gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *
                 if (pull)
                 {
                     SpmvPullFxOp op{g->in_w, (const uint32_t *)xq, (float *)yv};
-                    k_spmv_pull_fx<<<gg_persistent_grid((const void *)k_spmv_pull_fx, t->ntiles), GG_TILE_NT, 0, s>>>(
+                    k_spmv_pull_fx<<<gg_persistent_grid((const void *)k_spmv_pull_fx, t->ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0, s>>>(
                         g->in_off, g->in_adj, t->coord, t->ntiles, V, (unsigned long long *)t->acc, op);
                     k_spmv_pull_fx_fixup<<<grid_v(t->ntiles), 256, 0, s>>>(g->in_off, t->coord, t->ntiles, V,
                                                                           (unsigned long long *)t->acc, op);
@@ -425,7 +429,7 @@ extern "C" gg_status gg_spmv_pull_noalloc(uint32_t V, uint32_t E, const uint32_t
     GG_CUDA(cudaMemsetAsync(acc, 0, (size_t)ntiles * sizeof(float), s));
     GG_CHECK(gg_launch_tile_coords(in_off, V, E, ntiles, coord, s));
     SpmvPullOp<float> op{w, x, y};
-    k_spmv_pull<float><<<gg_persistent_grid((const void *)k_spmv_pull<float>, ntiles), GG_TILE_NT, 0, s>>>(
+    k_spmv_pull<float><<<gg_persistent_grid((const void *)k_spmv_pull<float>, ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0, s>>>(
         in_off, in_src, coord, ntiles, V, acc, op);
     k_spmv_pull_fixup<float><<<grid_v(ntiles), 256, 0, s>>>(in_off, coord, ntiles, V, acc, op);
     GG_CUDA(cudaGetLastError());
