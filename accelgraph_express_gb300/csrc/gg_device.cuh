@@ -55,6 +55,21 @@ __device__ __forceinline__ float fx_to_float(uint64_t f, double inv_scale)
     return __double2float_rn(__dmul_rn(__ull2double_rn(f), inv_scale));
 }
 
+/* Clear a sum slot that was just read.  The store is made to wait for the
+ * load (a branch on the value read): on GB300 a store issued to a sector
+ * whose L2 read miss is still outstanding stalls that sector, and a pass
+ * that read and cleared 64 MB with an independent store ran 7x slower than
+ * with this dependent one.  Slots already zero are left alone (-0.0 stays;
+ * the atomics that later add into it give the same sums). */
+__device__ __forceinline__ void clear_after_read(float *p, float seen)
+{
+    if (seen != 0.0f) *p = 0.0f;
+}
+__device__ __forceinline__ void clear_after_read(unsigned long long *p, unsigned long long seen)
+{
+    if (seen != 0ull) *p = 0ull;
+}
+
 /* ---- reductions --------------------------------------------------------- */
 
 template <class T> __device__ __forceinline__ T warp_sum(T v)
@@ -151,12 +166,9 @@ __device__ __forceinline__ unsigned long long atomic_take(unsigned long long *p)
  * multiplication", SC'16).  coord[t] = (rows ended, edges consumed) at
  * diagonal t*GG_TILE_ITEMS.  Each tile is consumed by one warp.
  *
- * A row whose items fall in more than one tile is finished after the launch:
- * every participating tile adds its partial into acc[first tile of the row]
- * and warp_pull_fixup, a separate launch, runs the row epilogue on the
- * total.  No tile waits for another.  A row lying wholly in one tile is
- * finished by that tile alone (the tile before it also lists it, as its
- * partial last row, when it ends exactly at the row's first edge).
+ * A row whose items fall in more than one tile gets each tile's partial
+ * sum added atomically; a row lying wholly in one tile is stored by that
+ * tile.  No tile waits for another.
  */
 
 __device__ __forceinline__ uint2 merge_path_search(uint32_t diag, const uint32_t *row_end, uint32_t nrows,
@@ -194,131 +206,190 @@ struct TileGeom
     }
 };
 
+/* Gather loads issued where they are written (inline PTX is not moved), so a
+ * tile's loads stay in flight while the previous tile is reduced; the
+ * values are read-only for the launch (non-coherent path). */
+__device__ __forceinline__ float ldg_val(const float *p)
+{
+    float v;
+    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint32_t ldg_val(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ unsigned long long ldg_val(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.global.nc.u64 %0, [%1];" : "=l"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint16_t ldg_val(const uint16_t *p)
+{
+    uint16_t v;
+    asm volatile("ld.global.nc.u16 %0, [%1];" : "=h"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint8_t ldg_val(const uint8_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.global.nc.u8 %0, [%1];" : "=r"(v) : "l"(p));
+    return (uint8_t)v;
+}
+__device__ __forceinline__ __nv_bfloat16 ldg_val(const __nv_bfloat16 *p)
+{
+    return __ushort_as_bfloat16(ldg_val(reinterpret_cast<const uint16_t *>(p)));
+}
+__device__ __forceinline__ __half ldg_val(const __half *p) { return __ushort_as_half(ldg_val(reinterpret_cast<const uint16_t *>(p))); }
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+/* wait until at most one committed group of this thread is still pending */
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+template <int IPT>
+__device__ __forceinline__ void load_ids(uint32_t (&id)[IPT], const uint32_t *adj, uint32_t j0, uint32_t j1,
+                                         uint32_t lane)
+{
+#pragma unroll
+    for (int g = 0; g < IPT; g++)
+    {
+        const uint32_t e = j0 + lane + 32u * g;
+        if (e < j1) id[g] = ldg_stream(adj + e);
+    }
+}
+
+/* rows of a tile with at least one item in it: i0 .. last row (row i1 when
+ * i1 < V has items here but ends in a later tile) */
+__device__ __forceinline__ uint32_t tile_rows(uint2 c0, uint2 c1, uint32_t V)
+{
+    const uint32_t last_row = c1.x < V ? c1.x : V - 1;
+    return (c1.x < V || c0.x < V) ? last_row - c0.x + 1 : 0;
+}
+
 /*
- * The pull engine (persistent warps).  Op supplies:
- *   typedef Acc;                        float or unsigned long long
- *   typedef RowPre;                     per-row data the epilogue needs
- *   Acc load1(uint32_t e, uint32_t u) const;
- *                                       value of edge e with neighbour u
- *                                       (the gather)
- *   RowPre prefetch(uint32_t row) const;
- *                                       per-row data, loaded directly
- *   static constexpr uint32_t PRE_WORDS;
- *   void stage(uint32_t i0, uint32_t n, uint32_t lane, uint32_t *s, uint32_t stride) const;
- *                                       the same data for rows i0..i0+n-1
- *                                       as PRE_WORDS planes of 32-bit words
- *                                       (plane p at s + p*stride), each
- *                                       copied with stage_words
- *   RowPre unstage(uint32_t row, const uint32_t *s, uint32_t j, uint32_t stride) const;
- *                                       row's data from index j of the planes
- *   void finish(uint32_t row, Acc sum, const RowPre &pre, double &err, uint32_t &act);
- *                                       row epilogue
- *   void warp_end(double err, uint32_t act);
- *                                       called by every lane at the end
- *                                       (warp reductions and atomics)
- * Per tile every load is issued up front, together: the neighbour ids (one
- * warp instruction covering 32 consecutive edges), the next tile's
- * coordinates, and, as asynchronous copies into shared memory, the tile's
- * row offsets and every row's epilogue data; then the neighbour values.  A
- * tile holds up to GG_TILE_ITEMS + 1 rows (R-MAT graphs have long runs of
- * in-degree-0 and -1 vertices), and the copies keep their loads from forming
- * one dependent round trip per 32 rows.  With the value gather saturating L2
- * sector requests, each extra dependent round trip per tile would cost a
- * full queueing latency.  The values are staged in shared memory and consumed
- * along the merge path (GG_TILE_IPT items per lane).  A row ended inside a
- * lane is stored directly; the partial sum of the row open at the end of
- * each lane is combined across lanes by a warp-shuffle segmented scan, so no
- * shared-memory atomics are needed.  Rows whose items span tiles add their
- * in-tile partial to acc[first tile of the row] with a fire-and-forget
- * reduction and are finished by warp_pull_fixup after the launch.  Only
- * __syncwarp orders the phases.
+ * The pull engine: sums[r] = sum over the CSC row r of op's edge terms, for
+ * every row, by persistent warps over merge-path tiles.  Op supplies:
+ *   typedef Acc;                       float or unsigned long long
+ *   typedef Raw;                       what one edge's gather loads
+ *   Raw load(uint32_t e, uint32_t u) const;
+ *                                      issue the loads of edge e with
+ *                                      neighbour u (ldg_val)
+ *   Acc value(const Raw &r) const;     the edge term, computed where the
+ *                                      loads are first used
+ * sums must be zero on entry for rows whose items span tiles: a row lying in
+ * one tile is stored, the partials of a spanning row are added atomically
+ * (the row epilogues that read sums clear it again).
+ *
+ * Each warp runs its tiles as a software pipeline: while tile A is reduced,
+ * tile B's gathers and tile C's neighbour ids are in flight and tile B's row
+ * offsets are landing in shared memory (cp.async, double-buffered), so a
+ * tile's dependent load chain (ids, then values) overlaps the reduction of
+ * the tile before it.  A tile is reduced along the merge path
+ * (GG_TILE_IPT items per lane): a row ended inside a lane is stored
+ * directly; the partial sum of the row open at the end of each lane is
+ * combined across lanes by a warp-shuffle segmented scan.  Only __syncwarp
+ * orders the phases.
  */
 template <int IPT, int WARPS, class Op>
-__device__ __forceinline__ void warp_pull(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                          uint32_t V, const uint2 *__restrict__ coord, uint32_t ntiles,
-                                          typename Op::Acc *g_acc, Op &op)
+__device__ __forceinline__ void warp_pull_sums(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                               uint32_t V, const uint2 *__restrict__ coord, uint32_t ntiles,
+                                               typename Op::Acc *sums, const Op &op)
 {
     typedef typename Op::Acc Acc;
+    typedef typename Op::Raw Raw;
     constexpr uint32_t TW = 32 * IPT;
-    /* staged planes hold up to 3 words before the tile's first row
-     * (stage_words) and stay 16-byte aligned; an Op without per-row data
-     * keeps a token 4-word array */
-    constexpr uint32_t OFFW = TW + 8, PREW = TW + 4;
-    constexpr uint32_t PRE_ALL = Op::PRE_WORDS > 0 ? Op::PRE_WORDS * PREW : 4;
-    __shared__ __align__(16) uint32_t sm_off[WARPS][OFFW];
-    __shared__ __align__(16) uint32_t sm_pre[WARPS][PRE_ALL];
+    /* staged offsets hold up to 3 words before the tile's first row
+     * (stage_words) and stay 16-byte aligned */
+    constexpr uint32_t OFFW = TW + 8;
+    __shared__ __align__(16) uint32_t sm_off[WARPS][2][OFFW];
     __shared__ Acc sm_val[WARPS][TW];
     __shared__ Acc sm_row[WARPS][TW + 1];
     const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t *const s_offb = sm_off[w];
     Acc *s_val = sm_val[w];
     Acc *s_row = sm_row[w];
-    uint32_t *const s_pre = sm_pre[w];
-    double err = 0.0;
-    uint32_t act = 0;
     const uint32_t nw = gridDim.x * WARPS;
     uint32_t tile = blockIdx.x * WARPS + w;
-    uint2 c0 = make_uint2(0, 0), c1 = make_uint2(0, 0);
-    if (tile < ntiles)
+    if (tile >= ntiles) return;
+
+    /* pipeline state: A = tile (gathers in flight in val, offsets staged in
+     * buffer buf), B = tile + nw (ids in flight in id, offsets staged in
+     * buf ^ 1), C = tile + 2nw (coordinates only) */
+    const uint2 zero2 = make_uint2(0, 0);
+    uint2 a0 = coord[tile], a1 = coord[tile + 1];
+    uint2 b0 = zero2, b1 = zero2, c0 = zero2, c1 = zero2;
+    if (tile + nw < ntiles) { b0 = coord[tile + nw]; b1 = coord[tile + nw + 1]; }
+    if (tile + 2 * nw < ntiles) { c0 = coord[tile + 2 * nw]; c1 = coord[tile + 2 * nw + 1]; }
+    uint32_t id[IPT];
+    Raw val[IPT];
+    load_ids<IPT>(id, adj, a0.y, a1.y, lane);
+    uint32_t buf = 0;
+    uint32_t shA = stage_words(sm_off[w][0], off, a0.x, tile_rows(a0, a1, V) + 1, lane);
+    cp_async_commit();
+    uint32_t shB = 0;
+    if (tile + nw < ntiles) shB = stage_words(sm_off[w][1], off, b0.x, tile_rows(b0, b1, V) + 1, lane);
+    cp_async_commit();
+#pragma unroll
+    for (int g = 0; g < IPT; g++)
     {
-        c0 = coord[tile];
-        c1 = coord[tile + 1];
+        const uint32_t e = a0.y + lane + 32u * g;
+        if (e < a1.y) val[g] = op.load(e, id[g]);
     }
+    if (tile + nw < ntiles) load_ids<IPT>(id, adj, b0.y, b1.y, lane);
+
     for (; tile < ntiles; tile += nw)
     {
-        TileGeom t;
-        t.i0 = c0.x; t.j0 = c0.y; t.i1 = c1.x; t.j1 = c1.y;
+        const bool hasB = tile + nw < ntiles, hasC = tile + 2 * nw < ntiles;
+        /* B's gathers, C's ids, D's coordinates */
+        Raw nv[IPT];
+        if (hasB)
         {
-            const uint32_t last_row = t.i1 < V ? t.i1 : V - 1;
-            t.nrows = (t.i1 < V || t.i0 < V) ? last_row - t.i0 + 1 : 0;
-            t.nedges = t.j1 - t.j0;
-            t.nitems = (t.i1 - t.i0) + t.nedges;
-        }
-        /* every load of this tile in flight together (nedges <= TW,
-         * nrows <= TW + 1) */
-        uint32_t id[IPT];
 #pragma unroll
-        for (int g = 0; g < IPT; g++)
-        {
-            const uint32_t e = t.j0 + lane + 32u * g;
-            if (e < t.j1) id[g] = ldg_stream(adj + e);
-        }
-        /* row i0+k of every staged plane sits at index shift+k */
-        const uint32_t shift = stage_words(s_offb, off, t.i0, t.nrows + 1, lane);
-        const uint32_t *s_off = s_offb + shift;
-        if constexpr (Op::PRE_WORDS > 0) op.stage(t.i0, t.nrows, lane, s_pre, PREW);
-        {
-            const uint32_t nt = tile + nw;
-            if (nt < ntiles)
+            for (int g = 0; g < IPT; g++)
             {
-                c0 = coord[nt];
-                c1 = coord[nt + 1];
+                const uint32_t e = b0.y + lane + 32u * g;
+                if (e < b1.y) nv[g] = op.load(e, id[g]);
             }
         }
+        if (hasC) load_ids<IPT>(id, adj, c0.y, c1.y, lane);
+        uint2 d0 = zero2, d1 = zero2;
+        if (tile + 3 * nw < ntiles)
+        {
+            d0 = coord[tile + 3 * nw];
+            d1 = coord[tile + 3 * nw + 1];
+        }
+
+        /* tile A */
+        const uint32_t i0 = a0.x, j0 = a0.y, i1 = a1.x, j1 = a1.y;
+        const uint32_t nedges = j1 - j0;
+        const uint32_t nend = i1 - i0; /* local rows whose end item is in this tile */
+        const uint32_t nitems = nend + nedges;
 #pragma unroll
         for (int g = 0; g < IPT; g++)
         {
-            const uint32_t e = t.j0 + lane + 32u * g;
-            if (e < t.j1) s_val[e - t.j0] = op.load1(e, id[g]);
+            const uint32_t e = j0 + lane + 32u * g;
+            if (e < j1) s_val[e - j0] = op.value(val[g]);
         }
-        cp_async_wait_all();
+        cp_async_wait_one();
         __syncwarp();
+        const uint32_t *s_off = sm_off[w][buf] + shA;
 
         /* merge-path consumption; the first row a lane ends may have begun
          * in earlier lanes, so its sum waits for the carry scan */
-        const uint32_t nend = t.i1 - t.i0; /* local rows whose end is in this tile */
         const uint32_t d = lane * IPT;
         uint32_t first_row = 0xffffffffu, key = 0xffffffffu;
         Acc first_sum = Acc(0), carry = Acc(0);
         bool first_done = false;
-        if (d < t.nitems)
+        if (d < nitems)
         {
-            uint2 p = merge_path_search(d, s_off + 1, nend, t.nedges, t.j0);
+            uint2 p = merge_path_search(d, s_off + 1, nend, nedges, j0);
             uint32_t ri = p.x, ej = p.y;
             first_row = ri;
-            uint32_t rend = ri < nend ? s_off[ri + 1] - t.j0 : 0xffffffffu;
+            uint32_t rend = ri < nend ? s_off[ri + 1] - j0 : 0xffffffffu;
             Acc sum = Acc(0);
-            const uint32_t dend = min(d + IPT, t.nitems);
+            const uint32_t dend = min(d + IPT, nitems);
             for (uint32_t k = d; k < dend; k++)
             {
                 if (ej < rend)
@@ -337,7 +408,7 @@ __device__ __forceinline__ void warp_pull(const uint32_t *__restrict__ off, cons
                         s_row[ri] = sum;
                     sum = Acc(0);
                     ri++;
-                    rend = ri < nend ? s_off[ri + 1] - t.j0 : 0xffffffffu;
+                    rend = ri < nend ? s_off[ri + 1] - j0 : 0xffffffffu;
                 }
             }
             key = ri;
@@ -357,7 +428,7 @@ __device__ __forceinline__ void warp_pull(const uint32_t *__restrict__ off, cons
             const Acc vp = __shfl_up_sync(0xffffffffu, carry, 1);
             if (first_done) s_row[first_row] = first_sum + ((lane > 0 && kp == first_row) ? vp : Acc(0));
             /* the row left open at the end of the tile (row i1) */
-            if (t.i1 < V)
+            if (i1 < V)
             {
                 const uint32_t m = __ballot_sync(0xffffffffu, key == nend);
                 const Acc tot = m ? __shfl_sync(0xffffffffu, carry, 31 - __clz((int)m)) : Acc(0);
@@ -366,60 +437,32 @@ __device__ __forceinline__ void warp_pull(const uint32_t *__restrict__ off, cons
         }
         __syncwarp();
 
-        /* row epilogue: rows wholly inside the tile are finished here; rows
-         * spanning tiles send their partial to the fix-up pass */
-        const uint64_t tlo = (uint64_t)tile * TW, thi = tlo + TW;
-        for (uint32_t k = lane; k < t.nrows; k += 32)
+        /* rows ending here are stored, except row i0 when it began in an
+         * earlier tile (off[i0] < j0); that one and the open row i1 add
+         * their partials to sums */
+        for (uint32_t k = lane; k < nend; k += 32)
         {
-            const uint32_t r = t.i0 + k;
-            const uint64_t first = (uint64_t)r + s_off[k];
-            const uint64_t last = (uint64_t)r + s_off[k + 1]; /* the row's end item */
-            const uint32_t t_first = (uint32_t)(first / TW), t_last = (uint32_t)(last / TW);
-            if (t_first == t_last)
+            if (k == 0 && s_off[0] < j0)
             {
-                if (t_first == tile) op.finish(r, s_row[k], op.unstage(r, s_pre, shift + k, PREW), err, act);
+                if (s_off[1] > j0) atomic_add_acc(&sums[i0], s_row[0]);
             }
             else
-            {
-                const uint64_t a = first > tlo ? first : tlo;
-                const uint64_t b = (last + 1) < thi ? (last + 1) : thi;
-                if (a < b) atomic_add_acc(&g_acc[t_first], s_row[k]);
-            }
+                sums[i0 + k] = s_row[k];
         }
+        if (lane == 0 && i1 < V && s_off[nend] < j1) atomic_add_acc(&sums[i1], s_row[nend]);
         __syncwarp();
-    }
-    op.warp_end(err, act);
-}
 
-/*
- * After warp_pull: finish every row whose items span tiles.  Such a row
- * starts in tile t and is left open at t's end, i.e. it is row coord[t+1].x
- * with at least one edge before coord[t+1].y and its first item inside t.
- * acc[t] holds the sum of all its tiles' partials (the launch boundary
- * orders them); it is reset for the next launch.  One thread per tile.
- */
-template <class Op>
-__device__ __forceinline__ void warp_pull_fixup(const uint32_t *__restrict__ off, uint32_t V,
-                                                const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t tw,
-                                                typename Op::Acc *g_acc, Op &op)
-{
-    typedef typename Op::Acc Acc;
-    double err = 0.0;
-    uint32_t act = 0;
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x)
-    {
-        const uint2 c1 = coord[t + 1];
-        const uint32_t r = c1.x;
-        if (r >= V) continue;
-        const uint32_t o = off[r];
-        if (o < c1.y && (uint64_t)r + o >= (uint64_t)t * tw)
-        {
-            const Acc total = g_acc[t];
-            g_acc[t] = Acc(0);
-            op.finish(r, total, op.prefetch(r), err, act);
-        }
+        /* C's offsets into A's buffer; rotate */
+        uint32_t shC = 0;
+        if (hasC) shC = stage_words(sm_off[w][buf], off, c0.x, tile_rows(c0, c1, V) + 1, lane);
+        cp_async_commit();
+#pragma unroll
+        for (int g = 0; g < IPT; g++) val[g] = nv[g];
+        a0 = b0; a1 = b1; b0 = c0; b1 = c1; c0 = d0; c1 = d1;
+        shA = shB; shB = shC;
+        buf ^= 1u;
     }
-    op.warp_end(err, act);
+    cp_async_wait_all();
 }
 
 /*
@@ -474,25 +517,6 @@ __device__ __forceinline__ void warp_push(const uint32_t *__restrict__ off, cons
         }
         __syncwarp();
     }
-}
-
-/* warp sums of the per-lane residual terms, then one atomic per warp */
-__device__ __forceinline__ void warp_reduce_to(double err, uint32_t act, double *err_dst, uint32_t *act_dst)
-{
-    err = warp_sum(err);
-    act = warp_sum(act);
-    if ((threadIdx.x & 31) == 0)
-    {
-        if (err != 0.0) atomicAdd(err_dst, err);
-        if (act) atomicAdd(act_dst, act);
-    }
-}
-
-__device__ __forceinline__ void warp_max_to(uint32_t v, uint32_t *dst)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_down_sync(0xffffffffu, v, o));
-    if ((threadIdx.x & 31) == 0 && v) atomicMax(dst, v);
 }
 
 } // namespace gg

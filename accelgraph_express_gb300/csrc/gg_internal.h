@@ -16,9 +16,9 @@
  * CTA-wide barrier sits on the hot path.  IPT is odd so that the lanes'
  * reads of the staged values hit distinct shared-memory banks.  Kernels run
  * persistent CTAs of GG_TILE_WARPS warps that stride over the tiles; small
- * CTAs keep each one's static shared staging (offsets, values, row sums and
- * per-row epilogue words for every warp) under 48 KB. */
-#define GG_TILE_IPT 11
+ * CTAs keep each one's static shared staging (double-buffered row offsets,
+ * values and row sums for every warp) under 48 KB. */
+#define GG_TILE_IPT 9
 #define GG_TILE_ITEMS (32 * GG_TILE_IPT)
 #define GG_TILE_WARPS 4
 #define GG_TILE_NT (32 * GG_TILE_WARPS)
@@ -31,7 +31,6 @@ struct gg_tiles
 {
     uint32_t ntiles = 0;
     uint2 *coord = nullptr;   /* ntiles+1 merge-path coordinates (row, edge) */
-    void *acc = nullptr;      /* ntiles cross-tile partial sums (8 bytes each), zero between launches */
 };
 
 /* Growable device scratch owned by a mapping. */

@@ -376,7 +376,6 @@ extern "C" gg_status gg_graph_extend(gg_graph *g, const struct GraphCSR *graph, 
 static void free_tiles(gg_graph *g, gg_tiles &t)
 {
     gg_dev_free(g, t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2));
-    gg_dev_free(g, t.acc, (size_t)t.ntiles * 8 + 8);
     t = gg_tiles();
 }
 
@@ -423,8 +422,6 @@ gg_status gg_tiles_get(gg_graph *g, int in, cudaStream_t s, gg_tiles **out)
         if (nt >= 0xffffffffull) return gg_fail(GG_ERR_INVALID, "graph too large for 32-bit tile ids");
         t.ntiles = (uint32_t)(nt ? nt : 1);
         GG_CHECK(gg_dev_alloc(g, (void **)&t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2)));
-        GG_CHECK(gg_dev_alloc(g, &t.acc, (size_t)t.ntiles * 8 + 8));
-        GG_CUDA(cudaMemsetAsync(t.acc, 0, (size_t)t.ntiles * 8 + 8, s));
         GG_CHECK(gg_launch_tile_coords(off, g->V, g->E, t.ntiles, t.coord, s));
     }
     *out = &t;

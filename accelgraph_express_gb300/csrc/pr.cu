@@ -2,10 +2,10 @@
  * PageRank on CSR, all fourteen variants of the reference's dispatcher
  * (02_capi_graph/src/algorithms/capi/pageRank.c:874-939), on one GPU.
  *
- * Topology-driven pull (modes 0, 2, 4, 9-13): one launch per iteration of
- * the merge-path tile gather over the CSC, fused with the reference's update
- * pass (pageRank.c:1055-1069) and with the next iteration's contribution
- * pass (pageRank.c:1026-1033):
+ * Topology-driven pull (modes 0, 2, 4, 9-13): per iteration the merge-path
+ * tile gather over the CSC writes every vertex's sum, then one vertex pass
+ * runs the reference's update (pageRank.c:1055-1069) fused with the next
+ * iteration's contribution pass (pageRank.c:1026-1033):
  *     sum      = sum over in-edges (u,v) of contrib[u]      (FP32 or u64)
  *     rank'    = 0.15 + 0.85*sum
  *     error   += |rank' - rank| / V   (FP64),  active += (|.| >= epsilon)
@@ -171,100 +171,34 @@ struct PrCommon
     IterRec *rec;      /* records of this run */
     uint32_t it;       /* iteration index of this launch */
     __device__ __forceinline__ bool skip() const { return it > 0 && rec[it - 1].active == 0u; }
-    /* pageRank.c:1057-1067: |rank' - rank| is a float difference, exact in
-     * FP64; the FP64 sum of the differences is divided by V once on the host
-     * (the reference divides each term), and `error >= epsilon` is the same
-     * test as e >= eps_f in FP32, so no FP64 division or compare runs per
-     * vertex (FP64 is 1/64 of the FP32 rate here) */
-    __device__ __forceinline__ void update(uint32_t r, float nr, double &err, uint32_t &act) const
-    {
-        float pr = rank[r];
-        rank[r] = nr;
-        float e = fabsf(__fsub_rn(nr, pr));
-        err += (double)e;
-        if (e >= eps_f) act++;
-    }
-    __device__ __forceinline__ void update_pre(uint32_t r, float nr, float pr, double &err, uint32_t &act) const
-    {
-        rank[r] = nr;
-        float e = fabsf(__fsub_rn(nr, pr));
-        err += (double)e;
-        if (e >= eps_f) act++;
-    }
     __device__ __forceinline__ void reduce(double err, uint32_t act) const
     {
         if (err != 0.0) atomicAdd(&rec[it].err, err);
         if (act) atomicAdd(&rec[it].active, act);
     }
-    __device__ __forceinline__ void warp_reduce(double err, uint32_t act) const
-    {
-        warp_reduce_to(err, act, &rec[it].err, &rec[it].active);
-    }
 };
 
-/* ---- pull: gather + fused update ------------------------------------------------ */
+/* ---- pull: gather, then vertex update ---------------------------------------------- */
 
+/* the edge term of the pull gather: the in-neighbour's stored contribution */
 template <int K>
-struct PullOp : PrCommon
+struct PrGather
 {
     typedef typename Fmt<K>::Acc Acc;
-    typedef typename Fmt<K>::CT CT;
-    const CT *cin;
-    CT *cout;
-    float *cf;         /* float contributions (quantised modes) */
-    uint32_t tmax = 0; /* this thread's largest new contribution (quantised modes) */
-
-    struct RowPre { float rank; uint32_t deg; };
-    static constexpr uint32_t PRE_WORDS = 2;
-    __device__ __forceinline__ Acc load1(uint32_t, uint32_t u) const { return decode<K>(cin[u]); }
-    __device__ __forceinline__ RowPre prefetch(uint32_t r) const { return RowPre{rank[r], outdeg[r]}; }
-    __device__ __forceinline__ void stage(uint32_t i0, uint32_t n, uint32_t lane, uint32_t *s, uint32_t stride) const
-    {
-        stage_words(s, reinterpret_cast<const uint32_t *>(rank), i0, n, lane);
-        stage_words(s + stride, outdeg, i0, n, lane);
-    }
-    __device__ __forceinline__ RowPre unstage(uint32_t, const uint32_t *s, uint32_t j, uint32_t stride) const
-    {
-        return RowPre{__uint_as_float(s[j]), s[stride + j]};
-    }
-    __device__ __forceinline__ void finish(uint32_t r, Acc sum, const RowPre &pre, double &err, uint32_t &act)
-    {
-        float qscale = 0.0f;
-        if constexpr (Fmt<K>::quant) qscale = quant_scale(rec[it].maxbits, Fmt<K>::bits);
-        float nr = next_rank<K>(base, damp, sum, qscale);
-        update_pre(r, nr, pre.rank, err, act);
-        const uint32_t d = pre.deg;
-        float c = contrib_of(nr, d);
-        if constexpr (Fmt<K>::quant)
-        {
-            cf[r] = c;
-            tmax = max(tmax, __float_as_uint(c));
-        }
-        else
-            cout[r] = encode<K>(c, d);
-    }
-    __device__ __forceinline__ void warp_end(double err, uint32_t act)
-    {
-        warp_reduce(err, act);
-        if constexpr (Fmt<K>::quant) warp_max_to(tmax, &rec[it + 1].maxbits);
-    }
+    typedef typename Fmt<K>::CT Raw;
+    const Raw *cin;
+    __device__ __forceinline__ Raw load(uint32_t, uint32_t u) const { return ldg_val(cin + u); }
+    __device__ __forceinline__ Acc value(const Raw &r) const { return decode<K>(r); }
 };
 
 template <int K>
 __global__ void __launch_bounds__(GG_TILE_NT) k_pr_pull(const uint32_t *__restrict__ off,
                                                         const uint32_t *__restrict__ adj, const uint2 *__restrict__ coord,
-                                                        uint32_t ntiles, typename Fmt<K>::Acc *g_acc, PullOp<K> op)
+                                                        uint32_t ntiles, uint32_t V, typename Fmt<K>::Acc *sums,
+                                                        PrGather<K> op, const IterRec *rec, uint32_t it)
 {
-    if (op.skip()) return;
-    warp_pull<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, op.V, coord, ntiles, g_acc, op);
-}
-
-template <int K>
-__global__ void __launch_bounds__(256) k_pr_pull_fixup(const uint32_t *__restrict__ off, const uint2 *__restrict__ coord,
-                                                       uint32_t ntiles, typename Fmt<K>::Acc *g_acc, PullOp<K> op)
-{
-    if (op.skip()) return;
-    warp_pull_fixup(off, op.V, coord, ntiles, GG_TILE_ITEMS, g_acc, op);
+    if (it > 0 && rec[it - 1].active == 0u) return;
+    warp_pull_sums<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, sums, op);
 }
 
 /* ---- init, quantise, finalise --------------------------------------------------- */
@@ -388,26 +322,43 @@ __global__ void __launch_bounds__(GG_TILE_NT) k_pr_push_q(const uint32_t *__rest
     warp_push<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, op);
 }
 
-/* vertex update after a push (pageRank.c:2067-2081) */
+/* vertex update from the gathered (pull) or scattered (push) sums
+ * (pageRank.c:1055-1069 and :2067-2081), fused with the next iteration's
+ * contribution pass (pageRank.c:1026-1033); clears sums for the next launch */
 template <int K>
-__global__ void k_pr_push_update(PrCommon c, typename Fmt<K>::Acc *next, typename Fmt<K>::CT *cout, float *cf)
+__global__ void k_pr_update(PrCommon c, typename Fmt<K>::Acc *sums, typename Fmt<K>::CT *cout, float *cf)
 {
     if (c.skip()) return;
     double err = 0.0;
     uint32_t act = 0, tmax = 0;
+    float qscale = 0.0f;
+    if constexpr (Fmt<K>::quant && K != K_Q8Z) qscale = quant_scale(c.rec[c.it].maxbits, Fmt<K>::bits);
+    typename Fmt<K>::Acc *__restrict__ sv = sums;
+    float *__restrict__ rank = c.rank;
+    const uint32_t *__restrict__ outdeg = c.outdeg;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < c.V; v += gridDim.x * blockDim.x)
     {
-        typename Fmt<K>::Acc s = next[v];
-        next[v] = 0;
+        const typename Fmt<K>::Acc s = sv[v];
+        const float pr = rank[v];
+        const uint32_t d = outdeg[v];
         float nr;
-        if constexpr (K == K_FX64)
-            nr = next_rank<K_FX64>(c.base, c.damp, s, 0.0f);
-        else
-            nr = __fadd_rn(c.base, __fmul_rn(c.damp, (float)s));
-        c.update(v, nr, err, act);
-        uint32_t d = c.outdeg[v];
-        float ctb = contrib_of(nr, d);
         if constexpr (K == K_Q8Z)
+            nr = __fadd_rn(c.base, __fmul_rn(c.damp, (float)s));
+        else
+            nr = next_rank<K>(c.base, c.damp, s, qscale);
+        clear_after_read(&sv[v], s);
+        rank[v] = nr;
+        /* pageRank.c:1057-1067: |rank' - rank| is a float difference, exact
+         * in FP64; the FP64 sum of the differences is divided by V once on
+         * the host (the reference divides each term), and `error >= epsilon`
+         * is the same test as e >= eps_f in FP32, so no FP64 division or
+         * compare runs per vertex (FP64 is a small fraction of the FP32 rate
+         * here) */
+        const float e = fabsf(__fsub_rn(nr, pr));
+        err += (double)e;
+        if (e >= c.eps_f) act++;
+        float ctb = contrib_of(nr, d);
+        if constexpr (Fmt<K>::quant)
         {
             cf[v] = ctb;
             tmax = max(tmax, __float_as_uint(ctb));
@@ -415,7 +366,7 @@ __global__ void k_pr_push_update(PrCommon c, typename Fmt<K>::Acc *next, typenam
         else
             cout[v] = encode<K>(ctb, d);
     }
-    if constexpr (K == K_Q8Z) block_max_bits<256>(tmax, &c.rec[c.it + 1].maxbits);
+    if constexpr (Fmt<K>::quant) block_max_bits<256>(tmax, &c.rec[c.it + 1].maxbits);
     block_sum2<256>(err, act);
     if (threadIdx.x == 0) c.reduce(err, act);
 }
@@ -430,62 +381,49 @@ __global__ void k_dd_contrib(const float *__restrict__ rank, const uint32_t *__r
         cf[v] = contrib_of(rank[v], outdeg[v]);
 }
 
-/* data-driven pull: only worklist vertices update; a vertex that moved by at
- * least epsilon keeps its new rank and activates its out-neighbours */
-struct DdPullOp : PrCommon
+/* data-driven pull (pageRank.c:2810-2905): every row is gathered; only
+ * worklist vertices update, and a vertex that moved by at least epsilon
+ * keeps its new rank and activates its out-neighbours */
+struct DdGather
 {
     typedef float Acc;
+    typedef float Raw;
     const float *cf;
-    const uint8_t *wl_curr;
-    uint8_t *wl_next;
-    const uint32_t *out_off, *out_adj;
-    struct RowPre { float rank; uint32_t on; };
-    static constexpr uint32_t PRE_WORDS = 2;
-    __device__ __forceinline__ float load1(uint32_t, uint32_t u) const { return cf[u]; }
-    __device__ __forceinline__ RowPre prefetch(uint32_t r) const { return RowPre{rank[r], wl_curr[r]}; }
-    /* the flag bytes travel as the aligned 4-byte words holding them: word
-     * c of the second plane holds rows (i0 & ~3) + 4c .. +3 (the worklists
-     * are allocated with 16 bytes of slack past V) */
-    __device__ __forceinline__ void stage(uint32_t i0, uint32_t n, uint32_t lane, uint32_t *s, uint32_t stride) const
-    {
-        stage_words(s, reinterpret_cast<const uint32_t *>(rank), i0, n, lane);
-        const uint32_t base = i0 & ~3u, nw = ((i0 & 3u) + n + 3u) >> 2;
-        for (uint32_t c = lane; c < nw; c += 32) cp_async4(s + stride + c, wl_curr + base + 4u * c);
-    }
-    __device__ __forceinline__ RowPre unstage(uint32_t, const uint32_t *s, uint32_t j, uint32_t stride) const
-    {
-        return RowPre{__uint_as_float(s[j]), (s[stride + (j >> 2)] >> (8u * (j & 3u))) & 0xffu};
-    }
-    __device__ __forceinline__ void finish(uint32_t r, float sum, const RowPre &pre, double &err, uint32_t &act)
-    {
-        if (!pre.on) return;
-        float nr = __fadd_rn(base, __fmul_rn(damp, sum));
-        float pr = pre.rank;
-        float e = fabsf(__fsub_rn(nr, pr));
-        err += (double)e;
-        if (e >= eps_f)
-        {
-            rank[r] = nr;
-            for (uint32_t j = out_off[r]; j < out_off[r + 1]; j++) wl_next[out_adj[j]] = 1;
-            act++;
-        }
-    }
-    __device__ __forceinline__ void warp_end(double err, uint32_t act) { warp_reduce(err, act); }
+    __device__ __forceinline__ float load(uint32_t, uint32_t u) const { return ldg_val(cf + u); }
+    __device__ __forceinline__ float value(float r) const { return r; }
 };
 
 __global__ void __launch_bounds__(GG_TILE_NT) k_dd_pull(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                                        const uint2 *__restrict__ coord, uint32_t ntiles, float *g_acc,
-                                                        DdPullOp op)
+                                                        const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t V,
+                                                        float *sums, DdGather op, const IterRec *rec, uint32_t it)
 {
-    if (op.skip()) return;
-    warp_pull<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, op.V, coord, ntiles, g_acc, op);
+    if (it > 0 && rec[it - 1].active == 0u) return;
+    warp_pull_sums<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, sums, op);
 }
 
-__global__ void __launch_bounds__(256) k_dd_pull_fixup(const uint32_t *__restrict__ off, const uint2 *__restrict__ coord,
-                                                       uint32_t ntiles, float *g_acc, DdPullOp op)
+__global__ void k_dd_update(PrCommon c, float *sums, const uint8_t *__restrict__ wl_curr, uint8_t *wl_next,
+                            const uint32_t *__restrict__ out_off, const uint32_t *__restrict__ out_adj)
 {
-    if (op.skip()) return;
-    warp_pull_fixup(off, op.V, coord, ntiles, GG_TILE_ITEMS, g_acc, op);
+    if (c.skip()) return;
+    double err = 0.0;
+    uint32_t act = 0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < c.V; v += gridDim.x * blockDim.x)
+    {
+        const float sum = sums[v];
+        clear_after_read(&sums[v], sum);
+        if (!wl_curr[v]) continue;
+        float nr = __fadd_rn(c.base, __fmul_rn(c.damp, sum));
+        float e = fabsf(__fsub_rn(nr, c.rank[v]));
+        err += (double)e;
+        if (e >= c.eps_f)
+        {
+            c.rank[v] = nr;
+            for (uint32_t j = out_off[v]; j < out_off[v + 1]; j++) wl_next[out_adj[j]] = 1;
+            act++;
+        }
+    }
+    block_sum2<256>(err, act);
+    if (threadIdx.x == 0) c.reduce(err, act);
 }
 
 /* data-driven push (mode 7) and pull-push (mode 8): one warp per worklist
@@ -595,7 +533,6 @@ struct Run
 };
 
 int grid_v(uint32_t V) { int b = (int)((V + 255) / 256); int cap = gg_sm_count() * 8; return b < 1 ? 1 : (b > cap ? cap : b); }
-int fixup_grid(uint32_t ntiles) { return grid_v(ntiles); }
 
 gg_status timed_begin(Run &R)
 {
@@ -617,10 +554,13 @@ gg_status run_pull(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
     const uint32_t V = g->V;
     gg_tiles *t;
     GG_CHECK(gg_tiles_get(g, 1, R.s, &t));
-    void *c0, *c1, *cf = nullptr;
+    void *c0, *c1, *cf = nullptr, *sums;
     GG_CHECK(gg_work(g, 2, ((size_t)V + 16) * sizeof(CT), &c0));
     GG_CHECK(gg_work(g, 3, ((size_t)V + 16) * sizeof(CT), &c1));
     if (Fmt<K>::quant) GG_CHECK(gg_work(g, 4, ((size_t)V + 16) * sizeof(float), &cf));
+    /* row sums, zero between launches (k_pr_update clears what it reads) */
+    GG_CHECK(gg_work(g, 5, ((size_t)V + 16) * sizeof(Acc), &sums));
+    GG_CUDA(cudaMemsetAsync(sums, 0, ((size_t)V + 16) * sizeof(Acc), R.s));
     CT *cb[2] = {(CT *)c0, (CT *)c1};
 
     k_pr_init<K><<<grid_v(V), 256, 0, R.s>>>(rank, g->out_deg, V, init, Fmt<K>::quant ? nullptr : cb[0],
@@ -633,17 +573,15 @@ gg_status run_pull(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
             k_quantize<CT><<<grid_v(V), 256, 0, R.s>>>((const float *)cf, cb[0], V, Fmt<K>::bits, 0, rec, it, nullptr);
             R.launches++;
         }
-        PullOp<K> op;
-        op.rank = rank; op.outdeg = g->out_deg; op.V = V; op.base = base; op.damp = R.p->damp;
-        op.eps_f = R.eps_f; op.eps_fl = R.eps_fl; op.rec = rec; op.it = it;
-        op.cin = Fmt<K>::quant ? cb[0] : cb[it & 1];
-        op.cout = cb[(it + 1) & 1];
-        op.cf = (float *)cf;
+        PrGather<K> op{Fmt<K>::quant ? cb[0] : cb[it & 1]};
         GG_CHECK(timed_begin(R));
         k_pr_pull<K><<<gg_persistent_grid((const void *)k_pr_pull<K>, t->ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0, R.s>>>(
-            g->in_off, g->in_adj, t->coord, t->ntiles, (Acc *)t->acc, op);
-        k_pr_pull_fixup<K><<<fixup_grid(t->ntiles), 256, 0, R.s>>>(g->in_off, t->coord, t->ntiles, (Acc *)t->acc, op);
+            g->in_off, g->in_adj, t->coord, t->ntiles, V, (Acc *)sums, op, rec, it);
         GG_CHECK(timed_end(R));
+        PrCommon c;
+        c.rank = rank; c.outdeg = g->out_deg; c.V = V; c.base = base; c.damp = R.p->damp;
+        c.eps_f = R.eps_f; c.eps_fl = R.eps_fl; c.rec = rec; c.it = it;
+        k_pr_update<K><<<grid_v(V), 256, 0, R.s>>>(c, (Acc *)sums, cb[(it + 1) & 1], (float *)cf);
         R.launches += 2;
         R.gather_launches++;
     }
@@ -707,11 +645,11 @@ gg_status run_push(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
         c.rank = rank; c.outdeg = g->out_deg; c.V = V; c.base = base; c.damp = R.p->damp;
         c.eps_f = R.eps_f; c.eps_fl = R.eps_fl; c.rec = rec; c.it = it;
         if constexpr (K == K_FX64)
-            k_pr_push_update<K_FX64><<<grid_v(V), 256, 0, R.s>>>(c, (unsigned long long *)nx, (unsigned long long *)c0, nullptr);
+            k_pr_update<K_FX64><<<grid_v(V), 256, 0, R.s>>>(c, (unsigned long long *)nx, (unsigned long long *)c0, nullptr);
         else if constexpr (K == K_Q8Z)
-            k_pr_push_update<K_Q8Z><<<grid_v(V), 256, 0, R.s>>>(c, (float *)nx, nullptr, (float *)cf);
+            k_pr_update<K_Q8Z><<<grid_v(V), 256, 0, R.s>>>(c, (float *)nx, nullptr, (float *)cf);
         else
-            k_pr_push_update<K><<<grid_v(V), 256, 0, R.s>>>(c, (float *)nx, (CT *)c0, nullptr);
+            k_pr_update<K><<<grid_v(V), 256, 0, R.s>>>(c, (float *)nx, (CT *)c0, nullptr);
         R.launches++;
     }
     (void)KI;
@@ -735,22 +673,23 @@ gg_status run_dd(Run &R, int mode, IterRec *rec, float *rank, uint32_t iters, fl
     uint8_t *wl[2] = {(uint8_t *)wa, (uint8_t *)wb};
     if (mode == GG_PR_DD_PULL)
     {
+        void *sums;
+        GG_CHECK(gg_work(g, 5, ((size_t)V + 16) * 4, &sums));
+        GG_CUDA(cudaMemsetAsync(sums, 0, ((size_t)V + 16) * 4, R.s));
         GG_CUDA(cudaMemsetAsync(wa, 1, V, R.s));
         gg_tiles *t;
         GG_CHECK(gg_tiles_get(g, 1, R.s, &t));
         for (uint32_t it = 0; it < iters; it++)
         {
             k_dd_contrib<<<grid_v(V), 256, 0, R.s>>>(rank, g->out_deg, (float *)cf, V, rec, it);
-            DdPullOp op;
-            op.rank = rank; op.outdeg = g->out_deg; op.V = V; op.base = base; op.damp = R.p->damp;
-            op.eps_f = R.eps_f; op.eps_fl = R.eps_fl; op.rec = rec; op.it = it;
-            op.cf = (const float *)cf; op.wl_curr = wl[it & 1]; op.wl_next = wl[(it + 1) & 1];
-            op.out_off = g->out_off; op.out_adj = g->out_adj;
+            PrCommon c;
+            c.rank = rank; c.outdeg = g->out_deg; c.V = V; c.base = base; c.damp = R.p->damp;
+            c.eps_f = R.eps_f; c.eps_fl = R.eps_fl; c.rec = rec; c.it = it;
             GG_CHECK(timed_begin(R));
             k_dd_pull<<<gg_persistent_grid((const void *)k_dd_pull, t->ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0, R.s>>>(
-                g->in_off, g->in_adj, t->coord, t->ntiles, (float *)t->acc, op);
-            k_dd_pull_fixup<<<fixup_grid(t->ntiles), 256, 0, R.s>>>(g->in_off, t->coord, t->ntiles, (float *)t->acc, op);
+                g->in_off, g->in_adj, t->coord, t->ntiles, V, (float *)sums, DdGather{(const float *)cf}, rec, it);
             GG_CHECK(timed_end(R));
+            k_dd_update<<<grid_v(V), 256, 0, R.s>>>(c, (float *)sums, wl[it & 1], wl[(it + 1) & 1], g->out_off, g->out_adj);
             k_clear_bytes<<<grid_v(V), 256, 0, R.s>>>(wl[it & 1], V, rec, it);
             R.launches += 4;
             R.gather_launches++;

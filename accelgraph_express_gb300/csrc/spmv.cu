@@ -26,73 +26,57 @@ namespace {
 
 using namespace gg;
 
+/* the edge term of the pull product: w[e] * x[u] (SPMV.c:735-760) */
 template <class T>
-struct SpmvPullOp
+struct SpmvGather
 {
     typedef float Acc;
+    struct Raw { T w, x; };
     const T *w;
     const T *x;
-    float *y;
-    struct RowPre {};
-    static constexpr uint32_t PRE_WORDS = 0;
-    __device__ __forceinline__ RowPre unstage(uint32_t, const uint32_t *, uint32_t, uint32_t) const { return RowPre{}; }
-    __device__ __forceinline__ float load1(uint32_t e, uint32_t u) const
-    {
-        return __fmul_rn(to_f32(w[e]), to_f32(x[u]));
-    }
-    __device__ __forceinline__ RowPre prefetch(uint32_t) const { return RowPre{}; }
-    __device__ __forceinline__ void finish(uint32_t r, float sum, const RowPre &, double &, uint32_t &) { y[r] = sum; }
-    __device__ __forceinline__ void warp_end(double, uint32_t) const {}
+    __device__ __forceinline__ Raw load(uint32_t e, uint32_t u) const { return Raw{ldg_val(w + e), ldg_val(x + u)}; }
+    __device__ __forceinline__ float value(const Raw &r) const { return __fmul_rn(to_f32(r.w), to_f32(r.x)); }
 };
 
 template <class T>
 __global__ void __launch_bounds__(GG_TILE_NT) k_spmv_pull(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
                                                           const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t V,
-                                                          float *g_acc, SpmvPullOp<T> op)
+                                                          float *y, SpmvGather<T> op)
 {
-    warp_pull<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, g_acc, op);
+    warp_pull_sums<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, y, op);
 }
 
-template <class T>
-__global__ void __launch_bounds__(256) k_spmv_pull_fixup(const uint32_t *__restrict__ off, const uint2 *__restrict__ coord,
-                                                         uint32_t ntiles, uint32_t V, float *g_acc, SpmvPullOp<T> op)
-{
-    warp_pull_fixup(off, V, coord, ntiles, GG_TILE_ITEMS, g_acc, op);
-}
-
-struct SpmvPullFxOp
+/* fixed-point pull (SPMV.c:775-815): x in Q16.16, weights converted per
+ * edge, products truncated to Q16.16 and summed exactly in 64 bits */
+struct SpmvFxGather
 {
     typedef unsigned long long Acc;
+    struct Raw { float w; uint32_t x; };
     const float *w;
     const uint32_t *x32;
-    float *y;
-    struct RowPre {};
-    static constexpr uint32_t PRE_WORDS = 0;
-    __device__ __forceinline__ RowPre unstage(uint32_t, const uint32_t *, uint32_t, uint32_t) const { return RowPre{}; }
-    __device__ __forceinline__ unsigned long long load1(uint32_t e, uint32_t u) const
+    __device__ __forceinline__ Raw load(uint32_t e, uint32_t u) const { return Raw{ldg_val(w + e), ldg_val(x32 + u)}; }
+    __device__ __forceinline__ unsigned long long value(const Raw &r) const
     {
-        return ((unsigned long long)x32[u] * fx_from_float(w[e], 65536.0, 0xffffffffu)) >> 16;
+        return ((unsigned long long)r.x * fx_from_float(r.w, 65536.0, 0xffffffffu)) >> 16;
     }
-    __device__ __forceinline__ RowPre prefetch(uint32_t) const { return RowPre{}; }
-    __device__ __forceinline__ void finish(uint32_t r, unsigned long long sum, const RowPre &, double &, uint32_t &)
-    {
-        y[r] = fx_to_float(sum, 1.0 / 65536.0);
-    }
-    __device__ __forceinline__ void warp_end(double, uint32_t) const {}
 };
 
 __global__ void __launch_bounds__(GG_TILE_NT) k_spmv_pull_fx(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
                                                              const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t V,
-                                                             unsigned long long *g_acc, SpmvPullFxOp op)
+                                                             unsigned long long *y64, SpmvFxGather op)
 {
-    warp_pull<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, g_acc, op);
+    warp_pull_sums<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, y64, op);
 }
 
-__global__ void __launch_bounds__(256) k_spmv_pull_fx_fixup(const uint32_t *__restrict__ off, const uint2 *__restrict__ coord,
-                                                            uint32_t ntiles, uint32_t V, unsigned long long *g_acc,
-                                                            SpmvPullFxOp op)
+/* y = Q16.16 sums as float; clears the sums for the next product */
+__global__ void k_spmv_fx_pull_out(unsigned long long *y64, float *y, uint32_t V)
 {
-    warp_pull_fixup(off, V, coord, ntiles, GG_TILE_ITEMS, g_acc, op);
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    {
+        const unsigned long long s = y64[v];
+        y[v] = fx_to_float(s, 1.0 / 65536.0);
+        clear_after_read(&y64[v], s);
+    }
 }
 
 template <class T>
@@ -216,11 +200,11 @@ gg_status spmv_fp(gg_graph *g, const gg_spmv_params *p, const float *x_dev, floa
         }
         if (pull)
         {
-            SpmvPullOp<T> op{w, xv, y};
+            /* y is the row-sum array: zero, then the gather stores rows and
+             * adds the partials of rows spanning tiles */
+            GG_CUDA(cudaMemsetAsync(y, 0, (size_t)V * sizeof(float), s));
             k_spmv_pull<T><<<gg_persistent_grid((const void *)k_spmv_pull<T>, t->ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0, s>>>(
-                g->in_off, g->in_adj, t->coord, t->ntiles, V, (float *)t->acc, op);
-            k_spmv_pull_fixup<T><<<grid_v(t->ntiles), 256, 0, s>>>(g->in_off, t->coord, t->ntiles, V, (float *)t->acc, op);
-            launches++;
+                g->in_off, g->in_adj, t->coord, t->ntiles, V, y, SpmvGather<T>{w, xv});
         }
         else
             k_spmv_push<T><<<gg_persistent_grid((const void *)k_spmv_push<T>, t->ntiles), GG_TILE_NT, 0, s>>>(
@@ -284,11 +268,8 @@ extern "C" gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *
             GG_CHECK(gg_tiles_get(g, pull ? 1 : 0, s, &t));
             void *xq, *y64 = nullptr;
             GG_CHECK(gg_work(g, 12, ((size_t)V + 16) * 8, &xq));
-            if (!pull)
-            {
-                GG_CHECK(gg_work(g, 14, ((size_t)V + 16) * 8, &y64));
-                GG_CUDA(cudaMemsetAsync(y64, 0, ((size_t)V + 16) * 8, s));
-            }
+            GG_CHECK(gg_work(g, 14, ((size_t)V + 16) * 8, &y64));
+            GG_CUDA(cudaMemsetAsync(y64, 0, ((size_t)V + 16) * 8, s));
             k_spmv_x<float><<<grid_v(V), 256, 0, s>>>(g->out_deg, (const float *)xin, (float *)xf, nullptr,
                                                       pull ? (uint32_t *)xq : nullptr,
                                                       pull ? nullptr : (unsigned long long *)xq, (float *)yv, V);
@@ -304,11 +285,10 @@ extern "C" gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *
                 }
                 if (pull)
                 {
-                    SpmvPullFxOp op{g->in_w, (const uint32_t *)xq, (float *)yv};
                     k_spmv_pull_fx<<<gg_persistent_grid((const void *)k_spmv_pull_fx, t->ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0, s>>>(
-                        g->in_off, g->in_adj, t->coord, t->ntiles, V, (unsigned long long *)t->acc, op);
-                    k_spmv_pull_fx_fixup<<<grid_v(t->ntiles), 256, 0, s>>>(g->in_off, t->coord, t->ntiles, V,
-                                                                          (unsigned long long *)t->acc, op);
+                        g->in_off, g->in_adj, t->coord, t->ntiles, V, (unsigned long long *)y64,
+                        SpmvFxGather{g->in_w, (const uint32_t *)xq});
+                    k_spmv_fx_pull_out<<<grid_v(V), 256, 0, s>>>((unsigned long long *)y64, (float *)yv, V);
                     launches++;
                 }
                 else
@@ -358,9 +338,9 @@ extern "C" gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *
  * whose device memory is fully reserved up front).  gg_spmv needs a
  * gg_graph mapping and work buffers that the runtime allocates; this entry
  * point instead takes the caller's device arrays and keeps its scratch (the
- * merge-path tile coordinates and the cross-tile partial sums) in the
- * file-scope array below, which exists on every GPU that loads the library
- * until the process exits.
+ * merge-path tile coordinates) in the file-scope array below, which exists
+ * on every GPU that loads the library until the process exits; partial sums
+ * of rows spanning tiles accumulate in the caller's y.
  */
 #define GG_NOALLOC_SCRATCH_BYTES (4u << 20)
 
@@ -378,14 +358,14 @@ size_t noalloc_coord_bytes(uint32_t ntiles) { return (((size_t)ntiles + 1) * siz
 
 extern "C" uint64_t gg_spmv_pull_noalloc_max_items(void)
 {
-    /* the largest V + E whose tile scratch fits: (ntiles+1) coordinates of
-     * 8 bytes (rounded to 256) and ntiles partial sums of 4 bytes */
-    uint64_t lo = 0, hi = (uint64_t)GG_NOALLOC_SCRATCH_BYTES / 4 * GG_TILE_ITEMS;
+    /* the largest V + E whose tile coordinates fit: (ntiles+1) of 8 bytes,
+     * rounded to 256 */
+    uint64_t lo = 0, hi = (uint64_t)GG_NOALLOC_SCRATCH_BYTES / 8 * GG_TILE_ITEMS;
     while (lo < hi)
     {
         const uint64_t mid = (lo + hi + 1) / 2;
         const uint64_t nt = (mid + GG_TILE_ITEMS - 1) / GG_TILE_ITEMS;
-        if (noalloc_coord_bytes((uint32_t)nt) + nt * 4 <= GG_NOALLOC_SCRATCH_BYTES)
+        if (noalloc_coord_bytes((uint32_t)nt) <= GG_NOALLOC_SCRATCH_BYTES)
             lo = mid;
         else
             hi = mid - 1;
@@ -422,16 +402,13 @@ extern "C" gg_status gg_spmv_pull_noalloc(uint32_t V, uint32_t E, const uint32_t
     }
     const uint32_t ntiles = (uint32_t)((items + GG_TILE_ITEMS - 1) / GG_TILE_ITEMS);
     uint2 *coord = (uint2 *)base;
-    float *acc = (float *)((unsigned char *)base + noalloc_coord_bytes(ntiles));
     cudaStream_t s = (cudaStream_t)stream;
-    /* the array keeps the previous call's contents: the partial sums must
-     * start at zero, the coordinates are rewritten */
-    GG_CUDA(cudaMemsetAsync(acc, 0, (size_t)ntiles * sizeof(float), s));
+    /* the coordinates are rewritten on every call; y is the row-sum array
+     * and starts at zero (rows spanning tiles are added into it) */
     GG_CHECK(gg_launch_tile_coords(in_off, V, E, ntiles, coord, s));
-    SpmvPullOp<float> op{w, x, y};
+    GG_CUDA(cudaMemsetAsync(y, 0, (size_t)V * sizeof(float), s));
     k_spmv_pull<float><<<gg_persistent_grid((const void *)k_spmv_pull<float>, ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0, s>>>(
-        in_off, in_src, coord, ntiles, V, acc, op);
-    k_spmv_pull_fixup<float><<<grid_v(ntiles), 256, 0, s>>>(in_off, coord, ntiles, V, acc, op);
+        in_off, in_src, coord, ntiles, V, y, SpmvGather<float>{w, x});
     GG_CUDA(cudaGetLastError());
     return GG_OK;
 }

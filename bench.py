@@ -128,7 +128,15 @@ def load_traffic(kernel):
 
 
 def pr_bytes(V, E, s):
+    """Algorithmic bytes of one PageRank pull iteration: CSC ids, offsets,
+    and per vertex rank read+write, out-degree, contribution read+write."""
     return 4 * E + 4 * (V + 1) + (12 + 2 * s) * V
+
+
+def pr_gather_bytes(V, E, s):
+    """Algorithmic bytes of one k_pr_pull launch (the gather): CSC ids,
+    offsets, each contribution once, and the row sums it writes."""
+    return 4 * E + 4 * (V + 1) + s * V + 4 * V
 
 
 def cpu_pagerank(graph, O, iters, threads):
@@ -245,9 +253,13 @@ def main():
     # roofline of the gather kernel
     peak, peak_kind = load_peaks()
     per_launch_ms = gather_ms / max(gather_n, 1)
-    alg = pr_bytes(V, E, 4)
+    alg = pr_gather_bytes(V, E, 4)
     achieved = alg / (per_launch_ms / 1e3) / 1e9
     traffic = load_traffic("k_pr_pull")
+    # the whole iteration (gather + vertex update) against the algorithm's bytes
+    iter_ms = elapsed_ms / (a.steps * ITERS)
+    iteration = {"alg_bytes": pr_bytes(V, E, 4), "ms": iter_ms,
+                 "frac": pr_bytes(V, E, 4) / (iter_ms / 1e3) / 1e9 / peak}
 
     # e2e through the drop-in entry point on host arrays
     gg.set_gpu_options(storage="f32", device=local, keep_resident=False, verbose=False)
@@ -274,7 +286,7 @@ def main():
                    "parallelism": f"replicas x{world}", "graph_build_s": round(t_build, 2)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": "k_pr_pull", "alg_bytes_per_launch": alg,
-                     "launch_ms": per_launch_ms, "peak_source": peak_kind},
+                     "launch_ms": per_launch_ms, "peak_source": peak_kind, "iteration": iteration},
         "e2e": {"value": e2e_value, "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "call": "pageRankGraphCSR"},
         "gpu_launches": launches,
@@ -442,7 +454,8 @@ def extras(gg, graph, dg, V, E, sptr, torch, peak):
         launch_ms = gms / reps
         out[f"pr_pull_{storage}"] = {
             "gteps": E * ITERS / (ms / 1e3) / 1e9, "ms_per_run": ms, "launch_ms": launch_ms,
-            "hbm_frac": pr_bytes(V, E, s) / (launch_ms / 1e3) / 1e9 / peak,
+            "hbm_frac": pr_gather_bytes(V, E, s) / (launch_ms / 1e3) / 1e9 / peak,
+            "iteration_hbm_frac": pr_bytes(V, E, s) / (ms / ITERS / 1e3) / 1e9 / peak,
             "l1_vs_fp64": l1, "linf_vs_fp64": linf, "l1_relative": l1 / float(np.abs(exact).sum())}
     out["fp64_oracle_s"] = round(f64_s, 2)
     out.update(spmv_extras(gg, graph, V, E, sptr, torch, peak))
