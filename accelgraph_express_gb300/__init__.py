@@ -129,6 +129,16 @@ class SpmvParams(C.Structure):
                 ("profile", C.c_uint32)]
 
 
+class PprParams(C.Structure):
+    _fields_ = [("num_vectors", C.c_uint32), ("iterations", C.c_uint32), ("damp", C.c_float),
+                ("storage", C.c_uint32), ("profile", C.c_uint32)]
+
+
+class PprResult(C.Structure):
+    _fields_ = [("gather_ms", C.c_float), ("gather_launches", C.c_uint32), ("launches", C.c_uint32),
+                ("padded_vectors", C.c_uint32)]
+
+
 class SpmvResult(C.Structure):
     _fields_ = [("checksum", C.c_double), ("spmv_ms", C.c_float), ("spmv_launches", C.c_uint32),
                 ("launches", C.c_uint32)]
@@ -174,6 +184,9 @@ def lib() -> C.CDLL:
         L.gg_spmv.argtypes = [C.c_void_p, P(SpmvParams), C.c_void_p, C.c_void_p, C.c_void_p, P(SpmvResult),
                               C.c_void_p]
         L.gg_set_wait_timeout_ms.argtypes = [C.c_uint32]
+        L.gg_ppr.argtypes = [C.c_void_p, P(PprParams), C.c_void_p, C.c_void_p, C.c_void_p, P(PprResult), C.c_void_p]
+        L.gg_ppr_device_ranks.argtypes = [C.c_void_p, P(C.c_uint32)]
+        L.gg_ppr_device_ranks.restype = C.c_void_p
         L.newEdgeList.argtypes = [C.c_uint32, C.c_uint32, C.c_int]
         L.newEdgeList.restype = P(EdgeList)
         L.freeEdgeList.argtypes = [P(EdgeList)]
@@ -422,6 +435,23 @@ class DeviceGraph:
                              None if xo is None else xo.ctypes.data, None if y is None else y.ctypes.data,
                              C.byref(r), stream), "gg_spmv")
         return xo, y, {k: getattr(r, k) for k, _ in SpmvResult._fields_}
+
+    def ppr(self, seed_sets, iterations=20, storage="bf16", damp=0.85, profile=False, copy_out=True, stream=None):
+        """Batched personalised PageRank: one rank vector per seed set (1..64
+        sets).  Returns (ranks as a V x K array or None, result dict)."""
+        K = len(seed_sets)
+        off = np.zeros(K + 1, np.uint32)
+        for k, sset in enumerate(seed_sets):
+            off[k + 1] = off[k] + len(sset)
+        seeds = (np.concatenate([np.asarray(x, np.uint32).ravel() for x in seed_sets]) if off[-1]
+                 else np.zeros(1, np.uint32))
+        seeds = np.ascontiguousarray(seeds, np.uint32)
+        p = PprParams(K, iterations, damp, STORE[storage], int(profile))
+        r = PprResult()
+        ranks = np.empty((self.graph.V, K), np.float32) if copy_out else None
+        _check(lib().gg_ppr(self.h, C.byref(p), off.ctypes.data, seeds.ctypes.data,
+                            None if ranks is None else ranks.ctypes.data, C.byref(r), stream), "gg_ppr")
+        return ranks, {k: getattr(r, k) for k, _ in PprResult._fields_}
 
     def free(self):
         if self.h:

@@ -65,7 +65,11 @@ struct gg_graph
     void *out_w16[3] = {nullptr, nullptr, nullptr};
 
     /* work buffers, grown on demand */
-    gg_buf work[16];
+    gg_buf work[32];
+    /* merge-path tiles of the batched PageRank gather (own tile size) */
+    gg_tiles ppr_tiles;
+    const float *ppr_ranks = nullptr;
+    uint32_t ppr_stride = 0;
 
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
     /* timing events reused across calls (profile mode) */
@@ -107,8 +111,9 @@ gg_status gg_event_at(gg_graph *g, uint32_t i, cudaEvent_t *out);
 float gg_event_ms(cudaEvent_t a, cudaEvent_t b);
 
 /* launch helpers implemented in the kernel translation units */
+/* coord[t] = (rows ended, edges consumed) at merge diagonal t * tile_items */
 gg_status gg_launch_tile_coords(const uint32_t *off, uint32_t V, uint32_t E, uint32_t ntiles,
-                                uint2 *coord, cudaStream_t s);
+                                uint2 *coord, cudaStream_t s, uint32_t tile_items = GG_TILE_ITEMS);
 gg_status gg_launch_to_half(const float *src, void *dst, size_t n, int storage, cudaStream_t s);
 int gg_sm_count();
 /* persistent grid for a tile kernel: one CTA per resident slot, no more

@@ -398,6 +398,7 @@ extern "C" gg_status gg_graph_unmap(gg_graph *g)
     }
     free_tiles(g, g->in_tiles);
     free_tiles(g, g->out_tiles);
+    free_tiles(g, g->ppr_tiles);
     for (auto &b : g->work) gg_dev_free(g, b.ptr, b.bytes);
     for (uint32_t i = 0; i < g->ev_count; i++) cudaEventDestroy(g->ev_pool[i]);
     free(g->ev_pool);
@@ -447,12 +448,12 @@ gg_status gg_weights16(gg_graph *g, int in, int storage, cudaStream_t s, const v
 /* ---- small kernels used by the runtime ------------------------------------------- */
 
 __global__ void k_tile_coords(const uint32_t *__restrict__ off, uint32_t V, uint32_t E, uint32_t ntiles,
-                              uint2 *__restrict__ coord)
+                              uint32_t tile_items, uint2 *__restrict__ coord)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t > ntiles) return;
     const uint64_t items = (uint64_t)V + E;
-    uint64_t d = (uint64_t)t * GG_TILE_ITEMS;
+    uint64_t d = (uint64_t)t * tile_items;
     if (d > items) d = items;
     /* rows ended before diagonal d: largest i with off[i] + (i-1) < d over row ends off[1..V] */
     uint64_t lo = d > E ? d - E : 0, hi = d < V ? d : V;
@@ -468,10 +469,10 @@ __global__ void k_tile_coords(const uint32_t *__restrict__ off, uint32_t V, uint
 }
 
 gg_status gg_launch_tile_coords(const uint32_t *off, uint32_t V, uint32_t E, uint32_t ntiles, uint2 *coord,
-                                cudaStream_t s)
+                                cudaStream_t s, uint32_t tile_items)
 {
     const uint32_t n = ntiles + 1;
-    k_tile_coords<<<(n + 255) / 256, 256, 0, s>>>(off, V, E, ntiles, coord);
+    k_tile_coords<<<(n + 255) / 256, 256, 0, s>>>(off, V, E, ntiles, tile_items, coord);
     GG_CUDA(cudaGetLastError());
     return GG_OK;
 }

@@ -1,0 +1,420 @@
+/*
+ * Batched personalised PageRank: K rank vectors over one graph, all advanced
+ * by one pull gather per iteration.  There is no counterpart in the
+ * reference's C API; per vector the arithmetic is the reference's pull
+ * PageRank (pageRank.c:1026-1069: contribution = rank / outdeg, 0 for
+ * outdeg 0, no dangling redistribution) with the uniform teleport replaced
+ * by a teleport to the vector's seed set S_k:
+ *     rank_0[v][k]  = c_k(v) / |S_k|              (c_k(v): occurrences of v in S_k)
+ *     contrib[v][k] = rank[v][k] / outdeg(v)
+ *     rank'[v][k]   = (1-d) c_k(v) / |S_k| + d * sum over in-edges (u,v) of contrib[u][k]
+ *
+ * Layout: contributions vertex-major, [V][KP] with KP = K rounded up to 16,
+ * 32 or 64, stored in FP32 or BF16 and summed in FP32.  At KP = 64 BF16 one
+ * vertex's contributions are one 128-byte line, so every edge of the CSC
+ * gathers one full line.  A group of KP/2 lanes owns a merge-path tile and
+ * walks it edge by edge, each lane summing two vectors; a batch of edges'
+ * lines is in flight while the previous ones are summed.  Rows are finished
+ * where they end: rank = teleport + d * sum (the teleport row comes through a
+ * per-vertex seed index), contribution = rank / outdeg; FP32 ranks are only
+ * written by the last iteration.  Rows spanning tiles add their partial sums
+ * atomically into their first tile's slot and k_ppr_fixup finishes them.
+ */
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+
+#include "gg_device.cuh"
+
+namespace {
+
+using namespace gg;
+
+constexpr uint32_t PPR_TILE = 512; /* merge items per tile */
+constexpr uint32_t NO_SEED = 0xffffffffu;
+
+/* two stored values per lane */
+template <class CT> struct PairIO;
+template <> struct PairIO<float>
+{
+    typedef float2 Raw;
+    static __device__ __forceinline__ Raw load(const float *p)
+    {
+        float2 v;
+        asm volatile("ld.global.nc.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+        return v;
+    }
+    static __device__ __forceinline__ float2 unpack(Raw r) { return r; }
+    static __device__ __forceinline__ void store(float *p, float a, float b)
+    {
+        *reinterpret_cast<float2 *>(p) = make_float2(a, b);
+    }
+};
+template <> struct PairIO<__nv_bfloat16>
+{
+    typedef uint32_t Raw;
+    static __device__ __forceinline__ Raw load(const __nv_bfloat16 *p)
+    {
+        return ldg_val(reinterpret_cast<const uint32_t *>(p));
+    }
+    /* element 2i is the low half of the word (little-endian), BF16 -> FP32 is exact */
+    static __device__ __forceinline__ float2 unpack(Raw r)
+    {
+        return make_float2(__uint_as_float(r << 16), __uint_as_float(r & 0xffff0000u));
+    }
+    static __device__ __forceinline__ void store(__nv_bfloat16 *p, float a, float b)
+    {
+        *reinterpret_cast<__nv_bfloat162 *>(p) = __floats2bfloat162_rn(a, b);
+    }
+};
+
+template <class CT>
+struct PprArgs
+{
+    const uint32_t *off, *adj, *outdeg, *seed_idx;
+    const uint2 *coord;
+    uint32_t ntiles, V, E;
+    const CT *cin;
+    CT *cout;
+    float *rank;       /* [V][KP], written when not null (last iteration) */
+    const float *tele; /* [nseeds][KP]: (1-d) c_k(v) / |S_k| of seed vertex i */
+    float *acc;        /* [ntiles][KP] partial sums of rows spanning tiles, zero between launches */
+    float damp;
+};
+
+/* rank and contribution of row r from its (two-vector) sum */
+template <int KP, class CT>
+__device__ __forceinline__ void ppr_finish(const PprArgs<CT> &a, uint32_t r, float s0, float s1, uint32_t si,
+                                           uint32_t deg, uint32_t gl)
+{
+    float r0 = __fmul_rn(a.damp, s0), r1 = __fmul_rn(a.damp, s1);
+    if (si != NO_SEED)
+    {
+        const float2 t = *reinterpret_cast<const float2 *>(a.tele + (size_t)si * KP + 2 * gl);
+        r0 = __fadd_rn(t.x, r0);
+        r1 = __fadd_rn(t.y, r1);
+    }
+    float c0 = 0.0f, c1 = 0.0f;
+    if (deg)
+    {
+        const float fd = __uint2float_rn(deg);
+        c0 = __fdiv_rn(r0, fd);
+        c1 = __fdiv_rn(r1, fd);
+    }
+    const size_t o = (size_t)r * KP + 2 * gl;
+    PairIO<CT>::store(a.cout + o, c0, c1);
+    if (a.rank) *reinterpret_cast<float2 *>(a.rank + o) = make_float2(r0, r1);
+}
+
+template <int KP>
+__device__ __forceinline__ void ppr_partial(float *acc, uint64_t first_item, float s0, float s1, uint32_t gl)
+{
+    float *p = acc + (size_t)(first_item / PPR_TILE) * KP + 2 * gl;
+    atomicAdd(p, s0);
+    atomicAdd(p + 1, s1);
+}
+
+/* one group of KP/2 lanes per tile; U edges' lines in flight per batch */
+template <int KP, class CT, int U>
+__global__ void __launch_bounds__(256) k_ppr_pull(PprArgs<CT> a)
+{
+    constexpr uint32_t LPE = KP / 2;
+    static_assert(U <= (int)LPE, "one id load per batch");
+    const uint32_t lane = threadIdx.x & 31, gl = lane % LPE;
+    const unsigned gmask = LPE == 32 ? 0xffffffffu : (((1u << LPE) - 1u) << (lane - gl));
+    const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) / LPE;
+    const uint32_t ngroups = (gridDim.x * blockDim.x) / LPE;
+    for (uint32_t tile = gid; tile < a.ntiles; tile += ngroups)
+    {
+        const uint2 c0 = a.coord[tile], c1 = a.coord[tile + 1];
+        const uint32_t i0 = c0.x, j0 = c0.y, i1 = c1.x, j1 = c1.y;
+        /* rows rb .. rb+LPE-1, one per lane: end offset, seed index, out-degree */
+        uint32_t rb = i0, w_end = 0, w_seed = NO_SEED, w_deg = 0;
+        auto fetch = [&](uint32_t base) {
+            rb = base;
+            const uint32_t row = base + gl;
+            w_end = a.E;
+            w_seed = NO_SEED;
+            w_deg = 0;
+            if (row < a.V)
+            {
+                w_end = a.off[row + 1];
+                w_seed = a.seed_idx[row];
+                w_deg = a.outdeg[row];
+            }
+        };
+        fetch(i0);
+        /* row i0 began in an earlier tile when its first edge precedes j0 */
+        const uint32_t start0 = i0 < a.V ? a.off[i0] : a.E;
+        uint32_t r = i0;
+        uint32_t re = __shfl_sync(gmask, w_end, 0, LPE);
+        float s0 = 0.0f, s1 = 0.0f;
+        /* finish row r (it ends in this tile) and move to r+1 */
+        auto next_row = [&]() {
+            const uint32_t k = r - rb;
+            const uint32_t si = __shfl_sync(gmask, w_seed, k, LPE);
+            const uint32_t deg = __shfl_sync(gmask, w_deg, k, LPE);
+            if (r == i0 && start0 < j0)
+                ppr_partial<KP>(a.acc, (uint64_t)i0 + start0, s0, s1, gl);
+            else
+                ppr_finish<KP, CT>(a, r, s0, s1, si, deg, gl);
+            s0 = 0.0f;
+            s1 = 0.0f;
+            r++;
+            if (r - rb >= LPE) fetch(r);
+            re = __shfl_sync(gmask, w_end, r - rb, LPE);
+        };
+        for (uint32_t e = j0; e < j1; e += U)
+        {
+            const uint32_t nb = min((uint32_t)U, j1 - e);
+            uint32_t myid = 0;
+            if (gl < nb) myid = ldg_stream(a.adj + e + gl);
+            typename PairIO<CT>::Raw v[U];
+#pragma unroll
+            for (int i = 0; i < U; i++)
+            {
+                const uint32_t u = __shfl_sync(gmask, myid, i, LPE);
+                if ((uint32_t)i < nb) v[i] = PairIO<CT>::load(a.cin + (size_t)u * KP + 2 * gl);
+            }
+#pragma unroll
+            for (int i = 0; i < U; i++)
+            {
+                if ((uint32_t)i < nb)
+                {
+                    /* rows ending before this edge, zero-degree rows included */
+                    while (e + i >= re) next_row();
+                    const float2 f = PairIO<CT>::unpack(v[i]);
+                    s0 += f.x;
+                    s1 += f.y;
+                }
+            }
+        }
+        /* rows whose end items follow the tile's last edge */
+        while (r < i1) next_row();
+        /* row i1 continues in the next tile: add what it gathered here */
+        if (i1 < a.V && j1 > j0)
+        {
+            const uint32_t o = a.off[i1];
+            if (o < j1) ppr_partial<KP>(a.acc, (uint64_t)i1 + o, s0, s1, gl);
+        }
+    }
+}
+
+/* finish the rows spanning tiles: tile t's slot belongs to the row that
+ * begins in t and is still open at t's end (row coord[t+1].x) */
+template <int KP, class CT>
+__global__ void __launch_bounds__(256) k_ppr_fixup(PprArgs<CT> a)
+{
+    constexpr uint32_t LPE = KP / 2;
+    const uint32_t lane = threadIdx.x & 31, gl = lane % LPE;
+    const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) / LPE;
+    const uint32_t ngroups = (gridDim.x * blockDim.x) / LPE;
+    for (uint32_t t = gid; t < a.ntiles; t += ngroups)
+    {
+        const uint32_t r = a.coord[t + 1].x;
+        if (r >= a.V) continue;
+        const uint32_t o = a.off[r];
+        if (((uint64_t)r + o) / PPR_TILE != t) continue;
+        float *p = a.acc + (size_t)t * KP + 2 * gl;
+        const float2 tot = *reinterpret_cast<const float2 *>(p);
+        ppr_finish<KP, CT>(a, r, tot.x, tot.y, a.seed_idx[r], a.outdeg[r], gl);
+        clear_after_read(p, tot.x);
+        clear_after_read(p + 1, tot.y);
+    }
+}
+
+/* contributions of the seed vertices at iteration 0 (the rest is zero) */
+template <int KP, class CT>
+__global__ void k_ppr_seed_init(const uint32_t *__restrict__ seed_vertex, uint32_t nseeds,
+                                const float *__restrict__ init, const uint32_t *__restrict__ outdeg, CT *cin,
+                                uint32_t *seed_idx)
+{
+    const uint64_t n = (uint64_t)nseeds * (KP / 2);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const uint32_t s = (uint32_t)(i / (KP / 2)), gl = (uint32_t)(i % (KP / 2));
+        const uint32_t v = seed_vertex[s];
+        if (gl == 0) seed_idx[v] = s;
+        const uint32_t deg = outdeg[v];
+        const float2 r = *reinterpret_cast<const float2 *>(init + (size_t)s * KP + 2 * gl);
+        float c0 = 0.0f, c1 = 0.0f;
+        if (deg)
+        {
+            const float fd = __uint2float_rn(deg);
+            c0 = __fdiv_rn(r.x, fd);
+            c1 = __fdiv_rn(r.y, fd);
+        }
+        PairIO<CT>::store(cin + (size_t)v * KP + 2 * gl, c0, c1);
+    }
+}
+
+template <class K>
+int occupancy_grid(K kernel, int threads, size_t work_groups, int lanes_per_group)
+{
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, threads, 0) != cudaSuccess || bps < 1)
+    {
+        cudaGetLastError();
+        bps = 1;
+    }
+    const size_t groups_per_block = (size_t)threads / lanes_per_group;
+    const size_t need = (work_groups + groups_per_block - 1) / groups_per_block;
+    const size_t cap = (size_t)gg_sm_count() * bps;
+    const size_t g = need < cap ? need : cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+template <int KP, class CT>
+gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const uint32_t *d_seedv, const float *d_init,
+                  const float *d_tele, uint32_t *d_seed_idx, float *d_rank, cudaStream_t s, gg_ppr_result &res,
+                  std::vector<cudaEvent_t> &evs)
+{
+    constexpr int LPE = KP / 2;
+    constexpr int U = LPE < 16 ? LPE : 16;
+    const uint32_t V = g->V;
+    gg_tiles &t = g->ppr_tiles;
+    if (!t.coord)
+    {
+        const uint64_t nt = ((uint64_t)V + g->E + PPR_TILE - 1) / PPR_TILE;
+        if (nt >= 0xffffffffull) return gg_fail(GG_ERR_INVALID, "graph too large for 32-bit tile ids");
+        t.ntiles = (uint32_t)(nt ? nt : 1);
+        GG_CHECK(gg_dev_alloc(g, (void **)&t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2)));
+        GG_CHECK(gg_launch_tile_coords(g->in_off, V, g->E, t.ntiles, t.coord, s, PPR_TILE));
+        res.launches++;
+    }
+    void *c0, *c1, *acc;
+    GG_CHECK(gg_work(g, 16, (size_t)V * KP * sizeof(CT), &c0));
+    GG_CHECK(gg_work(g, 17, (size_t)V * KP * sizeof(CT), &c1));
+    GG_CHECK(gg_work(g, 18, (size_t)t.ntiles * KP * sizeof(float), &acc));
+    GG_CUDA(cudaMemsetAsync(acc, 0, (size_t)t.ntiles * KP * sizeof(float), s));
+    GG_CUDA(cudaMemsetAsync(c0, 0, (size_t)V * KP * sizeof(CT), s));
+    GG_CUDA(cudaMemsetAsync(d_seed_idx, 0xff, (size_t)V * sizeof(uint32_t), s));
+    k_ppr_seed_init<KP, CT><<<gg_sm_count() * 2, 256, 0, s>>>(d_seedv, nseedv, d_init, g->out_deg, (CT *)c0, d_seed_idx);
+    res.launches++;
+
+    PprArgs<CT> a;
+    a.off = g->in_off; a.adj = g->in_adj; a.outdeg = g->out_deg; a.seed_idx = d_seed_idx;
+    a.coord = t.coord; a.ntiles = t.ntiles; a.V = V; a.E = g->E;
+    a.tele = d_tele; a.acc = (float *)acc; a.damp = p->damp;
+    CT *cb[2] = {(CT *)c0, (CT *)c1};
+    const int grid = occupancy_grid(k_ppr_pull<KP, CT, U>, 256, t.ntiles, LPE);
+    const int fgrid = occupancy_grid(k_ppr_fixup<KP, CT>, 256, t.ntiles, LPE);
+    for (uint32_t it = 0; it < p->iterations; it++)
+    {
+        a.cin = cb[it & 1];
+        a.cout = cb[(it + 1) & 1];
+        a.rank = it + 1 == p->iterations ? d_rank : nullptr;
+        if (p->profile)
+        {
+            cudaEvent_t e;
+            GG_CHECK(gg_event_at(g, (uint32_t)evs.size(), &e));
+            GG_CUDA(cudaEventRecord(e, s));
+            evs.push_back(e);
+        }
+        k_ppr_pull<KP, CT, U><<<grid, 256, 0, s>>>(a);
+        if (p->profile)
+        {
+            cudaEvent_t e;
+            GG_CHECK(gg_event_at(g, (uint32_t)evs.size(), &e));
+            GG_CUDA(cudaEventRecord(e, s));
+            evs.push_back(e);
+        }
+        k_ppr_fixup<KP, CT><<<fgrid, 256, 0, s>>>(a);
+        res.launches += 2;
+        res.gather_launches++;
+    }
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+}
+
+} // namespace
+
+extern "C" gg_status gg_ppr(gg_graph *g, const gg_ppr_params *p, const uint32_t *seed_off, const uint32_t *seeds,
+                            float *ranks, gg_ppr_result *r, void *stream)
+{
+    if (!g || !p || !seed_off) return gg_fail(GG_ERR_INVALID, "NULL argument");
+    const uint32_t K = p->num_vectors;
+    if (K < 1 || K > 64) return gg_fail(GG_ERR_INVALID, "num_vectors must be 1..64");
+    if (p->iterations < 1) return gg_fail(GG_ERR_INVALID, "iterations must be at least 1");
+    if (p->storage != GG_STORE_F32 && p->storage != GG_STORE_BF16)
+        return gg_fail(GG_ERR_INVALID, "batched PageRank stores FP32 or BF16 contributions");
+    if (!g->in_off || !g->out_deg) return gg_fail(GG_ERR_INVALID, "batched PageRank needs GG_MAP_IN");
+    if (seed_off[0] != 0) return gg_fail(GG_ERR_INVALID, "seed_off[0] must be 0");
+    for (uint32_t k = 0; k < K; k++)
+        if (seed_off[k + 1] < seed_off[k]) return gg_fail(GG_ERR_INVALID, "seed_off must be non-decreasing");
+    const uint32_t nseeds = seed_off[K];
+    if (nseeds && !seeds) return gg_fail(GG_ERR_INVALID, "NULL seeds");
+    const uint32_t V = g->V;
+    for (uint32_t i = 0; i < nseeds; i++)
+        if (seeds[i] >= V) return gg_fail(GG_ERR_INVALID, "seed vertex out of range");
+    const uint32_t KP = K <= 16 ? 16 : (K <= 32 ? 32 : 64);
+    cudaStream_t s = gg_stream(g, stream);
+    gg_ppr_result res;
+    memset(&res, 0, sizeof(res));
+    res.padded_vectors = KP;
+
+    /* seed vertices, each with its initial-rank and teleport rows */
+    std::vector<uint32_t> verts;
+    std::unordered_map<uint32_t, uint32_t> index;
+    for (uint32_t i = 0; i < nseeds; i++)
+        if (index.emplace(seeds[i], (uint32_t)verts.size()).second) verts.push_back(seeds[i]);
+    const uint32_t nv = (uint32_t)verts.size();
+    std::vector<double> share((size_t)nv * KP, 0.0);
+    for (uint32_t k = 0; k < K; k++)
+    {
+        const uint32_t n = seed_off[k + 1] - seed_off[k];
+        for (uint32_t i = seed_off[k]; i < seed_off[k + 1]; i++)
+            share[(size_t)index[seeds[i]] * KP + k] += 1.0 / (double)n;
+    }
+    std::vector<float> tables((size_t)nv * KP * 2);
+    for (size_t i = 0; i < share.size(); i++)
+    {
+        tables[i] = (float)share[i];
+        tables[share.size() + i] = (float)((1.0 - (double)p->damp) * share[i]);
+    }
+    void *d_seedv = nullptr, *d_tab = nullptr, *d_idx, *d_rank;
+    if (V > 0)
+    {
+        GG_CHECK(gg_work(g, 19, ((size_t)nv + 1) * 4, &d_seedv));
+        GG_CHECK(gg_work(g, 20, (tables.size() + 4) * sizeof(float), &d_tab));
+        GG_CHECK(gg_work(g, 21, (size_t)V * 4, &d_idx));
+        GG_CHECK(gg_work(g, 22, (size_t)V * KP * sizeof(float), &d_rank));
+        if (nv)
+        {
+            GG_CUDA(cudaMemcpyAsync(d_seedv, verts.data(), (size_t)nv * 4, cudaMemcpyHostToDevice, s));
+            GG_CUDA(cudaMemcpyAsync(d_tab, tables.data(), tables.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+        }
+        std::vector<cudaEvent_t> evs;
+        const float *d_init = (const float *)d_tab, *d_tele = (const float *)d_tab + (size_t)nv * KP;
+        gg_status st;
+#define GG_PPR_RUN(KPV, CTV)                                                                                          \
+    run_ppr<KPV, CTV>(g, p, nv, (const uint32_t *)d_seedv, d_init, d_tele, (uint32_t *)d_idx, (float *)d_rank, s,     \
+                      res, evs)
+        if (p->storage == GG_STORE_BF16)
+            st = KP == 16 ? GG_PPR_RUN(16, __nv_bfloat16) : KP == 32 ? GG_PPR_RUN(32, __nv_bfloat16) : GG_PPR_RUN(64, __nv_bfloat16);
+        else
+            st = KP == 16 ? GG_PPR_RUN(16, float) : KP == 32 ? GG_PPR_RUN(32, float) : GG_PPR_RUN(64, float);
+#undef GG_PPR_RUN
+        if (st != GG_OK) return st;
+        if (ranks)
+            GG_CUDA(cudaMemcpy2DAsync(ranks, (size_t)K * sizeof(float), d_rank, (size_t)KP * sizeof(float),
+                                      (size_t)K * sizeof(float), V, cudaMemcpyDeviceToHost, s));
+        GG_CHECK(gg_wait(s));
+        for (size_t i = 0; i + 1 < evs.size(); i += 2) res.gather_ms += gg_event_ms(evs[i], evs[i + 1]);
+        g->ppr_ranks = (const float *)d_rank;
+        g->ppr_stride = KP;
+    }
+    if (r) *r = res;
+    return GG_OK;
+}
+
+extern "C" const float *gg_ppr_device_ranks(const gg_graph *g, uint32_t *stride)
+{
+    if (!g) return nullptr;
+    if (stride) *stride = g->ppr_stride;
+    return g->ppr_ranks;
+}

@@ -216,6 +216,43 @@ gg_status gg_spmv_pull_noalloc(uint32_t V, uint32_t E, const uint32_t *in_off, c
 /* Largest V + E that gg_spmv_pull_noalloc accepts. */
 uint64_t gg_spmv_pull_noalloc_max_items(void);
 
+/* ---- batched personalised PageRank -------------------------------------------- */
+
+/*
+ * K personalised PageRank vectors over one graph, advanced together by one
+ * pull gather per iteration (no counterpart in the reference's C API; per
+ * vector it is the pull PageRank of pageRank.c:1026-1069 with the teleport
+ * going to the vector's seed set S_k instead of every vertex):
+ *     rank_0(v)  = c(v)/|S_k|,   rank'(v) = (1-d) c(v)/|S_k| + d * sum_{u->v} rank(u)/outdeg(u)
+ * where c(v) counts v in S_k (seeds may repeat).  Exactly `iterations`
+ * iterations run (no convergence test).  Needs GG_MAP_IN.
+ */
+typedef struct gg_ppr_params
+{
+    uint32_t num_vectors;     /* K, 1..64 */
+    uint32_t iterations;      /* >= 1 */
+    float damp;               /* 0.85 */
+    uint32_t storage;         /* GG_STORE_F32 or GG_STORE_BF16 contributions; sums are FP32 */
+    uint32_t profile;         /* 1: time every gather launch */
+} gg_ppr_params;
+
+typedef struct gg_ppr_result
+{
+    float gather_ms;          /* profile: summed device time of the gather launches */
+    uint32_t gather_launches;
+    uint32_t launches;
+    uint32_t padded_vectors;  /* vectors per vertex row on the device: 16, 32 or 64 */
+} gg_ppr_result;
+
+/* Seeds of vector k are seeds[seed_off[k] .. seed_off[k+1]) (host arrays,
+ * K+1 offsets, seed_off[0] = 0).  `ranks` (host, V*K floats, vertex-major:
+ * ranks[v*K + k]) receives the result when not NULL. */
+gg_status gg_ppr(gg_graph *g, const gg_ppr_params *p, const uint32_t *seed_off, const uint32_t *seeds,
+                 float *ranks, gg_ppr_result *r, void *stream);
+/* Device pointer to the last gg_ppr's ranks (V rows of *stride floats),
+ * valid until the next call on `g`. */
+const float *gg_ppr_device_ranks(const gg_graph *g, uint32_t *stride);
+
 /* ---- drop-in side options ---------------------------------------------------- */
 
 /*

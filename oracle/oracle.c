@@ -513,12 +513,20 @@ void orc_pagerank_f64(const orc_csr *g, uint32_t executed, int init_one_over_n, 
     free(contrib);
 }
 
-void orc_ppr_f64(const orc_csr *g, uint32_t seed, uint32_t iterations, double damp, double *ranks)
+/* Personalised PageRank with a seed set S (seeds[0..nseeds), repeats
+ * allowed): the reference's pull iteration (pageRank.c:1026-1069, no
+ * dangling redistribution) with the uniform teleport replaced by one to the
+ * seeds, each occurrence carrying 1/|S|:
+ *   rank_0(v) = c(v)/|S|,  rank'(v) = (1-d) c(v)/|S| + d * sum_{u in in(v)} rank(u)/outdeg(u)
+ * where c(v) counts v in S.  All in FP64, in-edges in CSC order. */
+void orc_ppr_f64_multi(const orc_csr *g, const uint32_t *seeds, uint32_t nseeds, uint32_t iterations, double damp,
+                       double *ranks)
 {
     const uint32_t V = g->V;
     double *contrib = (double *)malloc(((size_t)V + 1) * sizeof(double));
-    for (uint32_t v = 0; v < V; v++)
-        ranks[v] = v == seed ? 1.0 : 0.0;
+    double *tele = (double *)calloc((size_t)V + 1, sizeof(double));
+    for (uint32_t i = 0; i < nseeds; i++) tele[seeds[i]] += 1.0 / (double)nseeds;
+    for (uint32_t v = 0; v < V; v++) ranks[v] = tele[v];
     for (uint32_t it = 0; it < iterations; it++)
     {
         for (uint32_t v = 0; v < V; v++)
@@ -531,10 +539,16 @@ void orc_ppr_f64(const orc_csr *g, uint32_t seed, uint32_t iterations, double da
             double s = 0.0;
             for (uint32_t j = g->in_off[v]; j < g->in_off[v + 1]; j++)
                 s += contrib[g->in_adj[j]];
-            ranks[v] = (v == seed ? 1.0 - damp : 0.0) + damp * s;
+            ranks[v] = (1.0 - damp) * tele[v] + damp * s;
         }
     }
+    free(tele);
     free(contrib);
+}
+
+void orc_ppr_f64(const orc_csr *g, uint32_t seed, uint32_t iterations, double damp, double *ranks)
+{
+    orc_ppr_f64_multi(g, &seed, 1, iterations, damp, ranks);
 }
 
 /* ------------------------------------------------------------------------ */

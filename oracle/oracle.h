@@ -106,6 +106,10 @@ void orc_pagerank_f64(const orc_csr *g, uint32_t executed, int init_one_over_n, 
  * r0 = e_seed, exactly `iterations` pull iterations (dangling mass dropped as
  * in the global variant).  ranks: V doubles out. */
 void orc_ppr_f64(const orc_csr *g, uint32_t seed, uint32_t iterations, double damp, double *ranks);
+/* The same with a seed set (repeats allowed): each occurrence carries 1/nseeds
+ * of the initial rank and of the (1-d) teleport. */
+void orc_ppr_f64_multi(const orc_csr *g, const uint32_t *seeds, uint32_t nseeds, uint32_t iterations, double damp,
+                       double *ranks);
 
 /* ---- BFS ---------------------------------------------------------------- */
 

@@ -66,6 +66,7 @@ def lib():
         L.orc_pagerank.restype = C.c_int
         L.orc_pagerank_f64.argtypes = [C.POINTER(OrcCsr), C.c_uint32, C.c_int, f64p]
         L.orc_ppr_f64.argtypes = [C.POINTER(OrcCsr), C.c_uint32, C.c_uint32, C.c_double, f64p]
+        L.orc_ppr_f64_multi.argtypes = [C.POINTER(OrcCsr), u32p, C.c_uint32, C.c_uint32, C.c_double, f64p]
         L.orc_bfs.argtypes = [C.POINTER(OrcCsr), C.c_int, C.c_int, i32p, u32p, C.POINTER(OrcBfsOut), C.c_int]
         L.orc_spmv.argtypes = [C.POINTER(OrcCsr), C.c_int, C.c_uint32, C.c_void_p, f32p, f32p,
                                C.POINTER(C.c_double), C.c_int]
@@ -207,6 +208,15 @@ def ppr_f64(g: Csr, seed_vertex, iterations, damp=0.85):
     r = np.empty(g.V, np.float64)
     cs = g.c()
     lib().orc_ppr_f64(C.byref(cs), seed_vertex, iterations, damp, r)
+    return r
+
+
+def ppr_f64_multi(g: Csr, seeds, iterations, damp=0.85):
+    """FP64 personalised PageRank from a seed set (repeats allowed)."""
+    s = np.ascontiguousarray(seeds, np.uint32)
+    r = np.empty(g.V, np.float64)
+    cs = g.c()
+    lib().orc_ppr_f64_multi(C.byref(cs), s, len(s), iterations, damp, r)
     return r
 
 

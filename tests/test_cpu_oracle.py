@@ -103,3 +103,17 @@ def test_oracle_planted_error_is_caught(orc):
     gb = orc.Csr.from_arrays(g.V, g.E, g.out_off, g.out_adj, g.in_off, bad_adj)
     rb, _ = orc.pagerank(gb, 2, 10, 1e-4)
     assert not np.array_equal(r, rb)
+
+
+def test_oracle_ppr_seed_sets(orc):
+    """Personalised PageRank from a seed set: one seed is the single-seed
+    oracle, and the map from teleport vector to ranks is linear, so seeds
+    {a, b} give the mean of the two single-seed vectors; repeats weigh."""
+    g = orc.rmat_csr(11, 16)
+    a, b = 5, 77
+    ra, rb = orc.ppr_f64(g, a, 20), orc.ppr_f64(g, b, 20)
+    np.testing.assert_array_equal(orc.ppr_f64_multi(g, [a], 20), ra)
+    np.testing.assert_allclose(orc.ppr_f64_multi(g, [a, b], 20), 0.5 * (ra + rb), rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(orc.ppr_f64_multi(g, [a, a, b], 20), (2 * ra + rb) / 3, rtol=1e-12, atol=1e-15)
+    # mass leaks only through vertices without out-edges
+    assert orc.ppr_f64_multi(g, [a, b], 20).sum() <= 1.0 + 1e-12
