@@ -329,6 +329,50 @@ def splitmix_sources(V, deg, n, seed):
     return out
 
 
+def ppr_extras(gg, torch, peak, scale=22, K=64, iters=20):
+    """Batched personalised PageRank: K one-hot seed vectors (SplitMix64 from
+    vertices with out-edges) over a directed R-MAT graph, one multi-vector
+    pull gather per iteration; aggregate GTEPS = K*E*iters/t, roofline
+    against 4E + 8V + K*V*4s bytes per iteration, L1 vs FP64 for 4 vectors."""
+    import numpy as np
+    from oracle import oracle_ctypes as O
+
+    g = gg.Graph.rmat(scale, 16, seed=SEED)
+    V, E = g.V, g.E
+    dg = gg.DeviceGraph(g, gg.MAP_IN)
+    deg = g.views()["out_degree"]
+    seeds = splitmix_sources(V, deg, K, SEED + 3)
+    sets = [[s] for s in seeds]
+    out = {"graph": f"R-MAT-{scale} directed, V={V}, E={E}", "vectors": K, "iterations": iters}
+    a = g.arrays()
+    o = O.Csr.from_arrays(V, E, a["out_off"], a["out_adj"], a["in_off"], a["in_adj"])
+    check = [0, 1, K // 2, K - 1]
+    exact = {k: O.ppr_f64_multi(o, sets[k], iters, float(np.float32(0.85))) for k in check}
+    for storage, s in [("bf16", 2), ("f32", 4)]:
+        for _ in range(2):
+            dg.ppr(sets, iterations=iters, storage=storage, copy_out=False)
+        torch.cuda.synchronize()
+        reps, gms = 5, 0.0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            _, r = dg.ppr(sets, iterations=iters, storage=storage, copy_out=False, profile=True)
+            gms += r["gather_ms"] / max(r["gather_launches"], 1)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        ranks, _ = dg.ppr(sets, iterations=iters, storage=storage)
+        l1 = max(float(np.abs(ranks[:, k] - exact[k]).sum()) for k in check)
+        alg = 4 * E + 8 * V + K * V * 4 * s
+        out[storage] = {"gteps": K * E * iters / (ms / 1e3) / 1e9, "ms_per_run": ms,
+                        "gather_launch_ms": gms / reps,
+                        "iteration_hbm_frac": alg / (ms / iters / 1e3) / 1e9 / peak,
+                        "alg_bytes_per_iteration": alg, "l1_vs_fp64_max": l1}
+    dg.free()
+    g.free()
+    return out
+
+
 def bfs_extras(gg, torch, peak, scale=22):
     """BFS direction-optimising on an undirected R-MAT graph (each generated
     edge inserted both ways), 64 sources of nonzero degree; TEPS by the
@@ -461,6 +505,7 @@ def extras(gg, graph, dg, V, E, sptr, torch, peak):
     out.update(spmv_extras(gg, graph, V, E, sptr, torch, peak))
     dg.free()
     out["bfs_do"] = bfs_extras(gg, torch, peak)
+    out["ppr_batched"] = ppr_extras(gg, torch, peak)
     return out
 
 
