@@ -104,7 +104,10 @@ class ArrayQueue(C.Structure):
 class PrParams(C.Structure):
     _fields_ = [("mode", C.c_uint32), ("storage", C.c_uint32), ("max_iterations", C.c_uint32),
                 ("init_one_over_n", C.c_uint32), ("epsilon", C.c_double), ("damp", C.c_float),
-                ("profile", C.c_uint32)]
+                ("profile", C.c_uint32), ("flags", C.c_uint32)]
+
+
+PR_CUDA_GRAPH = 0x1
 
 
 class PrResult(C.Structure):
@@ -197,6 +200,11 @@ def lib() -> C.CDLL:
         L.generateRMATEdgeList.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
                                            C.c_uint64, C.c_int, C.c_uint64, C.c_int]
         L.generateRMATEdgeList.restype = P(EdgeList)
+        L.generateRMATBatchEdgeList.argtypes = [C.c_uint32, C.c_void_p, C.c_uint32, C.c_double, C.c_double,
+                                                C.c_double, C.c_uint64, C.c_void_p]
+        L.generateRMATBatchEdgeList.restype = P(EdgeList)
+        L.gg_pagerank_batch.argtypes = [C.c_void_p, P(PrParams), C.c_uint32, C.c_void_p, C.c_void_p, P(PrResult),
+                                        C.c_void_p]
         L.graphCSRFromEdgeList.argtypes = [P(EdgeList)]
         L.graphCSRFromEdgeList.restype = P(GraphCSR)
         L.graphCSRFree.argtypes = [P(GraphCSR)]
@@ -303,6 +311,21 @@ class Graph:
             L.freeEdgeList(el)
 
     @classmethod
+    def rmat_batch(cls, scales, edge_factor=8, a=0.57, b=0.19, c=0.19, seed0=27491095 + 4):
+        """The union of len(scales) R-MAT graphs, graph i drawn with seed
+        seed0 + i and renumbered from vertex_off[i]; returns (graph, vertex_off)."""
+        sc = np.ascontiguousarray(scales, np.uint32)
+        voff = np.empty(len(sc) + 1, np.uint32)
+        L = lib()
+        el = L.generateRMATBatchEdgeList(len(sc), sc.ctypes.data, edge_factor, a, b, c, seed0, voff.ctypes.data)
+        if not el:
+            raise GgError("generateRMATBatchEdgeList failed")
+        try:
+            return cls(L.graphCSRFromEdgeList(el)), voff
+        finally:
+            L.freeEdgeList(el)
+
+    @classmethod
     def rmat(cls, scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=27491095, weighted=False,
              weight_seed=27491095 + 2, symmetric=False):
         L = lib()
@@ -404,13 +427,27 @@ class DeviceGraph:
         return int(lib().gg_graph_device_bytes(self.h))
 
     def pagerank(self, mode="pull", storage="f32", iterations=20, epsilon=1e-4, init_one_over_n=False,
-                 damp=0.85, profile=False, copy_out=True, stream=None):
+                 damp=0.85, profile=False, copy_out=True, stream=None, cuda_graph=False):
         p = PrParams(PR_MODES[mode] if isinstance(mode, str) else mode, STORE[storage], iterations,
-                     int(init_one_over_n), epsilon, damp, int(profile))
+                     int(init_one_over_n), epsilon, damp, int(profile), PR_CUDA_GRAPH if cuda_graph else 0)
         r = PrResult()
         ranks = np.empty(self.graph.V, np.float32) if copy_out else None
         _check(lib().gg_pagerank(self.h, C.byref(p), None if ranks is None else ranks.ctypes.data, C.byref(r),
                                  stream), "gg_pagerank")
+        return ranks, {k: getattr(r, k) for k, _ in PrResult._fields_}
+
+    def pagerank_batch(self, vertex_off, mode="pull", storage="f32", iterations=20, epsilon=1e-4, damp=0.85,
+                       profile=False, copy_out=True, stream=None, cuda_graph=False):
+        """PageRank of a union of graphs (vertex ranges vertex_off[i] ..
+        vertex_off[i+1]); each vertex normalised by its own graph's size."""
+        voff = np.ascontiguousarray(vertex_off, np.uint32)
+        p = PrParams(PR_MODES[mode] if isinstance(mode, str) else mode, STORE[storage], iterations, 0, epsilon,
+                     damp, int(profile), PR_CUDA_GRAPH if cuda_graph else 0)
+        r = PrResult()
+        ranks = np.empty(self.graph.V, np.float32) if copy_out else None
+        _check(lib().gg_pagerank_batch(self.h, C.byref(p), len(voff) - 1, voff.ctypes.data,
+                                       None if ranks is None else ranks.ctypes.data, C.byref(r), stream),
+               "gg_pagerank_batch")
         return ranks, {k: getattr(r, k) for k, _ in PrResult._fields_}
 
     def bfs(self, source, mode="do", profile=False, copy_out=True, stream=None):

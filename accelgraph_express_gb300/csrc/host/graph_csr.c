@@ -172,6 +172,25 @@ struct EdgeList *readEdgeListsText(const char *fname, int weighted)
     return e;
 }
 
+/* edge i of the R-MAT graph of 2^scale vertices drawn with `seed` */
+static inline void rmat_edge(uint64_t seed, uint64_t i, uint32_t scale, double t1, double t2, double t3,
+                             uint32_t *src, uint32_t *dst)
+{
+    uint32_t s = 0, d = 0;
+    for (uint32_t l = 0; l < scale; l++)
+    {
+        const uint64_t r = mix64(seed + (i * scale + l + 1) * PHI);
+        const double u = (double)(r >> 11) * (1.0 / 9007199254740992.0);
+        const uint32_t bit = 1u << (scale - 1 - l);
+        if (u < t1) { }
+        else if (u < t2) d |= bit;
+        else if (u < t3) s |= bit;
+        else { s |= bit; d |= bit; }
+    }
+    *src = s;
+    *dst = d;
+}
+
 struct EdgeList *generateRMATEdgeList(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
                                       uint64_t seed, int weighted, uint64_t weight_seed, int symmetric)
 {
@@ -194,17 +213,8 @@ struct EdgeList *generateRMATEdgeList(uint32_t scale, uint32_t edge_factor, doub
 #pragma omp parallel for schedule(static)
     for (uint64_t i = 0; i < E0; i++)
     {
-        uint32_t s = 0, d = 0;
-        for (uint32_t l = 0; l < scale; l++)
-        {
-            const uint64_t r = mix64(seed + (i * scale + l + 1) * PHI);
-            const double u = (double)(r >> 11) * (1.0 / 9007199254740992.0);
-            const uint32_t bit = 1u << (scale - 1 - l);
-            if (u < t1) { }
-            else if (u < t2) d |= bit;
-            else if (u < t3) s |= bit;
-            else { s |= bit; d |= bit; }
-        }
+        uint32_t s, d;
+        rmat_edge(seed, i, scale, t1, t2, t3, &s, &d);
         src[i] = s;
         dst[i] = d;
         if (symmetric)
@@ -226,6 +236,63 @@ struct EdgeList *generateRMATEdgeList(uint32_t scale, uint32_t edge_factor, doub
         for (uint64_t i = 0; i < E; i++)
             if (w[i] > wmax) wmax = w[i];
     e->max_weight = wmax;
+    return e;
+}
+
+struct EdgeList *generateRMATBatchEdgeList(uint32_t ngraphs, const uint32_t *scales, uint32_t edge_factor, double a,
+                                           double b, double c, uint64_t seed0, uint32_t *vertex_off)
+{
+    if (!scales || !vertex_off)
+        return NULL;
+    uint64_t *eoff = (uint64_t *)malloc(((size_t)ngraphs + 1) * sizeof(uint64_t));
+    if (!eoff)
+        return NULL;
+    uint64_t V = 0, E = 0;
+    eoff[0] = 0;
+    for (uint32_t g = 0; g < ngraphs; g++)
+    {
+        if (scales[g] == 0 || scales[g] > 31)
+        {
+            free(eoff);
+            return NULL;
+        }
+        vertex_off[g] = (uint32_t)V;
+        V += 1ull << scales[g];
+        E += (1ull << scales[g]) * edge_factor;
+        eoff[g + 1] = E;
+        if (V >= 0xffffffffull || E >= 0xffffffffull)
+        {
+            fprintf(stderr, "generateRMATBatchEdgeList: %llu vertices / %llu edges do not fit 32-bit ids\n",
+                    (unsigned long long)V, (unsigned long long)E);
+            free(eoff);
+            return NULL;
+        }
+    }
+    vertex_off[ngraphs] = (uint32_t)V;
+    struct EdgeList *e = newEdgeList((uint32_t)E, (uint32_t)V, 0);
+    if (!e)
+    {
+        free(eoff);
+        return NULL;
+    }
+    const double t1 = a, t2 = a + b, t3 = a + b + c;
+    uint32_t *src = e->edges_array_src, *dst = e->edges_array_dest;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t g = 0; g < (int64_t)ngraphs; g++)
+    {
+        const uint32_t base = vertex_off[g], sc = scales[g];
+        const uint64_t n = eoff[g + 1] - eoff[g];
+        uint32_t *sp = src + eoff[g], *dp = dst + eoff[g];
+        for (uint64_t i = 0; i < n; i++)
+        {
+            uint32_t s, d;
+            rmat_edge(seed0 + (uint64_t)g, i, sc, t1, t2, t3, &s, &d);
+            sp[i] = base + s;
+            dp[i] = base + d;
+        }
+    }
+    e->num_vertices = (uint32_t)V;
+    free(eoff);
     return e;
 }
 

@@ -259,6 +259,33 @@ __global__ void k_pr_finalize(float *__restrict__ rank, uint32_t V, int divide, 
     if (threadIdx.x == 0 && s != 0.0) atomicAdd(sum, s);
 }
 
+/* final normalisation of a batch of graphs (vertex ranges voff[g] ..
+ * voff[g+1]): each vertex is divided by its own graph's vertex count */
+__global__ void k_pr_finalize_seg(float *__restrict__ rank, uint32_t V, const uint32_t *__restrict__ voff,
+                                  uint32_t ngraphs, double *sum)
+{
+    double s = 0.0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    {
+        /* graph of v: the last g with voff[g] <= v */
+        uint32_t lo = 0, hi = ngraphs - 1;
+        while (lo < hi)
+        {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (voff[mid] <= v)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const float r = __fdiv_rn(rank[v], __uint2float_rn(voff[lo + 1] - voff[lo]));
+        rank[v] = r;
+        s += (double)r;
+    }
+    uint32_t dummy = 0;
+    block_sum2<256>(s, dummy);
+    if (threadIdx.x == 0 && s != 0.0) atomicAdd(sum, s);
+}
+
 /* ---- push: scatter + vertex update ---------------------------------------------- */
 
 template <int K>
@@ -719,38 +746,13 @@ gg_status run_dd(Run &R, int mode, IterRec *rec, float *rank, uint32_t iters, fl
     return GG_OK;
 }
 
-} // namespace
-
-extern "C" gg_status gg_pagerank(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_result *r, void *stream)
+/* every launch of one PageRank run, queued on R.s */
+gg_status pagerank_enqueue(Run &R, const gg_pr_params *p, IterRec *rec, float *rank, void *sum_v, uint32_t ngraphs,
+                           const uint32_t *voff)
 {
-    if (!g || !p) return gg_fail(GG_ERR_INVALID, "NULL argument");
-    if (p->mode > 13) return gg_fail(GG_ERR_INVALID, "unknown PageRank mode");
-    if (p->storage > 2) return gg_fail(GG_ERR_INVALID, "unknown storage");
-    const int pull = !(p->mode == GG_PR_PUSH || p->mode == GG_PR_PUSH_FX64 || p->mode == GG_PR_PUSH_Q ||
-                       p->mode == GG_PR_DD_PUSH || p->mode == GG_PR_DD_PULLPUSH);
-    if (pull && !g->in_off) return gg_fail(GG_ERR_INVALID, "pull PageRank needs GG_MAP_IN");
-    if (!pull && !g->out_off) return gg_fail(GG_ERR_INVALID, "push PageRank needs GG_MAP_OUT");
-    if (!g->out_deg) return gg_fail(GG_ERR_INVALID, "mapping has no out-degrees");
-
-    Run R;
-    R.g = g;
-    R.s = gg_stream(g, stream);
-    R.p = p;
-    R.eps_f = gg_float_ceil(p->epsilon);
-    R.eps_fl = gg_float_floor(p->epsilon);
-    const uint32_t V = g->V, iters = p->max_iterations;
-    gg_pr_result res;
-    memset(&res, 0, sizeof(res));
-
-    void *rank_v, *rec_v, *sum_v;
-    GG_CHECK(gg_work(g, 0, ((size_t)V + 16) * 4, &rank_v));
-    GG_CHECK(gg_work(g, 1, ((size_t)iters + 2) * sizeof(IterRec), &rec_v));
-    GG_CHECK(gg_work(g, 10, 64, &sum_v));
-    IterRec *rec = (IterRec *)rec_v;
-    float *rank = (float *)rank_v;
+    const uint32_t V = R.g->V, iters = p->max_iterations;
     GG_CUDA(cudaMemsetAsync(rec, 0, ((size_t)iters + 2) * sizeof(IterRec), R.s));
     GG_CUDA(cudaMemsetAsync(sum_v, 0, 64, R.s));
-
     const float damp = p->damp;
     const float base_pr = 1.0f - damp;
     const float base = p->init_one_over_n ? base_pr / (float)V : base_pr;
@@ -783,10 +785,81 @@ extern "C" gg_status gg_pagerank(gg_graph *g, const gg_pr_params *p, float *rank
         default: st = run_dd(R, (int)p->mode, rec, rank, iters, base, init); break;
         }
         if (st != GG_OK) return st;
-        k_pr_finalize<<<grid_v(V), 256, 0, R.s>>>(rank, V, p->init_one_over_n ? 0 : 1, (double *)sum_v);
+        if (ngraphs)
+            k_pr_finalize_seg<<<grid_v(V), 256, 0, R.s>>>(rank, V, voff, ngraphs, (double *)sum_v);
+        else
+            k_pr_finalize<<<grid_v(V), 256, 0, R.s>>>(rank, V, p->init_one_over_n ? 0 : 1, (double *)sum_v);
         R.launches++;
         GG_CUDA(cudaGetLastError());
     }
+    return GG_OK;
+}
+
+
+/* one PageRank run; with ngraphs > 0 the mapping is the union of ngraphs
+ * graphs (vertex ranges h_voff[g] .. h_voff[g+1]) and the final
+ * normalisation divides each vertex by its own graph's vertex count */
+gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_result *r, void *stream,
+                        uint32_t ngraphs, const uint32_t *h_voff)
+{
+    if (!g || !p) return gg_fail(GG_ERR_INVALID, "NULL argument");
+    if (p->mode > 13) return gg_fail(GG_ERR_INVALID, "unknown PageRank mode");
+    if (p->storage > 2) return gg_fail(GG_ERR_INVALID, "unknown storage");
+    const int pull = !(p->mode == GG_PR_PUSH || p->mode == GG_PR_PUSH_FX64 || p->mode == GG_PR_PUSH_Q ||
+                       p->mode == GG_PR_DD_PUSH || p->mode == GG_PR_DD_PULLPUSH);
+    if (pull && !g->in_off) return gg_fail(GG_ERR_INVALID, "pull PageRank needs GG_MAP_IN");
+    if (!pull && !g->out_off) return gg_fail(GG_ERR_INVALID, "push PageRank needs GG_MAP_OUT");
+    if (!g->out_deg) return gg_fail(GG_ERR_INVALID, "mapping has no out-degrees");
+
+    Run R;
+    R.g = g;
+    R.s = gg_stream(g, stream);
+    R.p = p;
+    R.eps_f = gg_float_ceil(p->epsilon);
+    R.eps_fl = gg_float_floor(p->epsilon);
+    const uint32_t V = g->V, iters = p->max_iterations;
+    gg_pr_result res;
+    memset(&res, 0, sizeof(res));
+
+    void *rank_v, *rec_v, *sum_v, *voff_v = nullptr;
+    GG_CHECK(gg_work(g, 0, ((size_t)V + 16) * 4, &rank_v));
+    GG_CHECK(gg_work(g, 1, ((size_t)iters + 2) * sizeof(IterRec), &rec_v));
+    GG_CHECK(gg_work(g, 10, 64, &sum_v));
+    IterRec *rec = (IterRec *)rec_v;
+    float *rank = (float *)rank_v;
+    if (ngraphs)
+    {
+        GG_CHECK(gg_work(g, 23, ((size_t)ngraphs + 1) * 4, &voff_v));
+        GG_CUDA(cudaMemcpyAsync(voff_v, h_voff, ((size_t)ngraphs + 1) * 4, cudaMemcpyHostToDevice, R.s));
+    }
+
+    /* with GG_PR_CUDA_GRAPH everything from here to the final normalisation
+     * is captured into one CUDA graph and launched once (relaxed capture:
+     * buffers first used inside it are allocated during the capture) */
+    const bool as_graph = (p->flags & GG_PR_CUDA_GRAPH) != 0;
+    if (as_graph) GG_CUDA(cudaStreamBeginCapture(R.s, cudaStreamCaptureModeRelaxed));
+    gg_status st = pagerank_enqueue(R, p, rec, rank, sum_v, ngraphs, (const uint32_t *)voff_v);
+    if (as_graph)
+    {
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(R.s, &graph);
+        if (st == GG_OK && e != cudaSuccess) st = gg_cuda_fail(e, "cudaStreamEndCapture");
+        cudaGraphExec_t exec = nullptr;
+        if (st == GG_OK)
+        {
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            if (e != cudaSuccess) st = gg_cuda_fail(e, "cudaGraphInstantiate");
+        }
+        if (st == GG_OK)
+        {
+            e = cudaGraphLaunch(exec, R.s);
+            if (e != cudaSuccess) st = gg_cuda_fail(e, "cudaGraphLaunch");
+        }
+        if (st == GG_OK) st = gg_wait(R.s);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+    if (st != GG_OK) return st;
 
     std::vector<IterRec> h(iters + 2);
     double sum = 0.0;
@@ -819,6 +892,26 @@ extern "C" gg_status gg_pagerank(gg_graph *g, const gg_pr_params *p, float *rank
     g->last_ranks = rank;
     if (r) *r = res;
     return GG_OK;
+}
+
+} // namespace
+
+extern "C" gg_status gg_pagerank(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_result *r, void *stream)
+{
+    return pagerank_impl(g, p, ranks, r, stream, 0, nullptr);
+}
+
+extern "C" gg_status gg_pagerank_batch(gg_graph *g, const gg_pr_params *p, uint32_t ngraphs, const uint32_t *vertex_off,
+                                       float *ranks, gg_pr_result *r, void *stream)
+{
+    if (!g || !p || !vertex_off || ngraphs == 0) return gg_fail(GG_ERR_INVALID, "NULL argument or no graphs");
+    if (p->init_one_over_n)
+        return gg_fail(GG_ERR_INVALID, "batched PageRank uses the reference formulation (init_one_over_n = 0)");
+    if (vertex_off[0] != 0 || vertex_off[ngraphs] != g->V)
+        return gg_fail(GG_ERR_INVALID, "vertex_off must run from 0 to the mapping's vertex count");
+    for (uint32_t i = 0; i < ngraphs; i++)
+        if (vertex_off[i + 1] <= vertex_off[i]) return gg_fail(GG_ERR_INVALID, "every graph needs a vertex");
+    return pagerank_impl(g, p, ranks, r, stream, ngraphs, vertex_off);
 }
 
 extern "C" const float *gg_pagerank_device_ranks(const gg_graph *g) { return g ? g->last_ranks : nullptr; }

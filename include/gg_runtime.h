@@ -100,7 +100,12 @@ typedef struct gg_pr_params
     double epsilon;
     float damp;               /* 0.85f in the reference */
     uint32_t profile;         /* 1: time every gather launch with CUDA events */
+    uint32_t flags;           /* GG_PR_CUDA_GRAPH */
 } gg_pr_params;
+
+/* Run the whole call (initialisation, every iteration, normalisation) as
+ * one CUDA graph launch; per-launch timing (profile) is not available then. */
+#define GG_PR_CUDA_GRAPH 0x1u
 
 typedef struct gg_pr_result
 {
@@ -119,6 +124,15 @@ gg_status gg_pagerank(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_re
 /* Device pointer to the last run's final ranks (V floats), valid until the
  * next call on `g`. */
 const float *gg_pagerank_device_ranks(const gg_graph *g);
+/* PageRank over a mapping that is the union of `ngraphs` graphs occupying
+ * vertex ranges vertex_off[i] .. vertex_off[i+1] (host array, ngraphs+1
+ * entries, from 0 to V; no counterpart in the reference): the iterations of
+ * gg_pagerank over the union, then each vertex divided by its own graph's
+ * vertex count, so with no edges between the ranges every graph gets its own
+ * PageRank.  The reference formulation only (init_one_over_n = 0); the stop
+ * rule and error_total are over the union. */
+gg_status gg_pagerank_batch(gg_graph *g, const gg_pr_params *p, uint32_t ngraphs, const uint32_t *vertex_off,
+                            float *ranks, gg_pr_result *r, void *stream);
 
 /* ---- BFS -------------------------------------------------------------------- */
 

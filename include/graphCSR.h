@@ -106,6 +106,17 @@ struct EdgeList *generateRMATEdgeList(uint32_t scale, uint32_t edge_factor,
                                       uint64_t seed, int weighted, uint64_t weight_seed,
                                       int symmetric);
 
+/*
+ * The block-diagonal union of `ngraphs` R-MAT graphs (no counterpart in the
+ * reference; it feeds batched runs over many small graphs): graph g has
+ * 2^scales[g] vertices, renumbered from vertex_off[g], and is exactly
+ * generateRMATEdgeList(scales[g], edge_factor, a, b, c, seed0 + g, 0, 0, 0)
+ * shifted by vertex_off[g].  vertex_off (ngraphs + 1 entries) is written;
+ * vertex_off[ngraphs] is the total vertex count.  Unweighted.
+ */
+struct EdgeList *generateRMATBatchEdgeList(uint32_t ngraphs, const uint32_t *scales, uint32_t edge_factor,
+                                           double a, double b, double c, uint64_t seed0, uint32_t *vertex_off);
+
 /* ---- CSR ------------------------------------------------------------------ */
 
 /*

@@ -45,7 +45,7 @@ def test_struct_sizes_match_c_layout(gg, tmp_path):
                "SPMVStats": gg.SPMVStats, "Bitmap": gg.Bitmap, "ArrayQueue": gg.ArrayQueue}
     typedefs = {"gg_pr_params": gg.PrParams, "gg_pr_result": gg.PrResult, "gg_bfs_params": gg.BfsParams,
                 "gg_bfs_result": gg.BfsResult, "gg_spmv_params": gg.SpmvParams, "gg_spmv_result": gg.SpmvResult,
-                "GraphGpuOptions": gg.GraphGpuOptions}
+                "GraphGpuOptions": gg.GraphGpuOptions, "gg_ppr_params": gg.PprParams, "gg_ppr_result": gg.PprResult}
     src = ['#include <stdio.h>', '#include "pageRank.h"', '#include "BFS.h"', '#include "SPMV.h"',
            '#include "gg_runtime.h"', "int main(void){"]
     for n in structs:
@@ -162,3 +162,20 @@ def test_gpu_calls_fail_loudly_without_device(gg):
     g = gg.Graph.rmat(6, 4)
     assert not gg.lib().pageRankGraphCSR(C.byref(gg.default_arguments()), g.ptr)
     assert gg.lib().graphGpuLastError() != 0
+
+
+def test_rmat_batch_is_union_of_single_graphs(gg):
+    """generateRMATBatchEdgeList: block i of the union is exactly the R-MAT
+    graph of scale scales[i] and seed seed0 + i, renumbered from vertex_off[i]."""
+    scales = [4, 6, 3, 7, 5]
+    g, voff = gg.Graph.rmat_batch(scales, edge_factor=8, seed0=1234)
+    assert list(voff) == list(np.cumsum([0] + [1 << s for s in scales]))
+    a = g.arrays()
+    for i, sc in enumerate(scales):
+        one = gg.Graph.rmat(sc, 8, seed=1234 + i).arrays()
+        lo, hi = int(voff[i]), int(voff[i + 1])
+        for side in ("out", "in"):
+            off, adj = a[side + "_off"], a[side + "_adj"]
+            blk = off[lo:hi + 1] - off[lo]
+            np.testing.assert_array_equal(blk, one[side + "_off"])
+            np.testing.assert_array_equal(adj[off[lo]:off[hi]] - lo, one[side + "_adj"])

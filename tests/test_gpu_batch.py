@@ -1,0 +1,67 @@
+"""PageRank over a batch of graphs (gg_pagerank_batch) and whole runs
+launched as one CUDA graph (GG_PR_CUDA_GRAPH).
+
+The batch is the block-diagonal union of small R-MAT graphs; each graph's
+ranks must match the oracle's PageRank of that graph alone
+(pageRank.c:942-1109, normalised by the graph's own vertex count).  A run
+captured into a CUDA graph must give what the same run gives launch by
+launch (bit for bit in the exact integer formats).
+"""
+import numpy as np
+import pytest
+
+from fpcheck import assert_fp_as_accurate
+from graphs import pair
+
+pytestmark = pytest.mark.gpu
+
+SCALES = [5, 9, 7, 10, 6, 8]
+SEED0 = 2024
+
+
+@pytest.fixture(scope="module")
+def batch(gpu):
+    return gpu.Graph.rmat_batch(SCALES, edge_factor=8, seed0=SEED0)
+
+
+@pytest.mark.parametrize("cuda_graph", [False, True])
+def test_batch_pagerank_matches_each_graph(gpu, orc, batch, cuda_graph):
+    g, voff = batch
+    dg = gpu.DeviceGraph(g, gpu.MAP_IN)
+    ranks, res = dg.pagerank_batch(voff, iterations=20, epsilon=0.0, cuda_graph=cuda_graph)
+    dg.free()
+    assert res["iterations"] == 20
+    for i, sc in enumerate(SCALES):
+        o = orc.rmat_csr(sc, 8, seed=SEED0 + i)
+        ref, info = orc.pagerank(o, 0, 20, 0.0)
+        ex = orc.pagerank_f64(o, info["executed"])
+        assert_fp_as_accurate(ranks[voff[i]:voff[i + 1]], ref, ex, f"graph {i} (scale {sc})")
+
+
+@pytest.mark.parametrize("mode", ["pull", "pull_fx64", "push", "dd_pull", "pull_q16"])
+def test_cuda_graph_run_equals_launch_by_launch(gpu, orc, mode):
+    g, o = pair(gpu, orc, gpu.Graph.rmat(12, 16))
+    dg = gpu.DeviceGraph(g, gpu.MAP_ALL)
+    a, ra = dg.pagerank(mode, iterations=20, epsilon=1e-4)
+    b, rb = dg.pagerank(mode, iterations=20, epsilon=1e-4, cuda_graph=True)
+    dg.free()
+    assert ra["iterations"] == rb["iterations"]
+    if mode in ("pull_fx64", "pull_q16"):
+        np.testing.assert_array_equal(a, b)
+    else:
+        np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-12)
+
+
+def test_batch_rejects_bad_arguments(gpu, batch):
+    g, voff = batch
+    dg = gpu.DeviceGraph(g, gpu.MAP_IN)
+    with pytest.raises(gpu.GgError):
+        dg.pagerank_batch(voff[:-1])            # does not reach V
+    bad = voff.copy()
+    bad[2] = bad[1]
+    with pytest.raises(gpu.GgError):
+        dg.pagerank_batch(bad)                  # an empty graph
+    p = gpu.PrParams(0, 0, 20, 1, 0.0, 0.85, 0, 0)
+    r = gpu.PrResult()
+    assert gpu.lib().gg_pagerank_batch(dg.h, p, len(voff) - 1, voff.ctypes.data, None, r, None) == 1
+    dg.free()
