@@ -373,6 +373,59 @@ def ppr_extras(gg, torch, peak, scale=22, K=64, iters=20):
     return out
 
 
+def splitmix_unit(seed):
+    """A uniform double in [0, 1) from one SplitMix64 output (53 bits)."""
+    mask = (1 << 64) - 1
+    z = (seed + 0x9E3779B97F4A7C15) & mask
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & mask
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & mask
+    z ^= z >> 31
+    return (z >> 11) / float(1 << 53)
+
+
+def batch_extras(gg, torch, peak, n=4096, iters=20):
+    """Many small graphs in one run: n R-MAT graphs, graph i of scale
+    round(10 + 7u) with u uniform from SplitMix64(seed+4+i) (V = 2^scale,
+    log-uniform between 2^10 and 2^17), edge factor 8, R-MAT seed seed+4+i;
+    their union is ranked by one pull PageRank of `iters` iterations launched
+    as a single CUDA graph, every vertex normalised by its own graph's size."""
+    import numpy as np
+    from oracle import oracle_ctypes as O
+
+    scales = [int(round(10 + 7 * splitmix_unit(SEED + 4 + i))) for i in range(n)]
+    t0 = time.perf_counter()
+    g, voff = gg.Graph.rmat_batch(scales, edge_factor=8, seed0=SEED + 4)
+    build_s = time.perf_counter() - t0
+    V, E = g.V, g.E
+    dg = gg.DeviceGraph(g, gg.MAP_IN)
+    for _ in range(2):
+        dg.pagerank_batch(voff, iterations=iters, epsilon=0.0, copy_out=False, cuda_graph=True)
+    torch.cuda.synchronize()
+    reps = 5
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        dg.pagerank_batch(voff, iterations=iters, epsilon=0.0, copy_out=False, cuda_graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    ranks, _ = dg.pagerank_batch(voff, iterations=iters, epsilon=0.0, cuda_graph=True)
+    dg.free()
+    g.free()
+    # parity on the smallest, a middle and the largest graph
+    order = np.argsort(scales, kind="stable")
+    worst = 0.0
+    for i in (int(order[0]), int(order[n // 2]), int(order[-1])):
+        o = O.rmat_csr(scales[i], 8, seed=SEED + 4 + i)
+        ex = O.pagerank_f64(o, iters)
+        part = ranks[voff[i]:voff[i + 1]]
+        worst = max(worst, float(np.abs(part - ex).sum() / np.abs(ex).sum()))
+    return {"graphs": n, "vertices": V, "edges": E, "iterations": iters, "build_s": round(build_s, 1),
+            "ms_per_run": ms, "gteps": E * iters / (ms / 1e3) / 1e9,
+            "iteration_hbm_frac": pr_bytes(V, E, 4) / (ms / iters / 1e3) / 1e9 / peak,
+            "l1_relative_vs_fp64_max": worst, "launch": "one CUDA graph per run"}
+
+
 def bfs_extras(gg, torch, peak, scale=22):
     """BFS direction-optimising on an undirected R-MAT graph (each generated
     edge inserted both ways), 64 sources of nonzero degree; TEPS by the
@@ -506,6 +559,7 @@ def extras(gg, graph, dg, V, E, sptr, torch, peak):
     dg.free()
     out["bfs_do"] = bfs_extras(gg, torch, peak)
     out["ppr_batched"] = ppr_extras(gg, torch, peak)
+    out["many_graphs"] = batch_extras(gg, torch, peak)
     return out
 
 
