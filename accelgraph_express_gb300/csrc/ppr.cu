@@ -17,8 +17,11 @@
  * lines is in flight while the previous ones are summed.  Rows are finished
  * where they end: rank = teleport + d * sum (the teleport row comes through a
  * per-vertex seed index), contribution = rank / outdeg; FP32 ranks are only
- * written by the last iteration.  Rows spanning tiles add their partial sums
- * atomically into their first tile's slot and k_ppr_fixup finishes them.
+ * written by the last iteration.  A row spanning tiles leaves its partial
+ * sum in per-tile slots (the tile where it began or that it crosses: `tail`;
+ * the tile where it ends: `head`) and k_ppr_fixup adds them in tile order, so
+ * every vector's result is deterministic and independent of the vectors
+ * batched with it.
  */
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
@@ -82,7 +85,8 @@ struct PprArgs
     CT *cout;
     float *rank;       /* [V][KP], written when not null (last iteration) */
     const float *tele; /* [nseeds][KP]: (1-d) c_k(v) / |S_k| of seed vertex i */
-    float *acc;        /* [ntiles][KP] partial sums of rows spanning tiles, zero between launches */
+    float *head;       /* [ntiles][KP]: partial of the row that ends in the tile but began before it */
+    float *tail;       /* [ntiles][KP]: partial of the row left open at the tile's end */
     float damp;
 };
 
@@ -111,11 +115,9 @@ __device__ __forceinline__ void ppr_finish(const PprArgs<CT> &a, uint32_t r, flo
 }
 
 template <int KP>
-__device__ __forceinline__ void ppr_partial(float *acc, uint64_t first_item, float s0, float s1, uint32_t gl)
+__device__ __forceinline__ void ppr_slot(float *slots, uint32_t tile, float s0, float s1, uint32_t gl)
 {
-    float *p = acc + (size_t)(first_item / PPR_TILE) * KP + 2 * gl;
-    atomicAdd(p, s0);
-    atomicAdd(p + 1, s1);
+    *reinterpret_cast<float2 *>(slots + (size_t)tile * KP + 2 * gl) = make_float2(s0, s1);
 }
 
 /* one group of KP/2 lanes per tile; U edges' lines in flight per batch */
@@ -159,7 +161,7 @@ __global__ void __launch_bounds__(256) k_ppr_pull(PprArgs<CT> a)
             const uint32_t si = __shfl_sync(gmask, w_seed, k, LPE);
             const uint32_t deg = __shfl_sync(gmask, w_deg, k, LPE);
             if (r == i0 && start0 < j0)
-                ppr_partial<KP>(a.acc, (uint64_t)i0 + start0, s0, s1, gl);
+                ppr_slot<KP>(a.head, tile, s0, s1, gl);
             else
                 ppr_finish<KP, CT>(a, r, s0, s1, si, deg, gl);
             s0 = 0.0f;
@@ -195,21 +197,22 @@ __global__ void __launch_bounds__(256) k_ppr_pull(PprArgs<CT> a)
         }
         /* rows whose end items follow the tile's last edge */
         while (r < i1) next_row();
-        /* row i1 continues in the next tile: add what it gathered here */
+        /* row i1 continues in the next tile: leave what it gathered here */
         if (i1 < a.V && j1 > j0)
         {
             const uint32_t o = a.off[i1];
-            if (o < j1) ppr_partial<KP>(a.acc, (uint64_t)i1 + o, s0, s1, gl);
+            if (o < j1) ppr_slot<KP>(a.tail, tile, s0, s1, gl);
         }
     }
 }
 
-/* finish the rows spanning tiles: tile t's slot belongs to the row that
- * begins in t and is still open at t's end (row coord[t+1].x) */
+/* finish the rows spanning tiles: the row that begins in tile t and is
+ * still open at t's end (row coord[t+1].x) sums tail[t], the tails of the
+ * tiles it crosses and the head of the tile where it ends, in tile order */
 template <int KP, class CT>
 __global__ void __launch_bounds__(256) k_ppr_fixup(PprArgs<CT> a)
 {
-    constexpr uint32_t LPE = KP / 2;
+    constexpr uint32_t LPE = KP / 2, B = 8;
     const uint32_t lane = threadIdx.x & 31, gl = lane % LPE;
     const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) / LPE;
     const uint32_t ngroups = (gridDim.x * blockDim.x) / LPE;
@@ -217,13 +220,28 @@ __global__ void __launch_bounds__(256) k_ppr_fixup(PprArgs<CT> a)
     {
         const uint32_t r = a.coord[t + 1].x;
         if (r >= a.V) continue;
-        const uint32_t o = a.off[r];
-        if (((uint64_t)r + o) / PPR_TILE != t) continue;
-        float *p = a.acc + (size_t)t * KP + 2 * gl;
-        const float2 tot = *reinterpret_cast<const float2 *>(p);
+        if (((uint64_t)r + a.off[r]) / PPR_TILE != t) continue;
+        /* the tile of the row's end item */
+        const uint32_t t_last = (uint32_t)(((uint64_t)r + a.off[r + 1]) / PPR_TILE);
+        float2 tot = *reinterpret_cast<const float2 *>(a.tail + (size_t)t * KP + 2 * gl);
+        for (uint32_t m = t + 1; m < t_last; m += B)
+        {
+            float2 v[B];
+#pragma unroll
+            for (uint32_t i = 0; i < B; i++)
+                if (m + i < t_last) v[i] = *reinterpret_cast<const float2 *>(a.tail + (size_t)(m + i) * KP + 2 * gl);
+#pragma unroll
+            for (uint32_t i = 0; i < B; i++)
+                if (m + i < t_last)
+                {
+                    tot.x += v[i].x;
+                    tot.y += v[i].y;
+                }
+        }
+        const float2 h = *reinterpret_cast<const float2 *>(a.head + (size_t)t_last * KP + 2 * gl);
+        tot.x += h.x;
+        tot.y += h.y;
         ppr_finish<KP, CT>(a, r, tot.x, tot.y, a.seed_idx[r], a.outdeg[r], gl);
-        clear_after_read(p, tot.x);
-        clear_after_read(p + 1, tot.y);
     }
 }
 
@@ -286,11 +304,10 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
         GG_CHECK(gg_launch_tile_coords(g->in_off, V, g->E, t.ntiles, t.coord, s, PPR_TILE));
         res.launches++;
     }
-    void *c0, *c1, *acc;
+    void *c0, *c1, *slots;
     GG_CHECK(gg_work(g, 16, (size_t)V * KP * sizeof(CT), &c0));
     GG_CHECK(gg_work(g, 17, (size_t)V * KP * sizeof(CT), &c1));
-    GG_CHECK(gg_work(g, 18, (size_t)t.ntiles * KP * sizeof(float), &acc));
-    GG_CUDA(cudaMemsetAsync(acc, 0, (size_t)t.ntiles * KP * sizeof(float), s));
+    GG_CHECK(gg_work(g, 18, (size_t)t.ntiles * KP * sizeof(float) * 2, &slots));
     GG_CUDA(cudaMemsetAsync(c0, 0, (size_t)V * KP * sizeof(CT), s));
     GG_CUDA(cudaMemsetAsync(d_seed_idx, 0xff, (size_t)V * sizeof(uint32_t), s));
     k_ppr_seed_init<KP, CT><<<gg_sm_count() * 2, 256, 0, s>>>(d_seedv, nseedv, d_init, g->out_deg, (CT *)c0, d_seed_idx);
@@ -299,7 +316,9 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
     PprArgs<CT> a;
     a.off = g->in_off; a.adj = g->in_adj; a.outdeg = g->out_deg; a.seed_idx = d_seed_idx;
     a.coord = t.coord; a.ntiles = t.ntiles; a.V = V; a.E = g->E;
-    a.tele = d_tele; a.acc = (float *)acc; a.damp = p->damp;
+    a.tele = d_tele; a.damp = p->damp;
+    a.head = (float *)slots;
+    a.tail = (float *)slots + (size_t)t.ntiles * KP;
     CT *cb[2] = {(CT *)c0, (CT *)c1};
     const int grid = occupancy_grid(k_ppr_pull<KP, CT, U>, 256, t.ntiles, LPE);
     const int fgrid = occupancy_grid(k_ppr_fixup<KP, CT>, 256, t.ntiles, LPE);

@@ -98,16 +98,21 @@ def test_ppr_hub_rows_span_tiles(gpu, orc, hub):
     assert err[1:].sum(0).max() <= 1e-6
 
 
-def test_ppr_vector_independent_of_batch(gpu, rg):
+@pytest.mark.parametrize("storage", ["f32", "bf16"])
+def test_ppr_vector_independent_of_batch(gpu, rg, storage):
+    """A vector's result is bit-identical alone, in a batch of 64 and in the
+    same batch reordered: each vector's sums run in CSC edge order and rows
+    spanning tiles add their per-tile partials in tile order."""
     g, _ = rg
     sets = seed_sets(g.V, 64, g.arrays()["out_degree"], np.random.default_rng(3))
     dg = gpu.DeviceGraph(g, gpu.MAP_IN)
-    batch, _ = dg.ppr(sets, iterations=ITERS, storage="f32")
+    batch, _ = dg.ppr(sets, iterations=ITERS, storage=storage)
+    perm = np.random.default_rng(4).permutation(64)
+    shuffled, _ = dg.ppr([sets[i] for i in perm], iterations=ITERS, storage=storage)
+    np.testing.assert_array_equal(shuffled, batch[:, perm])
     for k in (0, 1, 2, 40, 63):
-        alone, _ = dg.ppr([sets[k]], iterations=ITERS, storage="f32")
-        # rows summed across tiles take their partials in arrival order, so
-        # the comparison allows FP32 reassociation, nothing more
-        np.testing.assert_allclose(alone[:, 0], batch[:, k], rtol=1e-5, atol=1e-9)
+        alone, _ = dg.ppr([sets[k]], iterations=ITERS, storage=storage)
+        np.testing.assert_array_equal(alone[:, 0], batch[:, k])
     dg.free()
 
 
