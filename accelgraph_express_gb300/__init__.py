@@ -142,6 +142,17 @@ class PprResult(C.Structure):
                 ("padded_vectors", C.c_uint32)]
 
 
+class ServerParams(C.Structure):
+    _fields_ = [("max_ppr_batch", C.c_uint32), ("ppr_iterations", C.c_uint32), ("damp", C.c_float),
+                ("ppr_storage", C.c_uint32), ("mem_budget_bytes", C.c_uint64)]
+
+
+class QueryInfo(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("status", C.c_uint32), ("submit_s", C.c_double), ("start_s", C.c_double),
+                ("done_s", C.c_double), ("batch_size", C.c_uint32), ("bfs_levels", C.c_uint32),
+                ("bfs_reached", C.c_uint32)]
+
+
 class SpmvResult(C.Structure):
     _fields_ = [("checksum", C.c_double), ("spmv_ms", C.c_float), ("spmv_launches", C.c_uint32),
                 ("launches", C.c_uint32)]
@@ -190,6 +201,13 @@ def lib() -> C.CDLL:
         L.gg_ppr.argtypes = [C.c_void_p, P(PprParams), C.c_void_p, C.c_void_p, C.c_void_p, P(PprResult), C.c_void_p]
         L.gg_ppr_device_ranks.argtypes = [C.c_void_p, P(C.c_uint32)]
         L.gg_ppr_device_ranks.restype = C.c_void_p
+        L.gg_server_start.argtypes = [C.c_void_p, P(ServerParams), P(C.c_void_p)]
+        L.gg_server_submit_ppr.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, P(C.c_uint64)]
+        L.gg_server_submit_bfs.argtypes = [C.c_void_p, C.c_uint32, P(C.c_uint64)]
+        L.gg_server_take.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, P(QueryInfo), C.c_void_p, C.c_void_p,
+                                     C.c_void_p]
+        L.gg_server_stop.argtypes = [C.c_void_p]
+        L.gg_graph_share.argtypes = [C.c_void_p, P(C.c_void_p)]
         L.newEdgeList.argtypes = [C.c_uint32, C.c_uint32, C.c_int]
         L.newEdgeList.restype = P(EdgeList)
         L.freeEdgeList.argtypes = [P(EdgeList)]
@@ -517,6 +535,59 @@ def default_arguments(**kw) -> Arguments:
 def set_gpu_options(storage="f32", device=0, keep_resident=False, verbose=False):
     o = GraphGpuOptions(STORE[storage], device, int(keep_resident), int(verbose))
     lib().graphGpuSetOptions(C.byref(o))
+
+
+class Server:
+    """Query server over a DeviceGraph mapped with MAP_IN | MAP_OUT
+    (include/gg_server.h): batched personalised PageRank and BFS queries,
+    results held on the device until taken."""
+
+    QUERY_PPR, QUERY_BFS = 0, 1
+
+    def __init__(self, dg, max_ppr_batch=64, ppr_iterations=20, damp=0.85, ppr_storage="f32",
+                 mem_budget_bytes=None):
+        self.dg = dg
+        self.V = dg.graph.V
+        budget = mem_budget_bytes if mem_budget_bytes is not None else 256 * 8 * self.V
+        p = ServerParams(max_ppr_batch, ppr_iterations, damp, STORE[ppr_storage], budget)
+        self.h = C.c_void_p()
+        _check(lib().gg_server_start(dg.h, C.byref(p), C.byref(self.h)), "gg_server_start")
+
+    def submit_ppr(self, seeds):
+        s = np.ascontiguousarray(seeds, np.uint32)
+        t = C.c_uint64()
+        _check(lib().gg_server_submit_ppr(self.h, s.ctypes.data, len(s), C.byref(t)), "gg_server_submit_ppr")
+        return t.value
+
+    def submit_bfs(self, source):
+        t = C.c_uint64()
+        _check(lib().gg_server_submit_bfs(self.h, source, C.byref(t)), "gg_server_submit_bfs")
+        return t.value
+
+    def take(self, ticket, timeout_ms=60000, copy_out=True):
+        """(result, info dict): PPR ranks (V floats) or BFS (parents,
+        distances); None when copy_out is False."""
+        info = QueryInfo()
+        ppr = par = dist = None
+        kind = None
+        if copy_out:
+            ppr = np.empty(self.V, np.float32)
+            par = np.empty(self.V, np.int32)
+            dist = np.empty(self.V, np.uint32)
+        _check(lib().gg_server_take(self.h, ticket, timeout_ms, C.byref(info),
+                                    None if ppr is None else ppr.ctypes.data,
+                                    None if par is None else par.ctypes.data,
+                                    None if dist is None else dist.ctypes.data), "gg_server_take")
+        d = {k: getattr(info, k) for k, _ in QueryInfo._fields_}
+        kind = d["kind"]
+        if not copy_out:
+            return None, d
+        return (ppr if kind == self.QUERY_PPR else (par, dist)), d
+
+    def stop(self):
+        if self.h:
+            lib().gg_server_stop(self.h)
+            self.h = C.c_void_p()
 
 
 def pagerank_csr(graph: Graph, args: Arguments, fn="pageRankGraphCSR"):

@@ -361,6 +361,14 @@ gg_status bfs_setup(Bfs &B, gg_graph *g, void *stream, int profile)
 
 } // namespace
 
+extern "C" gg_status gg_bfs_device_results(const gg_graph *g, const int32_t **parents, const uint32_t **distances)
+{
+    if (!g || !g->work[0].ptr || !g->work[1].ptr) return gg_fail(GG_ERR_INVALID, "no BFS has run on this mapping");
+    if (parents) *parents = (const int32_t *)g->work[0].ptr;
+    if (distances) *distances = (const uint32_t *)g->work[1].ptr;
+    return GG_OK;
+}
+
 extern "C" gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parents, uint32_t *distances,
                             gg_bfs_result *r, void *stream)
 {

@@ -44,6 +44,9 @@ struct gg_graph
 {
     uint32_t V = 0, E = 0;
     uint32_t what = 0;
+    /* false for a view made by gg_graph_share: the graph arrays belong to
+     * the mapping it was made from */
+    bool owns_arrays = true;
     int device = 0;
     cudaStream_t own_stream = nullptr;
 

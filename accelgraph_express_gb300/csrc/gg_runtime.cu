@@ -365,9 +365,36 @@ extern "C" gg_status gg_graph_map(const struct GraphCSR *graph, uint32_t what, v
     return GG_OK;
 }
 
+extern "C" gg_status gg_graph_share(const gg_graph *src, gg_graph **out)
+{
+    if (!out) return gg_fail(GG_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!src) return gg_fail(GG_ERR_INVALID, "src is NULL");
+    gg_graph *g = new gg_graph();
+    g->V = src->V;
+    g->E = src->E;
+    g->what = src->what;
+    g->device = src->device;
+    g->owns_arrays = false;
+    g->out_off = src->out_off; g->out_adj = src->out_adj; g->out_w = src->out_w;
+    g->in_off = src->in_off; g->in_adj = src->in_adj; g->in_w = src->in_w;
+    g->out_deg = src->out_deg;
+    cudaError_t e = cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess)
+    {
+        delete g;
+        return gg_cuda_fail(e, "cudaStreamCreate");
+    }
+    cudaEventCreate(&g->ev_begin);
+    cudaEventCreate(&g->ev_end);
+    *out = g;
+    return GG_OK;
+}
+
 extern "C" gg_status gg_graph_extend(gg_graph *g, const struct GraphCSR *graph, uint32_t what, void *stream)
 {
     if (!g || !graph) return gg_fail(GG_ERR_INVALID, "NULL argument");
+    if (!g->owns_arrays) return gg_fail(GG_ERR_INVALID, "a shared view cannot be extended");
     if (graph->num_vertices != g->V || graph->num_edges != g->E)
         return gg_fail(GG_ERR_INVALID, "graph size differs from the mapping");
     return map_arrays(g, graph, what, gg_stream(g, stream));
@@ -384,13 +411,16 @@ extern "C" gg_status gg_graph_unmap(gg_graph *g)
     if (!g) return GG_OK;
     if (g->own_stream) cudaStreamSynchronize(g->own_stream);
     const size_t off_bytes = ((size_t)g->V + 1) * 4, edge_alloc = ((size_t)g->E + GG_EDGE_PAD) * 4;
-    gg_dev_free(g, g->out_off, off_bytes);
-    gg_dev_free(g, g->out_adj, edge_alloc);
-    gg_dev_free(g, g->out_w, edge_alloc);
-    gg_dev_free(g, g->in_off, off_bytes);
-    gg_dev_free(g, g->in_adj, edge_alloc);
-    gg_dev_free(g, g->in_w, edge_alloc);
-    gg_dev_free(g, g->out_deg, (size_t)g->V * 4 + 16);
+    if (g->owns_arrays)
+    {
+        gg_dev_free(g, g->out_off, off_bytes);
+        gg_dev_free(g, g->out_adj, edge_alloc);
+        gg_dev_free(g, g->out_w, edge_alloc);
+        gg_dev_free(g, g->in_off, off_bytes);
+        gg_dev_free(g, g->in_adj, edge_alloc);
+        gg_dev_free(g, g->in_w, edge_alloc);
+        gg_dev_free(g, g->out_deg, (size_t)g->V * 4 + 16);
+    }
     for (int i = 0; i < 3; i++)
     {
         gg_dev_free(g, g->in_w16[i], edge_alloc);

@@ -74,6 +74,10 @@ void gg_set_wait_timeout_ms(uint32_t ms);
 /* Copy the arrays selected by `what` to HBM.  Offsets are padded so that
  * every array starts on a 256-byte boundary.  The host graph is only read. */
 gg_status gg_graph_map(const struct GraphCSR *graph, uint32_t what, void *stream, gg_graph **out);
+/* A second handle on the same device graph (no copy): its own stream and
+ * work buffers, so calls on `src` and on the view may run concurrently.
+ * The view must be unmapped before `src`; it cannot be extended. */
+gg_status gg_graph_share(const gg_graph *src, gg_graph **out);
 /* Upload any arrays in `what` that the mapping does not carry yet. */
 gg_status gg_graph_extend(gg_graph *g, const struct GraphCSR *graph, uint32_t what, void *stream);
 gg_status gg_graph_unmap(gg_graph *g);
@@ -165,6 +169,11 @@ typedef struct gg_bfs_result
  * `parents` (int32, V) and `distances` (uint32, V) are host outputs (may be NULL). */
 gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parents, uint32_t *distances,
                  gg_bfs_result *r, void *stream);
+
+/* Device pointers to the last gg_bfs's parents and distances on `g` (V
+ * entries each, the same values gg_bfs copies out), valid until the next
+ * call on `g`. */
+gg_status gg_bfs_device_results(const gg_graph *g, const int32_t **parents, const uint32_t **distances);
 
 /* One frontier step on host state, for the reference's step functions.
  * direction 0: top-down from `frontier` (a queue of `frontier_len` ids when
