@@ -11,10 +11,14 @@ e2e        the same metric through the drop-in pageRankGraphCSR call on host
            arrays: every step uploads the CSC (offsets, neighbour ids) and
            out-degrees and reads the ranks back.
 roofline   the gather kernel (k_pr_pull): algorithmic bytes per launch
-           4E + 4(V+1) + (12 + 2s)V with s = 4 bytes of FP32 contribution
-           (CSC ids, CSC offsets, out-degree, rank read+write, contribution
-           written and gathered once), / its mean CUDA-event duration, vs the
-           measured HBM copy bandwidth.
+           4E + 4(V+1) + sV + 4V with s = 4 bytes of FP32 contribution (CSC
+           ids, CSC offsets, each contribution once, the row sums written),
+           / its mean CUDA-event duration, vs the measured HBM copy
+           bandwidth; `iteration` rates a whole iteration (gather + vertex
+           update) against the algorithm's 4E + 4(V+1) + (12 + 2s)V.
+extras     BF16/FP16 PageRank, SpMV pull, BFS (R-MAT-22 undirected, 64
+           sources), batched personalised PageRank (K = 64), 4096 graphs in
+           one CUDA-graph launch, and the query server under Poisson load.
 cpu_baseline  the oracle's OpenMP restatement of the reference's pull loop
            (pageRank.c:1026-1085 with the gather as at :2890-2906) on all host
            cores, on a bounded number of iterations of the same graph.
@@ -426,6 +430,94 @@ def batch_extras(gg, torch, peak, n=4096, iters=20):
             "l1_relative_vs_fp64_max": worst, "launch": "one CUDA graph per run"}
 
 
+def serving_extras(gg, scale=23, n=1500, rate=150.0):
+    """The query server under Poisson arrivals (seed+5): 70% personalised
+    PageRank from 1-32 random seeds, 30% BFS from a random vertex with
+    out-edges, on a directed R-MAT graph with CSR and CSC resident.  Reports
+    latency percentiles (server clock, submit to result in device memory),
+    throughput, PPR batch sizes, and checks sampled queries: PPR bit-identical
+    alone and within L1 1e-6 of FP64, BFS distances exact."""
+    import threading
+    import numpy as np
+    from oracle import oracle_ctypes as O
+
+    g = gg.Graph.rmat(scale, 16, seed=SEED)
+    V = g.V
+    dg = gg.DeviceGraph(g, gg.MAP_IN | gg.MAP_OUT)
+    rng = np.random.default_rng(SEED + 5)
+    deg = g.views()["out_degree"]
+    nz = np.flatnonzero(deg)
+    qs = []
+    for _ in range(n):
+        if rng.random() < 0.7:
+            qs.append(("ppr", rng.integers(0, V, int(rng.integers(1, 33))).astype(np.uint32)))
+        else:
+            qs.append(("bfs", int(nz[rng.integers(0, len(nz))])))
+    gaps = rng.exponential(1.0 / rate, n)
+    sample = {0, 1, 2, 3, 5, 8, 13, 21, 34}
+    srv = gg.Server(dg, max_ppr_batch=64, ppr_iterations=20, ppr_storage="f32")
+    srv.take(srv.submit_ppr([0]))      # warm-up: work buffers, tiles
+    srv.take(srv.submit_bfs(int(nz[0])))
+    tickets = [None] * n
+    ready = threading.Semaphore(0)
+
+    def producer():
+        t0 = time.perf_counter()
+        due = t0
+        for i, (kind, arg) in enumerate(qs):
+            due += gaps[i]
+            d = due - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            tickets[i] = srv.submit_ppr(arg) if kind == "ppr" else srv.submit_bfs(arg)
+            ready.release()
+
+    th = threading.Thread(target=producer)
+    th.start()
+    infos, kept = [], {}
+    for i in range(n):
+        ready.acquire()
+        res, info = srv.take(tickets[i], copy_out=i in sample)
+        infos.append(info)
+        if i in sample:
+            kept[i] = res
+    th.join()
+    # the sampled queries again, each alone
+    alone_ok, acc_ok = True, True
+    a = g.arrays()
+    o = O.Csr.from_arrays(V, g.E, a["out_off"], a["out_adj"], a["in_off"], a["in_adj"])
+    l1_checked = 0
+    for i in sorted(sample):
+        kind, arg = qs[i]
+        res, _ = srv.take(srv.submit_ppr(arg) if kind == "ppr" else srv.submit_bfs(arg))
+        if kind == "ppr":
+            alone_ok &= bool(np.array_equal(res, kept[i]))
+            if l1_checked < 1:
+                acc_ok &= bool(np.abs(kept[i] - O.ppr_f64_multi(o, arg, 20, float(np.float32(0.85)))).sum() <= 1e-6)
+                l1_checked += 1
+        else:
+            alone_ok &= bool(np.array_equal(res[1], kept[i][1]))
+            _, rd, _ = O.bfs(o, 2, arg)
+            acc_ok &= bool(np.array_equal(kept[i][1], rd))
+    srv.stop()
+    dg.free()
+    g.free()
+    lat = np.array([(x["done_s"] - x["submit_s"]) * 1e3 for x in infos])
+    kinds = np.array([x["kind"] for x in infos])
+    span = max(x["done_s"] for x in infos) - min(x["submit_s"] for x in infos)
+    out = {"graph": f"R-MAT-{scale} directed, V={V}", "queries": n, "offered_qps": rate,
+           "achieved_qps": n / span, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "ppr_batch_mean": float(np.mean([x["batch_size"] for x in infos if x["kind"] == 0])),
+           "alone_equals_mixed": alone_ok, "sampled_results_match_oracle": acc_ok,
+           "all_ok": all(x["status"] == 0 for x in infos)}
+    for k, name in ((0, "ppr"), (1, "bfs")):
+        sel = lat[kinds == k]
+        if len(sel):
+            out[f"{name}_p50_ms"] = float(np.percentile(sel, 50))
+            out[f"{name}_p99_ms"] = float(np.percentile(sel, 99))
+    return out
+
+
 def bfs_extras(gg, torch, peak, scale=22):
     """BFS direction-optimising on an undirected R-MAT graph (each generated
     edge inserted both ways), 64 sources of nonzero degree; TEPS by the
@@ -560,6 +652,7 @@ def extras(gg, graph, dg, V, E, sptr, torch, peak):
     out["bfs_do"] = bfs_extras(gg, torch, peak)
     out["ppr_batched"] = ppr_extras(gg, torch, peak)
     out["many_graphs"] = batch_extras(gg, torch, peak)
+    out["serving"] = serving_extras(gg)
     return out
 
 
