@@ -35,7 +35,7 @@ struct Counters
     uint32_t qlen;   /* next queue length */
     uint32_t mf;     /* top-down: sum of -parent of claimed vertices */
     uint32_t nf;     /* bottom-up: vertices found */
-    uint32_t pad;
+    uint32_t nheavy; /* top-down: frontier vertices deferred to k_td_heavy */
     unsigned long long edges;
 };
 
@@ -65,10 +65,45 @@ __device__ __forceinline__ bool bit_of(const uint32_t *bm, uint32_t v) { return 
 
 /* top-down step from a queue; writes the next queue and, when nbm is set,
  * the next frontier bitmap */
+/* claim out-neighbour u of v for the next level; returns whether this
+ * thread won it (the reference's CAS, BFS.c:721-735) */
+__device__ __forceinline__ bool td_claim(uint32_t u, uint32_t v, int32_t *parents, uint32_t *dist, uint32_t newdist,
+                                         uint32_t *visited, uint32_t *nbm, uint32_t &mf)
+{
+    const int32_t p = parents[u];
+    if (p < 0 && atomicCAS(&parents[u], p, (int32_t)v) == p)
+    {
+        mf += (uint32_t)(-p);
+        dist[u] = newdist;
+        atomicOr(&visited[u >> 5], 1u << (u & 31));
+        if (nbm) atomicOr(&nbm[u >> 5], 1u << (u & 31));
+        return true;
+    }
+    return false;
+}
+
+/* warp-aggregated append of the claimed vertices to the next queue */
+__device__ __forceinline__ void td_enqueue(bool claimed, uint32_t u, uint32_t lane, uint32_t *nq, Counters *c)
+{
+    const uint32_t m = __ballot_sync(0xffffffffu, claimed);
+    if (m)
+    {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&c->qlen, (uint32_t)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (claimed) nq[base + __popc(m & ((1u << lane) - 1u))] = u;
+    }
+}
+
+/* frontier vertices with more out-edges than this go to k_td_heavy, at most
+ * TD_MAX_HEAVY of them per step (further ones stay with their warp) */
+#define TD_HEAVY 1024u
+#define TD_MAX_HEAVY 4096u
+
 __global__ void __launch_bounds__(256) k_td(const uint32_t *__restrict__ q, uint32_t qlen,
                                             const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
                                             int32_t *parents, uint32_t *dist, uint32_t newdist, uint32_t *visited,
-                                            uint32_t *nq, uint32_t *nbm, Counters *c)
+                                            uint32_t *nq, uint32_t *nbm, Counters *c, uint4 *heavy)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -80,6 +115,17 @@ __global__ void __launch_bounds__(256) k_td(const uint32_t *__restrict__ q, uint
         const uint32_t v = q[i];
         const uint32_t s = off[v], e = off[v + 1];
         if (lane == 0) edges += e - s;
+        if (e - s > TD_HEAVY)
+        {
+            uint32_t slot = 0;
+            if (lane == 0) slot = atomicAdd(&c->nheavy, 1u);
+            slot = __shfl_sync(0xffffffffu, slot, 0);
+            if (slot < TD_MAX_HEAVY)
+            {
+                if (lane == 0) heavy[slot] = make_uint4(v, s, e, 0u);
+                continue;
+            }
+        }
         for (uint32_t b = s; b < e; b += 32)
         {
             const uint32_t j = b + lane;
@@ -88,24 +134,9 @@ __global__ void __launch_bounds__(256) k_td(const uint32_t *__restrict__ q, uint
             if (j < e)
             {
                 u = adj[j];
-                int32_t p = parents[u];
-                if (p < 0 && atomicCAS(&parents[u], p, (int32_t)v) == p)
-                {
-                    claimed = true;
-                    mf += (uint32_t)(-p);
-                    dist[u] = newdist;
-                    atomicOr(&visited[u >> 5], 1u << (u & 31));
-                    if (nbm) atomicOr(&nbm[u >> 5], 1u << (u & 31));
-                }
+                claimed = td_claim(u, v, parents, dist, newdist, visited, nbm, mf);
             }
-            const uint32_t m = __ballot_sync(0xffffffffu, claimed);
-            if (m)
-            {
-                uint32_t base = 0;
-                if (lane == 0) base = atomicAdd(&c->qlen, (uint32_t)__popc(m));
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (claimed) nq[base + __popc(m & ((1u << lane) - 1u))] = u;
-            }
+            td_enqueue(claimed, u, lane, nq, c);
         }
     }
     mf = warp_sum(mf);
@@ -115,6 +146,79 @@ __global__ void __launch_bounds__(256) k_td(const uint32_t *__restrict__ q, uint
         if (mf) atomicAdd(&c->mf, mf);
         if (edges) atomicAdd(&c->edges, edges);
     }
+}
+
+/* the deferred high-degree frontier vertices: their out-edges, concatenated,
+ * are split evenly over the whole grid; every CTA scans the list's degrees
+ * in shared memory and maps an edge index to its vertex by binary search */
+__global__ void __launch_bounds__(256) k_td_heavy(const uint4 *__restrict__ heavy, const uint32_t *__restrict__ adj,
+                                                  int32_t *parents, uint32_t *dist, uint32_t newdist,
+                                                  uint32_t *visited, uint32_t *nq, uint32_t *nbm, Counters *c)
+{
+    __shared__ uint32_t pre[TD_MAX_HEAVY + 1];
+    __shared__ uint32_t wsum[8];
+    const uint32_t nh = min(c->nheavy, TD_MAX_HEAVY);
+    if (nh == 0) return;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    /* exclusive scan of the degrees: 16 consecutive entries per thread, then
+     * the 256 thread totals through warp shuffles */
+    constexpr uint32_t CH = TD_MAX_HEAVY / 256;
+    uint32_t loc[CH], tot = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < CH; k++)
+    {
+        const uint32_t i = tid * CH + k;
+        loc[k] = i < nh ? heavy[i].z - heavy[i].y : 0u;
+        tot += loc[k];
+    }
+    uint32_t incl = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    uint32_t wbase = 0;
+    for (uint32_t k = 0; k < w; k++) wbase += wsum[k];
+    uint32_t run = wbase + incl - tot;
+#pragma unroll
+    for (uint32_t k = 0; k < CH; k++)
+    {
+        pre[tid * CH + k] = run;
+        run += loc[k];
+    }
+    if (tid == 255) pre[TD_MAX_HEAVY] = run;
+    __syncthreads();
+    const uint32_t H = pre[nh];
+    uint32_t mf = 0;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x + (tid & ~31u); base < H; base += stride)
+    {
+        const uint32_t k = base + lane;
+        bool claimed = false;
+        uint32_t u = 0;
+        if (k < H)
+        {
+            /* the last i with pre[i] <= k */
+            uint32_t lo = 0, hi = nh - 1;
+            while (lo < hi)
+            {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (pre[mid] <= k)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const uint4 h = heavy[lo];
+            u = adj[h.y + (k - pre[lo])];
+            claimed = td_claim(u, h.x, parents, dist, newdist, visited, nbm, mf);
+        }
+        td_enqueue(claimed, u, lane, nq, c);
+    }
+    mf = warp_sum(mf);
+    if (lane == 0 && mf) atomicAdd(&c->mf, mf);
 }
 
 /* bottom-up step: front -> next over in-edges */
@@ -264,7 +368,8 @@ struct Bfs
     int32_t *parents;
     uint32_t *dist, *visited, *qa, *qb, *bma, *bmb;
     Counters *c;
-    Counters h;
+    uint4 *heavy;      /* TD_MAX_HEAVY deferred frontier vertices (v, first, end) */
+    Counters *h;       /* page-locked copy of *c */
     int profile;
     uint32_t launches = 0;
     std::vector<cudaEvent_t> evs;
@@ -283,9 +388,9 @@ gg_status mark(Bfs &B)
 
 gg_status read_counters(Bfs &B)
 {
-    GG_CUDA(cudaMemcpyAsync(&B.h, B.c, sizeof(Counters), cudaMemcpyDeviceToHost, B.s));
+    GG_CUDA(cudaMemcpyAsync(B.h, B.c, sizeof(Counters), cudaMemcpyDeviceToHost, B.s));
     GG_CHECK(gg_wait(B.s));
-    B.res.edges_examined += B.h.edges;
+    B.res.edges_examined += B.h->edges;
     return GG_OK;
 }
 
@@ -296,10 +401,14 @@ gg_status td_step(Bfs &B, const uint32_t *q, uint32_t qlen, uint32_t *nq, uint32
     if (nbm) GG_CUDA(cudaMemsetAsync(nbm, 0, (size_t)B.words * 4, B.s));
     GG_CHECK(mark(B));
     if (qlen)
+    {
         k_td<<<cap_blocks((uint64_t)qlen * 32), 256, 0, B.s>>>(q, qlen, B.g->out_off, B.g->out_adj, B.parents, B.dist,
-                                                                newdist, B.visited, nq, nbm, B.c);
+                                                                newdist, B.visited, nq, nbm, B.c, B.heavy);
+        k_td_heavy<<<gg_sm_count() * 8, 256, 0, B.s>>>(B.heavy, B.g->out_adj, B.parents, B.dist, newdist, B.visited,
+                                                       nq, nbm, B.c);
+        B.launches += 2;
+    }
     GG_CHECK(mark(B));
-    B.launches++;
     B.res.top_down_steps++;
     GG_CUDA(cudaGetLastError());
     return read_counters(B);
@@ -324,9 +433,9 @@ gg_status compact(Bfs &B, const uint32_t *bm, uint32_t *q, uint32_t *qlen)
     k_compact<<<cap_blocks(B.words), 256, 0, B.s>>>(bm, B.words, q, B.c);
     B.launches++;
     GG_CUDA(cudaGetLastError());
-    GG_CUDA(cudaMemcpyAsync(&B.h, B.c, sizeof(Counters), cudaMemcpyDeviceToHost, B.s));
+    GG_CUDA(cudaMemcpyAsync(B.h, B.c, sizeof(Counters), cudaMemcpyDeviceToHost, B.s));
     GG_CHECK(gg_wait(B.s));
-    *qlen = B.h.qlen;
+    *qlen = B.h->qlen;
     return GG_OK;
 }
 
@@ -356,6 +465,8 @@ gg_status bfs_setup(Bfs &B, gg_graph *g, void *stream, int profile)
     GG_CHECK(gg_work(g, 5, wb, &p)); B.bmb = (uint32_t *)p;
     GG_CHECK(gg_work(g, 6, wb, &p)); B.visited = (uint32_t *)p;
     GG_CHECK(gg_work(g, 7, 256, &p)); B.c = (Counters *)p;
+    GG_CHECK(gg_pinned(g, sizeof(Counters), &p)); B.h = (Counters *)p;
+    GG_CHECK(gg_work(g, 8, (size_t)TD_MAX_HEAVY * sizeof(uint4), &p)); B.heavy = (uint4 *)p;
     return GG_OK;
 }
 
@@ -410,7 +521,7 @@ extern "C" gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parent
         while (nf)
         {
             GG_CHECK(bu_step(B, bm, nbm, 0, level + 1));
-            nf = B.h.nf;
+            nf = B.h->nf;
             std::swap(bm, nbm);
             processed += nf;
             level++;
@@ -424,7 +535,7 @@ extern "C" gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parent
         while (qlen)
         {
             GG_CHECK(td_step(B, q, qlen, nq, p->mode == GG_BFS_PUSH_BITMAP ? nbm : nullptr, level + 1));
-            qlen = B.h.qlen;
+            qlen = B.h->qlen;
             std::swap(q, nq);
             std::swap(bm, nbm);
             processed += qlen;
@@ -447,7 +558,7 @@ extern "C" gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parent
                 {
                     nf_prev = nf;
                     GG_CHECK(bu_step(B, bm, nbm, 1, level + 1));
-                    nf = B.h.nf;
+                    nf = B.h->nf;
                     std::swap(bm, nbm);
                     processed += nf;
                     level++;
@@ -459,8 +570,8 @@ extern "C" gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parent
             {
                 mu -= mf;
                 GG_CHECK(td_step(B, q, qlen, nq, nullptr, level + 1));
-                mf = B.h.mf;
-                qlen = B.h.qlen;
+                mf = B.h->mf;
+                qlen = B.h->qlen;
                 std::swap(q, nq);
                 processed += qlen;
                 level++;
@@ -527,15 +638,15 @@ extern "C" gg_status gg_bfs_step_host(gg_graph *g, int direction, const uint32_t
     {
         if (frontier_is_bitmap) GG_CHECK(compact(B, B.bma, B.qa, &qlen));
         GG_CHECK(td_step(B, B.qa, qlen, B.qb, B.bmb, newdist));
-        cnt = B.h.mf;
-        nlen = B.h.qlen;
+        cnt = B.h->mf;
+        nlen = B.h->qlen;
         if (next_queue && nlen) GG_CUDA(cudaMemcpyAsync(next_queue, B.qb, (size_t)nlen * 4, cudaMemcpyDeviceToHost, B.s));
     }
     else
     {
         GG_CHECK(bu_step(B, B.bma, B.bmb, 1, newdist));
-        cnt = B.h.nf;
-        nlen = B.h.nf;
+        cnt = B.h->nf;
+        nlen = B.h->nf;
         if (next_queue)
         {
             uint32_t ql = 0;

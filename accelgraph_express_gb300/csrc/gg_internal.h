@@ -73,6 +73,9 @@ struct gg_graph
     gg_tiles ppr_tiles;
     const float *ppr_ranks = nullptr;
     uint32_t ppr_stride = 0;
+    /* page-locked host scratch for small per-step read-backs */
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
 
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
     /* timing events reused across calls (profile mode) */
@@ -101,6 +104,8 @@ gg_status gg_dev_alloc(gg_graph *g, void **p, size_t bytes);
 void gg_dev_free(gg_graph *g, void *p, size_t bytes);
 /* work buffer slot `slot`, at least `bytes` long (contents undefined) */
 gg_status gg_work(gg_graph *g, int slot, size_t bytes, void **out);
+/* the mapping's page-locked host scratch, at least `bytes` long */
+gg_status gg_pinned(gg_graph *g, size_t bytes, void **out);
 cudaStream_t gg_stream(gg_graph *g, void *user_stream);
 /* host wait on all work queued on `s`, bounded by the wait limit */
 gg_status gg_wait(cudaStream_t s);

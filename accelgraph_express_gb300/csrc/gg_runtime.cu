@@ -189,6 +189,20 @@ gg_status gg_work(gg_graph *g, int slot, size_t bytes, void **out)
     return GG_OK;
 }
 
+gg_status gg_pinned(gg_graph *g, size_t bytes, void **out)
+{
+    if (g->pinned_bytes < bytes)
+    {
+        if (g->pinned) cudaFreeHost(g->pinned);
+        g->pinned = nullptr;
+        g->pinned_bytes = 0;
+        GG_CUDA(cudaHostAlloc(&g->pinned, bytes, cudaHostAllocDefault));
+        g->pinned_bytes = bytes;
+    }
+    *out = g->pinned;
+    return GG_OK;
+}
+
 cudaStream_t gg_stream(gg_graph *g, void *user_stream)
 {
     return user_stream ? (cudaStream_t)user_stream : g->own_stream;
@@ -208,7 +222,6 @@ gg_status gg_wait(cudaStream_t s)
     }
     const auto t0 = std::chrono::steady_clock::now();
     const uint32_t limit = wait_timeout_ms();
-    uint32_t spins = 0;
     for (;;)
     {
         e = cudaEventQuery(ev);
@@ -218,13 +231,16 @@ gg_status gg_wait(cudaStream_t s)
             cudaEventDestroy(ev);
             return gg_cuda_fail(e, "device work");
         }
-        auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
-        if ((uint64_t)ms > limit)
+        const auto us =
+            std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
+        if ((uint64_t)us > (uint64_t)limit * 1000)
         {
             cudaEventDestroy(ev);
             return gg_fail(GG_ETIMEDOUT, "device work did not finish within the wait limit");
         }
-        if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(20));
+        /* spin through the first half millisecond (per-level BFS waits and
+         * short calls end within it), then nap briefly between polls */
+        if (us > 500) std::this_thread::sleep_for(std::chrono::microseconds(5));
     }
     cudaEventDestroy(ev);
     return GG_OK;
@@ -430,6 +446,7 @@ extern "C" gg_status gg_graph_unmap(gg_graph *g)
     free_tiles(g, g->out_tiles);
     free_tiles(g, g->ppr_tiles);
     for (auto &b : g->work) gg_dev_free(g, b.ptr, b.bytes);
+    if (g->pinned) cudaFreeHost(g->pinned);
     for (uint32_t i = 0; i < g->ev_count; i++) cudaEventDestroy(g->ev_pool[i]);
     free(g->ev_pool);
     if (g->ev_begin) cudaEventDestroy(g->ev_begin);
