@@ -188,6 +188,42 @@ def run_reference(a, world, rank):
     print(json.dumps(line), flush=True)
 
 
+class Replicas:
+    """The N > 1 plumbing of the replicas: one process per GPU, each running
+    the whole workload on its own graph copy; no collective on the data path,
+    only a barrier around the timed region and the max of the ranks' times.
+    (backend/device: "nccl"/"cuda" on GPUs; "gloo"/"cpu" in the CPU tests.)"""
+
+    def __init__(self, world, backend="nccl", device="cuda"):
+        self.world, self.device, self.dist = world, device, None
+        if world > 1:
+            import torch.distributed as dist
+            if not dist.is_initialized():
+                dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x):
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+    def value(self, units_per_rank, slowest_ms):
+        """Whole-job throughput: every rank's units over the slowest rank's time."""
+        return self.world * units_per_rank / (slowest_ms / 1e3)
+
+
 def main():
     a = parse()
     world, rank, local = dist_env()
@@ -201,21 +237,8 @@ def main():
     import accelgraph_express_gb300 as gg
 
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-
-    def barrier():
-        if dist:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    reps = Replicas(world, "nccl", "cuda")
+    barrier, max_over_ranks = reps.barrier, reps.max
 
     gg.device_init(local)
     t_build = time.perf_counter()
@@ -252,7 +275,7 @@ def main():
     barrier()
     clk = clocks.stop()
     elapsed_ms = max_over_ranks(ev0.elapsed_time(ev1))
-    value = world * E * ITERS * a.steps / (elapsed_ms / 1e3) / 1e9
+    value = reps.value(E * ITERS * a.steps, elapsed_ms) / 1e9
 
     # roofline of the gather kernel
     peak, peak_kind = load_peaks()
@@ -313,8 +336,7 @@ def main():
         print(json.dumps(line), flush=True)
     if dg.h:
         dg.free()
-    if dist:
-        dist.destroy_process_group()
+    reps.close()
 
 
 def splitmix_sources(V, deg, n, seed):
