@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--edge-factor", type=int, default=16)
     p.add_argument("--no-extras", action="store_true", help="skip the BF16/BFS/SpMV side measurements")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--leg", choices=["c1", "bfs", "ppr", "batch", "serve"],
+                   help="run one side measurement alone and print its JSON (for profiling)")
     return p.parse_args()
 
 
@@ -224,11 +226,28 @@ class Replicas:
         return self.world * units_per_rank / (slowest_ms / 1e3)
 
 
+def run_leg(leg):
+    """One side measurement alone, its JSON on stdout."""
+    import torch
+
+    import accelgraph_express_gb300 as gg
+
+    gg.device_init(0)
+    peak, _ = load_peaks()
+    fn = {"c1": lambda: c1_extras(gg, torch), "bfs": lambda: bfs_extras(gg, torch, peak),
+          "ppr": lambda: ppr_extras(gg, torch, peak), "batch": lambda: batch_extras(gg, torch, peak),
+          "serve": lambda: serving_extras(gg)}[leg]
+    print(json.dumps({"leg": leg, **fn()}), flush=True)
+
+
 def main():
     a = parse()
     world, rank, local = dist_env()
     if a.impl == "reference":
         run_reference(a, world, rank)
+        return
+    if a.leg:
+        run_leg(a.leg)
         return
 
     import numpy as np
@@ -394,6 +413,47 @@ def ppr_extras(gg, torch, peak, scale=22, K=64, iters=20):
                         "gather_launch_ms": gms / reps,
                         "iteration_hbm_frac": alg / (ms / iters / 1e3) / 1e9 / peak,
                         "alg_bytes_per_iteration": alg, "l1_vs_fp64_max": l1}
+    dg.free()
+    g.free()
+    return out
+
+
+def c1_extras(gg, torch, scale=16):
+    """The CPU-runnable configuration: PageRank pull on R-MAT-16 (65,536
+    vertices, 1,048,576 edges), epsilon 1e-4, at most 20 iterations, in the
+    reference's formulation (start 0.15, divide by V at the end) and with
+    1/N initialisation; ranks against the FP64 oracle (L1, L-inf),
+    iterations against the reference's FP32 loop, GTEPS over the iterations
+    run, the oracle's OpenMP loop timed beside it."""
+    import numpy as np
+    from oracle import oracle_ctypes as O
+
+    g = gg.Graph.rmat(scale, 16, seed=SEED)
+    V, E = g.V, g.E
+    a = g.arrays()
+    o = O.Csr.from_arrays(V, E, a["out_off"], a["out_adj"], a["in_off"], a["in_adj"])
+    dg = gg.DeviceGraph(g, gg.MAP_IN)
+    out = {"graph": f"R-MAT-{scale}, V={V}, E={E}", "epsilon": 1e-4, "max_iterations": 20}
+    for name, one_over_n in (("reference_formulation", False), ("init_1_over_n", True)):
+        for _ in range(3):
+            dg.pagerank("pull", iterations=20, epsilon=1e-4, init_one_over_n=one_over_n, copy_out=False)
+        reps = 20
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            _, r = dg.pagerank("pull", iterations=20, epsilon=1e-4, init_one_over_n=one_over_n, copy_out=False)
+        ms = (time.perf_counter() - t0) * 1e3 / reps
+        ranks, r = dg.pagerank("pull", iterations=20, epsilon=1e-4, init_one_over_n=one_over_n)
+        ref, info = O.pagerank(o, 0, 20, 1e-4, init_one_over_n=one_over_n)
+        ex = O.pagerank_f64(o, info["executed"], init_one_over_n=one_over_n)
+        t0 = time.perf_counter()
+        O.pagerank(o, 0, 20, 1e-4, init_one_over_n=one_over_n, nthreads=os.cpu_count() or 1)
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        out[name] = {"iterations": r["iterations"], "iterations_reference_loop": info["iterations"],
+                     "ms_per_call": ms, "gteps": E * (info["executed"]) / (ms / 1e3) / 1e9,
+                     "l1_vs_fp64": float(np.abs(ranks - ex).sum()), "linf_vs_fp64": float(np.abs(ranks - ex).max()),
+                     "l1_reference_fp32_loop_vs_fp64": float(np.abs(ref - ex).sum()),
+                     "cpu_gteps": E * info["executed"] / (cpu_ms / 1e3) / 1e9}
     dg.free()
     g.free()
     return out
@@ -672,6 +732,7 @@ def extras(gg, graph, dg, V, E, sptr, torch, peak):
             "iteration_hbm_frac": pr_bytes(V, E, s) / (ms / ITERS / 1e3) / 1e9 / peak,
             "l1_vs_fp64": l1, "linf_vs_fp64": linf, "l1_relative": l1 / float(np.abs(exact).sum())}
     out["fp64_oracle_s"] = round(f64_s, 2)
+    out["c1_rmat16"] = c1_extras(gg, torch)
     out.update(spmv_extras(gg, graph, V, E, sptr, torch, peak))
     dg.free()
     out["bfs_do"] = bfs_extras(gg, torch, peak)
