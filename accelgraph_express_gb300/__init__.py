@@ -107,7 +107,16 @@ class PrParams(C.Structure):
                 ("profile", C.c_uint32), ("flags", C.c_uint32)]
 
 
-PR_CUDA_GRAPH = 0x1
+PR_CUDA_GRAPH, PR_HOT_OFF, PR_HOT_ON = 0x1, 0x2, 0x4
+
+
+def _pr_flags(cuda_graph, hot):
+    f = PR_CUDA_GRAPH if cuda_graph else 0
+    if hot is True:
+        f |= PR_HOT_ON
+    elif hot is False:
+        f |= PR_HOT_OFF
+    return f
 
 
 class PrResult(C.Structure):
@@ -445,9 +454,11 @@ class DeviceGraph:
         return int(lib().gg_graph_device_bytes(self.h))
 
     def pagerank(self, mode="pull", storage="f32", iterations=20, epsilon=1e-4, init_one_over_n=False,
-                 damp=0.85, profile=False, copy_out=True, stream=None, cuda_graph=False):
+                 damp=0.85, profile=False, copy_out=True, stream=None, cuda_graph=False, hot=None):
+        """hot: None = the library's choice (hot-vertex table from 1M vertices),
+        True / False = force it on / off (pull FP32/BF16/FP16)."""
         p = PrParams(PR_MODES[mode] if isinstance(mode, str) else mode, STORE[storage], iterations,
-                     int(init_one_over_n), epsilon, damp, int(profile), PR_CUDA_GRAPH if cuda_graph else 0)
+                     int(init_one_over_n), epsilon, damp, int(profile), _pr_flags(cuda_graph, hot))
         r = PrResult()
         ranks = np.empty(self.graph.V, np.float32) if copy_out else None
         _check(lib().gg_pagerank(self.h, C.byref(p), None if ranks is None else ranks.ctypes.data, C.byref(r),
@@ -455,12 +466,12 @@ class DeviceGraph:
         return ranks, {k: getattr(r, k) for k, _ in PrResult._fields_}
 
     def pagerank_batch(self, vertex_off, mode="pull", storage="f32", iterations=20, epsilon=1e-4, damp=0.85,
-                       profile=False, copy_out=True, stream=None, cuda_graph=False):
+                       profile=False, copy_out=True, stream=None, cuda_graph=False, hot=None):
         """PageRank of a union of graphs (vertex ranges vertex_off[i] ..
         vertex_off[i+1]); each vertex normalised by its own graph's size."""
         voff = np.ascontiguousarray(vertex_off, np.uint32)
         p = PrParams(PR_MODES[mode] if isinstance(mode, str) else mode, STORE[storage], iterations, 0, epsilon,
-                     damp, int(profile), PR_CUDA_GRAPH if cuda_graph else 0)
+                     damp, int(profile), _pr_flags(cuda_graph, hot))
         r = PrResult()
         ranks = np.empty(self.graph.V, np.float32) if copy_out else None
         _check(lib().gg_pagerank_batch(self.h, C.byref(p), len(voff) - 1, voff.ctypes.data,

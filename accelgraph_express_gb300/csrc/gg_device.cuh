@@ -293,25 +293,34 @@ __device__ __forceinline__ uint32_t tile_rows(uint2 c0, uint2 c1, uint32_t V)
  * combined across lanes by a warp-shuffle segmented scan.  Only __syncwarp
  * orders the phases.
  */
-template <int IPT, int WARPS, class Op>
-__device__ __forceinline__ void warp_pull_sums(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                               uint32_t V, const uint2 *__restrict__ coord, uint32_t ntiles,
-                                               typename Op::Acc *sums, const Op &op)
+/* Per-warp shared staging of the pull engine: two buffers of row offsets
+ * (each holding up to 3 words before the tile's first row, see stage_words,
+ * 16-byte aligned), the tile's values and its row sums. */
+template <int IPT, class Acc>
+struct PullStage
+{
+    static constexpr uint32_t TW = 32 * IPT;
+    static constexpr uint32_t OFFW = TW + 8;
+    static constexpr size_t OFF_BYTES = (size_t)2 * OFFW * 4;
+    static constexpr size_t VAL_BYTES = ((size_t)TW * sizeof(Acc) + 15) / 16 * 16;
+    static constexpr size_t ROW_BYTES = ((size_t)(TW + 1) * sizeof(Acc) + 15) / 16 * 16;
+    static constexpr size_t BYTES = OFF_BYTES + VAL_BYTES + ROW_BYTES;
+};
+
+/* The engine proper: this warp's tiles are tile, tile + nw, ...; s_offs
+ * (2 * OFFW words), s_val (TW) and s_row (TW + 1) are its staging. */
+template <int IPT, class Op>
+__device__ __forceinline__ void warp_pull_sums_core(uint32_t *s_offs, typename Op::Acc *s_val,
+                                                    typename Op::Acc *s_row, uint32_t tile, uint32_t nw,
+                                                    const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                                    uint32_t V, const uint2 *__restrict__ coord, uint32_t ntiles,
+                                                    typename Op::Acc *sums, const Op &op)
 {
     typedef typename Op::Acc Acc;
     typedef typename Op::Raw Raw;
-    constexpr uint32_t TW = 32 * IPT;
-    /* staged offsets hold up to 3 words before the tile's first row
-     * (stage_words) and stay 16-byte aligned */
-    constexpr uint32_t OFFW = TW + 8;
-    __shared__ __align__(16) uint32_t sm_off[WARPS][2][OFFW];
-    __shared__ Acc sm_val[WARPS][TW];
-    __shared__ Acc sm_row[WARPS][TW + 1];
-    const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    Acc *s_val = sm_val[w];
-    Acc *s_row = sm_row[w];
-    const uint32_t nw = gridDim.x * WARPS;
-    uint32_t tile = blockIdx.x * WARPS + w;
+    constexpr uint32_t TW = PullStage<IPT, Acc>::TW;
+    constexpr uint32_t OFFW = PullStage<IPT, Acc>::OFFW;
+    const uint32_t lane = threadIdx.x & 31;
     if (tile >= ntiles) return;
 
     /* pipeline state: A = tile (gathers in flight in val, offsets staged in
@@ -326,10 +335,10 @@ __device__ __forceinline__ void warp_pull_sums(const uint32_t *__restrict__ off,
     Raw val[IPT];
     load_ids<IPT>(id, adj, a0.y, a1.y, lane);
     uint32_t buf = 0;
-    uint32_t shA = stage_words(sm_off[w][0], off, a0.x, tile_rows(a0, a1, V) + 1, lane);
+    uint32_t shA = stage_words(s_offs, off, a0.x, tile_rows(a0, a1, V) + 1, lane);
     cp_async_commit();
     uint32_t shB = 0;
-    if (tile + nw < ntiles) shB = stage_words(sm_off[w][1], off, b0.x, tile_rows(b0, b1, V) + 1, lane);
+    if (tile + nw < ntiles) shB = stage_words((s_offs + OFFW), off, b0.x, tile_rows(b0, b1, V) + 1, lane);
     cp_async_commit();
 #pragma unroll
     for (int g = 0; g < IPT; g++)
@@ -374,7 +383,7 @@ __device__ __forceinline__ void warp_pull_sums(const uint32_t *__restrict__ off,
         }
         cp_async_wait_one();
         __syncwarp();
-        const uint32_t *s_off = sm_off[w][buf] + shA;
+        const uint32_t *s_off = (s_offs + buf * OFFW) + shA;
 
         /* merge-path consumption; the first row a lane ends may have begun
          * in earlier lanes, so its sum waits for the carry scan */
@@ -454,7 +463,7 @@ __device__ __forceinline__ void warp_pull_sums(const uint32_t *__restrict__ off,
 
         /* C's offsets into A's buffer; rotate */
         uint32_t shC = 0;
-        if (hasC) shC = stage_words(sm_off[w][buf], off, c0.x, tile_rows(c0, c1, V) + 1, lane);
+        if (hasC) shC = stage_words((s_offs + buf * OFFW), off, c0.x, tile_rows(c0, c1, V) + 1, lane);
         cp_async_commit();
 #pragma unroll
         for (int g = 0; g < IPT; g++) val[g] = nv[g];
@@ -463,6 +472,39 @@ __device__ __forceinline__ void warp_pull_sums(const uint32_t *__restrict__ off,
         buf ^= 1u;
     }
     cp_async_wait_all();
+}
+
+/* the engine with static per-warp staging, WARPS warps per CTA */
+template <int IPT, int WARPS, class Op>
+__device__ __forceinline__ void warp_pull_sums(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                               uint32_t V, const uint2 *__restrict__ coord, uint32_t ntiles,
+                                               typename Op::Acc *sums, const Op &op)
+{
+    typedef typename Op::Acc Acc;
+    constexpr uint32_t TW = PullStage<IPT, Acc>::TW, OFFW = PullStage<IPT, Acc>::OFFW;
+    __shared__ __align__(16) uint32_t sm_off[WARPS][2 * OFFW];
+    __shared__ Acc sm_val[WARPS][TW];
+    __shared__ Acc sm_row[WARPS][TW + 1];
+    const uint32_t w = threadIdx.x >> 5;
+    warp_pull_sums_core<IPT>(sm_off[w], sm_val[w], sm_row[w], blockIdx.x * WARPS + w, gridDim.x * WARPS, off, adj,
+                             V, coord, ntiles, sums, op);
+}
+
+/* the engine with per-warp staging carved from dynamic shared memory at
+ * `base` (blockDim.x / 32 warps of PullStage<IPT, Acc>::BYTES each) */
+template <int IPT, class Op>
+__device__ __forceinline__ void warp_pull_sums_dyn(unsigned char *base, const uint32_t *__restrict__ off,
+                                                   const uint32_t *__restrict__ adj, uint32_t V,
+                                                   const uint2 *__restrict__ coord, uint32_t ntiles,
+                                                   typename Op::Acc *sums, const Op &op)
+{
+    typedef typename Op::Acc Acc;
+    typedef PullStage<IPT, Acc> S;
+    const uint32_t w = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    unsigned char *p = base + (size_t)w * S::BYTES;
+    warp_pull_sums_core<IPT>(reinterpret_cast<uint32_t *>(p), reinterpret_cast<Acc *>(p + S::OFF_BYTES),
+                             reinterpret_cast<Acc *>(p + S::OFF_BYTES + S::VAL_BYTES), blockIdx.x * warps + w,
+                             gridDim.x * warps, off, adj, V, coord, ntiles, sums, op);
 }
 
 /*

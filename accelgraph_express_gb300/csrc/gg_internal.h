@@ -73,6 +73,12 @@ struct gg_graph
     gg_tiles ppr_tiles;
     const float *ppr_ranks = nullptr;
     uint32_t ppr_stride = 0;
+    /* hot-vertex table: flag-encoded copy of in_adj and the slot -> vertex list */
+    uint32_t *hot_adj = nullptr;
+    uint32_t *hot_list = nullptr;  /* GG_HOT_ENTRIES slots */
+    uint32_t hot_n = 0;            /* slots in use */
+    uint32_t hot_cap = 0;          /* table capacity the encoding was made for */
+    gg_tiles hot_tiles;            /* tiles of 32 * GG_HOT_IPT items over the CSC */
     /* page-locked host scratch for small per-step read-backs */
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -106,6 +112,10 @@ void gg_dev_free(gg_graph *g, void *p, size_t bytes);
 gg_status gg_work(gg_graph *g, int slot, size_t bytes, void **out);
 /* the mapping's page-locked host scratch, at least `bytes` long */
 gg_status gg_pinned(gg_graph *g, size_t bytes, void **out);
+/* build the hot-vertex table of the mapping for a table of `cap` entries
+ * (<= GG_HOT_ENTRIES; rebuilt only when cap changes; needs GG_MAP_IN), and
+ * the tiles of the hot kernels */
+gg_status gg_hot_prepare(gg_graph *g, cudaStream_t s, uint32_t cap);
 cudaStream_t gg_stream(gg_graph *g, void *user_stream);
 /* host wait on all work queued on `s`, bounded by the wait limit */
 gg_status gg_wait(cudaStream_t s);
@@ -135,6 +145,19 @@ int gg_persistent_grid(const void *kernel, uint32_t ntiles, int ctas_per_sm = 0)
  * in-neighbours' values (skewed graphs concentrate most gathers on a few
  * thousand sectors); more hide more latency. */
 #define GG_PULL_CTAS_PER_SM 5
+
+/* Hot-vertex table of the pull gather (hot.cu): up to GG_HOT_ENTRIES
+ * vertices with the most out-edges are read from a shared-memory table of
+ * GG_HOT_TABLE_BYTES (as many entries as the stored value type fits: 8K FP32,
+ * 16K BF16/FP16); a copy of the CSC ids marks them as GG_HOT_FLAG | slot.
+ * The kernels that use it run one CTA of GG_HOT_WARPS warps per SM sharing
+ * the table (measured on R-MAT-24: many warps per SM matter more than a
+ * bigger table or longer tiles). */
+#define GG_HOT_FLAG 0x80000000u
+#define GG_HOT_ENTRIES 16384u
+#define GG_HOT_TABLE_BYTES 32768u
+#define GG_HOT_WARPS 32
+#define GG_HOT_IPT 7
 /* smallest float f with (double)f >= x, and largest float f with (double)f <= x */
 float gg_float_ceil(double x);
 float gg_float_floor(double x);

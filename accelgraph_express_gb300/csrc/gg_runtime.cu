@@ -445,6 +445,9 @@ extern "C" gg_status gg_graph_unmap(gg_graph *g)
     free_tiles(g, g->in_tiles);
     free_tiles(g, g->out_tiles);
     free_tiles(g, g->ppr_tiles);
+    gg_dev_free(g, g->hot_adj, ((size_t)g->E + GG_EDGE_PAD) * 4);
+    gg_dev_free(g, g->hot_list, (size_t)GG_HOT_ENTRIES * 4);
+    free_tiles(g, g->hot_tiles);
     for (auto &b : g->work) gg_dev_free(g, b.ptr, b.bytes);
     if (g->pinned) cudaFreeHost(g->pinned);
     for (uint32_t i = 0; i < g->ev_count; i++) cudaEventDestroy(g->ev_pool[i]);

@@ -191,6 +191,85 @@ struct PrGather
     __device__ __forceinline__ Acc value(const Raw &r) const { return decode<K>(r); }
 };
 
+/* the gather with the hot-vertex table: flagged ids read the table */
+template <int K>
+struct PrGatherHot
+{
+    typedef typename Fmt<K>::Acc Acc;
+    typedef typename Fmt<K>::CT Raw;
+    const Raw *cin;
+    const Raw *s_hot;
+    __device__ __forceinline__ Raw load(uint32_t, uint32_t u) const
+    {
+        if (u & GG_HOT_FLAG) return s_hot[u & ~GG_HOT_FLAG];
+        return ldg_val(cin + u);
+    }
+    __device__ __forceinline__ Acc value(const Raw &r) const { return decode<K>(r); }
+};
+
+template <int K>
+__host__ __device__ constexpr uint32_t hot_entries()
+{
+    return GG_HOT_TABLE_BYTES / sizeof(typename Fmt<K>::CT) < GG_HOT_ENTRIES
+               ? (uint32_t)(GG_HOT_TABLE_BYTES / sizeof(typename Fmt<K>::CT))
+               : GG_HOT_ENTRIES;
+}
+template <int K>
+__host__ __device__ constexpr size_t hot_stage_bytes()
+{
+    return (size_t)GG_HOT_WARPS * PullStage<GG_HOT_IPT, typename Fmt<K>::Acc>::BYTES;
+}
+template <int K>
+__host__ __device__ constexpr size_t hot_smem_bytes()
+{
+    return hot_stage_bytes<K>() + ((size_t)hot_entries<K>() * sizeof(typename Fmt<K>::CT) + 15) / 16 * 16;
+}
+
+/* one CTA of GG_HOT_WARPS warps per SM: the CTA fills the table with the
+ * hot vertices' stored contributions, then its warps run the engine */
+template <int K>
+__global__ void __launch_bounds__(GG_HOT_WARPS * 32, 1)
+    k_pr_pull_hot(const uint32_t *__restrict__ off, const uint32_t *__restrict__ hot_adj,
+                  const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t V, typename Fmt<K>::Acc *sums,
+                  const typename Fmt<K>::CT *__restrict__ cin, const uint32_t *__restrict__ hot_list, uint32_t hot_n,
+                  const IterRec *rec, uint32_t it)
+{
+    typedef typename Fmt<K>::CT CT;
+    extern __shared__ __align__(16) unsigned char gg_dyn[];
+    if (it > 0 && rec[it - 1].active == 0u) return;
+    CT *s_hot = reinterpret_cast<CT *>(gg_dyn + hot_stage_bytes<K>());
+    for (uint32_t i = threadIdx.x; i < hot_n; i += blockDim.x) s_hot[i] = cin[hot_list[i]];
+    __syncthreads();
+    warp_pull_sums_dyn<GG_HOT_IPT>(gg_dyn, off, hot_adj, V, coord, ntiles, sums, PrGatherHot<K>{cin, s_hot});
+}
+
+/* grid of k_pr_pull_hot<K>: one CTA per SM, the carve-out sized to its
+ * shared memory (the rest of the array stays L1) */
+template <int K>
+int hot_grid(uint32_t ntiles)
+{
+    static int ok = -1;
+    if (ok < 0)
+    {
+        int dev = 0, smem_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        const size_t need = hot_smem_bytes<K>();
+        cudaError_t e = cudaFuncSetAttribute(k_pr_pull_hot<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+        if (e == cudaSuccess && smem_sm > 0)
+        {
+            int pct = (int)ceil(100.0 * (double)(need + 1024) / (double)smem_sm);
+            e = cudaFuncSetAttribute(k_pr_pull_hot<K>, cudaFuncAttributePreferredSharedMemoryCarveout, pct > 100 ? 100 : pct);
+        }
+        ok = e == cudaSuccess ? 1 : 0;
+        if (!ok) cudaGetLastError();
+    }
+    if (!ok) return 0;
+    const uint32_t need = (ntiles + GG_HOT_WARPS - 1) / GG_HOT_WARPS;
+    const uint32_t cap = (uint32_t)gg_sm_count();
+    return (int)(need < cap ? (need ? need : 1) : cap);
+}
+
 template <int K>
 __global__ void __launch_bounds__(GG_TILE_NT) k_pr_pull(const uint32_t *__restrict__ off,
                                                         const uint32_t *__restrict__ adj, const uint2 *__restrict__ coord,
@@ -553,6 +632,7 @@ struct Run
     cudaStream_t s;
     const gg_pr_params *p;
     float eps_f = 0.0f, eps_fl = 0.0f;
+    bool use_hot = false; /* pull gather through the hot-vertex table */
     uint32_t launches = 0;
     uint32_t gather_launches = 0;
     float gather_ms = 0.0f;
@@ -600,10 +680,18 @@ gg_status run_pull(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
             k_quantize<CT><<<grid_v(V), 256, 0, R.s>>>((const float *)cf, cb[0], V, Fmt<K>::bits, 0, rec, it, nullptr);
             R.launches++;
         }
-        PrGather<K> op{Fmt<K>::quant ? cb[0] : cb[it & 1]};
+        const CT *cin = Fmt<K>::quant ? cb[0] : cb[it & 1];
         GG_CHECK(timed_begin(R));
-        k_pr_pull<K><<<gg_persistent_grid((const void *)k_pr_pull<K>, t->ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0, R.s>>>(
-            g->in_off, g->in_adj, t->coord, t->ntiles, V, (Acc *)sums, op, rec, it);
+        int hg = 0;
+        if constexpr (sizeof(Acc) == 4)
+            if (R.use_hot && g->hot_cap == hot_entries<K>()) hg = hot_grid<K>(g->hot_tiles.ntiles);
+        if (hg)
+            k_pr_pull_hot<K><<<hg, GG_HOT_WARPS * 32, hot_smem_bytes<K>(), R.s>>>(
+                g->in_off, g->hot_adj, g->hot_tiles.coord, g->hot_tiles.ntiles, V, (Acc *)sums, cin, g->hot_list,
+                g->hot_n, rec, it);
+        else
+            k_pr_pull<K><<<gg_persistent_grid((const void *)k_pr_pull<K>, t->ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0,
+                           R.s>>>(g->in_off, g->in_adj, t->coord, t->ntiles, V, (Acc *)sums, PrGather<K>{cin}, rec, it);
         GG_CHECK(timed_end(R));
         PrCommon c;
         c.rank = rank; c.outdeg = g->out_deg; c.V = V; c.base = base; c.damp = R.p->damp;
@@ -831,6 +919,16 @@ gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_
     {
         GG_CHECK(gg_work(g, 23, ((size_t)ngraphs + 1) * 4, &voff_v));
         GG_CUDA(cudaMemcpyAsync(voff_v, h_voff, ((size_t)ngraphs + 1) * 4, cudaMemcpyHostToDevice, R.s));
+    }
+
+    /* the hot-vertex table for the FP pull modes (prepared before any
+     * capture: preparation reads back to the host) */
+    if (p->mode == GG_PR_PULL && !(p->flags & GG_PR_HOT_OFF) && ((p->flags & GG_PR_HOT_ON) || V >= (1u << 20)) &&
+        V < GG_HOT_FLAG && V > 0)
+    {
+        const uint32_t cap = GG_HOT_TABLE_BYTES / (p->storage == GG_STORE_F32 ? 4u : 2u);
+        GG_CHECK(gg_hot_prepare(g, R.s, cap < GG_HOT_ENTRIES ? cap : GG_HOT_ENTRIES));
+        R.use_hot = true;
     }
 
     /* with GG_PR_CUDA_GRAPH everything from here to the final normalisation

@@ -104,12 +104,18 @@ typedef struct gg_pr_params
     double epsilon;
     float damp;               /* 0.85f in the reference */
     uint32_t profile;         /* 1: time every gather launch with CUDA events */
-    uint32_t flags;           /* GG_PR_CUDA_GRAPH */
+    uint32_t flags;           /* GG_PR_CUDA_GRAPH, GG_PR_HOT_OFF, GG_PR_HOT_ON */
 } gg_pr_params;
 
 /* Run the whole call (initialisation, every iteration, normalisation) as
  * one CUDA graph launch; per-launch timing (profile) is not available then. */
 #define GG_PR_CUDA_GRAPH 0x1u
+/* The pull gather of the FP32/BF16/FP16 modes serves the contributions of
+ * the 16K vertices with the most out-edges from a shared-memory table (built
+ * once per mapping; an extra copy of the CSC ids).  By default from 1M
+ * vertices up; HOT_OFF never, HOT_ON on any graph.  Results are the same. */
+#define GG_PR_HOT_OFF 0x2u
+#define GG_PR_HOT_ON 0x4u
 
 typedef struct gg_pr_result
 {
