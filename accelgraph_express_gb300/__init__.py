@@ -122,7 +122,7 @@ def _pr_flags(cuda_graph, hot):
 class PrResult(C.Structure):
     _fields_ = [("iterations", C.c_uint32), ("active", C.c_uint32), ("error_total", C.c_double),
                 ("rank_sum", C.c_double), ("gather_ms", C.c_float), ("gather_launches", C.c_uint32),
-                ("launches", C.c_uint32)]
+                ("launches", C.c_uint32), ("hot_table", C.c_uint32)]
 
 
 class BfsParams(C.Structure):

@@ -26,10 +26,26 @@ namespace {
 
 constexpr uint32_t NO_SLOT = 0xffffffffu;
 
-__global__ void k_deg_hist(const uint32_t *__restrict__ outdeg, uint32_t V, uint32_t *hist)
+/* out-degree histogram (clamped at 65535): degrees below 4096 -- nearly all
+ * of them on skewed graphs, so global atomics on those bins would serialise
+ * -- are counted in shared memory per CTA and flushed once */
+__global__ void __launch_bounds__(256) k_deg_hist(const uint32_t *__restrict__ outdeg, uint32_t V, uint32_t *hist)
 {
+    constexpr uint32_t LOW = 4096;
+    __shared__ uint32_t s[LOW];
+    for (uint32_t i = threadIdx.x; i < LOW; i += blockDim.x) s[i] = 0;
+    __syncthreads();
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
-        atomicAdd(&hist[min(outdeg[v], 65535u)], 1u);
+    {
+        const uint32_t d = min(outdeg[v], 65535u);
+        if (d < LOW)
+            atomicAdd(&s[d], 1u);
+        else
+            atomicAdd(&hist[d], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < LOW; i += blockDim.x)
+        if (s[i]) atomicAdd(&hist[i], s[i]);
 }
 
 __global__ void k_hot_mark(const uint32_t *__restrict__ outdeg, uint32_t V, uint32_t T, uint32_t above,
@@ -89,7 +105,7 @@ gg_status gg_hot_prepare(gg_graph *g, cudaStream_t s, uint32_t cap)
     GG_CUDA(cudaMemsetAsync(hist, 0, 65536 * 4, s));
     GG_CUDA(cudaMemsetAsync(cnt, 0, 16, s));
     const int grid = gg_sm_count() * 8;
-    k_deg_hist<<<grid, 256, 0, s>>>(g->out_deg, V, (uint32_t *)hist);
+    k_deg_hist<<<gg_sm_count() * 2, 256, 0, s>>>(g->out_deg, V, (uint32_t *)hist);
     GG_CUDA(cudaGetLastError());
     std::vector<uint32_t> h(65536);
     GG_CUDA(cudaMemcpyAsync(h.data(), hist, 65536 * 4, cudaMemcpyDeviceToHost, s));

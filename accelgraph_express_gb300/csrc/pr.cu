@@ -981,6 +981,7 @@ gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_
     res.rank_sum = sum;
     res.launches = R.launches;
     res.gather_launches = R.gather_launches;
+    res.hot_table = R.use_hot ? 1u : 0u;
     if (p->profile)
     {
         float ms = 0.0f;

@@ -10,7 +10,8 @@ value      GTEPS with the graph resident in HBM, device time (CUDA events on
 e2e        the same metric through the drop-in pageRankGraphCSR call on host
            arrays: every step uploads the CSC (offsets, neighbour ids) and
            out-degrees and reads the ranks back.
-roofline   the gather kernel (k_pr_pull): algorithmic bytes per launch
+roofline   the gather kernel (k_pr_pull_hot from 1M vertices: the pull gather
+           with the hot-vertex table; k_pr_pull below): algorithmic bytes per launch
            4E + 4(V+1) + sV + 4V with s = 4 bytes of FP32 contribution (CSC
            ids, CSC offsets, each contribution once, the row sums written),
            / its mean CUDA-event duration, vs the measured HBM copy
@@ -283,12 +284,13 @@ def main():
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    gather_ms, gather_n, launches = 0.0, 0, 0
+    gather_ms, gather_n, launches, hot = 0.0, 0, 0, 0
     for _ in range(a.steps):
         r = step()
         gather_ms += r["gather_ms"]
         gather_n += r["gather_launches"]
         launches += r["launches"]
+        hot = r["hot_table"]
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -301,7 +303,8 @@ def main():
     per_launch_ms = gather_ms / max(gather_n, 1)
     alg = pr_gather_bytes(V, E, 4)
     achieved = alg / (per_launch_ms / 1e3) / 1e9
-    traffic = load_traffic("k_pr_pull")
+    kernel = "k_pr_pull_hot" if hot else "k_pr_pull"
+    traffic = load_traffic(kernel)
     # the whole iteration (gather + vertex update) against the algorithm's bytes
     iter_ms = elapsed_ms / (a.steps * ITERS)
     iteration = {"alg_bytes": pr_bytes(V, E, 4), "ms": iter_ms,
@@ -331,7 +334,7 @@ def main():
                    "l2": "inputs larger than L2 (4E = %.2f GB CSC ids per iteration)" % (4 * E / 1e9),
                    "parallelism": f"replicas x{world}", "graph_build_s": round(t_build, 2)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "k_pr_pull", "alg_bytes_per_launch": alg,
+                     "traffic": traffic, "kernel": kernel, "alg_bytes_per_launch": alg,
                      "launch_ms": per_launch_ms, "peak_source": peak_kind, "iteration": iteration},
         "e2e": {"value": e2e_value, "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "call": "pageRankGraphCSR"},

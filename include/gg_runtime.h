@@ -126,6 +126,7 @@ typedef struct gg_pr_result
     float gather_ms;          /* profile: summed device time of the gather launches */
     uint32_t gather_launches; /* gather launches timed */
     uint32_t launches;        /* kernels launched by the call */
+    uint32_t hot_table;       /* 1: the gather read the hot-vertex table (GG_PR_HOT_*) */
 } gg_pr_result;
 
 /* Run PageRank on a mapping that carries GG_MAP_IN (pull) or GG_MAP_OUT (push).
