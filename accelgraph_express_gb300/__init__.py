@@ -138,7 +138,7 @@ class BfsResult(C.Structure):
 
 class SpmvParams(C.Structure):
     _fields_ = [("mode", C.c_uint32), ("storage", C.c_uint32), ("iterations", C.c_uint32),
-                ("profile", C.c_uint32)]
+                ("profile", C.c_uint32), ("flags", C.c_uint32)]
 
 
 class PprParams(C.Structure):
@@ -489,9 +489,10 @@ class DeviceGraph:
                             None if dist is None else dist.ctypes.data, C.byref(r), stream), "gg_bfs")
         return parents, dist, {k: getattr(r, k) for k, _ in BfsResult._fields_}
 
-    def spmv(self, mode="pull", storage="f32", iterations=1, x=None, profile=False, copy_out=True, stream=None):
+    def spmv(self, mode="pull", storage="f32", iterations=1, x=None, profile=False, copy_out=True, stream=None,
+             hot=None):
         p = SpmvParams(SPMV_MODES[mode] if isinstance(mode, str) else mode, STORE[storage], iterations,
-                       int(profile))
+                       int(profile), _pr_flags(False, hot))
         r = SpmvResult()
         V = self.graph.V
         xin = None if x is None else np.ascontiguousarray(x, np.float32)

@@ -12,6 +12,7 @@
  * x and the weights may be stored as BF16/FP16 (FP32 products and sums).
  */
 #include <cuda_runtime.h>
+#include <cmath>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -44,6 +45,80 @@ __global__ void __launch_bounds__(GG_TILE_NT) k_spmv_pull(const uint32_t *__rest
                                                           float *y, SpmvGather<T> op)
 {
     warp_pull_sums<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, y, op);
+}
+
+/* the pull product with the hot-vertex table: x of the flagged in-neighbours
+ * comes from shared memory (the same table as the PageRank gather's) */
+template <class T>
+struct SpmvGatherHot
+{
+    typedef float Acc;
+    typedef typename SpmvGather<T>::Raw Raw;
+    const T *w;
+    const T *x;
+    const T *s_hot;
+    __device__ __forceinline__ Raw load(uint32_t e, uint32_t u) const
+    {
+        const T wv = ldg_val(w + e);
+        if (u & GG_HOT_FLAG) return Raw{wv, s_hot[u & ~GG_HOT_FLAG]};
+        return Raw{wv, ldg_val(x + u)};
+    }
+    __device__ __forceinline__ float value(const Raw &r) const { return __fmul_rn(to_f32(r.w), to_f32(r.x)); }
+};
+
+template <class T>
+__host__ __device__ constexpr size_t spmv_hot_stage_bytes()
+{
+    return (size_t)GG_HOT_WARPS * PullStage<GG_HOT_IPT, float>::BYTES;
+}
+template <class T>
+__host__ __device__ constexpr uint32_t spmv_hot_entries()
+{
+    return GG_HOT_TABLE_BYTES / sizeof(T) < GG_HOT_ENTRIES ? (uint32_t)(GG_HOT_TABLE_BYTES / sizeof(T)) : GG_HOT_ENTRIES;
+}
+template <class T>
+__host__ __device__ constexpr size_t spmv_hot_smem_bytes()
+{
+    return spmv_hot_stage_bytes<T>() + ((size_t)spmv_hot_entries<T>() * sizeof(T) + 15) / 16 * 16;
+}
+
+template <class T>
+__global__ void __launch_bounds__(GG_HOT_WARPS * 32, 1)
+    k_spmv_pull_hot(const uint32_t *__restrict__ off, const uint32_t *__restrict__ hot_adj,
+                    const uint2 *__restrict__ coord, uint32_t ntiles, uint32_t V, float *y, const T *w,
+                    const T *__restrict__ x, const uint32_t *__restrict__ hot_list, uint32_t hot_n)
+{
+    extern __shared__ __align__(16) unsigned char gg_dyn[];
+    T *s_hot = reinterpret_cast<T *>(gg_dyn + spmv_hot_stage_bytes<T>());
+    for (uint32_t i = threadIdx.x; i < hot_n; i += blockDim.x) s_hot[i] = x[hot_list[i]];
+    __syncthreads();
+    warp_pull_sums_dyn<GG_HOT_IPT>(gg_dyn, off, hot_adj, V, coord, ntiles, y, SpmvGatherHot<T>{w, x, s_hot});
+}
+
+/* one CTA of GG_HOT_WARPS warps per SM, carve-out sized to its shared memory */
+template <class T>
+int spmv_hot_grid(uint32_t ntiles)
+{
+    static int ok = -1;
+    if (ok < 0)
+    {
+        int dev = 0, smem_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        const size_t need = spmv_hot_smem_bytes<T>();
+        cudaError_t e = cudaFuncSetAttribute(k_spmv_pull_hot<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+        if (e == cudaSuccess && smem_sm > 0)
+        {
+            int pct = (int)ceil(100.0 * (double)(need + 1024) / (double)smem_sm);
+            e = cudaFuncSetAttribute(k_spmv_pull_hot<T>, cudaFuncAttributePreferredSharedMemoryCarveout, pct > 100 ? 100 : pct);
+        }
+        ok = e == cudaSuccess ? 1 : 0;
+        if (!ok) cudaGetLastError();
+    }
+    if (!ok) return 0;
+    const uint32_t need = (ntiles + GG_HOT_WARPS - 1) / GG_HOT_WARPS;
+    const uint32_t cap = (uint32_t)gg_sm_count();
+    return (int)(need < cap ? (need ? need : 1) : cap);
 }
 
 /* fixed-point pull (SPMV.c:775-815): x in Q16.16, weights converted per
@@ -189,6 +264,13 @@ gg_status spmv_fp(gg_graph *g, const gg_spmv_params *p, const float *x_dev, floa
     k_spmv_x<T><<<grid_v(V), 256, 0, s>>>(g->out_deg, x_dev, xf, (T *)xs, nullptr, nullptr, y, V);
     launches++;
     const T *xv = sizeof(T) == 4 ? (const T *)xf : (const T *)xs;
+    /* the hot-vertex table (as for the PageRank pull): by default from 1M vertices */
+    bool use_hot = false;
+    if (pull && !(p->flags & GG_PR_HOT_OFF) && ((p->flags & GG_PR_HOT_ON) || V >= (1u << 20)) && V < GG_HOT_FLAG)
+    {
+        GG_CHECK(gg_hot_prepare(g, s, spmv_hot_entries<T>()));
+        use_hot = g->hot_cap == spmv_hot_entries<T>();
+    }
     for (uint32_t it = 0; it < p->iterations; it++)
     {
         if (p->profile)
@@ -203,8 +285,13 @@ gg_status spmv_fp(gg_graph *g, const gg_spmv_params *p, const float *x_dev, floa
             /* y is the row-sum array: zero, then the gather stores rows and
              * adds the partials of rows spanning tiles */
             GG_CUDA(cudaMemsetAsync(y, 0, (size_t)V * sizeof(float), s));
-            k_spmv_pull<T><<<gg_persistent_grid((const void *)k_spmv_pull<T>, t->ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0, s>>>(
-                g->in_off, g->in_adj, t->coord, t->ntiles, V, y, SpmvGather<T>{w, xv});
+            const int hg = use_hot ? spmv_hot_grid<T>(g->hot_tiles.ntiles) : 0;
+            if (hg)
+                k_spmv_pull_hot<T><<<hg, GG_HOT_WARPS * 32, spmv_hot_smem_bytes<T>(), s>>>(
+                    g->in_off, g->hot_adj, g->hot_tiles.coord, g->hot_tiles.ntiles, V, y, w, xv, g->hot_list, g->hot_n);
+            else
+                k_spmv_pull<T><<<gg_persistent_grid((const void *)k_spmv_pull<T>, t->ntiles, GG_PULL_CTAS_PER_SM),
+                                 GG_TILE_NT, 0, s>>>(g->in_off, g->in_adj, t->coord, t->ntiles, V, y, SpmvGather<T>{w, xv});
         }
         else
             k_spmv_push<T><<<gg_persistent_grid((const void *)k_spmv_push<T>, t->ntiles), GG_TILE_NT, 0, s>>>(

@@ -208,6 +208,7 @@ typedef struct gg_spmv_params
     uint32_t storage;         /* gg_storage of x and of the edge weights (pull/push FP modes) */
     uint32_t iterations;
     uint32_t profile;
+    uint32_t flags;           /* GG_PR_HOT_OFF / GG_PR_HOT_ON: the hot-vertex table for the FP pull */
 } gg_spmv_params;
 
 typedef struct gg_spmv_result

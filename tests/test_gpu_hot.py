@@ -45,3 +45,20 @@ def test_hot_table_in_a_cuda_graph_run(gpu, orc, graphs):
     b, _ = dg.pagerank("pull", iterations=20, epsilon=0.0, hot=True)
     dg.free()
     np.testing.assert_allclose(a, b, rtol=2e-6, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["rmat12", "hubs"])
+@pytest.mark.parametrize("storage", ["f32", "bf16", "f16"])
+def test_hot_table_spmv_pull(gpu, orc, graphs, name, storage):
+    g, o = graphs[name]
+    if name == "rmat12":
+        g, o = pair(gpu, orc, gpu.Graph.rmat(12, 16, weighted=True))
+    dg = gpu.DeviceGraph(g, gpu.MAP_IN | gpu.MAP_IN_W)
+    x = np.random.default_rng(9).random(g.V).astype(np.float32)
+    _, hot, _ = dg.spmv("pull", storage=storage, x=x, hot=True)
+    _, plain, _ = dg.spmv("pull", storage=storage, x=x, hot=False)
+    dg.free()
+    np.testing.assert_allclose(hot, plain, rtol=2e-6, atol=1e-9)
+    if storage == "f32":
+        _, y32, _ = orc.spmv(o, 0, 1, x=x)
+        assert_fp_as_accurate(hot, y32, orc.spmv_f64(o, x), f"{name} spmv hot")
