@@ -7,17 +7,24 @@
  * bitmaps.  Kernels:
  *   k_td  top-down step (BFS.c:688-750): one warp per frontier vertex, lanes
  *         over its out-edges, CAS claim of parents[u], warp-aggregated
- *         enqueue (ballot + popc + one atomic per warp), mf += -old parent
+ *         enqueue (ballot + popc + one atomic per warp), mf += -old parent;
+ *         vertices above TD_HEAVY out-edges go to k_td_heavy, which spreads
+ *         their edges over the whole grid
  *   k_bu  bottom-up step (BFS.c:752-803): one warp per 32-vertex bitmap word;
  *         each unvisited lane checks its first in-neighbours alone, longer
  *         lists are scanned by the whole warp 32 at a time with a ballot, so
  *         the parent is the first in-CSC neighbour in the frontier as in the
  *         reference; the warp owns its words of the next-frontier and visited
  *         bitmaps and writes them without atomics
- *   k_compact  bitmap -> queue (ballot/popc compaction)
- * The host drives the direction switch with the reference's uint32
- * arithmetic (alpha 15, beta 18, mu/mf/nf, BFS.c:555-650), reading three
- * counters after each step.
+ *   k_compact  bitmap -> queue (block-wide scan, one atomic per block pass)
+ * Step counters are added and read once per block, not per warp: atomics
+ * and loads of one address from every warp queue at one L2 slice.
+ * The direction switch follows the reference's uint32 arithmetic (alpha 15,
+ * beta 18, mu/mf/nf, BFS.c:555-650).  Without profiling, the
+ * direction-optimised modes run the whole level loop in one cooperative
+ * launch (k_bfs_do, grid barriers between steps); the other modes and
+ * profiled searches drive the steps from the host, reading the step counters
+ * after each one.
  */
 #include <cuda_runtime.h>
 
@@ -41,17 +48,53 @@ struct Counters
 
 constexpr int BU_SERIAL = 4;  /* in-neighbours a lane checks before the warp helps */
 
-__global__ void k_bfs_init(const uint32_t *__restrict__ outdeg, int32_t *parents, uint32_t *dist, uint32_t *visited,
-                           uint32_t V, uint32_t words)
+/* parents = -outdeg (-1 for no out-edges), distances 0, and the visited
+ * bitmap.  A vertex without in-edges can never be reached, so when the CSC
+ * is mapped its visited bit starts set: bottom-up steps then skip it without
+ * reading its (empty) in-edge range, which changes no count.  A thread takes
+ * four consecutive vertices with 16-byte accesses; eight threads make one
+ * bitmap word, joined by shuffles.  The arrays are allocation-aligned. */
+__global__ void k_bfs_init(const uint32_t *__restrict__ outdeg, const uint32_t *__restrict__ in_off, int32_t *parents,
+                           uint32_t *dist, uint32_t *visited, uint32_t V, uint32_t words)
 {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t nq = (uint64_t)words * 8, stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t nq32 = (nq + 31) & ~31ull; /* whole warps take part in the shuffles */
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nq32; t += stride)
     {
-        uint32_t d = outdeg[v];
-        parents[v] = d ? -(int32_t)d : -1;
-        dist[v] = 0u;
+        const uint64_t v0 = t * 4;
+        uint32_t bits = 0;
+        if (v0 + 4 <= V)
+        {
+            const uint4 d = reinterpret_cast<const uint4 *>(outdeg)[t];
+            reinterpret_cast<int4 *>(parents)[t] = make_int4(d.x ? -(int32_t)d.x : -1, d.y ? -(int32_t)d.y : -1,
+                                                             d.z ? -(int32_t)d.z : -1, d.w ? -(int32_t)d.w : -1);
+            reinterpret_cast<uint4 *>(dist)[t] = make_uint4(0u, 0u, 0u, 0u);
+            if (in_off)
+            {
+                const uint4 a = reinterpret_cast<const uint4 *>(in_off)[t];
+                const uint32_t b = in_off[v0 + 4];
+                bits = (uint32_t)(a.x == a.y) | (uint32_t)(a.y == a.z) << 1 | (uint32_t)(a.z == a.w) << 2 |
+                       (uint32_t)(a.w == b) << 3;
+            }
+        }
+        else if (v0 < V)
+        {
+            for (uint32_t k = 0; v0 + k < V; k++)
+            {
+                const uint64_t v = v0 + k;
+                const uint32_t d = outdeg[v];
+                parents[v] = d ? -(int32_t)d : -1;
+                dist[v] = 0u;
+                if (in_off && in_off[v + 1] == in_off[v]) bits |= 1u << k;
+            }
+        }
+        uint32_t m = bits << (4 * (lane & 7));
+        m |= __shfl_xor_sync(0xffffffffu, m, 1);
+        m |= __shfl_xor_sync(0xffffffffu, m, 2);
+        m |= __shfl_xor_sync(0xffffffffu, m, 4);
+        if ((lane & 7) == 0 && t < nq) visited[t >> 3] = m;
     }
-    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < words; w += gridDim.x * blockDim.x)
-        visited[w] = 0u;
 }
 
 __global__ void k_bfs_source(int32_t *parents, uint32_t *visited, uint32_t *queue, uint32_t src)
@@ -63,8 +106,34 @@ __global__ void k_bfs_source(int32_t *parents, uint32_t *visited, uint32_t *queu
 
 __device__ __forceinline__ bool bit_of(const uint32_t *bm, uint32_t v) { return (bm[v >> 5] >> (v & 31)) & 1u; }
 
-/* top-down step from a queue; writes the next queue and, when nbm is set,
- * the next frontier bitmap */
+/* adds the block's per-thread values to one 32-bit and one 64-bit counter
+ * with one atomic each (same-address atomics from every warp serialise at
+ * one L2 slice); every thread of the block calls it */
+__device__ __forceinline__ void block_flush(uint32_t *p32, uint32_t v32, unsigned long long *p64, unsigned long long v64)
+{
+    __shared__ uint32_t s32;
+    __shared__ unsigned long long s64;
+    if (threadIdx.x == 0)
+    {
+        s32 = 0u;
+        s64 = 0ull;
+    }
+    __syncthreads();
+    v32 = warp_sum(v32);
+    v64 = warp_sum(v64);
+    if ((threadIdx.x & 31) == 0)
+    {
+        if (v32) atomicAdd(&s32, v32);
+        if (v64) atomicAdd(&s64, v64);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        if (s32) atomicAdd(p32, s32);
+        if (s64 && p64) atomicAdd(p64, s64);
+    }
+}
+
 /* claim out-neighbour u of v for the next level; returns whether this
  * thread won it (the reference's CAS, BFS.c:721-735) */
 __device__ __forceinline__ bool td_claim(uint32_t u, uint32_t v, int32_t *parents, uint32_t *dist, uint32_t newdist,
@@ -97,13 +166,13 @@ __device__ __forceinline__ void td_enqueue(bool claimed, uint32_t u, uint32_t la
 
 /* frontier vertices with more out-edges than this go to k_td_heavy, at most
  * TD_MAX_HEAVY of them per step (further ones stay with their warp) */
-#define TD_HEAVY 1024u
+#define TD_HEAVY 64u
 #define TD_MAX_HEAVY 4096u
 
-__global__ void __launch_bounds__(256) k_td(const uint32_t *__restrict__ q, uint32_t qlen,
-                                            const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                            int32_t *parents, uint32_t *dist, uint32_t newdist, uint32_t *visited,
-                                            uint32_t *nq, uint32_t *nbm, Counters *c, uint4 *heavy)
+__device__ __forceinline__ void td_body(const uint32_t *q, uint32_t qlen,
+                                        const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                        int32_t *parents, uint32_t *dist, uint32_t newdist, uint32_t *visited,
+                                        uint32_t *nq, uint32_t *nbm, Counters *c, uint4 *heavy)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -139,25 +208,22 @@ __global__ void __launch_bounds__(256) k_td(const uint32_t *__restrict__ q, uint
             td_enqueue(claimed, u, lane, nq, c);
         }
     }
-    mf = warp_sum(mf);
-    edges = warp_sum(edges);
-    if (lane == 0)
-    {
-        if (mf) atomicAdd(&c->mf, mf);
-        if (edges) atomicAdd(&c->edges, edges);
-    }
+    block_flush(&c->mf, mf, &c->edges, edges);
 }
 
 /* the deferred high-degree frontier vertices: their out-edges, concatenated,
  * are split evenly over the whole grid; every CTA scans the list's degrees
  * in shared memory and maps an edge index to its vertex by binary search */
-__global__ void __launch_bounds__(256) k_td_heavy(const uint4 *__restrict__ heavy, const uint32_t *__restrict__ adj,
-                                                  int32_t *parents, uint32_t *dist, uint32_t newdist,
-                                                  uint32_t *visited, uint32_t *nq, uint32_t *nbm, Counters *c)
+__device__ __forceinline__ void td_heavy_body(const uint4 *heavy, const uint32_t *__restrict__ adj,
+                                              int32_t *parents, uint32_t *dist, uint32_t newdist,
+                                              uint32_t *visited, uint32_t *nq, uint32_t *nbm, Counters *c)
 {
     __shared__ uint32_t pre[TD_MAX_HEAVY + 1];
     __shared__ uint32_t wsum[8];
-    const uint32_t nh = min(c->nheavy, TD_MAX_HEAVY);
+    __shared__ uint32_t s_nh;
+    if (threadIdx.x == 0) s_nh = min(*(volatile uint32_t *)&c->nheavy, TD_MAX_HEAVY);
+    __syncthreads();
+    const uint32_t nh = s_nh;
     if (nh == 0) return;
     const uint32_t tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     /* exclusive scan of the degrees: 16 consecutive entries per thread, then
@@ -217,15 +283,15 @@ __global__ void __launch_bounds__(256) k_td_heavy(const uint4 *__restrict__ heav
         }
         td_enqueue(claimed, u, lane, nq, c);
     }
-    mf = warp_sum(mf);
-    if (lane == 0 && mf) atomicAdd(&c->mf, mf);
+    block_flush(&c->mf, mf, nullptr, 0ull);
 }
 
-/* bottom-up step: front -> next over in-edges */
-__global__ void __launch_bounds__(256) k_bu(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
-                                            int32_t *parents, uint32_t *dist, int write_dist, uint32_t newdist,
-                                            const uint32_t *__restrict__ front, uint32_t *next, uint32_t *visited,
-                                            uint32_t V, uint32_t words, Counters *c)
+/* bottom-up step: front -> next over in-edges; one warp per bitmap word
+ * (the warp owns its words of `next` and `visited`) */
+__device__ __forceinline__ void bu_body(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                        int32_t *parents, uint32_t *dist, int write_dist, uint32_t newdist,
+                                        const uint32_t *front, uint32_t *next, uint32_t *visited,
+                                        uint32_t V, uint32_t words, Counters *c)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -248,12 +314,18 @@ __global__ void __launch_bounds__(256) k_bu(const uint32_t *__restrict__ off, co
         {
             const uint32_t s = off[v], e = off[v + 1];
             const uint32_t kend = min(e, s + BU_SERIAL);
-            for (uint32_t j = s; j < kend; j++)
-            {
-                const uint32_t u = adj[j];
-                scanned++;
-                if (bit_of(front, u)) { found = true; parent = u; break; }
-            }
+            /* the candidates' ids, then their frontier bits, as independent
+             * loads; the count stops at the first hit as a serial scan would */
+            uint32_t u[BU_SERIAL];
+            bool hit[BU_SERIAL];
+#pragma unroll
+            for (int k = 0; k < BU_SERIAL; k++) u[k] = s + k < kend ? adj[s + k] : 0u;
+#pragma unroll
+            for (int k = 0; k < BU_SERIAL; k++) hit[k] = s + k < kend && bit_of(front, u[k]);
+#pragma unroll
+            for (int k = BU_SERIAL - 1; k >= 0; k--)
+                if (hit[k]) { found = true; parent = u[k]; scanned = (uint32_t)k + 1u; }
+            if (!found) scanned = kend - s;
             rs = kend;
             re = found ? kend : e;
         }
@@ -306,50 +378,305 @@ __global__ void __launch_bounds__(256) k_bu(const uint32_t *__restrict__ off, co
         }
         edges += scanned;
     }
-    edges = warp_sum(edges);
-    if (lane == 0)
-    {
-        if (nf) atomicAdd(&c->nf, nf);
-        if (edges) atomicAdd(&c->edges, edges);
-    }
+    block_flush(&c->nf, nf, &c->edges, edges);
 }
 
-/* frontier bitmap -> queue, one thread per word, warp-aggregated offsets */
-__global__ void k_compact(const uint32_t *__restrict__ bm, uint32_t words, uint32_t *q, Counters *c)
+/* frontier bitmap -> queue, one thread per word; offsets from a block-wide
+ * scan and one atomic per block pass (blockDim.x a multiple of 32, at most
+ * 1024).  With `clear` the words read are zeroed. */
+__device__ __forceinline__ void compact_body(uint32_t *bm, uint32_t words, uint32_t *q, Counters *c, bool clear)
 {
-    const uint32_t lane = threadIdx.x & 31;
-    for (uint32_t w0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; w0 < words; w0 += gridDim.x * blockDim.x)
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_base;
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < words; b0 += gridDim.x * blockDim.x)
     {
-        const uint32_t w = w0 + lane;
+        const uint32_t w = b0 + threadIdx.x;
         uint32_t bits = w < words ? bm[w] : 0u;
-        uint32_t n = (uint32_t)__popc(bits);
+        if (clear && bits) bm[w] = 0u;
+        const uint32_t n = (uint32_t)__popc(bits);
         uint32_t incl = n;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1)
         {
-            uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
             if ((int)lane >= o) incl += t;
         }
-        uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-        uint32_t base = 0;
-        if (lane == 0 && total) base = atomicAdd(&c->qlen, total);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        uint32_t at = base + incl - n;
+        if (lane == 31) s_warp[wid] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            uint32_t run = 0;
+            for (uint32_t k = 0; k < nwarps; k++)
+            {
+                const uint32_t x = s_warp[k];
+                s_warp[k] = run;
+                run += x;
+            }
+            s_base = run ? atomicAdd(&c->qlen, run) : 0u;
+        }
+        __syncthreads();
+        uint32_t at = s_base + s_warp[wid] + incl - n;
         while (bits)
         {
             const int b = __ffs(bits) - 1;
             bits &= bits - 1;
             q[at++] = w * 32 + (uint32_t)b;
         }
+        __syncthreads();
     }
 }
 
-__global__ void k_queue_to_bitmap(const uint32_t *__restrict__ q, uint32_t qlen, uint32_t *bm)
+__device__ __forceinline__ void q2bm_body(const uint32_t *q, uint32_t qlen, uint32_t *bm)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < qlen; i += gridDim.x * blockDim.x)
     {
         uint32_t v = q[i];
         atomicOr(&bm[v >> 5], 1u << (v & 31));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_td(const uint32_t *__restrict__ q, uint32_t qlen,
+                                            const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                            int32_t *parents, uint32_t *dist, uint32_t newdist, uint32_t *visited,
+                                            uint32_t *nq, uint32_t *nbm, Counters *c, uint4 *heavy)
+{
+    td_body(q, qlen, off, adj, parents, dist, newdist, visited, nq, nbm, c, heavy);
+}
+__global__ void __launch_bounds__(256) k_td_heavy(const uint4 *__restrict__ heavy, const uint32_t *__restrict__ adj,
+                                                  int32_t *parents, uint32_t *dist, uint32_t newdist,
+                                                  uint32_t *visited, uint32_t *nq, uint32_t *nbm, Counters *c)
+{
+    td_heavy_body(heavy, adj, parents, dist, newdist, visited, nq, nbm, c);
+}
+__global__ void __launch_bounds__(256) k_bu(const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                                            int32_t *parents, uint32_t *dist, int write_dist, uint32_t newdist,
+                                            const uint32_t *__restrict__ front, uint32_t *next, uint32_t *visited,
+                                            uint32_t V, uint32_t words, Counters *c)
+{
+    bu_body(off, adj, parents, dist, write_dist, newdist, front, next, visited, V, words, c);
+}
+__global__ void k_compact(const uint32_t *__restrict__ bm, uint32_t words, uint32_t *q, Counters *c)
+{
+    compact_body(const_cast<uint32_t *>(bm), words, q, c, false);
+}
+__global__ void k_queue_to_bitmap(const uint32_t *__restrict__ q, uint32_t qlen, uint32_t *bm)
+{
+    q2bm_body(q, qlen, bm);
+}
+
+/* ---- direction-optimised search in one cooperative launch ----
+ *
+ * The whole level loop of BFS.c:555-650 runs inside k_bfs_do: every thread
+ * keeps the reference's uint32 control variables (mu, mf, nf, nf_prev, qlen)
+ * in registers and updates them identically from the step counters after a
+ * grid barrier, so the direction schedule, level count and edge count are
+ * those of the host-driven loop without a host round trip per level.  Step
+ * s accumulates into counter slot s % 3 and clears slot (s + 1) % 3, whose
+ * last readers finished two barriers earlier. */
+
+/* control block of one search (work slot 7, CTL_BYTES, zeroed before the
+ * launch): three counter slots at 0, the results at 256, the barrier's
+ * root counter at 512, and per group of blocks an arrival counter at
+ * 1024 + 128 g and a release word at 4096 + 128 g -- separate 128-byte
+ * lines, so the spinning blocks of one group do not queue behind the
+ * arrivals or the other groups at one L2 slice */
+constexpr size_t CTL_BYTES = 8192;
+constexpr unsigned int BAR_GROUPS = 16;
+
+struct DoOut
+{
+    uint32_t processed, levels, td, bu;
+    unsigned long long edges;
+    uint32_t err, pad;
+};
+
+struct DoArgs
+{
+    const uint32_t *out_off, *out_adj, *in_off, *in_adj, *out_deg;
+    int32_t *parents;
+    uint32_t *dist, *visited, *q[2], *bm[2];
+    Counters *c;  /* three slots */
+    uint4 *heavy;
+    char *ctl;
+    uint32_t V, words, E, src, alpha, beta;
+};
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+/* grid-wide barrier over co-resident blocks (cooperative launch), two
+ * levels: blocks arrive at their group's counter, the last of a group at the
+ * root, and the last at the root releases every group.  A wait gives up
+ * after 2 s and records the failure in DoOut::err; the block then reports
+ * false and leaves, and the others give up at their next barrier. */
+constexpr unsigned long long BAR_LIMIT_NS = 2000000000ull;
+
+__device__ __forceinline__ bool grid_barrier(char *ctl, unsigned int &gen)
+{
+    __shared__ unsigned int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        unsigned int *root = (unsigned int *)(ctl + 512);
+        const unsigned int G = gridDim.x < BAR_GROUPS ? gridDim.x : BAR_GROUPS;
+        const unsigned int grp = blockIdx.x % G;
+        const unsigned int gsize = (gridDim.x - grp + G - 1) / G;
+        unsigned int *count = (unsigned int *)(ctl + 1024 + 128 * grp);
+        unsigned int *rel = (unsigned int *)(ctl + 4096 + 128 * grp);
+        const unsigned int target = gen + 1;
+        bool released = false, ok = true;
+        __threadfence();
+        if (atomicAdd(count, 1u) == gsize - 1)
+        {
+            atomicExch(count, 0u);
+            __threadfence();
+            if (atomicAdd(root, 1u) == G - 1)
+            {
+                atomicExch(root, 0u);
+                __threadfence();
+                for (unsigned int k = 0; k < G; k++) atomicExch((unsigned int *)(ctl + 4096 + 128 * k), target);
+                released = true;
+            }
+        }
+        if (!released)
+        {
+            const unsigned long long t0 = global_ns();
+            while (*(volatile unsigned int *)rel != target)
+            {
+                if (global_ns() - t0 > BAR_LIMIT_NS)
+                {
+                    atomicExch(&((DoOut *)(ctl + 256))->err, 1u);
+                    ok = false;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        s_ok = ok ? 1u : 0u;
+    }
+    __syncthreads();
+    gen++;
+    return s_ok != 0u;
+}
+
+/* one read of a counter slot per block, shared with its threads */
+__device__ __forceinline__ Counters read_counters_block(const Counters *c)
+{
+    __shared__ Counters s_c;
+    if (threadIdx.x == 0)
+    {
+        const volatile Counters *v = c;
+        s_c.qlen = v->qlen;
+        s_c.mf = v->mf;
+        s_c.nf = v->nf;
+        s_c.nheavy = v->nheavy;
+        s_c.edges = v->edges;
+    }
+    __syncthreads();
+    const Counters r = s_c;
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ void clear_slot(Counters *c)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        c->qlen = 0u;
+        c->mf = 0u;
+        c->nf = 0u;
+        c->nheavy = 0u;
+        c->edges = 0ull;
+    }
+}
+
+__global__ void __launch_bounds__(256, 6) k_bfs_do(DoArgs a)
+{
+    __shared__ uint32_t s_mf;
+    unsigned int gen = 0;
+    const uint32_t n = a.V;
+    if (threadIdx.x == 0) s_mf = a.out_deg[a.src];
+    __syncthreads();
+    uint32_t mu = a.E, mf = s_mf, nf = 0, nf_prev = 0, qlen = 1;
+    uint32_t processed = 1, level = 0, td = 0, bu = 0, qcur = 0, bcur = 0, s = 0;
+    unsigned long long edges = 0;
+    bool ok = true;
+    while (qlen && ok)
+    {
+        if (level > n + 1)
+        {
+            ok = false;
+            break;
+        }
+        if (mf > (mu / a.alpha))
+        {
+            /* queue -> bitmap (bm[bcur] is clear: the host cleared it and
+             * every compaction clears what it reads) */
+            q2bm_body(a.q[qcur], qlen, a.bm[bcur]);
+            if (!(ok = grid_barrier(a.ctl, gen))) break;
+            nf = qlen;
+            do
+            {
+                nf_prev = nf;
+                Counters *cs = a.c + s % 3;
+                clear_slot(a.c + (s + 1) % 3);
+                bu_body(a.in_off, a.in_adj, a.parents, a.dist, 1, level + 1, a.bm[bcur], a.bm[bcur ^ 1], a.visited,
+                        a.V, a.words, cs);
+                if (!(ok = grid_barrier(a.ctl, gen))) break;
+                const Counters k = read_counters_block(cs);
+                nf = k.nf;
+                edges += k.edges;
+                bu++;
+                bcur ^= 1;
+                processed += nf;
+                level++;
+                s++;
+            } while (((nf > nf_prev) || (nf > (n / a.beta))) && level <= n + 1);
+            if (!ok) break;
+            Counters *cs = a.c + s % 3;
+            clear_slot(a.c + (s + 1) % 3);
+            compact_body(a.bm[bcur], a.words, a.q[qcur], cs, true);
+            if (!(ok = grid_barrier(a.ctl, gen))) break;
+            qlen = read_counters_block(cs).qlen;
+            s++;
+            mf = 1;
+        }
+        else
+        {
+            mu -= mf;
+            Counters *cs = a.c + s % 3;
+            clear_slot(a.c + (s + 1) % 3);
+            td_body(a.q[qcur], qlen, a.out_off, a.out_adj, a.parents, a.dist, level + 1, a.visited, a.q[qcur ^ 1],
+                    nullptr, cs, a.heavy);
+            if (!(ok = grid_barrier(a.ctl, gen))) break;
+            td_heavy_body(a.heavy, a.out_adj, a.parents, a.dist, level + 1, a.visited, a.q[qcur ^ 1], nullptr, cs);
+            if (!(ok = grid_barrier(a.ctl, gen))) break;
+            const Counters k = read_counters_block(cs);
+            mf = k.mf;
+            qlen = k.qlen;
+            edges += k.edges;
+            td++;
+            qcur ^= 1;
+            processed += qlen;
+            level++;
+            s++;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        DoOut *out = (DoOut *)(a.ctl + 256);
+        out->processed = processed;
+        out->levels = level;
+        out->td = td;
+        out->bu = bu;
+        out->edges = edges;
+        if (!ok) atomicExch(&out->err, 1u);
     }
 }
 
@@ -464,9 +791,61 @@ gg_status bfs_setup(Bfs &B, gg_graph *g, void *stream, int profile)
     GG_CHECK(gg_work(g, 4, wb, &p)); B.bma = (uint32_t *)p;
     GG_CHECK(gg_work(g, 5, wb, &p)); B.bmb = (uint32_t *)p;
     GG_CHECK(gg_work(g, 6, wb, &p)); B.visited = (uint32_t *)p;
-    GG_CHECK(gg_work(g, 7, 256, &p)); B.c = (Counters *)p;
-    GG_CHECK(gg_pinned(g, sizeof(Counters), &p)); B.h = (Counters *)p;
+    GG_CHECK(gg_work(g, 7, CTL_BYTES, &p)); B.c = (Counters *)p;
+    GG_CHECK(gg_pinned(g, 256, &p)); B.h = (Counters *)p;
+    static_assert(3 * sizeof(Counters) <= 256 && sizeof(DoOut) <= 256 && 4096 + 128 * BAR_GROUPS <= CTL_BYTES,
+                  "control layout");
     GG_CHECK(gg_work(g, 8, (size_t)TD_MAX_HEAVY * sizeof(uint4), &p)); B.heavy = (uint4 *)p;
+    return GG_OK;
+}
+
+/* BFS.c:525-686 / :932-1060 as one cooperative launch of k_bfs_do; the
+ * control block (three counter slots, the barrier, the results) lives in
+ * work slot 7 and is read back once */
+gg_status do_search(Bfs &B, const gg_bfs_params *p)
+{
+    gg_graph *g = B.g;
+    char *ctl = (char *)B.c;
+    GG_CUDA(cudaMemsetAsync(ctl, 0, CTL_BYTES, B.s));
+    GG_CUDA(cudaMemsetAsync(B.bma, 0, (size_t)B.words * 4, B.s));
+    DoArgs a{};
+    a.out_off = g->out_off;
+    a.out_adj = g->out_adj;
+    a.in_off = g->in_off;
+    a.in_adj = g->in_adj;
+    a.out_deg = g->out_deg;
+    a.parents = B.parents;
+    a.dist = B.dist;
+    a.visited = B.visited;
+    a.q[0] = B.qa;
+    a.q[1] = B.qb;
+    a.bm[0] = B.bma;
+    a.bm[1] = B.bmb;
+    a.c = (Counters *)ctl;
+    a.heavy = B.heavy;
+    a.ctl = ctl;
+    a.V = B.V;
+    a.words = B.words;
+    a.E = g->E;
+    a.src = p->source;
+    a.alpha = p->alpha ? p->alpha : 15;
+    a.beta = p->beta ? p->beta : 18;
+    int per_sm = 0;
+    GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bfs_do, 256, 0));
+    if (per_sm < 1) return gg_fail(GG_ERR_CUDA, "k_bfs_do cannot be resident");
+    if (per_sm > 8) per_sm = 8;
+    void *args[] = {&a};
+    GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_bfs_do, dim3(gg_sm_count() * per_sm), dim3(256), args, 0, B.s));
+    B.launches++;
+    DoOut *h = (DoOut *)((char *)B.h + 64);
+    GG_CUDA(cudaMemcpyAsync(h, ctl + 256, sizeof(DoOut), cudaMemcpyDeviceToHost, B.s));
+    GG_CHECK(gg_wait(B.s));
+    if (h->err) return gg_fail(GG_ERR_KERNEL, "BFS grid barrier timed out");
+    B.res.processed_nodes = h->processed;
+    B.res.levels = h->levels;
+    B.res.top_down_steps = h->td;
+    B.res.bottom_up_steps = h->bu;
+    B.res.edges_examined = h->edges;
     return GG_OK;
 }
 
@@ -495,14 +874,19 @@ extern "C" gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parent
     Bfs B;
     GG_CHECK(bfs_setup(B, g, stream, p->profile));
     const uint32_t V = B.V, src = p->source;
-    k_bfs_init<<<cap_blocks(V), 256, 0, B.s>>>(g->out_deg, B.parents, B.dist, B.visited, V, B.words);
+    k_bfs_init<<<cap_blocks((uint64_t)B.words * 8), 256, 0, B.s>>>(g->out_deg, g->in_off, B.parents, B.dist,
+                                                                  B.visited, V, B.words);
     k_bfs_source<<<1, 1, 0, B.s>>>(B.parents, B.visited, B.qa, src);
     B.launches += 2;
     GG_CUDA(cudaGetLastError());
 
+    const bool device_loop = (p->mode == GG_BFS_DO || p->mode == GG_BFS_DO_BITMAP) && !p->profile;
     uint32_t outdeg_src = 0;
-    GG_CUDA(cudaMemcpyAsync(&outdeg_src, g->out_deg + src, 4, cudaMemcpyDeviceToHost, B.s));
-    GG_CHECK(gg_wait(B.s));
+    if (!device_loop)
+    {
+        GG_CUDA(cudaMemcpyAsync(&outdeg_src, g->out_deg + src, 4, cudaMemcpyDeviceToHost, B.s));
+        GG_CHECK(gg_wait(B.s));
+    }
 
     const uint32_t alpha = p->alpha ? p->alpha : 15, beta = p->beta ? p->beta : 18;
     uint32_t processed = 1; /* the reference counts the source (BFS.c:368, :474, :588, :881) */
@@ -546,6 +930,13 @@ extern "C" gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parent
     default:
     {
         /* BFS.c:525-686 and :932-1060: direction-optimised, uint32 accounting */
+        if (device_loop)
+        {
+            GG_CHECK(do_search(B, p));
+            processed = B.res.processed_nodes;
+            level = B.res.levels;
+            break;
+        }
         uint32_t mu = g->E, mf = outdeg_src, nf = 0, nf_prev = 0;
         const uint32_t n = V;
         while (qlen)

@@ -96,3 +96,23 @@ def test_bfs_many_sources_rmat16(graphs, dgs, orc):
 def test_bfs_invalid_source(gpu, dgs):
     with pytest.raises(gpu.GgError):
         dgs["rmat8"].bfs(256, "do")
+
+
+@pytest.mark.parametrize("mode", ["do", 4])
+def test_bfs_device_loop_matches_host_loop(graphs, dgs, mode):
+    """The direction-optimised modes run their level loop in one cooperative
+    launch unless profiled; profiled searches step from the host.  Both must
+    give the same schedule, counts and levels."""
+    rng = np.random.default_rng(11)
+    for name in ("rmat12u", "rmat16u", "rmat16", "rmat10"):
+        g, o = graphs[name]
+        deg = np.diff(o.out_off.astype(np.int64))
+        cand = np.nonzero(deg)[0]
+        for s in list(rng.choice(cand, 6, replace=False)) + [0]:
+            _, d0, r0 = dgs[name].bfs(int(s), mode, profile=False)
+            _, d1, r1 = dgs[name].bfs(int(s), mode, profile=True)
+            tag = f"{name} source {s}"
+            np.testing.assert_array_equal(d0, d1, err_msg=tag)
+            for k in ("processed_nodes", "levels", "top_down_steps", "bottom_up_steps", "edges_examined"):
+                assert r0[k] == r1[k], (tag, k, r0[k], r1[k])
+            assert r0["launches"] == 3, (tag, r0["launches"])
