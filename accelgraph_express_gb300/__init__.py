@@ -234,6 +234,12 @@ def lib() -> C.CDLL:
                                         C.c_void_p]
         L.graphCSRFromEdgeList.argtypes = [P(EdgeList)]
         L.graphCSRFromEdgeList.restype = P(GraphCSR)
+        L.graphCSRFromEdgeListDevice.argtypes = [P(EdgeList)]
+        L.graphCSRFromEdgeListDevice.restype = P(GraphCSR)
+        L.gg_graph_build.argtypes = [P(EdgeList), C.c_uint32, C.c_void_p, P(C.c_void_p)]
+        L.gg_graph_build_device.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                            C.c_void_p, P(C.c_void_p)]
+        L.gg_graph_download.argtypes = [C.c_void_p] + [C.c_void_p] * 6 + [P(C.c_float)]
         L.graphCSRFree.argtypes = [P(GraphCSR)]
         L.argumentsSetDefaults.argtypes = [P(Arguments)]
         for name in ["pageRankGraphCSR", "pageRankPullGraphCSR", "pageRankPushGraphCSR",
@@ -314,8 +320,9 @@ class Graph:
             raise GgError("graph construction failed")
         self.ptr = ptr
 
-    @classmethod
-    def from_edges(cls, src, dst, weights=None, num_vertices=None):
+    @staticmethod
+    def _edge_list(src, dst, weights=None, num_vertices=None):
+        """A library EdgeList holding copies of the arrays (free with freeEdgeList)."""
         src = np.ascontiguousarray(src, np.uint32)
         dst = np.ascontiguousarray(dst, np.uint32)
         E = len(src)
@@ -324,16 +331,24 @@ class Graph:
         el = L.newEdgeList(E, V, 1 if weights is not None else 0)
         if not el:
             raise GgError("newEdgeList failed")
+        if E:
+            C.memmove(el.contents.edges_array_src, src.ctypes.data, E * 4)
+            C.memmove(el.contents.edges_array_dest, dst.ctypes.data, E * 4)
+            if weights is not None:
+                w = np.ascontiguousarray(weights, np.float32)
+                C.memmove(el.contents.edges_array_weight, w.ctypes.data, E * 4)
+                el.contents.max_weight = float(w.max())
+        el.contents.num_vertices = V
+        return el
+
+    @classmethod
+    def from_edges(cls, src, dst, weights=None, num_vertices=None, device_build=False):
+        """device_build: sort on the GPU (graphCSRFromEdgeListDevice); the
+        arrays are identical to the host build's."""
+        L = lib()
+        el = cls._edge_list(src, dst, weights, num_vertices)
         try:
-            if E:
-                C.memmove(el.contents.edges_array_src, src.ctypes.data, E * 4)
-                C.memmove(el.contents.edges_array_dest, dst.ctypes.data, E * 4)
-                if weights is not None:
-                    w = np.ascontiguousarray(weights, np.float32)
-                    C.memmove(el.contents.edges_array_weight, w.ctypes.data, E * 4)
-                    el.contents.max_weight = float(w.max())
-            el.contents.num_vertices = V
-            return cls(L.graphCSRFromEdgeList(el))
+            return cls((L.graphCSRFromEdgeListDevice if device_build else L.graphCSRFromEdgeList)(el))
         finally:
             L.freeEdgeList(el)
 
@@ -354,13 +369,13 @@ class Graph:
 
     @classmethod
     def rmat(cls, scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=27491095, weighted=False,
-             weight_seed=27491095 + 2, symmetric=False):
+             weight_seed=27491095 + 2, symmetric=False, device_build=False):
         L = lib()
         el = L.generateRMATEdgeList(scale, edge_factor, a, b, c, seed, int(weighted), weight_seed, int(symmetric))
         if not el:
             raise GgError("generateRMATEdgeList failed")
         try:
-            return cls(L.graphCSRFromEdgeList(el))
+            return cls((L.graphCSRFromEdgeListDevice if device_build else L.graphCSRFromEdgeList)(el))
         finally:
             L.freeEdgeList(el)
 
@@ -439,6 +454,13 @@ class Graph:
 # device graphs (gg_runtime)
 # ---------------------------------------------------------------------------
 
+class _Shape:
+    """Sizes of a graph that exists only on the device."""
+
+    def __init__(self, V, E):
+        self.V, self.E, self.ptr = V, E, None
+
+
 class DeviceGraph:
     """A gg_graph mapping of a Graph (arrays resident in HBM)."""
 
@@ -447,7 +469,58 @@ class DeviceGraph:
         self.h = C.c_void_p()
         _check(lib().gg_graph_map(graph.ptr, what, stream, C.byref(self.h)), "gg_graph_map")
 
+    @classmethod
+    def build(cls, src, dst, weights=None, num_vertices=None, what=MAP_ALL, stream=None):
+        """CSR/CSC built on the device from an edge list: numpy arrays
+        (gg_graph_build uploads them) or CUDA tensors of 32-bit ids and FP32
+        weights (gg_graph_build_device reads them in place)."""
+        self = cls.__new__(cls)
+        self.h = C.c_void_p()
+        L = lib()
+        if hasattr(src, "is_cuda") and src.is_cuda:
+            E = int(src.numel())
+            if num_vertices is None:
+                raise GgError("num_vertices is required for device edge arrays")
+            for t in (src, dst) + ((weights,) if weights is not None else ()):
+                if not t.is_contiguous() or t.element_size() != 4 or t.numel() != E:
+                    raise GgError("device edge arrays must be contiguous 32-bit tensors of one length")
+            _check(L.gg_graph_build_device(int(num_vertices), E, src.data_ptr(), dst.data_ptr(),
+                                           None if weights is None else weights.data_ptr(), what, stream,
+                                           C.byref(self.h)), "gg_graph_build_device")
+            self.graph = _Shape(int(num_vertices), E)
+            return self
+        el = Graph._edge_list(src, dst, weights, num_vertices)
+        try:
+            V, E = int(el.contents.num_vertices), int(el.contents.num_edges)
+            _check(L.gg_graph_build(el, what, stream, C.byref(self.h)), "gg_graph_build")
+        finally:
+            L.freeEdgeList(el)
+        self.graph = _Shape(V, E)
+        return self
+
+    def download(self, weights=True):
+        """The mapping's arrays on the host, as Graph.arrays() names them
+        (offsets with E appended); weights None when not mapped."""
+        V, E = self.graph.V, self.graph.E
+        d = dict(out_off=np.empty(V + 1, np.uint32), out_adj=np.empty(E, np.uint32),
+                 in_off=np.empty(V + 1, np.uint32), in_adj=np.empty(E, np.uint32),
+                 out_w=np.empty(E, np.float32) if weights else None, in_w=np.empty(E, np.float32) if weights else None)
+        mw = C.c_float()
+
+        def ptr(a):
+            return None if a is None else a.ctypes.data
+
+        _check(lib().gg_graph_download(self.h, ptr(d["out_off"]), ptr(d["out_adj"]), ptr(d["out_w"]),
+                                       ptr(d["in_off"]), ptr(d["in_adj"]), ptr(d["in_w"]), C.byref(mw)),
+               "gg_graph_download")
+        d["out_off"][V] = E
+        d["in_off"][V] = E
+        d["max_weight"] = mw.value
+        return d
+
     def extend(self, what, stream=None):
+        if self.graph.ptr is None:
+            raise GgError("a mapping built on the device has no host graph to extend from")
         _check(lib().gg_graph_extend(self.h, self.graph.ptr, what, stream), "gg_graph_extend")
 
     def device_bytes(self):

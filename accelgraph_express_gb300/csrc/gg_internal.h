@@ -44,6 +44,7 @@ struct gg_graph
 {
     uint32_t V = 0, E = 0;
     uint32_t what = 0;
+    float max_weight = 0.0f; /* the edge list's, kept for host copies */
     /* false for a view made by gg_graph_share: the graph arrays belong to
      * the mapping it was made from */
     bool owns_arrays = true;
@@ -110,6 +111,13 @@ gg_status gg_dev_alloc(gg_graph *g, void **p, size_t bytes);
 void gg_dev_free(gg_graph *g, void *p, size_t bytes);
 /* work buffer slot `slot`, at least `bytes` long (contents undefined) */
 gg_status gg_work(gg_graph *g, int slot, size_t bytes, void **out);
+/* a mapping with its stream and events and no arrays */
+gg_status gg_graph_new(uint32_t V, uint32_t E, gg_graph **out);
+/* E + GG_EDGE_PAD weights of the reference's constant 0.0001f */
+gg_status gg_fill_constant_weights(gg_graph *g, float **dst, uint32_t E, cudaStream_t s);
+/* CSR/CSC of `g` from device edge arrays (build.cu) */
+gg_status gg_build_arrays(gg_graph *g, const uint32_t *src, const uint32_t *dst, const float *w, uint32_t what,
+                          cudaStream_t s);
 /* the mapping's page-locked host scratch, at least `bytes` long */
 gg_status gg_pinned(gg_graph *g, size_t bytes, void **out);
 /* build the hot-vertex table of the mapping for a table of `cap` entries

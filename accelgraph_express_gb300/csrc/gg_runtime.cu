@@ -282,7 +282,6 @@ static gg_status upload(gg_graph *g, void **dst, const void *src, size_t bytes, 
     return GG_OK;
 }
 
-static gg_status fill_constant_weights(gg_graph *g, float **dst, uint32_t E, cudaStream_t s);
 
 static gg_status map_arrays(gg_graph *g, const struct GraphCSR *graph, uint32_t what, cudaStream_t s)
 {
@@ -319,7 +318,7 @@ static gg_status map_arrays(gg_graph *g, const struct GraphCSR *graph, uint32_t 
         if (w)
             GG_CHECK(upload(g, (void **)&g->out_w, w, edge_bytes, edge_alloc, s));
         else
-            GG_CHECK(fill_constant_weights(g, &g->out_w, E, s));
+            GG_CHECK(gg_fill_constant_weights(g, &g->out_w, E, s));
     }
     if ((what & GG_MAP_IN_W) && !g->in_w)
     {
@@ -327,7 +326,7 @@ static gg_status map_arrays(gg_graph *g, const struct GraphCSR *graph, uint32_t 
         if (w)
             GG_CHECK(upload(g, (void **)&g->in_w, w, edge_bytes, edge_alloc, s));
         else
-            GG_CHECK(fill_constant_weights(g, &g->in_w, E, s));
+            GG_CHECK(gg_fill_constant_weights(g, &g->in_w, E, s));
     }
     g->what |= what;
     /* the copies read pageable host memory; make them complete before the
@@ -341,7 +340,7 @@ __global__ void k_fill(float *p, size_t n, float v)
         p[i] = v;
 }
 
-static gg_status fill_constant_weights(gg_graph *g, float **dst, uint32_t E, cudaStream_t s)
+gg_status gg_fill_constant_weights(gg_graph *g, float **dst, uint32_t E, cudaStream_t s)
 {
     /* the reference's unweighted build multiplies by 0.0001f (SPMV.c:804) */
     GG_CHECK(gg_dev_alloc(g, (void **)dst, ((size_t)E + GG_EDGE_PAD) * 4));
@@ -350,16 +349,14 @@ static gg_status fill_constant_weights(gg_graph *g, float **dst, uint32_t E, cud
     return GG_OK;
 }
 
-extern "C" gg_status gg_graph_map(const struct GraphCSR *graph, uint32_t what, void *stream, gg_graph **out)
+gg_status gg_graph_new(uint32_t V, uint32_t E, gg_graph **out)
 {
-    if (!out) return gg_fail(GG_ERR_INVALID, "out is NULL");
     *out = nullptr;
-    if (!graph) return gg_fail(GG_ERR_INVALID, "graph is NULL");
     int dev = 0;
     GG_CUDA(cudaGetDevice(&dev));
     gg_graph *g = new gg_graph();
-    g->V = graph->num_vertices;
-    g->E = graph->num_edges;
+    g->V = V;
+    g->E = E;
     g->device = dev;
     cudaError_t e = cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess)
@@ -369,6 +366,18 @@ extern "C" gg_status gg_graph_map(const struct GraphCSR *graph, uint32_t what, v
     }
     cudaEventCreate(&g->ev_begin);
     cudaEventCreate(&g->ev_end);
+    *out = g;
+    return GG_OK;
+}
+
+extern "C" gg_status gg_graph_map(const struct GraphCSR *graph, uint32_t what, void *stream, gg_graph **out)
+{
+    if (!out) return gg_fail(GG_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!graph) return gg_fail(GG_ERR_INVALID, "graph is NULL");
+    gg_graph *g = nullptr;
+    GG_CHECK(gg_graph_new(graph->num_vertices, graph->num_edges, &g));
+    g->max_weight = graph->max_weight;
     gg_status st = map_arrays(g, graph, what, gg_stream(g, stream));
     if (st != GG_OK)
     {
@@ -381,6 +390,90 @@ extern "C" gg_status gg_graph_map(const struct GraphCSR *graph, uint32_t what, v
     return GG_OK;
 }
 
+static gg_status build_common(uint32_t V, uint32_t E, const uint32_t *src, const uint32_t *dst, const float *w,
+                              bool host, float max_weight, uint32_t what, void *stream, gg_graph **out)
+{
+    if (!out) return gg_fail(GG_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (V == 0) return gg_fail(GG_ERR_INVALID, "a graph needs at least one vertex");
+    if (E && (!src || !dst)) return gg_fail(GG_ERR_INVALID, "edge arrays are NULL");
+    if (!(what & (GG_MAP_OUT | GG_MAP_IN | GG_MAP_OUT_W | GG_MAP_IN_W)))
+        return gg_fail(GG_ERR_INVALID, "nothing to build");
+    gg_graph *g = nullptr;
+    GG_CHECK(gg_graph_new(V, E, &g));
+    cudaStream_t s = gg_stream(g, stream);
+    uint32_t *ds = nullptr, *dd = nullptr;
+    float *dw = nullptr;
+    gg_status st = GG_OK;
+    const bool want_w = w && (what & (GG_MAP_OUT_W | GG_MAP_IN_W));
+    if (host)
+    {
+        /* the edge list to the device, freed once the build is done */
+        st = upload(g, (void **)&ds, src, (size_t)E * 4, (size_t)E * 4 + 16, s);
+        if (st == GG_OK) st = upload(g, (void **)&dd, dst, (size_t)E * 4, (size_t)E * 4 + 16, s);
+        if (st == GG_OK && want_w) st = upload(g, (void **)&dw, w, (size_t)E * 4, (size_t)E * 4 + 16, s);
+    }
+    if (st == GG_OK)
+        st = gg_build_arrays(g, host ? ds : src, host ? dd : dst, want_w ? (host ? dw : w) : nullptr, what, s);
+    if (host)
+    {
+        gg_wait(s);
+        gg_dev_free(g, ds, (size_t)E * 4 + 16);
+        gg_dev_free(g, dd, (size_t)E * 4 + 16);
+        gg_dev_free(g, dw, (size_t)E * 4 + 16);
+        if (st == GG_OK) g->max_weight = max_weight;
+    }
+    if (st != GG_OK)
+    {
+        std::string keep = t_last_error;
+        gg_graph_unmap(g);
+        t_last_error = keep;
+        return st;
+    }
+    *out = g;
+    return GG_OK;
+}
+
+extern "C" gg_status gg_graph_build(const struct EdgeList *edges, uint32_t what, void *stream, gg_graph **out)
+{
+    if (!edges) return gg_fail(GG_ERR_INVALID, "edge list is NULL");
+    return build_common(edges->num_vertices, edges->num_edges, edges->edges_array_src, edges->edges_array_dest,
+                        edges->edges_array_weight, true, edges->max_weight, what, stream, out);
+}
+
+extern "C" gg_status gg_graph_build_device(uint32_t num_vertices, uint32_t num_edges, const uint32_t *src,
+                                           const uint32_t *dst, const float *weights, uint32_t what, void *stream,
+                                           gg_graph **out)
+{
+    return build_common(num_vertices, num_edges, src, dst, weights, false, 0.0f, what, stream, out);
+}
+
+extern "C" gg_status gg_graph_download(const gg_graph *gc, uint32_t *out_idx, uint32_t *out_adj, float *out_w,
+                                       uint32_t *in_idx, uint32_t *in_adj, float *in_w, float *max_weight)
+{
+    if (!gc) return gg_fail(GG_ERR_INVALID, "graph is NULL");
+    gg_graph *g = const_cast<gg_graph *>(gc);
+    cudaStream_t s = g->own_stream;
+    const size_t vb = (size_t)g->V * 4, eb = (size_t)g->E * 4;
+    struct Part
+    {
+        void *host;
+        const void *dev;
+        size_t bytes;
+        const char *what;
+    } parts[] = {{out_idx, g->out_off, vb, "out-CSR"}, {out_adj, g->out_adj, eb, "out-CSR"},
+                 {out_w, g->out_w, eb, "out-edge weights"}, {in_idx, g->in_off, vb, "CSC"},
+                 {in_adj, g->in_adj, eb, "CSC"}, {in_w, g->in_w, eb, "in-edge weights"}};
+    for (const Part &p : parts)
+    {
+        if (!p.host) continue;
+        if (!p.dev) return gg_fail(GG_ERR_INVALID, std::string("the mapping has no ") + p.what);
+        if (p.bytes) GG_CUDA(cudaMemcpyAsync(p.host, p.dev, p.bytes, cudaMemcpyDeviceToHost, s));
+    }
+    if (max_weight) *max_weight = g->max_weight;
+    return gg_wait(s);
+}
+
 extern "C" gg_status gg_graph_share(const gg_graph *src, gg_graph **out)
 {
     if (!out) return gg_fail(GG_ERR_INVALID, "out is NULL");
@@ -390,6 +483,7 @@ extern "C" gg_status gg_graph_share(const gg_graph *src, gg_graph **out)
     g->V = src->V;
     g->E = src->E;
     g->what = src->what;
+    g->max_weight = src->max_weight;
     g->device = src->device;
     g->owns_arrays = false;
     g->out_off = src->out_off; g->out_adj = src->out_adj; g->out_w = src->out_w;

@@ -449,21 +449,19 @@ static void free_edges(struct EdgeList *e)
     freeEdgeList(e);
 }
 
-struct GraphCSR *graphCSRFromEdgeList(const struct EdgeList *in)
+/* the GraphCSR shell both builds fill: vertex arrays and the two sorted
+ * edge lists, sized for V and E */
+static struct GraphCSR *alloc_graph(uint32_t V, uint32_t E, int weighted, float max_weight)
 {
-    if (!in)
-        return NULL;
-    const uint32_t V = in->num_vertices, E = in->num_edges;
     struct GraphCSR *g = (struct GraphCSR *)calloc(1, sizeof(struct GraphCSR));
     if (!g)
         return NULL;
     g->num_vertices = V;
     g->num_edges = E;
-    g->max_weight = in->max_weight;
+    g->max_weight = max_weight;
     g->avg_degree = V ? E / V : 0;
     g->vertices = new_vertex(V);
     g->inverse_vertices = new_vertex(V);
-    const int weighted = in->edges_array_weight != NULL;
     g->sorted_edges_array = newEdgeList(E, V, weighted);
     g->inverse_sorted_edges_array = newEdgeList(E, V, weighted);
     if (!g->vertices || !g->inverse_vertices || !g->sorted_edges_array || !g->inverse_sorted_edges_array)
@@ -471,14 +469,14 @@ struct GraphCSR *graphCSRFromEdgeList(const struct EdgeList *in)
         graphCSRFree(g);
         return NULL;
     }
-    if (build_direction(V, E, in->edges_array_src, in->edges_array_dest, in->edges_array_weight, g->vertices,
-                        g->sorted_edges_array) != 0 ||
-        build_direction(V, E, in->edges_array_dest, in->edges_array_src, in->edges_array_weight,
-                        g->inverse_vertices, g->inverse_sorted_edges_array) != 0)
-    {
-        graphCSRFree(g);
-        return NULL;
-    }
+    return g;
+}
+
+/* degrees across directions, identity labels, page-locking for upload */
+static struct GraphCSR *finish_graph(struct GraphCSR *g)
+{
+    const uint32_t V = g->num_vertices, E = g->num_edges;
+    const int weighted = g->sorted_edges_array->edges_array_weight != NULL;
     /* the inverse direction stores (dst, src): edges_array_src holds the
      * destination and edges_array_dest the in-neighbour, as the reference's
      * inverse_sorted_edges_array does */
@@ -488,7 +486,7 @@ struct GraphCSR *graphCSRFromEdgeList(const struct EdgeList *in)
     {
         struct EdgeList *el = d ? g->inverse_sorted_edges_array : g->sorted_edges_array;
         el->num_vertices = V;
-        el->max_weight = in->max_weight;
+        el->max_weight = g->max_weight;
         el->label_array = (uint32_t *)xmalloc((size_t)V * 4 + 64);
         el->inverse_label_array = (uint32_t *)xmalloc((size_t)V * 4 + 64);
         if (!el->label_array || !el->inverse_label_array)
@@ -511,6 +509,74 @@ struct GraphCSR *graphCSRFromEdgeList(const struct EdgeList *in)
         gg_host_pin(g->inverse_sorted_edges_array->edges_array_weight, (size_t)E * 4);
     }
     return g;
+}
+
+struct GraphCSR *graphCSRFromEdgeList(const struct EdgeList *in)
+{
+    if (!in)
+        return NULL;
+    const uint32_t V = in->num_vertices, E = in->num_edges;
+    const int weighted = in->edges_array_weight != NULL;
+    struct GraphCSR *g = alloc_graph(V, E, weighted, in->max_weight);
+    if (!g)
+        return NULL;
+    if (build_direction(V, E, in->edges_array_src, in->edges_array_dest, in->edges_array_weight, g->vertices,
+                        g->sorted_edges_array) != 0 ||
+        build_direction(V, E, in->edges_array_dest, in->edges_array_src, in->edges_array_weight,
+                        g->inverse_vertices, g->inverse_sorted_edges_array) != 0)
+    {
+        graphCSRFree(g);
+        return NULL;
+    }
+    return finish_graph(g);
+}
+
+/* rows and degrees of one direction from its offsets */
+static void rows_from_offsets(uint32_t V, uint32_t E, const uint32_t *idx, uint32_t *row, uint32_t *deg)
+{
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (uint32_t v = 0; v < V; v++)
+    {
+        const uint32_t a = idx[v], b = v + 1 < V ? idx[v + 1] : E;
+        deg[v] = b - a;
+        for (uint32_t i = a; i < b; i++)
+            row[i] = v;
+    }
+}
+
+struct GraphCSR *graphCSRFromEdgeListDevice(const struct EdgeList *in)
+{
+    if (!in)
+        return NULL;
+    const uint32_t V = in->num_vertices, E = in->num_edges;
+    const int weighted = in->edges_array_weight != NULL;
+    gg_graph *d = NULL;
+    const uint32_t what = GG_MAP_OUT | GG_MAP_IN | (weighted ? (GG_MAP_OUT_W | GG_MAP_IN_W) : 0u);
+    gg_status bst = gg_graph_build(in, what, NULL, &d);
+    if (bst != GG_OK)
+    {
+        gpu_report("graphCSRFromEdgeListDevice", bst);
+        return NULL;
+    }
+    struct GraphCSR *g = alloc_graph(V, E, weighted, in->max_weight);
+    if (!g)
+    {
+        gg_graph_unmap(d);
+        return NULL;
+    }
+    struct EdgeList *fw = g->sorted_edges_array, *bw = g->inverse_sorted_edges_array;
+    gg_status st = gg_graph_download(d, g->vertices->edges_idx, fw->edges_array_dest, fw->edges_array_weight,
+                                     g->inverse_vertices->edges_idx, bw->edges_array_dest, bw->edges_array_weight, NULL);
+    gg_graph_unmap(d);
+    if (st != GG_OK)
+    {
+        gpu_report("graphCSRFromEdgeListDevice", st);
+        graphCSRFree(g);
+        return NULL;
+    }
+    rows_from_offsets(V, E, g->vertices->edges_idx, fw->edges_array_src, g->vertices->out_degree);
+    rows_from_offsets(V, E, g->inverse_vertices->edges_idx, bw->edges_array_src, g->inverse_vertices->out_degree);
+    return finish_graph(g);
 }
 
 void graphCSRFree(struct GraphCSR *g)

@@ -81,6 +81,26 @@ gg_status gg_graph_share(const gg_graph *src, gg_graph **out);
 /* Upload any arrays in `what` that the mapping does not carry yet. */
 gg_status gg_graph_extend(gg_graph *g, const struct GraphCSR *graph, uint32_t what, void *stream);
 gg_status gg_graph_unmap(gg_graph *g);
+
+/* Build the CSR and CSC on the device from an edge list, in place of the
+ * host sort + assignment (the reference's OpenGraph sortRunAlgorithms +
+ * graphCSRAssignEdgeList, called at SSSP.c:552-565 and bellmanFord.c:737-744;
+ * their sources are absent from the snapshot).  A stable LSD radix sort of
+ * (row << b | neighbour) words, b = bits for V, as graphCSRFromEdgeList does
+ * on the host: every array equals that build's.  `what` as for gg_graph_map;
+ * out-degrees always come along.  _W without weights gives the constant
+ * 0.0001f.  An id >= num_vertices is GG_ERR_INVALID.
+ * gg_graph_build reads a host EdgeList; gg_graph_build_device takes device
+ * arrays of num_edges entries (`weights` may be NULL) and records the largest
+ * weight above 0 as max_weight. */
+gg_status gg_graph_build(const struct EdgeList *edges, uint32_t what, void *stream, gg_graph **out);
+gg_status gg_graph_build_device(uint32_t num_vertices, uint32_t num_edges, const uint32_t *src, const uint32_t *dst,
+                                const float *weights, uint32_t what, void *stream, gg_graph **out);
+/* Copy a mapping's arrays to host buffers (any may be NULL): row offsets
+ * (V entries, as edges_idx), neighbours and weights (E entries) of the
+ * out-CSR and the CSC, and the edge list's max_weight. */
+gg_status gg_graph_download(const gg_graph *g, uint32_t *out_idx, uint32_t *out_adj, float *out_w, uint32_t *in_idx,
+                            uint32_t *in_adj, float *in_w, float *max_weight);
 /* Bytes of device memory held by the mapping (graph + work buffers). */
 size_t gg_graph_device_bytes(const gg_graph *g);
 

@@ -128,6 +128,10 @@ struct EdgeList *generateRMATBatchEdgeList(uint32_t ngraphs, const uint32_t *sca
  * device is present (graphCSRFree undoes that).
  */
 struct GraphCSR *graphCSRFromEdgeList(const struct EdgeList *edgeList);
+/* The same GraphCSR, every array identical, with the sorts run on the GPU
+ * (gg_graph_build, then the arrays copied back); NULL on failure (no
+ * device, id >= num_vertices, out of memory), with the reason printed. */
+struct GraphCSR *graphCSRFromEdgeListDevice(const struct EdgeList *edgeList);
 void graphCSRFree(struct GraphCSR *graph);
 
 #ifdef __cplusplus

@@ -1,0 +1,113 @@
+"""CSR / CSC built on the GPU (gg_graph_build, graphCSRFromEdgeListDevice)
+against the host build (graphCSRFromEdgeList), which sorts the same words
+(row << b | neighbour) with a stable LSD radix sort: every array must be
+identical — offsets, neighbour order within rows, the weights of duplicate
+edges (input order), degrees, max_weight."""
+import numpy as np
+import pytest
+
+from graphs import fixture_edges, special_edges
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("out_off", "out_adj", "in_off", "in_adj", "out_degree", "in_degree", "out_w", "in_w")
+
+
+def _same(a, b, tag):
+    for k in KEYS:
+        if a[k] is None or b[k] is None:
+            assert a[k] is None and b[k] is None, (tag, k)
+            continue
+        np.testing.assert_array_equal(a[k], b[k], err_msg=f"{tag} {k}")
+
+
+def _cases():
+    out = {}
+    for name, (s, d, w) in fixture_edges().items():
+        out[name] = (s, d, w, None)
+    for name, (s, d, w, V) in special_edges().items():
+        out[name] = (s, d, w, V)
+    rng = np.random.default_rng(5)
+    # duplicates of one edge with distinct weights: their order must be the input order
+    s = rng.integers(0, 50, 4000).astype(np.uint32)
+    d = rng.integers(0, 50, 4000).astype(np.uint32)
+    out["dups_weighted"] = (s, d, rng.random(4000).astype(np.float32), 64)
+    # vertex counts at and just past a power of two (the key width b changes)
+    for V in (1, 2, 3, 255, 256, 257, 65536, 65537):
+        E = 3 * V + 7
+        out[f"rand_v{V}"] = (rng.integers(0, V, E).astype(np.uint32), rng.integers(0, V, E).astype(np.uint32),
+                             rng.standard_normal(E).astype(np.float32), V)
+    out["no_edges"] = (np.zeros(0, np.uint32), np.zeros(0, np.uint32), None, 10)
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(_cases()))
+def test_device_build_matches_host(gpu, name):
+    s, d, w, V = _cases()[name]
+    host = gpu.Graph.from_edges(s, d, w, num_vertices=V).arrays()
+    dev_graph = gpu.Graph.from_edges(s, d, w, num_vertices=V, device_build=True)
+    _same(dev_graph.arrays(), host, name)
+    assert dev_graph.ptr.contents.max_weight == gpu.Graph.from_edges(s, d, w, num_vertices=V).ptr.contents.max_weight
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_device_build_rmat(gpu, weighted):
+    """R-MAT scale 18 (262K vertices, 4.2M edges: several radix tiles per
+    digit, skewed digits)."""
+    host = gpu.Graph.rmat(18, 16, weighted=weighted).arrays()
+    dev = gpu.Graph.rmat(18, 16, weighted=weighted, device_build=True).arrays()
+    _same(dev, host, f"rmat18 weighted={weighted}")
+
+
+def test_device_mapping_download(gpu):
+    """gg_graph_build's mapping, downloaded, equals the host build; the
+    mapping from device tensors equals the one from host arrays."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(9)
+    V, E = 100_003, 1_500_000
+    s = rng.integers(0, V, E).astype(np.uint32)
+    d = (rng.zipf(1.6, E) % V).astype(np.uint32)
+    w = rng.random(E).astype(np.float32)
+    host = gpu.Graph.from_edges(s, d, w, num_vertices=V).arrays()
+    dg = gpu.DeviceGraph.build(s, d, w, num_vertices=V)
+    got = dg.download()
+    for k in ("out_off", "out_adj", "in_off", "in_adj", "out_w", "in_w"):
+        np.testing.assert_array_equal(got[k], host[k], err_msg=k)
+    ts = torch.from_numpy(s.view(np.int32)).cuda()
+    td = torch.from_numpy(d.view(np.int32)).cuda()
+    tw = torch.from_numpy(w).cuda()
+    dg2 = gpu.DeviceGraph.build(ts, td, tw, num_vertices=V)
+    got2 = dg2.download()
+    for k in ("out_off", "out_adj", "in_off", "in_adj", "out_w", "in_w"):
+        np.testing.assert_array_equal(got2[k], host[k], err_msg="device input " + k)
+    assert got2["max_weight"] == np.float32(w.max())
+
+
+def test_device_built_mapping_runs_the_path(gpu, orc):
+    """PageRank, SpMV and BFS on a mapping built on the device give the same
+    results as on the host-built mapping of the same edges."""
+    g = gpu.Graph.rmat(14, 16, weighted=True)
+    a = g.arrays()
+    s = np.repeat(np.arange(g.V, dtype=np.uint32), np.diff(a["out_off"]).astype(np.int64))
+    dm = gpu.DeviceGraph.build(s, a["out_adj"], a["out_w"], num_vertices=g.V)
+    hm = gpu.DeviceGraph(g, gpu.MAP_ALL)
+    # the same arrays run the same kernels; rows split across tiles add FP32
+    # partials with atomics, so sums may differ in the last bit
+    r1, i1 = dm.pagerank("pull")
+    r2, i2 = hm.pagerank("pull")
+    np.testing.assert_allclose(r1, r2, rtol=1e-6, atol=0)
+    assert i1["iterations"] == i2["iterations"]
+    _, y1, _ = dm.spmv("pull")
+    _, y2, _ = hm.spmv("pull")
+    np.testing.assert_allclose(y1, y2, rtol=1e-6, atol=1e-30)
+    _, d1, b1 = dm.bfs(0, "do")
+    _, d2, b2 = hm.bfs(0, "do")
+    np.testing.assert_array_equal(d1, d2)
+    assert b1["edges_examined"] == b2["edges_examined"]
+
+
+def test_device_build_rejects_bad_ids(gpu):
+    s = np.array([0, 1, 7], np.uint32)
+    d = np.array([1, 2, 3], np.uint32)
+    with pytest.raises(gpu.GgError):
+        gpu.DeviceGraph.build(s, d, num_vertices=5)
