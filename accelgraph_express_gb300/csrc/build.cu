@@ -13,12 +13,15 @@
  *   k_make_keys   (src << b | dst) for the CSR or (dst << b | src) for the
  *                 CSC, with the edge weight as payload; ids >= V flagged
  *   per 8-bit digit, least significant first (2b bits in all):
- *     k_rdx_count    per-tile digit counts, digit-major (counts[d][tile])
- *     scan           exclusive scan of the counts: the first output slot of
- *                    every (digit, tile), in digit-then-tile order
- *     k_rdx_scatter  stable rank within the tile (per-warp digit counters
- *                    and __match_any_sync), the tile reordered by digit in
- *                    shared memory, then written out in runs
+ *     k_rdx_count    per-tile digit counts, tile-major (counts[tile][d])
+ *     column scan    k_col_reduce / k_col_top / k_col_down: counts[tile][d]
+ *                    becomes the first output slot of digit d's keys of that
+ *                    tile (keys of smaller digits, then of digit d in
+ *                    earlier tiles); every access is a coalesced row
+ *     k_rdx_scatter  stable rank within the tile (per-warp digit counters;
+ *                    lanes with equal digits found by eight ballots), the
+ *                    tile reordered by digit in shared memory, then written
+ *                    out in runs
  *   k_split       neighbour ids, row offsets from the row boundaries, and
  *                 the out-degrees
  *
@@ -40,15 +43,25 @@ constexpr int RDX_ITEMS = 16;
 constexpr int RDX_TILE = RDX_THREADS * RDX_ITEMS;
 constexpr int RDX_WARPS = RDX_THREADS / 32;
 
-constexpr int SCAN_THREADS = 1024;
-constexpr int SCAN_ITEMS = 8;
-constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_ITEMS;
-constexpr int SCAN_TOP_ITEMS = 64; /* the single-block pass scans up to 65536 chunk sums */
+constexpr int COL_TILES = 64; /* tiles per block of the column scan */
 
 __device__ __forceinline__ uint32_t digit_of(uint64_t k, int shift) { return (uint32_t)(k >> shift) & (RDX_BINS - 1); }
 
-/* an id that cannot collide with a digit: invalid lanes match only themselves */
-__device__ __forceinline__ uint32_t match_key(bool valid, uint32_t d, uint32_t lane) { return valid ? d : RDX_BINS + lane; }
+/* lanes of the warp holding a valid key with the same digit (warp
+ * multisplit: one ballot per digit bit, ALU work instead of a match
+ * instruction); meaningful for valid lanes only */
+__device__ __forceinline__ uint32_t digit_peers(bool valid, uint32_t d)
+{
+    uint32_t m = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+    for (int b = 0; b < 8; b++)
+    {
+        const uint32_t bit = (d >> b) & 1u;
+        const uint32_t v = __ballot_sync(0xffffffffu, bit);
+        m &= bit ? v : ~v;
+    }
+    return m;
+}
 
 __global__ void k_make_keys(const uint32_t *__restrict__ key, const uint32_t *__restrict__ other,
                             const float *__restrict__ w, uint64_t n, uint32_t V, int b, uint64_t *out, float *wout,
@@ -69,9 +82,9 @@ __global__ void k_make_keys(const uint32_t *__restrict__ key, const uint32_t *__
 __global__ void __launch_bounds__(RDX_THREADS) k_rdx_count(const uint64_t *__restrict__ keys, uint64_t n, int shift,
                                                            uint32_t ntiles, uint32_t *counts)
 {
-    __shared__ uint32_t h[RDX_WARPS][RDX_BINS];
+    __shared__ uint32_t h[RDX_BINS];
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5, tile = blockIdx.x;
-    for (int i = threadIdx.x; i < RDX_WARPS * RDX_BINS; i += RDX_THREADS) (&h[0][0])[i] = 0u;
+    h[threadIdx.x] = 0u;
     __syncthreads();
     const uint64_t base = (uint64_t)tile * RDX_TILE + (uint64_t)w * 32 * RDX_ITEMS + lane;
     uint64_t k[RDX_ITEMS];
@@ -86,21 +99,17 @@ __global__ void __launch_bounds__(RDX_THREADS) k_rdx_count(const uint64_t *__res
     {
         const bool valid = base + (uint64_t)it * 32 < n;
         const uint32_t d = digit_of(k[it], shift);
-        const uint32_t peers = __match_any_sync(0xffffffffu, match_key(valid, d, lane));
-        /* one lane per digit group adds it: bins of one warp have one writer */
-        if (valid && (peers & ((1u << lane) - 1u)) == 0u) h[w][d] += (uint32_t)__popc(peers);
-        __syncwarp();
+        const uint32_t peers = digit_peers(valid, d);
+        /* the lowest lane of each digit group adds the group's size */
+        if (valid && (peers & ((1u << lane) - 1u)) == 0u) atomicAdd(&h[d], (uint32_t)__popc(peers));
     }
     __syncthreads();
-    uint32_t t = 0;
-#pragma unroll
-    for (int ww = 0; ww < RDX_WARPS; ww++) t += h[ww][threadIdx.x];
-    counts[(size_t)threadIdx.x * ntiles + tile] = t;
+    counts[(size_t)tile * RDX_BINS + threadIdx.x] = h[threadIdx.x];
 }
 
 constexpr int SCATTER_SMEM = RDX_TILE * 12 + RDX_WARPS * RDX_BINS * 4 + 2 * RDX_BINS * 4 + RDX_WARPS * 4;
 
-__global__ void __launch_bounds__(RDX_THREADS) k_rdx_scatter(const uint64_t *__restrict__ keys,
+__global__ void __launch_bounds__(RDX_THREADS, 3) k_rdx_scatter(const uint64_t *__restrict__ keys,
                                                              const float *__restrict__ pay, uint64_t n, int shift,
                                                              uint32_t ntiles, const uint32_t *__restrict__ first,
                                                              uint64_t *__restrict__ okeys, float *__restrict__ opay)
@@ -118,7 +127,7 @@ __global__ void __launch_bounds__(RDX_THREADS) k_rdx_scatter(const uint64_t *__r
     uint32_t *wtot = tstart + RDX_BINS;
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5, tile = blockIdx.x;
     for (int i = threadIdx.x; i < RDX_WARPS * RDX_BINS; i += RDX_THREADS) (&wcnt[0][0])[i] = 0u;
-    gfirst[threadIdx.x] = first[(size_t)threadIdx.x * ntiles + tile];
+    gfirst[threadIdx.x] = first[(size_t)tile * RDX_BINS + threadIdx.x];
     __syncthreads();
     const uint64_t base = (uint64_t)tile * RDX_TILE + (uint64_t)w * 32 * RDX_ITEMS + lane;
     uint64_t k[RDX_ITEMS];
@@ -129,19 +138,22 @@ __global__ void __launch_bounds__(RDX_THREADS) k_rdx_scatter(const uint64_t *__r
         const uint64_t i = base + (uint64_t)it * 32;
         k[it] = i < n ? keys[i] : 0ull;
     }
-    /* rank among the warp's earlier keys of the same digit, in element order */
+    /* rank among the warp's earlier keys of the same digit, in element
+     * order: the group's lowest lane advances the warp's digit counter by
+     * the group size and hands the old value to its peers */
 #pragma unroll
     for (int it = 0; it < RDX_ITEMS; it++)
     {
         const bool valid = base + (uint64_t)it * 32 < n;
         const uint32_t d = digit_of(k[it], shift);
-        const uint32_t peers = __match_any_sync(0xffffffffu, match_key(valid, d, lane));
+        const uint32_t peers = digit_peers(valid, d);
         const uint32_t before = (uint32_t)__popc(peers & ((1u << lane) - 1u));
-        const uint32_t seen = valid ? wcnt[w][d] : 0u;
-        __syncwarp();
-        if (valid && before == 0u) wcnt[w][d] = seen + (uint32_t)__popc(peers);
-        __syncwarp();
+        const int leader = valid ? __ffs(peers) - 1 : (int)lane;
+        uint32_t seen = 0;
+        if (valid && before == 0u) seen = atomicAdd(&wcnt[w][d], (uint32_t)__popc(peers));
+        seen = __shfl_sync(0xffffffffu, seen, leader);
         rank[it] = seen + before;
+        __syncwarp();
     }
     __syncthreads();
     /* thread t = digit t: exclusive prefix over warps, then the tile's
@@ -194,96 +206,58 @@ __global__ void __launch_bounds__(RDX_THREADS) k_rdx_scatter(const uint64_t *__r
     }
 }
 
-/* ---- exclusive scan of a uint32 array (sums stay below 2^32) ---- */
+/* ---- column scan of the [tile][digit] counts (thread = digit) ---- */
 
-/* block-wide exclusive scan of SCAN_CHUNK values held SCAN_ITEMS per thread;
- * returns this thread's exclusive base and the chunk total in *total */
-__device__ __forceinline__ uint32_t block_scan_base(uint32_t mine, uint32_t *total)
+/* the column sums of each block of COL_TILES tiles */
+__global__ void __launch_bounds__(RDX_BINS) k_col_reduce(const uint32_t *__restrict__ counts, uint32_t ntiles,
+                                                         uint32_t *csum)
 {
-    __shared__ uint32_t ws[SCAN_THREADS / 32];
-    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t incl = mine;
+    const uint32_t t0 = blockIdx.x * COL_TILES, t1 = min(t0 + COL_TILES, ntiles);
+    uint32_t t = 0;
+    for (uint32_t tile = t0; tile < t1; tile++) t += counts[(size_t)tile * RDX_BINS + threadIdx.x];
+    csum[(size_t)blockIdx.x * RDX_BINS + threadIdx.x] = t;
+}
+
+/* one block: csum[b][d] becomes the first output slot of digit d in block
+ * b's tiles: the keys of all smaller digits plus digit d in earlier blocks */
+__global__ void __launch_bounds__(RDX_BINS) k_col_top(uint32_t *csum, uint32_t nblocks)
+{
+    __shared__ uint32_t wtot[RDX_BINS / 32];
+    const uint32_t d = threadIdx.x, lane = d & 31, w = d >> 5;
+    uint32_t run = 0;
+    for (uint32_t b = 0; b < nblocks; b++)
+    {
+        const uint32_t c = csum[(size_t)b * RDX_BINS + d];
+        csum[(size_t)b * RDX_BINS + d] = run;
+        run += c;
+    }
+    /* exclusive scan of the digit totals */
+    uint32_t incl = run;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1)
     {
         const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= (uint32_t)o) incl += y;
     }
-    if (lane == 31) ws[w] = incl;
+    if (lane == 31) wtot[w] = incl;
     __syncthreads();
-    static_assert(SCAN_THREADS == 1024, "one warp scans the 32 warp totals");
-    if (w == 0)
-    {
-        const uint32_t v = ws[lane];
-        uint32_t x = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= (uint32_t)o) x += y;
-        }
-        ws[lane] = x - v;
-        if (lane == 31) *total = x;
-    }
-    __syncthreads();
-    const uint32_t r = ws[w] + incl - mine;
-    __syncthreads();
-    return r;
+    uint32_t base = incl - run;
+    for (uint32_t k = 0; k < w; k++) base += wtot[k];
+    for (uint32_t b = 0; b < nblocks; b++) csum[(size_t)b * RDX_BINS + d] += base;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *__restrict__ a, uint64_t m, uint32_t *sums)
+__global__ void __launch_bounds__(RDX_BINS) k_col_down(uint32_t *counts, uint32_t ntiles,
+                                                       const uint32_t *__restrict__ csum)
 {
-    const uint64_t base = (uint64_t)blockIdx.x * SCAN_CHUNK + (uint64_t)threadIdx.x * SCAN_ITEMS;
-    uint32_t t = 0;
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; k++)
-        if (base + k < m) t += a[base + k];
-    __shared__ uint32_t tot;
-    block_scan_base(t, &tot);
-    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
-}
-
-/* one block: exclusive scan of the chunk sums in place (nb <= 65536) */
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_top(uint32_t *sums, uint32_t nb)
-{
-    const uint32_t base = threadIdx.x * SCAN_TOP_ITEMS;
-    uint32_t v[SCAN_TOP_ITEMS], t = 0;
-#pragma unroll
-    for (int k = 0; k < SCAN_TOP_ITEMS; k++)
+    const uint32_t t0 = blockIdx.x * COL_TILES, t1 = min(t0 + COL_TILES, ntiles);
+    uint32_t run = csum[(size_t)blockIdx.x * RDX_BINS + threadIdx.x];
+    for (uint32_t tile = t0; tile < t1; tile++)
     {
-        v[k] = base + k < nb ? sums[base + k] : 0u;
-        t += v[k];
+        uint32_t *p = counts + (size_t)tile * RDX_BINS + threadIdx.x;
+        const uint32_t c = *p;
+        *p = run;
+        run += c;
     }
-    __shared__ uint32_t tot;
-    uint32_t run = block_scan_base(t, &tot);
-#pragma unroll
-    for (int k = 0; k < SCAN_TOP_ITEMS; k++)
-        if (base + k < nb)
-        {
-            sums[base + k] = run;
-            run += v[k];
-        }
-}
-
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(uint32_t *a, uint64_t m, const uint32_t *__restrict__ sums)
-{
-    const uint64_t base = (uint64_t)blockIdx.x * SCAN_CHUNK + (uint64_t)threadIdx.x * SCAN_ITEMS;
-    uint32_t v[SCAN_ITEMS], t = 0;
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; k++)
-    {
-        v[k] = base + k < m ? a[base + k] : 0u;
-        t += v[k];
-    }
-    __shared__ uint32_t tot;
-    uint32_t run = sums[blockIdx.x] + block_scan_base(t, &tot);
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; k++)
-        if (base + k < m)
-        {
-            a[base + k] = run;
-            run += v[k];
-        }
 }
 
 /* neighbour ids, and off[v] = the first slot whose key is >= v (off[V] = n):
@@ -354,15 +328,13 @@ gg_status radix_sort(SortBufs &B, uint64_t n, int bits, cudaStream_t s)
         attr_set = true;
     }
     const uint32_t ntiles = (uint32_t)((n + RDX_TILE - 1) / RDX_TILE);
-    const uint64_t m = (uint64_t)RDX_BINS * ntiles;
-    const uint32_t nb = (uint32_t)((m + SCAN_CHUNK - 1) / SCAN_CHUNK);
-    if (nb > (uint32_t)SCAN_THREADS * SCAN_TOP_ITEMS) return gg_fail(GG_ERR_INVALID, "edge list too long to sort");
+    const uint32_t nb = (ntiles + COL_TILES - 1) / COL_TILES;
     for (int shift = 0; shift < bits; shift += 8)
     {
         k_rdx_count<<<ntiles, RDX_THREADS, 0, s>>>(B.keys, n, shift, ntiles, B.counts);
-        k_scan_reduce<<<nb, SCAN_THREADS, 0, s>>>(B.counts, m, B.sums);
-        k_scan_top<<<1, SCAN_THREADS, 0, s>>>(B.sums, nb);
-        k_scan_down<<<nb, SCAN_THREADS, 0, s>>>(B.counts, m, B.sums);
+        k_col_reduce<<<nb, RDX_BINS, 0, s>>>(B.counts, ntiles, B.sums);
+        k_col_top<<<1, RDX_BINS, 0, s>>>(B.sums, nb);
+        k_col_down<<<nb, RDX_BINS, 0, s>>>(B.counts, ntiles, B.sums);
         k_rdx_scatter<<<ntiles, RDX_THREADS, SCATTER_SMEM, s>>>(B.keys, B.pay, n, shift, ntiles, B.counts, B.tmp, B.ptmp);
         GG_CUDA(cudaGetLastError());
         std::swap(B.keys, B.tmp);
@@ -407,6 +379,7 @@ gg_status gg_build_arrays(gg_graph *g, const uint32_t *src, const uint32_t *dst,
     void *bad = nullptr;
     const uint64_t ntiles = ((uint64_t)E + RDX_TILE - 1) / RDX_TILE;
     const uint64_t m = (uint64_t)RDX_BINS * (ntiles ? ntiles : 1);
+    const size_t sums_bytes = ((ntiles + COL_TILES - 1) / COL_TILES + 1) * RDX_BINS * 4;
     gg_status st = GG_OK;
     do
     {
@@ -418,7 +391,7 @@ gg_status gg_build_arrays(gg_graph *g, const uint32_t *src, const uint32_t *dst,
             if ((st = gg_dev_alloc(g, (void **)&B.ptmp, (size_t)E * 4 + 16)) != GG_OK) break;
         }
         if ((st = gg_dev_alloc(g, (void **)&B.counts, (size_t)m * 4)) != GG_OK) break;
-        if ((st = gg_dev_alloc(g, (void **)&B.sums, ((m + SCAN_CHUNK - 1) / SCAN_CHUNK) * 4 + 16)) != GG_OK) break;
+        if ((st = gg_dev_alloc(g, (void **)&B.sums, sums_bytes)) != GG_OK) break;
         if ((st = gg_dev_alloc(g, &bad, 16)) != GG_OK) break;
         if (cudaMemsetAsync(bad, 0, 16, s) != cudaSuccess)
         {
@@ -480,7 +453,7 @@ gg_status gg_build_arrays(gg_graph *g, const uint32_t *src, const uint32_t *dst,
     gg_dev_free(g, B.pay, (size_t)E * 4 + 16);
     gg_dev_free(g, B.ptmp, (size_t)E * 4 + 16);
     gg_dev_free(g, B.counts, (size_t)m * 4);
-    gg_dev_free(g, B.sums, ((m + SCAN_CHUNK - 1) / SCAN_CHUNK) * 4 + 16);
+    gg_dev_free(g, B.sums, sums_bytes);
     gg_dev_free(g, bad, 16);
     if (st == GG_OK && !weighted)
     {

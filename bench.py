@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--edge-factor", type=int, default=16)
     p.add_argument("--no-extras", action="store_true", help="skip the BF16/BFS/SpMV side measurements")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    p.add_argument("--leg", choices=["c1", "bfs", "ppr", "batch", "serve"],
+    p.add_argument("--leg", choices=["c1", "bfs", "ppr", "batch", "serve", "csr"],
                    help="run one side measurement alone and print its JSON (for profiling)")
     return p.parse_args()
 
@@ -237,7 +237,7 @@ def run_leg(leg):
     peak, _ = load_peaks()
     fn = {"c1": lambda: c1_extras(gg, torch), "bfs": lambda: bfs_extras(gg, torch, peak),
           "ppr": lambda: ppr_extras(gg, torch, peak), "batch": lambda: batch_extras(gg, torch, peak),
-          "serve": lambda: serving_extras(gg)}[leg]
+          "serve": lambda: serving_extras(gg), "csr": lambda: csr_build_extras(gg, torch, peak)}[leg]
     print(json.dumps({"leg": leg, **fn()}), flush=True)
 
 
@@ -656,6 +656,69 @@ def bfs_extras(gg, torch, peak, scale=22):
     return out
 
 
+def csr_radix_bytes(V, E):
+    """Bytes the device CSR + CSC build moves per direction (unweighted):
+    keys made (8E read, 8E written), per 8-bit pass a count read (8E) and a
+    scatter read + write (16E), then ids and offsets split out (8E read,
+    4E + 4V written)."""
+    b = max(1, (max(V, 2) - 1).bit_length())
+    passes = (2 * b + 7) // 8
+    return 2 * (16 * E + 24 * E * passes + 12 * E + 4 * V), passes
+
+
+def csr_build_extras(gg, torch, peak, scale=24, edge_factor=16):
+    """CSR + CSC of the R-MAT edge list built on the GPU (stable LSD radix
+    sort, gg_graph_build_device on device-resident ids; gg_graph_build from
+    the host edge list, upload included) against the host build of the same
+    list (graphCSRFromEdgeList, all host cores); arrays compared in full."""
+    import ctypes as C
+
+    import numpy as np
+
+    L = gg.lib()
+    el = L.generateRMATEdgeList(scale, edge_factor, 0.57, 0.19, 0.19, SEED, 0, SEED + 2, 0)
+    V, E = int(el.contents.num_vertices), int(el.contents.num_edges)
+    try:
+        src = torch.from_numpy(np.ctypeslib.as_array(el.contents.edges_array_src, (E,)).view(np.int32)).cuda()
+        dst = torch.from_numpy(np.ctypeslib.as_array(el.contents.edges_array_dest, (E,)).view(np.int32)).cuda()
+        st = torch.cuda.current_stream()
+        what = gg.MAP_OUT | gg.MAP_IN
+        for _ in range(2):
+            gg.DeviceGraph.build(src, dst, num_vertices=V, what=what, stream=st.cuda_stream).free()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            dg = gg.DeviceGraph.build(src, dst, num_vertices=V, what=what, stream=st.cuda_stream)
+            e1.record(st)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            got = dg.download(weights=False)
+            dg.free()
+        del src, dst
+        h = C.c_void_p()
+        t0 = time.perf_counter()
+        gg._check(L.gg_graph_build(el, what, None, C.byref(h)), "gg_graph_build")
+        e2e_s = time.perf_counter() - t0
+        L.gg_graph_unmap(h)
+        t0 = time.perf_counter()
+        host = gg.Graph(L.graphCSRFromEdgeList(el))
+        host_s = time.perf_counter() - t0
+        a = host.arrays()
+        equal = all(np.array_equal(got[k], a[k]) for k in ("out_off", "out_adj", "in_off", "in_adj"))
+        host.free()
+    finally:
+        L.freeEdgeList(el)
+    dev_ms = float(np.median(ms))
+    alg, passes = csr_radix_bytes(V, E)
+    return {"graph": f"R-MAT-{scale} edge list, V={V}, E={E}", "device_ms": dev_ms,
+            "device_gedges_s": E / (dev_ms / 1e3) / 1e9, "e2e_from_host_ms": e2e_s * 1e3,
+            "host_build_ms": host_s * 1e3, "host_cores": os.cpu_count() or 1,
+            "radix_passes_per_direction": passes, "moved_bytes": alg,
+            "hbm_frac": alg / (dev_ms / 1e3) / 1e9 / peak, "arrays_equal_host_build": bool(equal)}
+
+
 def spmv_extras(gg, graph, V, E, sptr, torch, peak):
     """SpMV pull over the weighted R-MAT graph, FP32 and BF16 storage of x and
     the weights (FP32 products and sums), 30 products per run; L1 / L-inf vs
@@ -742,6 +805,7 @@ def extras(gg, graph, dg, V, E, sptr, torch, peak):
     out["ppr_batched"] = ppr_extras(gg, torch, peak)
     out["many_graphs"] = batch_extras(gg, torch, peak)
     out["serving"] = serving_extras(gg)
+    out["csr_build"] = csr_build_extras(gg, torch, peak)
     return out
 
 
