@@ -101,6 +101,26 @@ class ArrayQueue(C.Structure):
                 ("q_bitmap_next", C.POINTER(Bitmap))]
 
 
+class CCStats(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("neighbor_rounds", C.c_uint32), ("arguments", C.c_void_p),
+                ("num_vertices", C.c_uint32), ("components", C.POINTER(C.c_uint32)),
+                ("counts", C.POINTER(C.c_uint32)), ("labels", C.POINTER(C.c_uint32)), ("time_total", C.c_double)]
+
+
+class CcParams(C.Structure):
+    _fields_ = [("algorithm", C.c_uint32), ("neighbor_rounds", C.c_uint32), ("samples", C.c_uint32),
+                ("use_in_edges", C.c_uint32), ("max_iterations", C.c_uint32), ("profile", C.c_uint32),
+                ("seed", C.c_uint64)]
+
+
+class CcResult(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("components", C.c_uint32), ("launches", C.c_uint32),
+                ("skipped_label", C.c_uint32), ("kernel_ms", C.c_float)]
+
+
+CC_ALGORITHMS = {"sv": 0, "afforest": 1, "weakly": 2}
+
+
 class PrParams(C.Structure):
     _fields_ = [("mode", C.c_uint32), ("storage", C.c_uint32), ("max_iterations", C.c_uint32),
                 ("init_one_over_n", C.c_uint32), ("epsilon", C.c_double), ("damp", C.c_float),
@@ -261,6 +281,18 @@ def lib() -> C.CDLL:
                      "SPMVPushFixedPointGraphCSR"]:
             getattr(L, name).argtypes = [P(Arguments), P(GraphCSR)]
             getattr(L, name).restype = P(SPMVStats)
+        for name in ["connectedComponentsGraphCSR", "connectedComponentsShiloachVishkinGraphCSR",
+                     "connectedComponentsAfforestGraphCSR", "connectedComponentsWeaklyGraphCSR"]:
+            getattr(L, name).argtypes = [P(Arguments), P(GraphCSR)]
+            getattr(L, name).restype = P(CCStats)
+        L.freeCCStats.argtypes = [P(CCStats)]
+        L.newCCStatsGraphCSR.argtypes = [P(GraphCSR)]
+        L.newCCStatsGraphCSR.restype = P(CCStats)
+        L.compressNodes.argtypes = [C.c_uint32, C.c_void_p]
+        L.linkNodes.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p]
+        L.connectedComponentsVerifyGraphCSR.argtypes = [P(CCStats), P(GraphCSR)]
+        L.connectedComponentsVerifyGraphCSR.restype = C.c_uint32
+        L.gg_cc.argtypes = [C.c_void_p, P(CcParams), C.c_void_p, P(CcResult), C.c_void_p]
         L.freePageRankStats.argtypes = [P(PageRankStats)]
         L.freeBFSStats.argtypes = [P(BFSStats)]
         L.freeSPMVStats.argtypes = [P(SPMVStats)]
@@ -562,6 +594,18 @@ class DeviceGraph:
                             None if dist is None else dist.ctypes.data, C.byref(r), stream), "gg_bfs")
         return parents, dist, {k: getattr(r, k) for k, _ in BfsResult._fields_}
 
+    def cc(self, algorithm="afforest", use_in_edges=2, neighbor_rounds=0, samples=0, seed=27491095,
+           max_iterations=0, profile=False, copy_out=True, stream=None):
+        """Connected components: (labels or None, result dict); every label is
+        the smallest vertex id of the vertex's weakly connected component."""
+        p = CcParams(CC_ALGORITHMS[algorithm] if isinstance(algorithm, str) else algorithm, neighbor_rounds,
+                     samples, use_in_edges, max_iterations, int(profile), seed)
+        r = CcResult()
+        comp = np.empty(self.graph.V, np.uint32) if copy_out else None
+        _check(lib().gg_cc(self.h, C.byref(p), None if comp is None else comp.ctypes.data, C.byref(r), stream),
+               "gg_cc")
+        return comp, {k: getattr(r, k) for k, _ in CcResult._fields_}
+
     def spmv(self, mode="pull", storage="f32", iterations=1, x=None, profile=False, copy_out=True, stream=None,
              hot=None):
         p = SpmvParams(SPMV_MODES[mode] if isinstance(mode, str) else mode, STORE[storage], iterations,
@@ -689,6 +733,25 @@ def pagerank_csr(graph: Graph, args: Arguments, fn="pageRankGraphCSR"):
                        "realRanks": _np(st.realRanks, graph.V, np.uint32)}
     finally:
         L.freePageRankStats(s)
+
+
+def cc_csr(graph: Graph, args: Arguments, fn="connectedComponentsGraphCSR", verify=False):
+    """Call a connectedComponents*GraphCSR entry point; returns (components,
+    counts, labels, stats dict[, verify result])."""
+    L = lib()
+    s = getattr(L, fn)(C.byref(args), graph.ptr)
+    if not s:
+        raise GgError(f"{fn} failed: status {L.graphGpuLastError()}: {L.gg_last_error().decode()}")
+    try:
+        st = s.contents
+        V = graph.V
+        out = (_np(st.components, V, np.uint32), _np(st.counts, V, np.uint32), _np(st.labels, V, np.uint32),
+               {"iterations": st.iterations, "neighbor_rounds": st.neighbor_rounds, "time_total": st.time_total})
+        if verify:
+            out = out + (int(L.connectedComponentsVerifyGraphCSR(s, graph.ptr)),)
+        return out
+    finally:
+        L.freeCCStats(s)
 
 
 def bfs_csr(graph: Graph, args: Arguments, fn="breadthFirstSearchGraphCSR"):

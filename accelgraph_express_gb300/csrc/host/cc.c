@@ -1,0 +1,256 @@
+/*
+ * Drop-in connected-components entry points
+ * (02_capi_graph/include/algorithms/capi/connectedComponents.h:21-66) on the
+ * GPU runtime (gg_cc).
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <omp.h>
+
+#include "connectedComponents.h"
+#include "gg_host.h"
+
+#define CC_SEED 27491095ull
+
+struct CCStats *newCCStatsGraphCSR(struct GraphCSR *graph)
+{
+    struct CCStats *s = (struct CCStats *)calloc(1, sizeof(struct CCStats));
+    if (!s) return NULL;
+    const uint32_t V = graph->num_vertices;
+    s->num_vertices = V;
+    s->neighbor_rounds = 2;
+    s->components = (uint32_t *)malloc((size_t)V * 4 + 16);
+    s->counts = (uint32_t *)calloc((size_t)V + 4, 4);
+    s->labels = (uint32_t *)malloc((size_t)V * 4 + 16);
+    if (!s->components || !s->counts || !s->labels)
+    {
+        freeCCStats(s);
+        return NULL;
+    }
+    for (uint32_t v = 0; v < V; v++)
+        s->components[v] = s->labels[v] = v;
+    return s;
+}
+
+void freeCCStats(struct CCStats *s)
+{
+    if (!s) return;
+    free(s->components);
+    free(s->counts);
+    free(s->labels);
+    free(s);
+}
+
+uint32_t atomicMin(uint32_t *oldValue, uint32_t newValue)
+{
+    for (;;)
+    {
+        const uint32_t seen = __atomic_load_n(oldValue, __ATOMIC_RELAXED);
+        if (seen <= newValue) return 0;
+        if (__sync_bool_compare_and_swap(oldValue, seen, newValue)) return 1;
+    }
+}
+
+void linkNodes(uint32_t u, uint32_t v, uint32_t *components)
+{
+    uint32_t a = __atomic_load_n(&components[u], __ATOMIC_RELAXED);
+    uint32_t b = __atomic_load_n(&components[v], __ATOMIC_RELAXED);
+    while (a != b)
+    {
+        const uint32_t hi = a > b ? a : b, lo = a > b ? b : a;
+        const uint32_t parent = __atomic_load_n(&components[hi], __ATOMIC_RELAXED);
+        if (parent == lo) return;
+        if (parent == hi && __sync_bool_compare_and_swap(&components[hi], hi, lo)) return;
+        a = __atomic_load_n(&components[__atomic_load_n(&components[hi], __ATOMIC_RELAXED)], __ATOMIC_RELAXED);
+        b = __atomic_load_n(&components[lo], __ATOMIC_RELAXED);
+    }
+}
+
+void compressNodes(uint32_t num_vertices, uint32_t *components)
+{
+#pragma omp parallel for schedule(dynamic, 2048)
+    for (uint32_t n = 0; n < num_vertices; n++)
+    {
+        uint32_t c = components[n];
+        while (c != components[c])
+            c = components[c];
+        components[n] = c;
+    }
+}
+
+/* counts[label] = component size; labels = ids by descending count, ties
+ * by ascending id (a counting sort on the count) */
+static void fill_counts(struct CCStats *s)
+{
+    const uint32_t V = s->num_vertices;
+    memset(s->counts, 0, (size_t)V * 4);
+    for (uint32_t v = 0; v < V; v++)
+        s->counts[s->components[v]]++;
+    uint32_t *start = (uint32_t *)calloc((size_t)V + 2, 4);
+    if (!start) return;
+    for (uint32_t v = 0; v < V; v++)
+        start[V - s->counts[v]]++; /* key V - count: ascending key = descending count */
+    uint32_t run = 0;
+    for (uint32_t k = 0; k <= V; k++)
+    {
+        const uint32_t c = start[k];
+        start[k] = run;
+        run += c;
+    }
+    for (uint32_t v = 0; v < V; v++)
+        s->labels[start[V - s->counts[v]]++] = v;
+    free(start);
+}
+
+static struct CCStats *cc_run(struct Arguments *arguments, struct GraphCSR *graph, uint32_t algorithm)
+{
+    if (!arguments || !graph) return NULL;
+    struct CCStats *stats = newCCStatsGraphCSR(graph);
+    if (!stats) return NULL;
+    stats->arguments = arguments;
+    const uint32_t V = graph->num_vertices;
+    if (V == 0) return stats;
+    const double t0 = gg_seconds();
+    const int symmetric = arguments->symmetric != 0;
+    const uint32_t what = GG_MAP_OUT | ((algorithm == GG_CC_AFFOREST && !symmetric) ? GG_MAP_IN : 0u);
+    gg_graph *g = gpu_acquire(graph, what, 0);
+    if (!g)
+    {
+        freeCCStats(stats);
+        return NULL;
+    }
+    gg_cc_params p;
+    memset(&p, 0, sizeof(p));
+    p.algorithm = algorithm;
+    p.neighbor_rounds = stats->neighbor_rounds;
+    /* connectedComponents.c:475-479: 1024 samples, V / 2 on small graphs */
+    p.samples = V < 1024 ? (V / 2 ? V / 2 : 1) : 1024;
+    p.use_in_edges = symmetric ? 0 : 1;
+    p.seed = CC_SEED;
+    gg_cc_result r;
+    gg_status st = gg_cc(g, &p, stats->components, &r, NULL);
+    gpu_release_call(graph, g);
+    if (st != GG_OK)
+    {
+        gpu_report("connected components", st);
+        freeCCStats(stats);
+        return NULL;
+    }
+    stats->iterations = r.iterations;
+    stats->time_total = gg_seconds() - t0;
+    fill_counts(stats);
+    if (gpu_options()->verbose)
+    {
+        static const char *names[] = {"Shiloach-Vishkin", "Afforest", "Weakly"};
+        printf(" -----------------------------------------------------\n");
+        printf("| %-51s | \n", names[algorithm]);
+        printf(" -----------------------------------------------------\n");
+        printf("| %-15s | %-15s | %-15s | \n", "Iterations", "Components", "Time (S)");
+        printf(" -----------------------------------------------------\n");
+        printf("| %-15u | %-15u | %-15f | \n", stats->iterations, r.components, stats->time_total);
+        printf(" -----------------------------------------------------\n");
+        printCCStats(stats);
+    }
+    return stats;
+}
+
+struct CCStats *connectedComponentsGraphCSR(struct Arguments *arguments, struct GraphCSR *graph)
+{
+    if (!arguments) return NULL;
+    switch (arguments->pushpull)
+    {
+    case 0: return connectedComponentsShiloachVishkinGraphCSR(arguments, graph);
+    case 2: return connectedComponentsWeaklyGraphCSR(arguments, graph);
+    default: return connectedComponentsAfforestGraphCSR(arguments, graph);
+    }
+}
+
+struct CCStats *connectedComponentsShiloachVishkinGraphCSR(struct Arguments *arguments, struct GraphCSR *graph)
+{
+    return cc_run(arguments, graph, GG_CC_SHILOACH_VISHKIN);
+}
+
+struct CCStats *connectedComponentsAfforestGraphCSR(struct Arguments *arguments, struct GraphCSR *graph)
+{
+    return cc_run(arguments, graph, GG_CC_AFFOREST);
+}
+
+struct CCStats *connectedComponentsWeaklyGraphCSR(struct Arguments *arguments, struct GraphCSR *graph)
+{
+    return cc_run(arguments, graph, GG_CC_WEAKLY);
+}
+
+void printCCStats(struct CCStats *stats)
+{
+    if (!stats) return;
+    const uint32_t V = stats->num_vertices;
+    uint32_t n = 0;
+    for (uint32_t v = 0; v < V; v++)
+        n += stats->counts[v] != 0;
+    printf(" -----------------------------------------------------\n");
+    printf("| %-21s | %-27s | \n", "Top Clusters", "Count");
+    printf(" -----------------------------------------------------\n");
+    for (uint32_t i = 0; i < 5 && i < n; i++)
+        printf("| %-21u | %-27u | \n", stats->labels[i], stats->counts[stats->labels[i]]);
+    printf(" -----------------------------------------------------\n");
+    printf("| %-21s | %-27u | \n", "Num Components", n);
+    printf(" -----------------------------------------------------\n");
+}
+
+void printComponents(struct CCStats *stats)
+{
+    if (!stats) return;
+    for (uint32_t i = 0; i < stats->num_vertices; i++)
+        printf("v : %u comp : %u \n", i, stats->components[i]);
+}
+
+static uint32_t uf_root(uint32_t *p, uint32_t x)
+{
+    while (p[x] != x)
+    {
+        p[x] = p[p[x]];
+        x = p[x];
+    }
+    return x;
+}
+
+uint32_t connectedComponentsVerifyGraphCSR(struct CCStats *stats, struct GraphCSR *graph)
+{
+    if (!stats || !graph || stats->num_vertices != graph->num_vertices) return 0;
+    const uint32_t V = graph->num_vertices;
+    const uint32_t *comp = stats->components;
+    const uint32_t *idx = graph->vertices->edges_idx, *deg = graph->vertices->out_degree;
+    const uint32_t *adj = graph->sorted_edges_array->edges_array_dest;
+    /* closed under every edge, and every label is a vertex of its own class */
+    uint32_t bad = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : bad)
+    for (uint32_t u = 0; u < V; u++)
+    {
+        if (comp[u] >= V || comp[comp[u]] != comp[u]) bad++;
+        for (uint32_t j = idx[u]; j < idx[u] + deg[u]; j++)
+            bad += comp[adj[j]] != comp[u];
+    }
+    if (bad) return 0;
+    /* as many classes as components (union-find), so no class joins two */
+    uint32_t *p = (uint32_t *)malloc((size_t)V * 4 + 16);
+    if (!p) return 0;
+    for (uint32_t v = 0; v < V; v++)
+        p[v] = v;
+    uint32_t components = V;
+    for (uint32_t u = 0; u < V; u++)
+        for (uint32_t j = idx[u]; j < idx[u] + deg[u]; j++)
+        {
+            const uint32_t a = uf_root(p, u), b = uf_root(p, adj[j]);
+            if (a != b)
+            {
+                p[a > b ? a : b] = a > b ? b : a;
+                components--;
+            }
+        }
+    free(p);
+    uint32_t classes = 0;
+    for (uint32_t v = 0; v < V; v++)
+        classes += comp[v] == v;
+    return classes == components ? 1u : 0u;
+}

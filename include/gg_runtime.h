@@ -202,6 +202,45 @@ gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parents, uint32_t
  * call on `g`. */
 gg_status gg_bfs_device_results(const gg_graph *g, const int32_t **parents, const uint32_t **distances);
 
+/* ---- connected components ------------------------------------------------- */
+
+/* Algorithms use the reference's pushpull codes for connected components
+ * (connectedComponents.c:337-360). */
+typedef enum gg_cc_algorithm
+{
+    GG_CC_SHILOACH_VISHKIN = 0, GG_CC_AFFOREST = 1, GG_CC_WEAKLY = 2
+} gg_cc_algorithm;
+
+typedef struct gg_cc_params
+{
+    uint32_t algorithm;       /* gg_cc_algorithm */
+    uint32_t neighbor_rounds; /* Afforest sampling rounds; 0 = 2 (the reference's) */
+    uint32_t samples;         /* Afforest labels sampled to find the largest component; 0 = 1024 */
+    uint32_t use_in_edges;    /* Afforest final link over the CSC too: 0 no (the caller declares the graph
+                                 symmetric), 1 yes (needs GG_MAP_IN), 2 when mapped (else nothing is skipped) */
+    uint32_t max_iterations;  /* Shiloach-Vishkin / weakly: give up after this many (0 = V + 1) */
+    uint32_t profile;         /* 1: time the kernels with CUDA events */
+    uint64_t seed;            /* Afforest sample (SplitMix64) */
+} gg_cc_params;
+
+typedef struct gg_cc_result
+{
+    uint32_t iterations;      /* hook / propagation rounds run (Afforest: neighbor_rounds) */
+    uint32_t components;      /* distinct labels */
+    uint32_t launches;
+    uint32_t skipped_label;   /* Afforest: the sampled component left out of the final link, or ~0 */
+    float kernel_ms;          /* profile */
+} gg_cc_result;
+
+/* Label every vertex with the smallest vertex id of its weakly connected
+ * component (edges taken without direction); `components` (V entries, host,
+ * may be NULL).  Needs GG_MAP_OUT; Afforest uses the CSC as `use_in_edges`
+ * says. */
+gg_status gg_cc(gg_graph *g, const gg_cc_params *p, uint32_t *components, gg_cc_result *r, void *stream);
+/* Device pointer to the last gg_cc's labels on `g` (V entries), valid until
+ * the next call on `g`. */
+gg_status gg_cc_device_labels(const gg_graph *g, const uint32_t **components);
+
 /* One frontier step on host state, for the reference's step functions.
  * direction 0: top-down from `frontier` (a queue of `frontier_len` ids when
  * `frontier_is_bitmap` is 0, else a bitmap of ceil(V/32) words);

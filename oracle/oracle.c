@@ -976,3 +976,148 @@ void orc_spmv_f64(const orc_csr *g, const float *x, double *y)
         y[v] = s;
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* connected components                                                      */
+/* ------------------------------------------------------------------------ */
+
+static uint32_t uf_find(uint32_t *p, uint32_t x)
+{
+    while (p[x] != x)
+    {
+        p[x] = p[p[x]];
+        x = p[x];
+    }
+    return x;
+}
+
+void orc_cc_min_label(const orc_csr *g, uint32_t *comp)
+{
+    const uint32_t V = g->V;
+    for (uint32_t v = 0; v < V; v++)
+        comp[v] = v;
+    for (uint32_t u = 0; u < V; u++)
+        for (uint32_t j = g->out_off[u]; j < g->out_off[u + 1]; j++)
+        {
+            uint32_t a = uf_find(comp, u), b = uf_find(comp, g->out_adj[j]);
+            if (a == b)
+                continue;
+            /* the smaller id stays the root */
+            if (a < b)
+                comp[b] = a;
+            else
+                comp[a] = b;
+        }
+    for (uint32_t v = 0; v < V; v++)
+        comp[v] = uf_find(comp, v);
+}
+
+static void cc_compress(uint32_t V, uint32_t *comp)
+{
+    for (uint32_t n = 0; n < V; n++)
+        while (comp[n] != comp[comp[n]])
+            comp[n] = comp[comp[n]];
+}
+
+uint32_t orc_cc_sv(const orc_csr *g, uint32_t *comp)
+{
+    const uint32_t V = g->V;
+    for (uint32_t v = 0; v < V; v++)
+        comp[v] = v;
+    uint32_t iterations = 0, change = 1;
+    while (change)
+    {
+        change = 0;
+        iterations++;
+        for (uint32_t u = 0; u < V; u++)
+            for (uint32_t j = g->out_off[u]; j < g->out_off[u + 1]; j++)
+            {
+                const uint32_t cu = comp[u], cv = comp[g->out_adj[j]];
+                if (cu == cv)
+                    continue;
+                const uint32_t high = cu > cv ? cu : cv, low = cu > cv ? cv : cu;
+                if (comp[high] == high)
+                {
+                    comp[high] = low;
+                    change = 1;
+                }
+            }
+        cc_compress(V, comp);
+    }
+    return iterations;
+}
+
+/* union of the trees of u and v, the lower label becoming the parent
+ * (compare-and-swap on a root; retried while the roots move) */
+static void cc_link(uint32_t u, uint32_t v, uint32_t *comp)
+{
+    uint32_t a = comp[u], b = comp[v];
+    while (a != b)
+    {
+        const uint32_t hi = a > b ? a : b, lo = a > b ? b : a;
+        const uint32_t ph = comp[hi];
+        if (ph == lo)
+            break;
+        if (ph == hi && __sync_bool_compare_and_swap(&comp[hi], hi, lo))
+            break;
+        a = comp[comp[hi]];
+        b = comp[lo];
+    }
+}
+
+static void cc_compress_par(uint32_t V, uint32_t *comp, int nthreads)
+{
+#pragma omp parallel for schedule(dynamic, 2048) num_threads(nthreads)
+    for (uint32_t n = 0; n < V; n++)
+        while (comp[n] != comp[comp[n]])
+            comp[n] = comp[comp[n]];
+}
+
+void orc_cc_afforest(const orc_csr *g, uint32_t rounds, uint32_t samples, uint64_t seed, int use_in,
+                     uint32_t *comp, int nthreads)
+{
+    const uint32_t V = g->V;
+    for (uint32_t v = 0; v < V; v++)
+        comp[v] = v;
+    for (uint32_t r = 0; r < rounds; r++)
+    {
+#pragma omp parallel for schedule(dynamic, 2048) num_threads(nthreads)
+        for (uint32_t u = 0; u < V; u++)
+            if (g->out_off[u] + r < g->out_off[u + 1])
+                cc_link(u, g->out_adj[g->out_off[u] + r], comp);
+        cc_compress_par(V, comp, nthreads);
+    }
+    /* the most frequent label among `samples` vertices */
+    uint32_t skip = 0xffffffffu;
+    if (V && samples)
+    {
+        uint32_t *s = (uint32_t *)malloc((size_t)samples * 4);
+        for (uint32_t i = 0; i < samples; i++)
+            s[i] = comp[orc_splitmix64(seed + i) % V];
+        uint32_t best = 0;
+        for (uint32_t i = 0; i < samples; i++)
+        {
+            uint32_t c = 0;
+            for (uint32_t k = 0; k < samples; k++)
+                c += s[k] == s[i];
+            if (c > best || (c == best && s[i] < skip))
+            {
+                best = c;
+                skip = s[i];
+            }
+        }
+        free(s);
+    }
+#pragma omp parallel for schedule(dynamic, 2048) num_threads(nthreads)
+    for (uint32_t u = 0; u < V; u++)
+    {
+        if (comp[u] == skip)
+            continue;
+        for (uint32_t j = g->out_off[u] + rounds; j < g->out_off[u + 1]; j++)
+            cc_link(u, g->out_adj[j], comp);
+        if (use_in)
+            for (uint32_t j = g->in_off[u]; j < g->in_off[u + 1]; j++)
+                cc_link(u, g->in_adj[j], comp);
+    }
+    cc_compress_par(V, comp, nthreads);
+}

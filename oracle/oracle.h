@@ -147,6 +147,31 @@ int orc_spmv(const orc_csr *g, int mode, uint32_t iterations, const float *x_in,
 /* FP64 y = A^T x (one pull product, weights or 0.0001). */
 void orc_spmv_f64(const orc_csr *g, const float *x, double *y);
 
+/* ---- connected components -------------------------------------------- */
+
+/*
+ * Every vertex's label is the smallest vertex id of its weakly connected
+ * component (edges taken without direction).  The reference's three CSR
+ * algorithms (connectedComponents.c:337-720: Shiloach-Vishkin with roots
+ * hooked to the lower label and full compression, Afforest with link by the
+ * lower id, weakly connected components by atomicMin propagation) all end in
+ * this labelling; their iteration counts depend on thread interleaving.
+ * orc_cc_min_label: sequential union-find over the out-CSR.
+ * orc_cc_sv: the reference's Shiloach-Vishkin loop run serially (hook every
+ *   out-edge's higher root to the lower label, compress, repeat while any
+ *   hook happened); returns its iteration count.
+ * orc_cc_afforest: the reference's CPU Afforest (connectedComponents.c:470-626)
+ *   with OpenMP, as the timed CPU baseline: `rounds` neighbour rounds, a
+ *   sample of the labels picks the component whose vertices skip the final
+ *   link, the final link over the remaining out-edges and (use_in) all
+ *   in-edges, compression.  The sample is deterministic (SplitMix64 of
+ *   `seed`); any sample gives the same labels.
+ */
+void orc_cc_min_label(const orc_csr *g, uint32_t *comp);
+uint32_t orc_cc_sv(const orc_csr *g, uint32_t *comp);
+void orc_cc_afforest(const orc_csr *g, uint32_t rounds, uint32_t samples, uint64_t seed, int use_in,
+                     uint32_t *comp, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,6 +72,11 @@ def lib():
                                C.POINTER(C.c_double), C.c_int]
         L.orc_spmv.restype = C.c_int
         L.orc_spmv_f64.argtypes = [C.POINTER(OrcCsr), f32p, f64p]
+        L.orc_cc_min_label.argtypes = [C.POINTER(OrcCsr), u32p]
+        L.orc_cc_sv.argtypes = [C.POINTER(OrcCsr), u32p]
+        L.orc_cc_sv.restype = C.c_uint32
+        L.orc_cc_afforest.argtypes = [C.POINTER(OrcCsr), C.c_uint32, C.c_uint32, C.c_uint64, C.c_int, u32p,
+                                      C.c_int]
         _LIB = L
     return _LIB
 
@@ -253,6 +258,30 @@ def spmv_f64(g: Csr, x):
     cs = g.c()
     lib().orc_spmv_f64(C.byref(cs), np.ascontiguousarray(x, np.float32), y)
     return y
+
+
+def cc_min_label(g: Csr):
+    """Smallest vertex id of each vertex's weakly connected component."""
+    comp = np.empty(g.V, np.uint32)
+    cs = g.c()
+    lib().orc_cc_min_label(C.byref(cs), comp)
+    return comp
+
+
+def cc_sv(g: Csr):
+    """The reference's Shiloach-Vishkin loop, serial: (labels, iterations)."""
+    comp = np.empty(g.V, np.uint32)
+    cs = g.c()
+    it = lib().orc_cc_sv(C.byref(cs), comp)
+    return comp, int(it)
+
+
+def cc_afforest(g: Csr, rounds=2, samples=1024, seed=27491095, use_in=True, nthreads=1):
+    """The reference's CPU Afforest with OpenMP (the timed CPU baseline)."""
+    comp = np.empty(g.V, np.uint32)
+    cs = g.c()
+    lib().orc_cc_afforest(C.byref(cs), rounds, samples, seed, int(use_in), comp, nthreads)
+    return comp
 
 
 # ---------------------------------------------------------------------------

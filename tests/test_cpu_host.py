@@ -179,3 +179,35 @@ def test_rmat_batch_is_union_of_single_graphs(gg):
             blk = off[lo:hi + 1] - off[lo]
             np.testing.assert_array_equal(blk, one[side + "_off"])
             np.testing.assert_array_equal(adj[off[lo]:off[hi]] - lo, one[side + "_adj"])
+
+
+def test_cc_host_helpers_and_verify(gg, orc):
+    """The drop-in's host-side connected-components pieces, without a GPU:
+    linkNodes + compressNodes give the smallest-id labels; the verify
+    function accepts them and rejects identity labels and a planted error."""
+    import ctypes as C
+
+    rng = np.random.default_rng(4)
+    V = 500
+    s = rng.integers(0, V, 600).astype(np.uint32)
+    d = rng.integers(0, V, 600).astype(np.uint32)
+    g = gg.Graph.from_edges(s, d, num_vertices=V)
+    a = g.arrays()
+    gold = orc.cc_min_label(orc.Csr.from_arrays(V, g.E, a["out_off"], a["out_adj"], a["in_off"], a["in_adj"]))
+    L = gg.lib()
+    comp = np.arange(V, dtype=np.uint32)
+    for u, v in zip(s, d):
+        L.linkNodes(int(u), int(v), comp.ctypes.data)
+    L.compressNodes(V, comp.ctypes.data)
+    np.testing.assert_array_equal(comp, gold)
+    st = L.newCCStatsGraphCSR(g.ptr)
+    try:
+        assert L.connectedComponentsVerifyGraphCSR(st, g.ptr) == 0  # identity labels
+        C.memmove(st.contents.components, gold.ctypes.data, V * 4)
+        assert L.connectedComponentsVerifyGraphCSR(st, g.ptr) == 1
+        bad = gold.copy()
+        bad[np.flatnonzero(gold != np.arange(V))[0]] = V - 1 if gold[-1] != V - 1 else 0
+        C.memmove(st.contents.components, bad.ctypes.data, V * 4)
+        assert L.connectedComponentsVerifyGraphCSR(st, g.ptr) == 0
+    finally:
+        L.freeCCStats(st)

@@ -117,3 +117,39 @@ def test_oracle_ppr_seed_sets(orc):
     np.testing.assert_allclose(orc.ppr_f64_multi(g, [a, a, b], 20), (2 * ra + rb) / 3, rtol=1e-12, atol=1e-15)
     # mass leaks only through vertices without out-edges
     assert orc.ppr_f64_multi(g, [a, b], 20).sum() <= 1.0 + 1e-12
+
+
+def _cc_golden():
+    z = np.load(os.path.join(GOLDEN, "golden_cc.npz"))
+    names = sorted({k.rsplit("_", 1)[0] for k in z.files})
+    return z, names
+
+
+@pytest.mark.parametrize("name", _cc_golden()[1])
+def test_oracle_cc_matches_golden(orc, name):
+    """Connected components: the union-find oracle, the serial
+    Shiloach-Vishkin restatement and the OpenMP Afforest baseline all give
+    the golden labels (smallest id of each weakly connected component, from
+    scipy, tests/golden/make_cc_golden.py)."""
+    z, _ = _cc_golden()
+    V = int(z[name + "_V"])
+    g = orc.Csr(V, z[name + "_src"], z[name + "_dst"])
+    gold = z[name + "_comp"]
+    np.testing.assert_array_equal(orc.cc_min_label(g), gold)
+    comp, iters = orc.cc_sv(g)
+    np.testing.assert_array_equal(comp, gold)
+    assert iters >= 1
+    np.testing.assert_array_equal(orc.cc_afforest(g, nthreads=4), gold)
+    # Afforest with a sample that can only pick the largest component still
+    # needs the in-edges on a directed graph; with them any sample is exact
+    np.testing.assert_array_equal(orc.cc_afforest(g, samples=1, seed=5, nthreads=2), gold)
+
+
+def test_oracle_cc_planted_error_is_caught(orc):
+    """A labelling with one vertex moved to another component fails the
+    golden comparison."""
+    z, _ = _cc_golden()
+    g = orc.Csr(int(z["bridged_V"]), z["bridged_src"], z["bridged_dst"])
+    comp = orc.cc_min_label(g)
+    comp[150] = 0
+    assert not np.array_equal(comp, z["bridged_comp"])

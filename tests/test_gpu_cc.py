@@ -1,0 +1,104 @@
+"""Connected components on the GPU against the golden labels (smallest id of
+each weakly connected component, tests/golden/golden_cc.npz) and the oracle:
+bit-exact labels for all three algorithms (Shiloach-Vishkin, Afforest,
+weakly connected components), through gg_cc and the reference's drop-in
+entry points."""
+import os
+
+import numpy as np
+import pytest
+
+from graphs import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+Z = np.load(os.path.join(GOLDEN, "golden_cc.npz"))
+NAMES = sorted({k.rsplit("_", 1)[0] for k in Z.files})
+
+
+def _graph(gpu, name):
+    V = int(Z[name + "_V"])
+    return gpu.Graph.from_edges(Z[name + "_src"], Z[name + "_dst"], num_vertices=V), Z[name + "_comp"]
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("algorithm", ["sv", "afforest", "weakly"])
+def test_cc_matches_golden(gpu, name, algorithm):
+    g, gold = _graph(gpu, name)
+    dg = gpu.DeviceGraph(g, gpu.MAP_OUT | gpu.MAP_IN)
+    comp, r = dg.cc(algorithm)
+    np.testing.assert_array_equal(comp, gold, err_msg=f"{name} {algorithm}")
+    assert r["components"] == len(np.unique(gold))
+    assert r["iterations"] >= 1
+
+
+@pytest.mark.parametrize("samples", [1, 7, 1024])
+def test_cc_afforest_any_sample(gpu, samples):
+    """The sample only picks which component skips the final link."""
+    g, gold = _graph(gpu, "rmat14")
+    dg = gpu.DeviceGraph(g, gpu.MAP_OUT | gpu.MAP_IN)
+    for seed in (1, 2, 3):
+        comp, r = dg.cc("afforest", samples=samples, seed=seed)
+        np.testing.assert_array_equal(comp, gold)
+
+
+def test_cc_afforest_symmetric_out_edges_only(gpu):
+    """Declared symmetric, Afforest links out-edges only (no CSC needed)."""
+    g, gold = _graph(gpu, "rmat12u")
+    dg = gpu.DeviceGraph(g, gpu.MAP_OUT)
+    comp, r = dg.cc("afforest", use_in_edges=0)
+    np.testing.assert_array_equal(comp, gold)
+    # without the CSC and without the symmetric promise nothing is skipped
+    comp, r = dg.cc("afforest", use_in_edges=2)
+    np.testing.assert_array_equal(comp, gold)
+    assert r["skipped_label"] == 0xFFFFFFFF
+
+
+@pytest.mark.parametrize("symmetric", [False, True])
+def test_cc_rmat18_vs_oracle(gpu, orc, symmetric):
+    g = gpu.Graph.rmat(18, 8, symmetric=symmetric)
+    a = g.arrays()
+    o = orc.Csr.from_arrays(g.V, g.E, a["out_off"], a["out_adj"], a["in_off"], a["in_adj"])
+    gold = orc.cc_min_label(o)
+    dg = gpu.DeviceGraph(g, gpu.MAP_OUT | gpu.MAP_IN)
+    for algorithm in ("sv", "afforest", "weakly"):
+        comp, _ = dg.cc(algorithm)
+        np.testing.assert_array_equal(comp, gold, err_msg=algorithm)
+
+
+@pytest.mark.parametrize("pushpull", [0, 1, 2, 3])
+def test_cc_dropin(gpu, pushpull):
+    """connectedComponentsGraphCSR dispatches on pushpull (3 -> Afforest);
+    counts are the component sizes, labels ordered by size; the host verify
+    passes."""
+    gpu.set_gpu_options(keep_resident=False, verbose=False)
+    for name in ("v300_e2730", "rmat14", "bridged"):
+        g, gold = _graph(gpu, name)
+        args = gpu.default_arguments()
+        args.pushpull = pushpull
+        comp, counts, labels, info, ok = gpu.cc_csr(g, args, verify=True)
+        np.testing.assert_array_equal(comp, gold, err_msg=name)
+        np.testing.assert_array_equal(counts, np.bincount(gold, minlength=g.V).astype(np.uint32))
+        order = np.lexsort((np.arange(g.V), -counts.astype(np.int64)))
+        np.testing.assert_array_equal(labels, order.astype(np.uint32))
+        assert ok == 1
+        assert info["neighbor_rounds"] == 2
+
+
+def test_cc_named_entry_points(gpu):
+    g, gold = _graph(gpu, "rmat10")
+    args = gpu.default_arguments()
+    for fn in ("connectedComponentsShiloachVishkinGraphCSR", "connectedComponentsAfforestGraphCSR",
+               "connectedComponentsWeaklyGraphCSR"):
+        comp, _, _, _ = gpu.cc_csr(g, args, fn=fn)
+        np.testing.assert_array_equal(comp, gold, err_msg=fn)
+
+
+def test_cc_invalid(gpu):
+    g, _ = _graph(gpu, "rmat10")
+    dg = gpu.DeviceGraph(g, gpu.MAP_IN)
+    with pytest.raises(gpu.GgError):
+        dg.cc("sv")  # needs the out-CSR
+    dg2 = gpu.DeviceGraph(g, gpu.MAP_OUT)
+    with pytest.raises(gpu.GgError):
+        dg2.cc(7)
