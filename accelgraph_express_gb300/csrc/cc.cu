@@ -95,18 +95,22 @@ __global__ void __launch_bounds__(GG_TILE_NT) k_cc_hook(const uint32_t *__restri
                                                         const uint32_t *__restrict__ adj, const uint2 *__restrict__ coord,
                                                         uint32_t ntiles, uint32_t V, uint32_t *comp, CcFlags *f)
 {
+    /* the row's label is read once per row segment; a label read here may
+     * be older than another warp's hook in the same pass, which costs at most
+     * a repeat in the next pass (a pass that hooks nothing reads no stale
+     * value, so the stop test is exact) */
     struct Op
     {
         typedef uint32_t RowVal;
         uint32_t *comp;
         CcFlags *f;
-        __device__ __forceinline__ uint32_t row_value(uint32_t r) const { return r; }
-        __device__ __forceinline__ void scatter(uint32_t u, uint32_t, uint32_t v) const
+        __device__ __forceinline__ uint32_t row_value(uint32_t r) const { return comp[r]; }
+        __device__ __forceinline__ void scatter(uint32_t cu, uint32_t, uint32_t v) const
         {
-            const uint32_t cu = ld_comp(comp, u), cv = ld_comp(comp, v);
+            const uint32_t cv = comp[v];
             if (cu == cv) return;
             const uint32_t hi = cu > cv ? cu : cv, lo = cu > cv ? cv : cu;
-            if (ld_comp(comp, hi) == hi)
+            if (comp[hi] == hi)
             {
                 comp[hi] = lo;
                 *(volatile unsigned int *)&f->changed = 1u;
@@ -121,22 +125,28 @@ __global__ void __launch_bounds__(GG_TILE_NT) k_cc_minprop(const uint32_t *__res
                                                            const uint2 *__restrict__ coord, uint32_t ntiles,
                                                            uint32_t V, uint32_t *comp, CcFlags *f)
 {
+    /* the row's label is read once per row segment (a stale, larger label
+     * only propagates less in this pass) */
+    struct Row
+    {
+        uint32_t u, cu;
+    };
     struct Op
     {
-        typedef uint32_t RowVal;
+        typedef Row RowVal;
         uint32_t *comp;
         CcFlags *f;
-        __device__ __forceinline__ uint32_t row_value(uint32_t r) const { return r; }
-        __device__ __forceinline__ void scatter(uint32_t u, uint32_t, uint32_t v) const
+        __device__ __forceinline__ Row row_value(uint32_t r) const { return Row{r, comp[r]}; }
+        __device__ __forceinline__ void scatter(const Row &rv, uint32_t, uint32_t v) const
         {
-            const uint32_t cu = ld_comp(comp, u), cv = ld_comp(comp, v);
-            if (cu < cv)
+            const uint32_t cv = comp[v];
+            if (rv.cu < cv)
             {
-                if (atomicMin(comp + v, cu) > cu) *(volatile unsigned int *)&f->changed = 1u;
+                if (atomicMin(comp + v, rv.cu) > rv.cu) *(volatile unsigned int *)&f->changed = 1u;
             }
-            else if (cv < cu)
+            else if (cv < rv.cu)
             {
-                if (atomicMin(comp + u, cv) > cv) *(volatile unsigned int *)&f->changed = 1u;
+                if (atomicMin(comp + rv.u, cv) > cv) *(volatile unsigned int *)&f->changed = 1u;
             }
         }
     } op{comp, f};

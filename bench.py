@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--edge-factor", type=int, default=16)
     p.add_argument("--no-extras", action="store_true", help="skip the BF16/BFS/SpMV side measurements")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    p.add_argument("--leg", choices=["c1", "bfs", "ppr", "batch", "serve", "csr"],
+    p.add_argument("--leg", choices=["c1", "bfs", "ppr", "batch", "serve", "csr", "cc"],
                    help="run one side measurement alone and print its JSON (for profiling)")
     return p.parse_args()
 
@@ -237,7 +237,8 @@ def run_leg(leg):
     peak, _ = load_peaks()
     fn = {"c1": lambda: c1_extras(gg, torch), "bfs": lambda: bfs_extras(gg, torch, peak),
           "ppr": lambda: ppr_extras(gg, torch, peak), "batch": lambda: batch_extras(gg, torch, peak),
-          "serve": lambda: serving_extras(gg), "csr": lambda: csr_build_extras(gg, torch, peak)}[leg]
+          "serve": lambda: serving_extras(gg), "csr": lambda: csr_build_extras(gg, torch, peak),
+          "cc": lambda: cc_extras(gg, torch, peak)}[leg]
     print(json.dumps({"leg": leg, **fn()}), flush=True)
 
 
@@ -656,6 +657,56 @@ def bfs_extras(gg, torch, peak, scale=22):
     return out
 
 
+def cc_extras(gg, torch, peak):
+    """Connected components (all three algorithms) on R-MAT-22 undirected
+    (the BFS graph) and R-MAT-24 directed (the PageRank graph): device time
+    of one gg_cc call (CUDA events on its stream, labels left on the device),
+    edges per second, labels against the oracle; the CPU baseline is the
+    reference's Afforest restated with OpenMP on all host cores."""
+    import numpy as np
+    from oracle import oracle_ctypes as O
+
+    out = {}
+    threads = os.cpu_count() or 1
+    for name, scale, sym in (("rmat22u", 22, True), ("rmat24", 24, False)):
+        g = gg.Graph.rmat(scale, 16, seed=SEED, symmetric=sym)
+        V, E = g.V, g.E
+        dg = gg.DeviceGraph(g, gg.MAP_OUT | gg.MAP_IN)
+        st = torch.cuda.current_stream()
+        v = g.views()
+        o = O.Csr.from_arrays(V, E, np.append(v["out_edges_idx"], np.uint32(E)), v["out_adj"],
+                              np.append(v["in_edges_idx"], np.uint32(E)), v["in_adj"])
+        t0 = time.perf_counter()
+        cpu = O.cc_afforest(o, use_in=not sym, nthreads=threads)
+        cpu_s = time.perf_counter() - t0
+        gold = O.cc_min_label(o)
+        res = {"V": V, "E": E, "components": int(len(np.unique(gold))),
+               "cpu_afforest_ms": cpu_s * 1e3, "cpu_cores": threads,
+               "cpu_matches_oracle": bool(np.array_equal(cpu, gold))}
+        for alg in ("afforest", "sv", "weakly"):
+            use_in = 0 if sym else 1
+            for _ in range(2):
+                dg.cc(alg, use_in_edges=use_in, copy_out=False, stream=st.cuda_stream)
+            torch.cuda.synchronize()
+            ms = []
+            for _ in range(5):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                _, r = dg.cc(alg, use_in_edges=use_in, copy_out=False, stream=st.cuda_stream)
+                e1.record(st)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            comp, r = dg.cc(alg, use_in_edges=use_in, stream=st.cuda_stream)
+            t = float(np.median(ms))
+            res[alg] = {"ms": t, "gedges_s": E / (t / 1e3) / 1e9, "iterations": r["iterations"],
+                        "launches": r["launches"], "labels_match_oracle": bool(np.array_equal(comp, gold))}
+        res["afforest_vs_cpu"] = cpu_s * 1e3 / res["afforest"]["ms"]
+        out[name] = res
+        dg.free()
+        g.free()
+    return out
+
+
 def csr_radix_bytes(V, E):
     """Bytes the device CSR + CSC build moves per direction (unweighted):
     keys made (8E read, 8E written), per 8-bit pass a count read (8E) and a
@@ -806,6 +857,7 @@ def extras(gg, graph, dg, V, E, sptr, torch, peak):
     out["many_graphs"] = batch_extras(gg, torch, peak)
     out["serving"] = serving_extras(gg)
     out["csr_build"] = csr_build_extras(gg, torch, peak)
+    out["connected_components"] = cc_extras(gg, torch, peak)
     return out
 
 
