@@ -256,6 +256,10 @@ def lib() -> C.CDLL:
         L.graphCSRFromEdgeList.restype = P(GraphCSR)
         L.graphCSRFromEdgeListDevice.argtypes = [P(EdgeList)]
         L.graphCSRFromEdgeListDevice.restype = P(GraphCSR)
+        L.graphCSRFromEdgeListRelabelDevice.argtypes = [P(EdgeList), C.c_uint32, C.c_uint64]
+        L.graphCSRFromEdgeListRelabelDevice.restype = P(GraphCSR)
+        L.gg_relabel_order.argtypes = [P(EdgeList), C.c_uint32, C.c_uint64, C.c_void_p, C.c_void_p]
+        L.gg_graph_build_relabelled.argtypes = [P(EdgeList), C.c_void_p, C.c_uint32, C.c_void_p, P(C.c_void_p)]
         L.gg_graph_build.argtypes = [P(EdgeList), C.c_uint32, C.c_void_p, P(C.c_void_p)]
         L.gg_graph_build_device.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                                             C.c_void_p, P(C.c_void_p)]
@@ -372,6 +376,22 @@ class Graph:
                 el.contents.max_weight = float(w.max())
         el.contents.num_vertices = V
         return el
+
+    @classmethod
+    def from_edges_relabelled(cls, src, dst, weights=None, num_vertices=None, lmode=4, seed=27491095):
+        """The GPU build of the edge list relabelled by -l mode `lmode`; the
+        graph's label arrays hold the mapping (labels())."""
+        L = lib()
+        el = cls._edge_list(src, dst, weights, num_vertices)
+        try:
+            return cls(L.graphCSRFromEdgeListRelabelDevice(el, lmode, seed))
+        finally:
+            L.freeEdgeList(el)
+
+    def labels(self):
+        """(label_array, inverse_label_array): original id -> internal id and back."""
+        e = self.ptr.contents.sorted_edges_array.contents
+        return _np(e.label_array, self.V, np.uint32), _np(e.inverse_label_array, self.V, np.uint32)
 
     @classmethod
     def from_edges(cls, src, dst, weights=None, num_vertices=None, device_build=False):
@@ -733,6 +753,38 @@ def pagerank_csr(graph: Graph, args: Arguments, fn="pageRankGraphCSR"):
                        "realRanks": _np(st.realRanks, graph.V, np.uint32)}
     finally:
         L.freePageRankStats(s)
+
+
+def relabel_order(src, dst, num_vertices=None, lmode=4, seed=27491095):
+    """label[orig] = new for -l mode `lmode`, computed on the GPU (gg_relabel_order)."""
+    L = lib()
+    el = Graph._edge_list(src, dst, None, num_vertices)
+    try:
+        V = int(el.contents.num_vertices)
+        label = np.empty(V, np.uint32)
+        _check(L.gg_relabel_order(el, lmode, seed, label.ctypes.data, None), "gg_relabel_order")
+        return label
+    finally:
+        L.freeEdgeList(el)
+
+
+def build_relabelled(src, dst, label, weights=None, num_vertices=None, what=MAP_ALL, stream=None):
+    """DeviceGraph of the edge list with ids replaced by label[id] (a permutation)."""
+    L = lib()
+    el = Graph._edge_list(src, dst, weights, num_vertices)
+    try:
+        V, E = int(el.contents.num_vertices), int(el.contents.num_edges)
+        lab = np.ascontiguousarray(label, np.uint32)
+        if len(lab) != V:
+            raise GgError("label array must have num_vertices entries")
+        dg = DeviceGraph.__new__(DeviceGraph)
+        dg.h = C.c_void_p()
+        _check(L.gg_graph_build_relabelled(el, lab.ctypes.data, what, stream, C.byref(dg.h)),
+               "gg_graph_build_relabelled")
+        dg.graph = _Shape(V, E)
+        return dg
+    finally:
+        L.freeEdgeList(el)
 
 
 def cc_csr(graph: Graph, args: Arguments, fn="connectedComponentsGraphCSR", verify=False):

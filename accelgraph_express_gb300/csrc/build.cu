@@ -316,9 +316,9 @@ struct SortBufs
     uint32_t *counts, *sums;
 };
 
-/* stable LSD sort of n words on their low `bits` bits; the sorted words
- * (and payload) end in B.keys / B.pay */
-gg_status radix_sort(SortBufs &B, uint64_t n, int bits, cudaStream_t s)
+/* stable LSD sort of n words on their bits lo .. bits-1 (8-bit digits from
+ * bit lo up); the sorted words (and payload) end in B.keys / B.pay */
+gg_status radix_sort(SortBufs &B, uint64_t n, int bits, cudaStream_t s, int lo = 0)
 {
     if (n <= 1) return GG_OK;
     static bool attr_set = false; /* one device per process */
@@ -329,7 +329,7 @@ gg_status radix_sort(SortBufs &B, uint64_t n, int bits, cudaStream_t s)
     }
     const uint32_t ntiles = (uint32_t)((n + RDX_TILE - 1) / RDX_TILE);
     const uint32_t nb = (ntiles + COL_TILES - 1) / COL_TILES;
-    for (int shift = 0; shift < bits; shift += 8)
+    for (int shift = lo; shift < bits; shift += 8)
     {
         k_rdx_count<<<ntiles, RDX_THREADS, 0, s>>>(B.keys, n, shift, ntiles, B.counts);
         k_col_reduce<<<nb, RDX_BINS, 0, s>>>(B.counts, ntiles, B.sums);
@@ -463,4 +463,217 @@ gg_status gg_build_arrays(gg_graph *g, const uint32_t *src, const uint32_t *dst,
     }
     if (st == GG_OK) g->what = what | (g->in_off ? GG_MAP_IN : 0u) | (g->out_off ? GG_MAP_OUT : 0u);
     return st;
+}
+
+/* ---- degree-based relabelling (the reference's -l modes) ------------------
+ *
+ * The reference lists its relabelling modes (README.md:362-378: 1
+ * out-degree, 2 in-degree, 3 (in+out)-degree, 4/5 DBG out/in, 6/7 HUBSort
+ * out/in, 8/9 HUBCluster out/in, 10 random, 11 load from file); their code is
+ * in the absent OpenGraph submodule.  Each mode here is the published
+ * algorithm as one sort key per vertex, (key << b) | id, sorted by the radix
+ * sort above, so ties keep the original order:
+ *   degree (1-3)    descending degree
+ *   DBG (4/5)       degree-based grouping (Faldu et al., IISWC 2019): eight
+ *                   groups, group k >= 1 holding degrees in
+ *                   [avg/2 * 2^(k-1), avg/2 * 2^k) (the last one open), group
+ *                   0 the rest; hotter groups first, original order inside
+ *   HUBSort (6/7)   hubs (degree > avg) by descending degree, then the other
+ *                   vertices in original order (Zhang et al., 2017)
+ *   HUBCluster (8/9) hubs first, then the others, both in original order
+ *   random (10)     SplitMix64(seed ^ id), ties by id
+ * avg = E / V.  The result is label[orig] = new. */
+
+namespace {
+
+__global__ void k_degree_count(const uint32_t *__restrict__ ids, uint64_t n, uint32_t V, uint32_t *deg, uint32_t *bad)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const uint32_t v = ids[i];
+        if (v < V)
+            atomicAdd(deg + v, 1u);
+        else
+            atomicOr(bad, 1u);
+    }
+}
+
+__device__ __forceinline__ uint64_t mode_degree(uint32_t mode, const uint32_t *dout, const uint32_t *din, uint32_t v)
+{
+    switch (mode)
+    {
+    case 1: case 4: case 6: case 8: return dout[v];
+    case 2: case 5: case 7: case 9: return din[v];
+    case 3: return (uint64_t)dout[v] + din[v];
+    default: return 0;
+    }
+}
+
+__global__ void k_degree_max(const uint32_t *__restrict__ dout, const uint32_t *__restrict__ din, uint32_t V,
+                             uint32_t mode, unsigned long long *out)
+{
+    unsigned long long m = 0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    {
+        const unsigned long long d = mode_degree(mode, dout, din, v);
+        m = d > m ? d : m;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        const unsigned long long y = __shfl_xor_sync(0xffffffffu, m, o);
+        m = y > m ? y : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+__device__ __forceinline__ uint64_t relabel_key(uint32_t mode, uint64_t d, uint64_t dmax, uint64_t avg, uint64_t seed,
+                                                uint32_t v)
+{
+    switch (mode)
+    {
+    case 1: case 2: case 3: return dmax - d;
+    case 4: case 5:
+    {
+        const uint64_t r = 2 * d / (avg ? avg : 1);
+        const uint32_t group = r ? min(7u, 64u - (uint32_t)__clzll((long long)r)) : 0u;
+        return 7u - group;
+    }
+    case 6: case 7: return d > avg ? dmax - d : dmax + 1;
+    case 8: case 9: return d > avg ? 0u : 1u;
+    case 10:
+    {
+        uint64_t z = seed ^ v;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return (z ^ (z >> 31)) & 0xffffffffull;
+    }
+    default: return 0;
+    }
+}
+
+__global__ void k_relabel_keys(const uint32_t *__restrict__ dout, const uint32_t *__restrict__ din, uint32_t V,
+                               uint32_t mode, uint64_t dmax, uint64_t avg, uint64_t seed, int b, uint64_t *keys)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+        keys[v] = (relabel_key(mode, mode_degree(mode, dout, din, v), dmax, avg, seed, v) << b) | v;
+}
+
+__global__ void k_labels_from_order(const uint64_t *__restrict__ keys, uint32_t V, uint64_t mask, uint32_t *label)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x)
+        label[keys[i] & mask] = i;
+}
+
+/* checks label is a permutation of 0..V-1 (every new id hit once) */
+__global__ void k_perm_hits(const uint32_t *__restrict__ label, uint32_t V, uint32_t *hits, uint32_t *bad)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    {
+        const uint32_t l = label[v];
+        if (l >= V || atomicAdd(hits + l, 1u) != 0u) atomicOr(bad, 1u);
+    }
+}
+
+/* out may be ids (in place: each slot is read, then written, by one thread) */
+__global__ void k_apply_labels(const uint32_t *ids, uint64_t n, const uint32_t *__restrict__ label, uint32_t *out)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = label[ids[i]];
+}
+
+int bits_for64(uint64_t x)
+{
+    int b = 0;
+    while (b < 64 && (x >> b)) b++;
+    return b;
+}
+
+/* a device scratch allocation freed at scope exit */
+struct Scratch
+{
+    gg_graph *g;
+    void *p = nullptr;
+    size_t bytes = 0;
+    Scratch(gg_graph *g_) : g(g_) {}
+    gg_status alloc(size_t n)
+    {
+        bytes = n;
+        return gg_dev_alloc(g, &p, n);
+    }
+    ~Scratch() { gg_dev_free(g, p, bytes); }
+};
+
+} // namespace
+
+/* label[orig] = new for `mode` (1..10; 0 = identity) over device edge ids */
+gg_status gg_relabel_device(gg_graph *g, uint32_t V, uint64_t E, const uint32_t *src, const uint32_t *dst,
+                            uint32_t mode, uint64_t seed, uint32_t *label, cudaStream_t s)
+{
+    if (mode > 10) return gg_fail(GG_ERR_INVALID, "relabelling mode must be 0..10 (11 takes labels from the caller)");
+    Scratch degs(g), keys(g), tmp(g), counts(g), sums(g), flag(g);
+    GG_CHECK(degs.alloc((size_t)V * 8 + 64));
+    GG_CHECK(flag.alloc(64));
+    uint32_t *dout = (uint32_t *)degs.p, *din = dout + V;
+    GG_CUDA(cudaMemsetAsync(degs.p, 0, (size_t)V * 8 + 64, s));
+    GG_CUDA(cudaMemsetAsync(flag.p, 0, 64, s));
+    uint32_t *bad = (uint32_t *)flag.p;
+    unsigned long long *dmax_d = (unsigned long long *)((char *)flag.p + 8);
+    k_degree_count<<<grid_for(E, 256), 256, 0, s>>>(src, E, V, dout, bad);
+    k_degree_count<<<grid_for(E, 256), 256, 0, s>>>(dst, E, V, din, bad);
+    k_degree_max<<<grid_for(V, 256), 256, 0, s>>>(dout, din, V, mode, dmax_d);
+    GG_CUDA(cudaGetLastError());
+    unsigned long long hf[2] = {0, 0};
+    GG_CUDA(cudaMemcpyAsync(hf, flag.p, 16, cudaMemcpyDeviceToHost, s));
+    GG_CHECK(gg_wait(s));
+    if (hf[0] & 0xffffffffull) return gg_fail(GG_ERR_INVALID, "edge list has a vertex id >= num_vertices");
+    const uint64_t dmax = hf[1], avg = V ? E / V : 0;
+    const int b = bits_for(V);
+    int hi_bits = 0;
+    switch (mode)
+    {
+    case 0: hi_bits = 0; break;
+    case 1: case 2: case 3: hi_bits = bits_for64(dmax); break;
+    case 4: case 5: hi_bits = 3; break;
+    case 6: case 7: hi_bits = bits_for64(dmax + 1); break;
+    case 8: case 9: hi_bits = 1; break;
+    default: hi_bits = 32; break;
+    }
+    if (hi_bits + b > 64) return gg_fail(GG_ERR_INVALID, "degrees and ids do not fit one 64-bit sort key");
+    GG_CHECK(keys.alloc((size_t)V * 8 + 16));
+    GG_CHECK(tmp.alloc((size_t)V * 8 + 16));
+    const uint32_t ntiles = (uint32_t)(((uint64_t)V + RDX_TILE - 1) / RDX_TILE);
+    GG_CHECK(counts.alloc((size_t)RDX_BINS * (ntiles ? ntiles : 1) * 4));
+    GG_CHECK(sums.alloc(((ntiles + COL_TILES - 1) / COL_TILES + 1) * RDX_BINS * 4));
+    k_relabel_keys<<<grid_for(V, 256), 256, 0, s>>>(dout, din, V, mode, dmax, avg, seed, b, (uint64_t *)keys.p);
+    GG_CUDA(cudaGetLastError());
+    SortBufs B{(uint64_t *)keys.p, (uint64_t *)tmp.p, nullptr, nullptr, (uint32_t *)counts.p, (uint32_t *)sums.p};
+    /* the words start in id order, so a stable sort of the key bits alone
+     * leaves equal keys in id order */
+    GG_CHECK(radix_sort(B, V, hi_bits + b, s, b));
+    k_labels_from_order<<<grid_for(V, 256), 256, 0, s>>>(B.keys, V, (1ull << b) - 1ull, label);
+    GG_CUDA(cudaGetLastError());
+    return gg_wait(s);
+}
+
+gg_status gg_check_permutation(gg_graph *g, const uint32_t *label, uint32_t V, cudaStream_t s)
+{
+    Scratch hits(g), flag(g);
+    GG_CHECK(hits.alloc((size_t)V * 4 + 16));
+    GG_CHECK(flag.alloc(16));
+    GG_CUDA(cudaMemsetAsync(hits.p, 0, (size_t)V * 4 + 16, s));
+    GG_CUDA(cudaMemsetAsync(flag.p, 0, 16, s));
+    k_perm_hits<<<grid_for(V, 256), 256, 0, s>>>(label, V, (uint32_t *)hits.p, (uint32_t *)flag.p);
+    GG_CUDA(cudaGetLastError());
+    uint32_t bad = 0;
+    GG_CUDA(cudaMemcpyAsync(&bad, flag.p, 4, cudaMemcpyDeviceToHost, s));
+    GG_CHECK(gg_wait(s));
+    if (bad) return gg_fail(GG_ERR_INVALID, "label array is not a permutation of 0..V-1");
+    return GG_OK;
+}
+
+gg_status gg_apply_labels(const uint32_t *ids, uint64_t n, const uint32_t *label, uint32_t *out, cudaStream_t s)
+{
+    k_apply_labels<<<grid_for(n, 256), 256, 0, s>>>(ids, n, label, out);
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
 }

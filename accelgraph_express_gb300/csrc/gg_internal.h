@@ -118,6 +118,12 @@ gg_status gg_fill_constant_weights(gg_graph *g, float **dst, uint32_t E, cudaStr
 /* CSR/CSC of `g` from device edge arrays (build.cu) */
 gg_status gg_build_arrays(gg_graph *g, const uint32_t *src, const uint32_t *dst, const float *w, uint32_t what,
                           cudaStream_t s);
+/* relabelling (build.cu): label[orig] = new for the reference's -l modes
+ * 0..10 over device edge ids; a permutation check; ids -> labels */
+gg_status gg_relabel_device(gg_graph *g, uint32_t V, uint64_t E, const uint32_t *src, const uint32_t *dst,
+                            uint32_t mode, uint64_t seed, uint32_t *label, cudaStream_t s);
+gg_status gg_check_permutation(gg_graph *g, const uint32_t *label, uint32_t V, cudaStream_t s);
+gg_status gg_apply_labels(const uint32_t *ids, uint64_t n, const uint32_t *label, uint32_t *out, cudaStream_t s);
 /* the mapping's page-locked host scratch, at least `bytes` long */
 gg_status gg_pinned(gg_graph *g, size_t bytes, void **out);
 /* build the hot-vertex table of the mapping for a table of `cap` entries

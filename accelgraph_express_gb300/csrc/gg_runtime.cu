@@ -391,7 +391,8 @@ extern "C" gg_status gg_graph_map(const struct GraphCSR *graph, uint32_t what, v
 }
 
 static gg_status build_common(uint32_t V, uint32_t E, const uint32_t *src, const uint32_t *dst, const float *w,
-                              bool host, float max_weight, uint32_t what, void *stream, gg_graph **out)
+                              bool host, float max_weight, uint32_t what, void *stream, gg_graph **out,
+                              const uint32_t *label_host = nullptr)
 {
     if (!out) return gg_fail(GG_ERR_INVALID, "out is NULL");
     *out = nullptr;
@@ -413,8 +414,22 @@ static gg_status build_common(uint32_t V, uint32_t E, const uint32_t *src, const
         if (st == GG_OK) st = upload(g, (void **)&dd, dst, (size_t)E * 4, (size_t)E * 4 + 16, s);
         if (st == GG_OK && want_w) st = upload(g, (void **)&dw, w, (size_t)E * 4, (size_t)E * 4 + 16, s);
     }
+    uint32_t *dl = nullptr;
+    if (st == GG_OK && label_host)
+    {
+        /* relabel the uploaded ids in place: src' = label[src], dst' = label[dst] */
+        st = upload(g, (void **)&dl, label_host, (size_t)V * 4, (size_t)V * 4 + 16, s);
+        if (st == GG_OK) st = gg_check_permutation(g, dl, V, s);
+        if (st == GG_OK && E) st = gg_apply_labels(ds, E, dl, ds, s);
+        if (st == GG_OK && E) st = gg_apply_labels(dd, E, dl, dd, s);
+    }
     if (st == GG_OK)
         st = gg_build_arrays(g, host ? ds : src, host ? dd : dst, want_w ? (host ? dw : w) : nullptr, what, s);
+    if (dl)
+    {
+        gg_wait(s);
+        gg_dev_free(g, dl, (size_t)V * 4 + 16);
+    }
     if (host)
     {
         gg_wait(s);
@@ -439,6 +454,42 @@ extern "C" gg_status gg_graph_build(const struct EdgeList *edges, uint32_t what,
     if (!edges) return gg_fail(GG_ERR_INVALID, "edge list is NULL");
     return build_common(edges->num_vertices, edges->num_edges, edges->edges_array_src, edges->edges_array_dest,
                         edges->edges_array_weight, true, edges->max_weight, what, stream, out);
+}
+
+extern "C" gg_status gg_graph_build_relabelled(const struct EdgeList *edges, const uint32_t *label_array,
+                                               uint32_t what, void *stream, gg_graph **out)
+{
+    if (!edges || !label_array) return gg_fail(GG_ERR_INVALID, "NULL argument");
+    return build_common(edges->num_vertices, edges->num_edges, edges->edges_array_src, edges->edges_array_dest,
+                        edges->edges_array_weight, true, edges->max_weight, what, stream, out, label_array);
+}
+
+extern "C" gg_status gg_relabel_order(const struct EdgeList *edges, uint32_t lmode, uint64_t seed,
+                                      uint32_t *label_array, void *stream)
+{
+    if (!edges || !label_array) return gg_fail(GG_ERR_INVALID, "NULL argument");
+    const uint32_t V = edges->num_vertices, E = edges->num_edges;
+    if (V == 0) return GG_OK;
+    if (E && (!edges->edges_array_src || !edges->edges_array_dest)) return gg_fail(GG_ERR_INVALID, "edge arrays are NULL");
+    gg_graph *g = nullptr;
+    GG_CHECK(gg_graph_new(V, E, &g));
+    cudaStream_t s = gg_stream(g, stream);
+    uint32_t *ds = nullptr, *dd = nullptr, *dl = nullptr;
+    gg_status st = upload(g, (void **)&ds, edges->edges_array_src, (size_t)E * 4, (size_t)E * 4 + 16, s);
+    if (st == GG_OK) st = upload(g, (void **)&dd, edges->edges_array_dest, (size_t)E * 4, (size_t)E * 4 + 16, s);
+    if (st == GG_OK) st = gg_dev_alloc(g, (void **)&dl, (size_t)V * 4 + 16);
+    if (st == GG_OK) st = gg_relabel_device(g, V, E, ds, dd, lmode, seed, dl, s);
+    if (st == GG_OK && cudaMemcpyAsync(label_array, dl, (size_t)V * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        st = gg_fail(GG_ERR_CUDA, "cudaMemcpyAsync");
+    if (st == GG_OK) st = gg_wait(s);
+    gg_wait(s);
+    gg_dev_free(g, ds, (size_t)E * 4 + 16);
+    gg_dev_free(g, dd, (size_t)E * 4 + 16);
+    gg_dev_free(g, dl, (size_t)V * 4 + 16);
+    std::string keep = t_last_error;
+    gg_graph_unmap(g);
+    t_last_error = keep;
+    return st;
 }
 
 extern "C" gg_status gg_graph_build_device(uint32_t num_vertices, uint32_t num_edges, const uint32_t *src,

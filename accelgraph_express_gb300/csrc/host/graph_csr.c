@@ -544,18 +544,18 @@ static void rows_from_offsets(uint32_t V, uint32_t E, const uint32_t *idx, uint3
     }
 }
 
-struct GraphCSR *graphCSRFromEdgeListDevice(const struct EdgeList *in)
+/* the device build, copied back; with `labels` (orig -> new) the edge list
+ * is relabelled first and the label arrays record the mapping */
+static struct GraphCSR *device_build(const struct EdgeList *in, const uint32_t *labels, const char *who)
 {
-    if (!in)
-        return NULL;
     const uint32_t V = in->num_vertices, E = in->num_edges;
     const int weighted = in->edges_array_weight != NULL;
     gg_graph *d = NULL;
     const uint32_t what = GG_MAP_OUT | GG_MAP_IN | (weighted ? (GG_MAP_OUT_W | GG_MAP_IN_W) : 0u);
-    gg_status bst = gg_graph_build(in, what, NULL, &d);
+    gg_status bst = labels ? gg_graph_build_relabelled(in, labels, what, NULL, &d) : gg_graph_build(in, what, NULL, &d);
     if (bst != GG_OK)
     {
-        gpu_report("graphCSRFromEdgeListDevice", bst);
+        gpu_report(who, bst);
         return NULL;
     }
     struct GraphCSR *g = alloc_graph(V, E, weighted, in->max_weight);
@@ -570,13 +570,48 @@ struct GraphCSR *graphCSRFromEdgeListDevice(const struct EdgeList *in)
     gg_graph_unmap(d);
     if (st != GG_OK)
     {
-        gpu_report("graphCSRFromEdgeListDevice", st);
+        gpu_report(who, st);
         graphCSRFree(g);
         return NULL;
     }
     rows_from_offsets(V, E, g->vertices->edges_idx, fw->edges_array_src, g->vertices->out_degree);
     rows_from_offsets(V, E, g->inverse_vertices->edges_idx, bw->edges_array_src, g->inverse_vertices->out_degree);
-    return finish_graph(g);
+    g = finish_graph(g);
+    if (g && labels)
+        for (int k = 0; k < 2; k++)
+        {
+            struct EdgeList *el = k ? bw : fw;
+            for (uint32_t v = 0; v < V; v++)
+            {
+                el->label_array[v] = labels[v];
+                el->inverse_label_array[labels[v]] = v;
+            }
+        }
+    return g;
+}
+
+struct GraphCSR *graphCSRFromEdgeListDevice(const struct EdgeList *in)
+{
+    if (!in)
+        return NULL;
+    return device_build(in, NULL, "graphCSRFromEdgeListDevice");
+}
+
+struct GraphCSR *graphCSRFromEdgeListRelabelDevice(const struct EdgeList *in, uint32_t lmode, uint64_t seed)
+{
+    if (!in)
+        return NULL;
+    uint32_t *labels = (uint32_t *)malloc((size_t)in->num_vertices * 4 + 16);
+    if (!labels)
+        return NULL;
+    gg_status st = gg_relabel_order(in, lmode, seed, labels, NULL);
+    struct GraphCSR *g = NULL;
+    if (st != GG_OK)
+        gpu_report("graphCSRFromEdgeListRelabelDevice", st);
+    else
+        g = device_build(in, labels, "graphCSRFromEdgeListRelabelDevice");
+    free(labels);
+    return g;
 }
 
 void graphCSRFree(struct GraphCSR *g)

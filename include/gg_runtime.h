@@ -96,6 +96,22 @@ gg_status gg_graph_unmap(gg_graph *g);
 gg_status gg_graph_build(const struct EdgeList *edges, uint32_t what, void *stream, gg_graph **out);
 gg_status gg_graph_build_device(uint32_t num_vertices, uint32_t num_edges, const uint32_t *src, const uint32_t *dst,
                                 const float *weights, uint32_t what, void *stream, gg_graph **out);
+/* Degree-based relabelling (the reference's -l modes, README.md:362-378,
+ * code in the absent OpenGraph submodule), computed on the GPU from the edge
+ * list: label_array[orig] = new id (V entries, host).  lmode: 0 identity,
+ * 1 out-degree, 2 in-degree, 3 (in+out)-degree (descending degree), 4/5 DBG
+ * out/in (degree-based grouping: eight groups, group k >= 1 the degrees in
+ * [avg/2 * 2^(k-1), avg/2 * 2^k), hotter groups first), 6/7 HUBSort out/in
+ * (hubs, degree > E/V, by descending degree, then the rest), 8/9 HUBCluster
+ * out/in (hubs, then the rest), 10 random (SplitMix64(seed ^ id)).  Ties and
+ * groups keep the original order.  Mode 11 (labels from a file) needs no
+ * computation: pass those labels to gg_graph_build_relabelled. */
+gg_status gg_relabel_order(const struct EdgeList *edges, uint32_t lmode, uint64_t seed, uint32_t *label_array,
+                           void *stream);
+/* gg_graph_build of the edge list with every id replaced by
+ * label_array[id] (which must be a permutation of 0..V-1). */
+gg_status gg_graph_build_relabelled(const struct EdgeList *edges, const uint32_t *label_array, uint32_t what,
+                                    void *stream, gg_graph **out);
 /* Copy a mapping's arrays to host buffers (any may be NULL): row offsets
  * (V entries, as edges_idx), neighbours and weights (E entries) of the
  * out-CSR and the CSC, and the edge list's max_weight. */

@@ -132,6 +132,12 @@ struct GraphCSR *graphCSRFromEdgeList(const struct EdgeList *edgeList);
  * (gg_graph_build, then the arrays copied back); NULL on failure (no
  * device, id >= num_vertices, out of memory), with the reason printed. */
 struct GraphCSR *graphCSRFromEdgeListDevice(const struct EdgeList *edgeList);
+/* The GPU build of the edge list relabelled by mode `lmode` (gg_relabel_order:
+ * the reference's -l modes 0..10); both sorted edge lists carry the mapping:
+ * label_array[original id] = new id, inverse_label_array[new id] = original
+ * id (the drop-in BFS maps its source through label_array, as the reference
+ * does).  NULL on failure, with the reason printed. */
+struct GraphCSR *graphCSRFromEdgeListRelabelDevice(const struct EdgeList *edgeList, uint32_t lmode, uint64_t seed);
 void graphCSRFree(struct GraphCSR *graph);
 
 #ifdef __cplusplus

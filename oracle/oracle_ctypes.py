@@ -284,6 +284,48 @@ def cc_afforest(g: Csr, rounds=2, samples=1024, seed=27491095, use_in=True, nthr
     return comp
 
 
+def _splitmix64(z):
+    z = z.astype(np.uint64)
+    with np.errstate(over="ignore"):
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def relabel_order(src, dst, V, lmode, seed=27491095):
+    """label[orig] = new for the reference's -l modes 0..10, restated from the
+    published algorithms (degree sorts, DBG, HUBSort, HUBCluster, random) as
+    the product documents them: one key per vertex, ties in id order."""
+    src = np.asarray(src, np.int64)
+    dst = np.asarray(dst, np.int64)
+    E = len(src)
+    dout = np.bincount(src, minlength=V).astype(np.int64)
+    din = np.bincount(dst, minlength=V).astype(np.int64)
+    d = {1: dout, 4: dout, 6: dout, 8: dout, 2: din, 5: din, 7: din, 9: din, 3: dout + din}.get(lmode)
+    avg = E // V if V else 0
+    if lmode == 0:
+        key = np.zeros(V, np.int64)
+    elif lmode in (1, 2, 3):
+        key = d.max(initial=0) - d
+    elif lmode in (4, 5):
+        r = 2 * d // max(avg, 1)
+        group = np.minimum(7, np.array([int(x).bit_length() for x in r], np.int64))
+        key = 7 - group
+    elif lmode in (6, 7):
+        dmax = d.max(initial=0)
+        key = np.where(d > avg, dmax - d, dmax + 1)
+    elif lmode in (8, 9):
+        key = np.where(d > avg, 0, 1)
+    elif lmode == 10:
+        key = (_splitmix64(np.uint64(seed) ^ np.arange(V, dtype=np.uint64)) & np.uint64(0xFFFFFFFF)).astype(np.int64)
+    else:
+        raise ValueError(f"relabel mode {lmode}")
+    order = np.argsort(key, kind="stable")
+    label = np.empty(V, np.uint32)
+    label[order] = np.arange(V, dtype=np.uint32)
+    return label
+
+
 # ---------------------------------------------------------------------------
 # the reference's own code (where it was built)
 # ---------------------------------------------------------------------------
