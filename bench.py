@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--edge-factor", type=int, default=16)
     p.add_argument("--no-extras", action="store_true", help="skip the BF16/BFS/SpMV side measurements")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    p.add_argument("--leg", choices=["c1", "bfs", "ppr", "batch", "serve", "csr", "cc"],
+    p.add_argument("--leg", choices=["c1", "bfs", "ppr", "batch", "serve", "csr", "cc", "relabel"],
                    help="run one side measurement alone and print its JSON (for profiling)")
     return p.parse_args()
 
@@ -238,7 +238,7 @@ def run_leg(leg):
     fn = {"c1": lambda: c1_extras(gg, torch), "bfs": lambda: bfs_extras(gg, torch, peak),
           "ppr": lambda: ppr_extras(gg, torch, peak), "batch": lambda: batch_extras(gg, torch, peak),
           "serve": lambda: serving_extras(gg), "csr": lambda: csr_build_extras(gg, torch, peak),
-          "cc": lambda: cc_extras(gg, torch, peak)}[leg]
+          "cc": lambda: cc_extras(gg, torch, peak), "relabel": lambda: relabel_extras(gg, torch, peak)}[leg]
     print(json.dumps({"leg": leg, **fn()}), flush=True)
 
 
@@ -704,6 +704,58 @@ def cc_extras(gg, torch, peak):
         out[name] = res
         dg.free()
         g.free()
+    return out
+
+
+def relabel_extras(gg, torch, peak, scale=24):
+    """PageRank pull (FP32, hot-vertex table on) on R-MAT-24 relabelled by the
+    -l modes that group vertices by out-degree (the pull gather reads the
+    contributions of in-neighbours, so a vertex's value is read out-degree
+    times) and by DBG-in, against the natural order: gather time per launch and
+    the whole-iteration GTEPS; the relabel order and relabelled build timed
+    on the GPU (gg_relabel_order + gg_graph_build_relabelled, host edge list
+    in)."""
+    import ctypes as C
+
+    import numpy as np
+
+    L = gg.lib()
+    el = L.generateRMATEdgeList(scale, 16, 0.57, 0.19, 0.19, SEED, 0, SEED + 2, 0)
+    V, E = int(el.contents.num_vertices), int(el.contents.num_edges)
+    out = {"graph": f"R-MAT-{scale}, V={V}, E={E}"}
+    st = torch.cuda.current_stream()
+    try:
+        for lmode, name in ((0, "natural"), (1, "out-degree"), (4, "DBG-out"), (6, "HUBSort-out"),
+                            (8, "HUBCluster-out"), (5, "DBG-in")):
+            label = np.empty(V, np.uint32)
+            t0 = time.perf_counter()
+            gg._check(L.gg_relabel_order(el, lmode, SEED, label.ctypes.data, None), "gg_relabel_order")
+            t1 = time.perf_counter()
+            dg = gg.DeviceGraph.__new__(gg.DeviceGraph)
+            dg.h = C.c_void_p()
+            gg._check(L.gg_graph_build_relabelled(el, label.ctypes.data, gg.MAP_IN, None, C.byref(dg.h)),
+                      "gg_graph_build_relabelled")
+            t2 = time.perf_counter()
+            dg.graph = gg._Shape(V, E)
+            for _ in range(2):
+                dg.pagerank("pull", iterations=ITERS, epsilon=0.0, copy_out=False, stream=st.cuda_stream)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps, gms = 3, 0.0
+            e0.record(st)
+            for _ in range(reps):
+                _, r = dg.pagerank("pull", iterations=ITERS, epsilon=0.0, copy_out=False, profile=True,
+                                   stream=st.cuda_stream)
+                gms += r["gather_ms"] / max(r["gather_launches"], 1)
+            e1.record(st)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            out[name] = {"lmode": lmode, "relabel_order_ms": (t1 - t0) * 1e3, "build_ms": (t2 - t1) * 1e3,
+                         "gather_launch_ms": gms / reps, "gteps": E * ITERS / (ms / 1e3) / 1e9,
+                         "hot_table": r["hot_table"]}
+            dg.free()
+    finally:
+        L.freeEdgeList(el)
     return out
 
 
