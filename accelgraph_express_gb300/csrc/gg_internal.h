@@ -84,6 +84,17 @@ struct gg_graph
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
 
+    /* bumped whenever device memory of the mapping is freed (a work buffer
+     * regrown, scratch released): a cached CUDA graph recorded at another
+     * generation may point at freed memory and is captured again */
+    uint64_t mem_gen = 0;
+    /* the last GG_PR_CUDA_GRAPH call, instantiated, with the parameters it
+     * was captured for */
+    cudaGraphExec_t pr_exec = nullptr;
+    unsigned char pr_key[64] = {};
+    uint64_t pr_gen = 0;
+    uint32_t pr_launches = 0, pr_gather_launches = 0;
+
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
     /* timing events reused across calls (profile mode) */
     cudaEvent_t *ev_pool = nullptr;

@@ -169,6 +169,7 @@ gg_status gg_dev_alloc(gg_graph *g, void **p, size_t bytes)
 void gg_dev_free(gg_graph *g, void *p, size_t bytes)
 {
     if (!p) return;
+    g->mem_gen++;
     cudaFree(p);
     size_t b = align_up(bytes ? bytes : 256, 256);
     g->device_bytes = g->device_bytes >= b ? g->device_bytes - b : 0;
@@ -595,6 +596,7 @@ extern "C" gg_status gg_graph_unmap(gg_graph *g)
     free_tiles(g, g->hot_tiles);
     for (auto &b : g->work) gg_dev_free(g, b.ptr, b.bytes);
     if (g->pinned) cudaFreeHost(g->pinned);
+    if (g->pr_exec) cudaGraphExecDestroy(g->pr_exec);
     for (uint32_t i = 0; i < g->ev_count; i++) cudaEventDestroy(g->ev_pool[i]);
     free(g->ev_pool);
     if (g->ev_begin) cudaEventDestroy(g->ev_begin);

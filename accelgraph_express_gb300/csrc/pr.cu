@@ -932,31 +932,70 @@ gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_
     }
 
     /* with GG_PR_CUDA_GRAPH everything from here to the final normalisation
-     * is captured into one CUDA graph and launched once (relaxed capture:
-     * buffers first used inside it are allocated during the capture) */
+     * is captured into one CUDA graph (relaxed capture: buffers first used
+     * inside it are allocated during the capture) and instantiated; the
+     * instance stays with the mapping and is launched again by calls with
+     * the same parameters while no device memory of the mapping has been
+     * freed since (the buffers it writes are then the same) */
     const bool as_graph = (p->flags & GG_PR_CUDA_GRAPH) != 0;
-    if (as_graph) GG_CUDA(cudaStreamBeginCapture(R.s, cudaStreamCaptureModeRelaxed));
-    gg_status st = pagerank_enqueue(R, p, rec, rank, sum_v, ngraphs, (const uint32_t *)voff_v);
+    gg_status st = GG_OK;
     if (as_graph)
     {
-        cudaGraph_t graph = nullptr;
-        cudaError_t e = cudaStreamEndCapture(R.s, &graph);
-        if (st == GG_OK && e != cudaSuccess) st = gg_cuda_fail(e, "cudaStreamEndCapture");
-        cudaGraphExec_t exec = nullptr;
-        if (st == GG_OK)
+        struct Key
         {
-            e = cudaGraphInstantiate(&exec, graph, 0);
-            if (e != cudaSuccess) st = gg_cuda_fail(e, "cudaGraphInstantiate");
-        }
-        if (st == GG_OK)
+            uint32_t mode, storage, iters, init, flags, ngraphs, use_hot, V, E;
+            float damp;
+            double eps;
+        } key;
+        static_assert(sizeof(Key) <= sizeof(g->pr_key), "PageRank graph key");
+        memset(&key, 0, sizeof(key));
+        key.mode = p->mode; key.storage = p->storage; key.iters = iters; key.init = p->init_one_over_n;
+        key.flags = p->flags; key.ngraphs = ngraphs; key.use_hot = R.use_hot ? 1u : 0u; key.V = V; key.E = g->E;
+        key.damp = p->damp; key.eps = p->epsilon;
+        if (g->pr_exec && g->pr_gen == g->mem_gen && memcmp(g->pr_key, &key, sizeof(key)) == 0)
         {
-            e = cudaGraphLaunch(exec, R.s);
-            if (e != cudaSuccess) st = gg_cuda_fail(e, "cudaGraphLaunch");
+            GG_CUDA(cudaGraphLaunch(g->pr_exec, R.s));
+            R.launches = g->pr_launches;
+            R.gather_launches = g->pr_gather_launches;
         }
-        if (st == GG_OK) st = gg_wait(R.s);
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
+        else
+        {
+            if (g->pr_exec)
+            {
+                cudaGraphExecDestroy(g->pr_exec);
+                g->pr_exec = nullptr;
+            }
+            GG_CUDA(cudaStreamBeginCapture(R.s, cudaStreamCaptureModeRelaxed));
+            st = pagerank_enqueue(R, p, rec, rank, sum_v, ngraphs, (const uint32_t *)voff_v);
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamEndCapture(R.s, &graph);
+            if (st == GG_OK && e != cudaSuccess) st = gg_cuda_fail(e, "cudaStreamEndCapture");
+            cudaGraphExec_t exec = nullptr;
+            if (st == GG_OK)
+            {
+                e = cudaGraphInstantiate(&exec, graph, 0);
+                if (e != cudaSuccess) st = gg_cuda_fail(e, "cudaGraphInstantiate");
+            }
+            if (graph) cudaGraphDestroy(graph);
+            if (st == GG_OK)
+            {
+                e = cudaGraphLaunch(exec, R.s);
+                if (e != cudaSuccess) st = gg_cuda_fail(e, "cudaGraphLaunch");
+            }
+            if (st == GG_OK)
+            {
+                g->pr_exec = exec;
+                memcpy(g->pr_key, &key, sizeof(key));
+                g->pr_gen = g->mem_gen;
+                g->pr_launches = R.launches;
+                g->pr_gather_launches = R.gather_launches;
+            }
+            else if (exec)
+                cudaGraphExecDestroy(exec);
+        }
     }
+    else
+        st = pagerank_enqueue(R, p, rec, rank, sum_v, ngraphs, (const uint32_t *)voff_v);
     if (st != GG_OK) return st;
 
     std::vector<IterRec> h(iters + 2);

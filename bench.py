@@ -439,14 +439,21 @@ def c1_extras(gg, torch, scale=16):
     dg = gg.DeviceGraph(g, gg.MAP_IN)
     out = {"graph": f"R-MAT-{scale}, V={V}, E={E}", "epsilon": 1e-4, "max_iterations": 20}
     for name, one_over_n in (("reference_formulation", False), ("init_1_over_n", True)):
-        for _ in range(3):
-            dg.pagerank("pull", iterations=20, epsilon=1e-4, init_one_over_n=one_over_n, copy_out=False)
-        reps = 20
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            _, r = dg.pagerank("pull", iterations=20, epsilon=1e-4, init_one_over_n=one_over_n, copy_out=False)
-        ms = (time.perf_counter() - t0) * 1e3 / reps
+        # per call (wall time, results left on the device): the call as one
+        # cached CUDA graph launch, and as stream launches
+        timed = {}
+        for as_graph in (True, False):
+            for _ in range(3):
+                dg.pagerank("pull", iterations=20, epsilon=1e-4, init_one_over_n=one_over_n, copy_out=False,
+                            cuda_graph=as_graph)
+            reps = 20
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                _, r = dg.pagerank("pull", iterations=20, epsilon=1e-4, init_one_over_n=one_over_n,
+                                   copy_out=False, cuda_graph=as_graph)
+            timed[as_graph] = (time.perf_counter() - t0) * 1e3 / reps
+        ms = timed[True]
         ranks, r = dg.pagerank("pull", iterations=20, epsilon=1e-4, init_one_over_n=one_over_n)
         ref, info = O.pagerank(o, 0, 20, 1e-4, init_one_over_n=one_over_n)
         ex = O.pagerank_f64(o, info["executed"], init_one_over_n=one_over_n)
@@ -455,6 +462,8 @@ def c1_extras(gg, torch, scale=16):
         cpu_ms = (time.perf_counter() - t0) * 1e3
         out[name] = {"iterations": r["iterations"], "iterations_reference_loop": info["iterations"],
                      "ms_per_call": ms, "gteps": E * (info["executed"]) / (ms / 1e3) / 1e9,
+                     "ms_per_call_stream_launches": timed[False],
+                     "gteps_stream_launches": E * (info["executed"]) / (timed[False] / 1e3) / 1e9,
                      "l1_vs_fp64": float(np.abs(ranks - ex).sum()), "linf_vs_fp64": float(np.abs(ranks - ex).max()),
                      "l1_reference_fp32_loop_vs_fp64": float(np.abs(ref - ex).sum()),
                      "cpu_gteps": E * info["executed"] / (cpu_ms / 1e3) / 1e9}

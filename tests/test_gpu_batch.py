@@ -65,3 +65,29 @@ def test_batch_rejects_bad_arguments(gpu, batch):
     r = gpu.PrResult()
     assert gpu.lib().gg_pagerank_batch(dg.h, p, len(voff) - 1, voff.ctypes.data, None, r, None) == 1
     dg.free()
+
+
+def test_cuda_graph_cache_reuse_and_invalidation(gpu):
+    """GG_PR_CUDA_GRAPH keeps the instantiated graph on the mapping: a
+    repeat call with the same parameters relaunches it and gives the same
+    ranks; other parameters capture again; a BFS that regrows a shared work
+    buffer in between forces a new capture (the old graph would write freed
+    memory), and the ranks stay equal to the plain launches'."""
+    g = gpu.Graph.rmat(14, 16)
+    dg = gpu.DeviceGraph(g, gpu.MAP_IN | gpu.MAP_OUT)
+    plain, _ = dg.pagerank("pull", iterations=20, epsilon=1e-4)
+    a, ra = dg.pagerank("pull", iterations=20, epsilon=1e-4, cuda_graph=True)
+    b, rb = dg.pagerank("pull", iterations=20, epsilon=1e-4, cuda_graph=True)
+    np.testing.assert_allclose(a, plain, rtol=1e-6, atol=0)
+    np.testing.assert_allclose(b, plain, rtol=1e-6, atol=0)
+    assert ra["iterations"] == rb["iterations"] and ra["launches"] == rb["launches"]
+    c, rc = dg.pagerank("pull", iterations=7, epsilon=0.0, cuda_graph=True)
+    c_plain, rcp = dg.pagerank("pull", iterations=7, epsilon=0.0)
+    np.testing.assert_allclose(c, c_plain, rtol=1e-6, atol=0)
+    assert rc["iterations"] == rcp["iterations"] == 7
+    dg.bfs(0, "do")  # regrows work buffer 0, which the captured graph also writes
+    d, _ = dg.pagerank("pull", iterations=7, epsilon=0.0, cuda_graph=True)
+    np.testing.assert_allclose(d, c_plain, rtol=1e-6, atol=0)
+    e, _ = dg.pagerank("pull", iterations=20, epsilon=1e-4, storage="bf16", cuda_graph=True)
+    e_plain, _ = dg.pagerank("pull", iterations=20, epsilon=1e-4, storage="bf16")
+    np.testing.assert_allclose(e, e_plain, rtol=1e-6, atol=0)
