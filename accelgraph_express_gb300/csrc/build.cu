@@ -13,7 +13,8 @@
  *   k_make_keys   (src << b | dst) for the CSR or (dst << b | src) for the
  *                 CSC, with the edge weight as payload; ids >= V flagged
  *   per 8-bit digit, least significant first (2b bits in all):
- *     k_rdx_count    per-tile digit counts, tile-major (counts[tile][d])
+ *     k_rdx_count    per-tile digit counts, tile-major (counts[tile][d]), by
+ *                    shared atomics (one per warp when its keys share a digit)
  *     column scan    k_col_reduce / k_col_top / k_col_down: counts[tile][d]
  *                    becomes the first output slot of digit d's keys of that
  *                    tile (keys of smaller digits, then of digit d in
@@ -99,9 +100,17 @@ __global__ void __launch_bounds__(RDX_THREADS) k_rdx_count(const uint64_t *__res
     {
         const bool valid = base + (uint64_t)it * 32 < n;
         const uint32_t d = digit_of(k[it], shift);
-        const uint32_t peers = digit_peers(valid, d);
-        /* the lowest lane of each digit group adds the group's size */
-        if (valid && (peers & ((1u << lane) - 1u)) == 0u) atomicAdd(&h[d], (uint32_t)__popc(peers));
+        /* a warp whose keys all share one digit (frequent in the skewed
+         * high digits of row ids) adds 32 at once; otherwise every key adds
+         * itself */
+        /* every lane takes part in the shuffle and the vote */
+        const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
+        if (__all_sync(0xffffffffu, valid && d == d0))
+        {
+            if (lane == 0) atomicAdd(&h[d], 32u);
+        }
+        else if (valid)
+            atomicAdd(&h[d], 1u);
     }
     __syncthreads();
     counts[(size_t)tile * RDX_BINS + threadIdx.x] = h[threadIdx.x];
