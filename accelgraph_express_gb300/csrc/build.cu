@@ -330,12 +330,7 @@ struct SortBufs
 gg_status radix_sort(SortBufs &B, uint64_t n, int bits, cudaStream_t s, int lo = 0)
 {
     if (n <= 1) return GG_OK;
-    static bool attr_set = false; /* one device per process */
-    if (!attr_set)
-    {
-        GG_CUDA(cudaFuncSetAttribute(k_rdx_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, SCATTER_SMEM));
-        attr_set = true;
-    }
+    GG_CUDA(cudaFuncSetAttribute(k_rdx_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, SCATTER_SMEM));
     const uint32_t ntiles = (uint32_t)((n + RDX_TILE - 1) / RDX_TILE);
     const uint32_t nb = (ntiles + COL_TILES - 1) / COL_TILES;
     for (int shift = lo; shift < bits; shift += 8)

@@ -42,12 +42,14 @@ def test_struct_sizes_match_c_layout(gg, tmp_path):
     """The ctypes mirror has the C compiler's layout of every drop-in struct."""
     structs = {"Arguments": gg.Arguments, "GraphCSR": gg.GraphCSR, "EdgeList": gg.EdgeList,
                "Vertex": gg.Vertex, "PageRankStats": gg.PageRankStats, "BFSStats": gg.BFSStats,
-               "SPMVStats": gg.SPMVStats, "Bitmap": gg.Bitmap, "ArrayQueue": gg.ArrayQueue}
+               "SPMVStats": gg.SPMVStats, "Bitmap": gg.Bitmap, "ArrayQueue": gg.ArrayQueue,
+               "CCStats": gg.CCStats}
     typedefs = {"gg_pr_params": gg.PrParams, "gg_pr_result": gg.PrResult, "gg_bfs_params": gg.BfsParams,
                 "gg_bfs_result": gg.BfsResult, "gg_spmv_params": gg.SpmvParams, "gg_spmv_result": gg.SpmvResult,
-                "GraphGpuOptions": gg.GraphGpuOptions, "gg_ppr_params": gg.PprParams, "gg_ppr_result": gg.PprResult}
+                "GraphGpuOptions": gg.GraphGpuOptions, "gg_ppr_params": gg.PprParams, "gg_ppr_result": gg.PprResult,
+                "gg_cc_params": gg.CcParams, "gg_cc_result": gg.CcResult}
     src = ['#include <stdio.h>', '#include "pageRank.h"', '#include "BFS.h"', '#include "SPMV.h"',
-           '#include "gg_runtime.h"', "int main(void){"]
+           '#include "connectedComponents.h"', '#include "gg_runtime.h"', "int main(void){"]
     for n in structs:
         src.append(f'printf("{n} %zu\\n", sizeof(struct {n}));')
     for n in typedefs:
