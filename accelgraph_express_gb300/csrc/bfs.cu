@@ -329,40 +329,62 @@ __device__ __forceinline__ void bu_body(const uint32_t *__restrict__ off, const 
             rs = kend;
             re = found ? kend : e;
         }
+        /* the lanes still searching scan the rest of their lists together:
+         * their remaining candidates are concatenated in lane order and taken
+         * 32 per round, each lane finding the owner of its item by a binary
+         * search over the running totals; an owner's first frontier hit in
+         * its own range is its parent (the first in CSC order, as before),
+         * and lanes that found one drop out of the next round */
         uint32_t pending = __ballot_sync(0xffffffffu, unvis && !found && re > rs);
         while (pending)
         {
-            const int ln = __ffs(pending) - 1;
-            pending &= pending - 1;
-            const uint32_t ws = __shfl_sync(0xffffffffu, rs, ln), we = __shfl_sync(0xffffffffu, re, ln);
-            uint32_t cnt = 0, par = 0;
-            bool hit_any = false;
-            for (uint32_t b = ws; b < we; b += 32)
+            const bool mine = (pending >> lane) & 1u;
+            const uint32_t len = mine ? re - rs : 0u;
+            uint32_t incl = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
             {
-                const uint32_t j = b + lane;
-                uint32_t u = 0;
-                bool hit = false;
-                if (j < we)
-                {
-                    u = adj[j];
-                    hit = bit_of(front, u);
-                }
-                const uint32_t m = __ballot_sync(0xffffffffu, hit);
-                if (m)
-                {
-                    const int f = __ffs(m) - 1;
-                    par = __shfl_sync(0xffffffffu, u, f);
-                    cnt += (uint32_t)f + 1u;
-                    hit_any = true;
-                    break;
-                }
-                cnt += min(32u, we - b);
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (uint32_t)o) incl += y;
             }
-            if (lane == (uint32_t)ln)
+            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+            const uint32_t excl = incl - len;
+            /* owner of item `lane`: the number of lanes whose total is <= lane */
+            uint32_t owner = 0;
+#pragma unroll
+            for (uint32_t step = 16; step >= 1; step >>= 1)
+                if (__shfl_sync(0xffffffffu, incl, owner + step - 1) <= lane) owner += step;
+            const uint32_t o_excl = __shfl_sync(0xffffffffu, excl, owner);
+            const uint32_t o_rs = __shfl_sync(0xffffffffu, rs, owner);
+            uint32_t u = 0;
+            bool hit = false;
+            if (lane < total)
             {
-                scanned += cnt;
-                if (hit_any) { found = true; parent = par; }
+                u = adj[o_rs + (lane - o_excl)];
+                hit = bit_of(front, u);
             }
+            const uint32_t hits = __ballot_sync(0xffffffffu, hit);
+            /* this lane's items in the round are lanes [lo, hi) */
+            const uint32_t lo = min(excl, 32u), hi = min(incl, 32u);
+            const uint32_t range = (hi >= 32u ? 0xffffffffu : ((1u << hi) - 1u)) & ~(lo >= 32u ? 0xffffffffu : ((1u << lo) - 1u));
+            const uint32_t mh = mine ? (hits & range) : 0u;
+            const int fl = mh ? __ffs(mh) - 1 : (int)lane;
+            const uint32_t par = __shfl_sync(0xffffffffu, u, fl);
+            if (mine)
+            {
+                if (mh)
+                {
+                    found = true;
+                    parent = par;
+                    scanned += (uint32_t)fl - lo + 1u;
+                }
+                else
+                {
+                    scanned += hi - lo;
+                    rs += hi - lo;
+                }
+            }
+            pending = __ballot_sync(0xffffffffu, mine && !found && rs < re);
         }
         const uint32_t fm = __ballot_sync(0xffffffffu, found);
         if (found)
