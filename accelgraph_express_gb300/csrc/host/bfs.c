@@ -25,6 +25,7 @@ struct BFSStats *newBFSStatsGraphCSR(struct GraphCSR *graph)
         freeBFSStats(s);
         return NULL;
     }
+#pragma omp parallel for schedule(static)
     for (uint32_t v = 0; v < V; v++)
     {
         uint32_t d = graph->vertices->out_degree[v];

@@ -28,6 +28,7 @@ struct CCStats *newCCStatsGraphCSR(struct GraphCSR *graph)
         freeCCStats(s);
         return NULL;
     }
+#pragma omp parallel for schedule(static)
     for (uint32_t v = 0; v < V; v++)
         s->components[v] = s->labels[v] = v;
     return s;

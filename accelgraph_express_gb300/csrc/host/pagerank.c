@@ -27,9 +27,12 @@ struct PageRankStats *newPageRankStatsGraphCSR(struct GraphCSR *graph)
         freePageRankStats(s);
         return NULL;
     }
+    /* first touch of the fresh pages on all host threads */
+    const float base = s->base_pr;
+#pragma omp parallel for schedule(static)
     for (uint32_t v = 0; v < V; v++)
     {
-        s->pageRanks[v] = s->base_pr;
+        s->pageRanks[v] = base;
         s->realRanks[v] = v;
     }
     return s;
