@@ -997,8 +997,8 @@ extern "C" gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parent
     B.res.processed_nodes = processed;
     B.res.levels = level;
     B.res.launches = B.launches;
-    if (parents) GG_CUDA(cudaMemcpyAsync(parents, B.parents, (size_t)V * 4, cudaMemcpyDeviceToHost, B.s));
-    if (distances) GG_CUDA(cudaMemcpyAsync(distances, B.dist, (size_t)V * 4, cudaMemcpyDeviceToHost, B.s));
+    if (parents) GG_CHECK(gg_copy_d2h(parents, B.parents, (size_t)V * 4, B.s));
+    if (distances) GG_CHECK(gg_copy_d2h(distances, B.dist, (size_t)V * 4, B.s));
     GG_CHECK(gg_wait(B.s));
     if (p->profile)
         for (size_t i = 0; i + 1 < B.evs.size(); i += 2) B.res.step_ms += gg_event_ms(B.evs[i], B.evs[i + 1]);

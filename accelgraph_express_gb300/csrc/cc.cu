@@ -386,7 +386,7 @@ extern "C" gg_status gg_cc(gg_graph *g, const gg_cc_params *p, uint32_t *compone
     k_cc_roots<<<grid_for(V), 256, 0, C.s>>>(C.comp, V, C.f);
     C.launches++;
     GG_CUDA(cudaGetLastError());
-    if (components) GG_CUDA(cudaMemcpyAsync(components, C.comp, (size_t)V * 4, cudaMemcpyDeviceToHost, C.s));
+    if (components) GG_CHECK(gg_copy_d2h(components, C.comp, (size_t)V * 4, C.s));
     GG_CHECK(read_flags(C));
     res.components = C.h->roots;
     res.launches = C.launches;

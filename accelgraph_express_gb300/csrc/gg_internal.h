@@ -144,6 +144,12 @@ gg_status gg_hot_prepare(gg_graph *g, cudaStream_t s, uint32_t cap);
 cudaStream_t gg_stream(gg_graph *g, void *user_stream);
 /* host wait on all work queued on `s`, bounded by the wait limit */
 gg_status gg_wait(cudaStream_t s);
+/* host -> device copy; pageable sources go through page-locked staging
+ * filled by all host threads (returns with the copy queued on s) */
+gg_status gg_copy_h2d(void *dst, const void *src, size_t bytes, cudaStream_t s);
+/* device -> host copy, complete on return (waits for s); pageable
+ * destinations are filled from page-locked staging by all host threads */
+gg_status gg_copy_d2h(void *dst, const void *src, size_t bytes, cudaStream_t s);
 /* tiles of the CSC (in = 1) or CSR (in = 0), computed on first use */
 gg_status gg_tiles_get(gg_graph *g, int in, cudaStream_t s, gg_tiles **out);
 /* bf16 (storage 1) / f16 (storage 2) copy of the in- or out-edge weights */

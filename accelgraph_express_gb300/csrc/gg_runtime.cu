@@ -10,6 +10,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <omp.h>
+
 #include <atomic>
 #include <cmath>
 #include <chrono>
@@ -209,6 +211,28 @@ cudaStream_t gg_stream(gg_graph *g, void *user_stream)
     return user_stream ? (cudaStream_t)user_stream : g->own_stream;
 }
 
+/* Bounded host wait on a recorded event. */
+static gg_status wait_event(cudaEvent_t ev)
+{
+    cudaError_t e;
+    const auto t0 = std::chrono::steady_clock::now();
+    const uint32_t limit = wait_timeout_ms();
+    for (;;)
+    {
+        e = cudaEventQuery(ev);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) return gg_cuda_fail(e, "device work");
+        const auto us =
+            std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
+        if ((uint64_t)us > (uint64_t)limit * 1000)
+            return gg_fail(GG_ETIMEDOUT, "device work did not finish within the wait limit");
+        /* spin through the first half millisecond (per-level BFS waits and
+         * short calls end within it), then nap briefly between polls */
+        if (us > 500) std::this_thread::sleep_for(std::chrono::microseconds(5));
+    }
+    return GG_OK;
+}
+
 gg_status gg_wait(cudaStream_t s)
 {
     /* Bounded host wait: poll an event instead of blocking forever like the
@@ -221,29 +245,111 @@ gg_status gg_wait(cudaStream_t s)
         cudaEventDestroy(ev);
         return gg_cuda_fail(e, "cudaEventRecord");
     }
-    const auto t0 = std::chrono::steady_clock::now();
-    const uint32_t limit = wait_timeout_ms();
-    for (;;)
-    {
-        e = cudaEventQuery(ev);
-        if (e == cudaSuccess) break;
-        if (e != cudaErrorNotReady)
-        {
-            cudaEventDestroy(ev);
-            return gg_cuda_fail(e, "device work");
-        }
-        const auto us =
-            std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
-        if ((uint64_t)us > (uint64_t)limit * 1000)
-        {
-            cudaEventDestroy(ev);
-            return gg_fail(GG_ETIMEDOUT, "device work did not finish within the wait limit");
-        }
-        /* spin through the first half millisecond (per-level BFS waits and
-         * short calls end within it), then nap briefly between polls */
-        if (us > 500) std::this_thread::sleep_for(std::chrono::microseconds(5));
-    }
+    const gg_status st = wait_event(ev);
     cudaEventDestroy(ev);
+    return st;
+}
+
+/* ---- host -> device copies of pageable memory ---------------------------
+ * A copy from pageable host memory goes through the driver's own staging,
+ * whose rate varied several-fold between runs on this system.  Sources
+ * that are not page-locked are copied instead in 32 MB chunks through two
+ * page-locked buffers (kept for the process), each chunk filled by all host
+ * threads while the previous chunk's DMA runs. */
+namespace {
+constexpr size_t STAGE_BYTES = (size_t)32 << 20;
+std::mutex g_stage_mu;
+void *g_stage[2] = {nullptr, nullptr};
+cudaEvent_t g_stage_ev[2] = {nullptr, nullptr};
+
+void parallel_copy(void *to, const void *from, size_t n)
+{
+#pragma omp parallel
+    {
+        const size_t T = (size_t)omp_get_num_threads(), t = (size_t)omp_get_thread_num();
+        const size_t a = n * t / T / 64 * 64, e = t + 1 == T ? n : n * (t + 1) / T / 64 * 64;
+        if (e > a) memcpy((unsigned char *)to + a, (const unsigned char *)from + a, e - a);
+    }
+}
+
+bool host_pinned(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+} // namespace
+
+gg_status gg_copy_h2d(void *dst, const void *src, size_t bytes, cudaStream_t s)
+{
+    if (bytes < ((size_t)4 << 20) || host_pinned(src))
+    {
+        GG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+        return GG_OK;
+    }
+    std::lock_guard<std::mutex> lock(g_stage_mu);
+    for (int b = 0; b < 2; b++)
+        if (!g_stage[b])
+        {
+            GG_CUDA(cudaHostAlloc(&g_stage[b], STAGE_BYTES, cudaHostAllocDefault));
+            GG_CUDA(cudaEventCreateWithFlags(&g_stage_ev[b], cudaEventDisableTiming));
+        }
+    bool used[2] = {false, false};
+    for (size_t off = 0, i = 0; off < bytes; off += STAGE_BYTES, i++)
+    {
+        const int b = (int)(i & 1);
+        if (used[b]) GG_CHECK(wait_event(g_stage_ev[b])); /* its last DMA has read the buffer */
+        const size_t n = bytes - off < STAGE_BYTES ? bytes - off : STAGE_BYTES;
+        parallel_copy(g_stage[b], (const unsigned char *)src + off, n);
+        GG_CUDA(cudaMemcpyAsync((unsigned char *)dst + off, g_stage[b], n, cudaMemcpyHostToDevice, s));
+        GG_CUDA(cudaEventRecord(g_stage_ev[b], s));
+        used[b] = true;
+    }
+    /* the buffers go back to other callers only once their DMAs are done */
+    for (int b = 0; b < 2; b++)
+        if (used[b]) GG_CHECK(wait_event(g_stage_ev[b]));
+    return GG_OK;
+}
+
+gg_status gg_copy_d2h(void *dst, const void *src, size_t bytes, cudaStream_t s)
+{
+    if (bytes < ((size_t)4 << 20) || host_pinned(dst))
+    {
+        GG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+        return gg_wait(s);
+    }
+    std::lock_guard<std::mutex> lock(g_stage_mu);
+    for (int b = 0; b < 2; b++)
+        if (!g_stage[b])
+        {
+            GG_CUDA(cudaHostAlloc(&g_stage[b], STAGE_BYTES, cudaHostAllocDefault));
+            GG_CUDA(cudaEventCreateWithFlags(&g_stage_ev[b], cudaEventDisableTiming));
+        }
+    /* chunk i lands in buffer i & 1; while it is in flight the previous
+     * chunk is copied out by all host threads */
+    const size_t nchunks = (bytes + STAGE_BYTES - 1) / STAGE_BYTES;
+    for (size_t i = 0; i <= nchunks; i++)
+    {
+        if (i < nchunks)
+        {
+            const int b = (int)(i & 1);
+            const size_t off = i * STAGE_BYTES, n = bytes - off < STAGE_BYTES ? bytes - off : STAGE_BYTES;
+            GG_CUDA(cudaMemcpyAsync(g_stage[b], (const unsigned char *)src + off, n, cudaMemcpyDeviceToHost, s));
+            GG_CUDA(cudaEventRecord(g_stage_ev[b], s));
+        }
+        if (i > 0)
+        {
+            const size_t k = i - 1;
+            const int b = (int)(k & 1);
+            const size_t off = k * STAGE_BYTES, n = bytes - off < STAGE_BYTES ? bytes - off : STAGE_BYTES;
+            GG_CHECK(wait_event(g_stage_ev[b]));
+            parallel_copy((unsigned char *)dst + off, g_stage[b], n);
+        }
+    }
     return GG_OK;
 }
 
@@ -276,8 +382,7 @@ static gg_status upload(gg_graph *g, void **dst, const void *src, size_t bytes, 
                         cudaStream_t s)
 {
     GG_CHECK(gg_dev_alloc(g, dst, alloc_bytes));
-    if (bytes)
-        GG_CUDA(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, s));
+    if (bytes) GG_CHECK(gg_copy_h2d(*dst, src, bytes, s));
     if (alloc_bytes > bytes)
         GG_CUDA(cudaMemsetAsync((char *)*dst + bytes, 0, alloc_bytes - bytes, s));
     return GG_OK;

@@ -1002,7 +1002,7 @@ gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_
     double sum = 0.0;
     GG_CUDA(cudaMemcpyAsync(h.data(), rec, ((size_t)iters + 2) * sizeof(IterRec), cudaMemcpyDeviceToHost, R.s));
     GG_CUDA(cudaMemcpyAsync(&sum, sum_v, sizeof(double), cudaMemcpyDeviceToHost, R.s));
-    if (ranks && V) GG_CUDA(cudaMemcpyAsync(ranks, rank, (size_t)V * 4, cudaMemcpyDeviceToHost, R.s));
+    if (ranks && V) GG_CHECK(gg_copy_d2h(ranks, rank, (size_t)V * 4, R.s));
     GG_CHECK(gg_wait(R.s));
 
     /* reference loop convention: iterations = index of the breaking

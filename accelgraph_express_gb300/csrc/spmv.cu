@@ -404,8 +404,8 @@ extern "C" gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *
     }
     double checksum = 0.0;
     GG_CUDA(cudaMemcpyAsync(&checksum, chk, 8, cudaMemcpyDeviceToHost, s));
-    if (y && V) GG_CUDA(cudaMemcpyAsync(y, yv, (size_t)V * 4, cudaMemcpyDeviceToHost, s));
-    if (x_out && V) GG_CUDA(cudaMemcpyAsync(x_out, xf, (size_t)V * 4, cudaMemcpyDeviceToHost, s));
+    if (y && V) GG_CHECK(gg_copy_d2h(y, yv, (size_t)V * 4, s));
+    if (x_out && V) GG_CHECK(gg_copy_d2h(x_out, xf, (size_t)V * 4, s));
     GG_CHECK(gg_wait(s));
     res.checksum = checksum;
     res.launches = launches;

@@ -111,3 +111,26 @@ def test_device_build_rejects_bad_ids(gpu):
     d = np.array([1, 2, 3], np.uint32)
     with pytest.raises(gpu.GgError):
         gpu.DeviceGraph.build(s, d, num_vertices=5)
+
+
+def test_staged_copies_of_pageable_buffers(gpu, orc):
+    """Pageable host buffers above 4 MB go through page-locked staging in
+    32 MB chunks: an 80 MB edge list uploaded by gg_graph_build (three
+    chunks) and 33.5 MB of BFS distances copied back into a numpy array (two
+    chunks) arrive intact."""
+    rng = np.random.default_rng(12)
+    V, E = 1 << 23, 20_000_000
+    s = rng.integers(0, V, E).astype(np.uint32)
+    d = rng.integers(0, V, E).astype(np.uint32)
+    dg = gpu.DeviceGraph.build(s, d, num_vertices=V, what=gpu.MAP_OUT | gpu.MAP_IN)
+    got = dg.download(weights=False)
+    host = gpu.Graph.from_edges(s, d, num_vertices=V).arrays()
+    for k in ("out_off", "out_adj", "in_off", "in_adj"):
+        np.testing.assert_array_equal(got[k], host[k], err_msg=k)
+    src = int(s[0])
+    _, dist, _ = dg.bfs(src, "push")
+    g = gpu.Graph.from_edges(s, d, num_vertices=V)
+    a = g.arrays()
+    o = orc.Csr.from_arrays(V, E, a["out_off"], a["out_adj"], a["in_off"], a["in_adj"])
+    _, rd, _ = orc.bfs(o, 1, src)
+    np.testing.assert_array_equal(dist, rd)
