@@ -1,6 +1,6 @@
 """ctypes bindings of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
-Used by tests/, ``__graft_entry__.smoke()`` (as the checker) and the CPU
+Used by tests/, ``__graft_entry__.smoke()`` (to check its results) and the CPU
 baseline leg of ``bench.py``.  The product library never imports this module.
 
 ``liboracle.so`` is the plain-C restatement of the reference's CSR loops
