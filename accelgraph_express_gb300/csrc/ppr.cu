@@ -170,11 +170,13 @@ __global__ void __launch_bounds__(256) k_ppr_pull(PprArgs<CT> a)
             if (r - rb >= LPE) fetch(r);
             re = __shfl_sync(gmask, w_end, r - rb, LPE);
         };
+        /* the ids of a batch are loaded while the previous batch's rows are
+         * in flight, so a batch waits for one memory latency, not two */
+        uint32_t myid = 0;
+        if (j0 < j1 && gl < min((uint32_t)U, j1 - j0)) myid = ldg_stream(a.adj + j0 + gl);
         for (uint32_t e = j0; e < j1; e += U)
         {
             const uint32_t nb = min((uint32_t)U, j1 - e);
-            uint32_t myid = 0;
-            if (gl < nb) myid = ldg_stream(a.adj + e + gl);
             typename PairIO<CT>::Raw v[U];
 #pragma unroll
             for (int i = 0; i < U; i++)
@@ -182,6 +184,9 @@ __global__ void __launch_bounds__(256) k_ppr_pull(PprArgs<CT> a)
                 const uint32_t u = __shfl_sync(gmask, myid, i, LPE);
                 if ((uint32_t)i < nb) v[i] = PairIO<CT>::load(a.cin + (size_t)u * KP + 2 * gl);
             }
+            const uint32_t en = e + U;
+            myid = 0;
+            if (en < j1 && gl < min((uint32_t)U, j1 - en)) myid = ldg_stream(a.adj + en + gl);
 #pragma unroll
             for (int i = 0; i < U; i++)
             {
