@@ -677,8 +677,14 @@ __global__ void __launch_bounds__(256, 6) k_bfs_do(DoArgs a)
             td_body(a.q[qcur], qlen, a.out_off, a.out_adj, a.parents, a.dist, level + 1, a.visited, a.q[qcur ^ 1],
                     nullptr, cs, a.heavy);
             if (!(ok = grid_barrier(a.ctl, gen))) break;
-            td_heavy_body(a.heavy, a.out_adj, a.parents, a.dist, level + 1, a.visited, a.q[qcur ^ 1], nullptr, cs);
-            if (!(ok = grid_barrier(a.ctl, gen))) break;
+            /* the deferred high-degree vertices, when there are any (every
+             * block reads the same final count, so all skip together) */
+            if (read_counters_block(cs).nheavy)
+            {
+                td_heavy_body(a.heavy, a.out_adj, a.parents, a.dist, level + 1, a.visited, a.q[qcur ^ 1], nullptr,
+                              cs);
+                if (!(ok = grid_barrier(a.ctl, gen))) break;
+            }
             const Counters k = read_counters_block(cs);
             mf = k.mf;
             qlen = k.qlen;
