@@ -25,6 +25,9 @@
  *                    out in runs
  *   k_split       neighbour ids, row offsets from the row boundaries, and
  *                 the out-degrees
+ *   the CSC: k_swap_fields turns the CSR's sorted words into
+ *                 (dst << b | src) in (src, dst) order, and a stable sort of
+ *                 the dst field alone finishes it (b/8 passes, not 2b/8)
  *
  * A pass reads the keys twice and writes them once (the reduce-then-scan
  * form: no block waits on another).  Tiles are 4096 keys (256 threads x 16).
@@ -347,15 +350,22 @@ gg_status radix_sort(SortBufs &B, uint64_t n, int bits, cudaStream_t s, int lo =
     return GG_OK;
 }
 
-/* one direction: rows keyed by `key`, neighbours from `other` */
-gg_status build_direction(gg_graph *g, SortBufs &B, const uint32_t *key, const uint32_t *other, const float *w,
-                          uint32_t **off, uint32_t **adj, float **wout, uint32_t *bad, cudaStream_t s)
+/* (row, neighbour) -> (neighbour, row) in every word */
+__global__ void k_swap_fields(uint64_t *keys, uint64_t n, int b)
+{
+    const uint64_t mask = (1ull << b) - 1ull;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const uint64_t k = keys[i];
+        keys[i] = ((k & mask) << b) | (k >> b);
+    }
+}
+
+/* the sorted words of one direction -> its offsets, neighbours, weights */
+gg_status split_direction(gg_graph *g, SortBufs &B, uint32_t **off, uint32_t **adj, float **wout, cudaStream_t s)
 {
     const uint32_t V = g->V, E = g->E;
     const int b = bits_for(V);
-    k_make_keys<<<grid_for(E, 256), 256, 0, s>>>(key, other, w, E, V, b, B.keys, B.pay, bad);
-    GG_CUDA(cudaGetLastError());
-    GG_CHECK(radix_sort(B, E, 2 * b, s));
     GG_CHECK(gg_dev_alloc(g, (void **)off, ((size_t)V + 1) * 4));
     GG_CHECK(gg_dev_alloc(g, (void **)adj, ((size_t)E + GG_EDGE_PAD) * 4));
     GG_CUDA(cudaMemsetAsync(*adj + E, 0, GG_EDGE_PAD * 4, s));
@@ -367,6 +377,33 @@ gg_status build_direction(gg_graph *g, SortBufs &B, const uint32_t *key, const u
     k_split<<<grid_for((uint64_t)E + 1, 256), 256, 0, s>>>(B.keys, E, b, V, *off, *adj, B.pay, wout ? *wout : nullptr);
     GG_CUDA(cudaGetLastError());
     return GG_OK;
+}
+
+/* the CSR: words (src << b | dst) sorted on all 2b bits */
+gg_status build_csr(gg_graph *g, SortBufs &B, const uint32_t *src, const uint32_t *dst, const float *w,
+                    uint32_t **off, uint32_t **adj, float **wout, uint32_t *bad, cudaStream_t s)
+{
+    const uint32_t V = g->V, E = g->E;
+    const int b = bits_for(V);
+    k_make_keys<<<grid_for(E, 256), 256, 0, s>>>(src, dst, w, E, V, b, B.keys, B.pay, bad);
+    GG_CUDA(cudaGetLastError());
+    GG_CHECK(radix_sort(B, E, 2 * b, s));
+    return split_direction(g, B, off, adj, wout, s);
+}
+
+/* the CSC from the CSR's sorted words: with the fields swapped they are in
+ * (src, dst) order, so a stable sort on the dst field alone gives
+ * (dst, src) order with duplicates still in input order -- the order a
+ * full sort of (dst << b | src) from the input gives -- in b/8 passes
+ * instead of 2b/8 */
+gg_status build_csc_from_csr(gg_graph *g, SortBufs &B, uint32_t **off, uint32_t **adj, float **wout, cudaStream_t s)
+{
+    const uint32_t E = g->E;
+    const int b = bits_for(g->V);
+    k_swap_fields<<<grid_for(E, 256), 256, 0, s>>>(B.keys, E, b);
+    GG_CUDA(cudaGetLastError());
+    GG_CHECK(radix_sort(B, E, 2 * b, s, b));
+    return split_direction(g, B, off, adj, wout, s);
 }
 
 } // namespace
@@ -406,16 +443,16 @@ gg_status gg_build_arrays(gg_graph *g, const uint32_t *src, const uint32_t *dst,
         const bool need_out = what & (GG_MAP_OUT | GG_MAP_OUT_W), need_in = what & (GG_MAP_IN | GG_MAP_IN_W);
         /* the CSR is always built: the out-degrees come from it */
         SortBufs F = B;
-        if ((st = build_direction(g, F, src, dst, wp, &g->out_off, &g->out_adj,
-                                  (weighted && (what & GG_MAP_OUT_W)) ? &g->out_w : nullptr, (uint32_t *)bad, s)) != GG_OK)
+        if ((st = build_csr(g, F, src, dst, wp, &g->out_off, &g->out_adj,
+                            (weighted && (what & GG_MAP_OUT_W)) ? &g->out_w : nullptr, (uint32_t *)bad, s)) != GG_OK)
             break;
         if ((st = gg_dev_alloc(g, (void **)&g->out_deg, (size_t)V * 4 + 16)) != GG_OK) break;
         k_degrees<<<grid_for(V, 256), 256, 0, s>>>(g->out_off, V, g->out_deg);
         if (need_in)
         {
-            SortBufs I = B;
-            if ((st = build_direction(g, I, dst, src, wp, &g->in_off, &g->in_adj,
-                                      (weighted && (what & GG_MAP_IN_W)) ? &g->in_w : nullptr, (uint32_t *)bad, s)) != GG_OK)
+            /* F still holds the CSR's sorted words and weights */
+            if ((st = build_csc_from_csr(g, F, &g->in_off, &g->in_adj,
+                                         (weighted && (what & GG_MAP_IN_W)) ? &g->in_w : nullptr, s)) != GG_OK)
                 break;
         }
         if (!need_out)

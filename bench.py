@@ -781,13 +781,17 @@ def relabel_extras(gg, torch, peak, scale=24):
 
 
 def csr_radix_bytes(V, E):
-    """Bytes the device CSR + CSC build moves per direction (unweighted):
-    keys made (8E read, 8E written), per 8-bit pass a count read (8E) and a
-    scatter read + write (16E), then ids and offsets split out (8E read,
-    4E + 4V written)."""
+    """Bytes the device CSR + CSC build moves (unweighted): the CSR's keys
+    made (8E read, 8E written), per 8-bit pass a count read (8E) and a
+    scatter read + write (16E), ids and offsets split out (8E read, 4E + 4V
+    written); the CSC's fields swapped in place (16E), its passes over the
+    dst field only, and its split.  Returns (bytes, CSR passes)."""
     b = max(1, (max(V, 2) - 1).bit_length())
     passes = (2 * b + 7) // 8
-    return 2 * (16 * E + 24 * E * passes + 12 * E + 4 * V), passes
+    csc_passes = (b + 7) // 8
+    csr = 16 * E + 24 * E * passes + 12 * E + 4 * V
+    csc = 16 * E + 24 * E * csc_passes + 12 * E + 4 * V
+    return csr + csc, passes
 
 
 def csr_build_extras(gg, torch, peak, scale=24, edge_factor=16):
