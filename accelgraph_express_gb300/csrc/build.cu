@@ -220,42 +220,73 @@ __global__ void __launch_bounds__(RDX_THREADS, 3) k_rdx_scatter(const uint64_t *
 
 /* ---- column scan of the [tile][digit] counts (thread = digit) ---- */
 
-/* the column sums of each block of COL_TILES tiles */
+/* the column sums of each block of COL_TILES tiles (the loads of a block's
+ * rows are independent: unrolled so they are in flight together) */
 __global__ void __launch_bounds__(RDX_BINS) k_col_reduce(const uint32_t *__restrict__ counts, uint32_t ntiles,
                                                          uint32_t *csum)
 {
     const uint32_t t0 = blockIdx.x * COL_TILES, t1 = min(t0 + COL_TILES, ntiles);
     uint32_t t = 0;
+#pragma unroll 8
     for (uint32_t tile = t0; tile < t1; tile++) t += counts[(size_t)tile * RDX_BINS + threadIdx.x];
     csum[(size_t)blockIdx.x * RDX_BINS + threadIdx.x] = t;
 }
 
-/* one block: csum[b][d] becomes the first output slot of digit d in block
- * b's tiles: the keys of all smaller digits plus digit d in earlier blocks */
-__global__ void __launch_bounds__(RDX_BINS) k_col_top(uint32_t *csum, uint32_t nblocks)
+/* one block of COL_TOP_SPLIT * RDX_BINS threads: csum[b][d] becomes the
+ * first output slot of digit d in block b's tiles (the keys of all smaller
+ * digits plus digit d in earlier blocks); each digit's blocks are split over
+ * COL_TOP_SPLIT threads, combined through shared memory */
+constexpr uint32_t COL_TOP_SPLIT = 4;
+
+__global__ void __launch_bounds__(COL_TOP_SPLIT * RDX_BINS) k_col_top(uint32_t *csum, uint32_t nblocks)
 {
+    __shared__ uint32_t part[COL_TOP_SPLIT][RDX_BINS];
     __shared__ uint32_t wtot[RDX_BINS / 32];
-    const uint32_t d = threadIdx.x, lane = d & 31, w = d >> 5;
+    const uint32_t d = threadIdx.x % RDX_BINS, q = threadIdx.x / RDX_BINS;
+    const uint32_t b0 = (uint32_t)((uint64_t)nblocks * q / COL_TOP_SPLIT);
+    const uint32_t b1 = (uint32_t)((uint64_t)nblocks * (q + 1) / COL_TOP_SPLIT);
     uint32_t run = 0;
-    for (uint32_t b = 0; b < nblocks; b++)
+#pragma unroll 8
+    for (uint32_t b = b0; b < b1; b++) run += csum[(size_t)b * RDX_BINS + d];
+    part[q][d] = run;
+    __syncthreads();
+    /* digit d's total and the start of quarter q within it */
+    uint32_t before = 0, total = 0;
+    for (uint32_t k = 0; k < COL_TOP_SPLIT; k++)
+    {
+        if (k < q) before += part[k][d];
+        total += part[k][d];
+    }
+    /* exclusive scan of the digit totals (the first RDX_BINS threads) */
+    uint32_t base = 0;
+    if (q == 0)
+    {
+        const uint32_t lane = d & 31, w = d >> 5;
+        uint32_t incl = total;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        if (lane == 31) wtot[w] = incl;
+        base = incl - total;
+    }
+    __syncthreads();
+    if (q == 0)
+    {
+        for (uint32_t k = 0; k < (d >> 5); k++) base += wtot[k];
+        part[0][d] = base;
+    }
+    __syncthreads();
+    uint32_t at = part[0][d] + before;
+    __syncthreads();
+    for (uint32_t b = b0; b < b1; b++)
     {
         const uint32_t c = csum[(size_t)b * RDX_BINS + d];
-        csum[(size_t)b * RDX_BINS + d] = run;
-        run += c;
+        csum[(size_t)b * RDX_BINS + d] = at;
+        at += c;
     }
-    /* exclusive scan of the digit totals */
-    uint32_t incl = run;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= (uint32_t)o) incl += y;
-    }
-    if (lane == 31) wtot[w] = incl;
-    __syncthreads();
-    uint32_t base = incl - run;
-    for (uint32_t k = 0; k < w; k++) base += wtot[k];
-    for (uint32_t b = 0; b < nblocks; b++) csum[(size_t)b * RDX_BINS + d] += base;
 }
 
 __global__ void __launch_bounds__(RDX_BINS) k_col_down(uint32_t *counts, uint32_t ntiles,
@@ -263,7 +294,21 @@ __global__ void __launch_bounds__(RDX_BINS) k_col_down(uint32_t *counts, uint32_
 {
     const uint32_t t0 = blockIdx.x * COL_TILES, t1 = min(t0 + COL_TILES, ntiles);
     uint32_t run = csum[(size_t)blockIdx.x * RDX_BINS + threadIdx.x];
-    for (uint32_t tile = t0; tile < t1; tile++)
+    uint32_t tile = t0;
+    /* eight rows loaded together, then their running prefix written */
+    for (; tile + 8 <= t1; tile += 8)
+    {
+        uint32_t c[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) c[k] = counts[(size_t)(tile + k) * RDX_BINS + threadIdx.x];
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+        {
+            counts[(size_t)(tile + k) * RDX_BINS + threadIdx.x] = run;
+            run += c[k];
+        }
+    }
+    for (; tile < t1; tile++)
     {
         uint32_t *p = counts + (size_t)tile * RDX_BINS + threadIdx.x;
         const uint32_t c = *p;
@@ -340,7 +385,7 @@ gg_status radix_sort(SortBufs &B, uint64_t n, int bits, cudaStream_t s, int lo =
     {
         k_rdx_count<<<ntiles, RDX_THREADS, 0, s>>>(B.keys, n, shift, ntiles, B.counts);
         k_col_reduce<<<nb, RDX_BINS, 0, s>>>(B.counts, ntiles, B.sums);
-        k_col_top<<<1, RDX_BINS, 0, s>>>(B.sums, nb);
+        k_col_top<<<1, COL_TOP_SPLIT * RDX_BINS, 0, s>>>(B.sums, nb);
         k_col_down<<<nb, RDX_BINS, 0, s>>>(B.counts, ntiles, B.sums);
         k_rdx_scatter<<<ntiles, RDX_THREADS, SCATTER_SMEM, s>>>(B.keys, B.pay, n, shift, ntiles, B.counts, B.tmp, B.ptmp);
         GG_CUDA(cudaGetLastError());
