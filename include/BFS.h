@@ -15,7 +15,9 @@
  *     otherwise arguments->source is replaced by label_array[source];
  *   - direction optimisation uses alpha = 15, beta = 18 and the reference's
  *     uint32 edge accounting (mu, mf, nf);
- *   - processed_nodes counts the vertices discovered after the source;
+ *   - processed_nodes counts the reached vertices, the source included (the
+ *     reference adds it with `++stats->processed_nodes` inside a printf
+ *     argument, BFS.c:368);
  *   - pull (pushpull 0, the FPGA variant) runs every level bottom-up and, as
  *     on the FPGA, leaves `distances` untouched.
  * Levels are deterministic; parents found top-down depend on which CAS wins

@@ -199,7 +199,7 @@ typedef struct gg_bfs_params
 
 typedef struct gg_bfs_result
 {
-    uint32_t processed_nodes; /* vertices discovered after the source */
+    uint32_t processed_nodes; /* vertices reached, the source included (BFS.c:368 counts it) */
     uint32_t levels;          /* frontier steps run */
     uint32_t top_down_steps;
     uint32_t bottom_up_steps;
