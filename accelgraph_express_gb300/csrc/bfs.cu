@@ -54,11 +54,20 @@ constexpr int BU_SERIAL = 4;  /* in-neighbours a lane checks before the warp hel
  * reading its (empty) in-edge range, which changes no count.  A thread takes
  * four consecutive vertices with 16-byte accesses; eight threads make one
  * bitmap word, joined by shuffles.  The arrays are allocation-aligned. */
+/* The same pass places the source (parent = itself, visited, queue[0]) and
+ * clears `zero` words (the direction-optimised search's control block and
+ * first frontier bitmap; may be null). */
 __global__ void k_bfs_init(const uint32_t *__restrict__ outdeg, const uint32_t *__restrict__ in_off, int32_t *parents,
-                           uint32_t *dist, uint32_t *visited, uint32_t V, uint32_t words)
+                           uint32_t *dist, uint32_t *visited, uint32_t V, uint32_t words, uint32_t src,
+                           uint32_t *queue, uint32_t *zero_a, uint32_t zero_a_words, uint32_t *zero_b,
+                           uint32_t zero_b_words)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t nq = (uint64_t)words * 8, stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t gtid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gtid == 0) queue[0] = src;
+    for (uint64_t i = gtid; i < zero_a_words; i += stride) zero_a[i] = 0u;
+    for (uint64_t i = gtid; i < zero_b_words; i += stride) zero_b[i] = 0u;
     const uint64_t nq32 = (nq + 31) & ~31ull; /* whole warps take part in the shuffles */
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nq32; t += stride)
     {
@@ -67,8 +76,20 @@ __global__ void k_bfs_init(const uint32_t *__restrict__ outdeg, const uint32_t *
         if (v0 + 4 <= V)
         {
             const uint4 d = reinterpret_cast<const uint4 *>(outdeg)[t];
-            reinterpret_cast<int4 *>(parents)[t] = make_int4(d.x ? -(int32_t)d.x : -1, d.y ? -(int32_t)d.y : -1,
-                                                             d.z ? -(int32_t)d.z : -1, d.w ? -(int32_t)d.w : -1);
+            int4 p4 = make_int4(d.x ? -(int32_t)d.x : -1, d.y ? -(int32_t)d.y : -1, d.z ? -(int32_t)d.z : -1,
+                                d.w ? -(int32_t)d.w : -1);
+            if (src - v0 < 4)
+            {
+                const int32_t self = (int32_t)src;
+                switch ((uint32_t)(src - v0))
+                {
+                case 0: p4.x = self; break;
+                case 1: p4.y = self; break;
+                case 2: p4.z = self; break;
+                default: p4.w = self; break;
+                }
+            }
+            reinterpret_cast<int4 *>(parents)[t] = p4;
             reinterpret_cast<uint4 *>(dist)[t] = make_uint4(0u, 0u, 0u, 0u);
             if (in_off)
             {
@@ -84,7 +105,7 @@ __global__ void k_bfs_init(const uint32_t *__restrict__ outdeg, const uint32_t *
             {
                 const uint64_t v = v0 + k;
                 const uint32_t d = outdeg[v];
-                parents[v] = d ? -(int32_t)d : -1;
+                parents[v] = v == src ? (int32_t)src : (d ? -(int32_t)d : -1);
                 dist[v] = 0u;
                 if (in_off && in_off[v + 1] == in_off[v]) bits |= 1u << k;
             }
@@ -93,15 +114,9 @@ __global__ void k_bfs_init(const uint32_t *__restrict__ outdeg, const uint32_t *
         m |= __shfl_xor_sync(0xffffffffu, m, 1);
         m |= __shfl_xor_sync(0xffffffffu, m, 2);
         m |= __shfl_xor_sync(0xffffffffu, m, 4);
+        if ((t >> 3) == (uint64_t)(src >> 5)) m |= 1u << (src & 31);
         if ((lane & 7) == 0 && t < nq) visited[t >> 3] = m;
     }
-}
-
-__global__ void k_bfs_source(int32_t *parents, uint32_t *visited, uint32_t *queue, uint32_t src)
-{
-    parents[src] = (int32_t)src;
-    visited[src >> 5] |= 1u << (src & 31);
-    queue[0] = src;
 }
 
 __device__ __forceinline__ bool bit_of(const uint32_t *bm, uint32_t v) { return (bm[v >> 5] >> (v & 31)) & 1u; }
@@ -834,8 +849,7 @@ gg_status do_search(Bfs &B, const gg_bfs_params *p)
 {
     gg_graph *g = B.g;
     char *ctl = (char *)B.c;
-    GG_CUDA(cudaMemsetAsync(ctl, 0, CTL_BYTES, B.s));
-    GG_CUDA(cudaMemsetAsync(B.bma, 0, (size_t)B.words * 4, B.s));
+    /* the control block and the first bitmap were cleared by k_bfs_init */
     DoArgs a{};
     a.out_off = g->out_off;
     a.out_adj = g->out_adj;
@@ -902,13 +916,16 @@ extern "C" gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parent
     Bfs B;
     GG_CHECK(bfs_setup(B, g, stream, p->profile));
     const uint32_t V = B.V, src = p->source;
-    k_bfs_init<<<cap_blocks((uint64_t)B.words * 8), 256, 0, B.s>>>(g->out_deg, g->in_off, B.parents, B.dist,
-                                                                  B.visited, V, B.words);
-    k_bfs_source<<<1, 1, 0, B.s>>>(B.parents, B.visited, B.qa, src);
-    B.launches += 2;
+    const bool device_loop = (p->mode == GG_BFS_DO || p->mode == GG_BFS_DO_BITMAP) && !p->profile;
+    /* the device loop's control block and first bitmap are cleared by the
+     * same pass */
+    k_bfs_init<<<cap_blocks((uint64_t)B.words * 8), 256, 0, B.s>>>(
+        g->out_deg, g->in_off, B.parents, B.dist, B.visited, V, B.words, src, B.qa,
+        device_loop ? (uint32_t *)B.c : nullptr, device_loop ? (uint32_t)(CTL_BYTES / 4) : 0u,
+        device_loop ? B.bma : nullptr, device_loop ? B.words : 0u);
+    B.launches++;
     GG_CUDA(cudaGetLastError());
 
-    const bool device_loop = (p->mode == GG_BFS_DO || p->mode == GG_BFS_DO_BITMAP) && !p->profile;
     uint32_t outdeg_src = 0;
     if (!device_loop)
     {
