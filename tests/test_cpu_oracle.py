@@ -153,3 +153,53 @@ def test_oracle_cc_planted_error_is_caught(orc):
     comp = orc.cc_min_label(g)
     comp[150] = 0
     assert not np.array_equal(comp, z["bridged_comp"])
+
+
+def test_cc_golden_reproduces_from_its_script():
+    """tests/golden/golden_cc.npz is what make_cc_golden.py computes (scipy)."""
+    pytest.importorskip("scipy")
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_cc_golden", os.path.join(GOLDEN, "make_cc_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    z, names = _cc_golden()
+    for name in names:
+        V = int(z[name + "_V"])
+        np.testing.assert_array_equal(mod.min_labels(V, z[name + "_src"], z[name + "_dst"]), z[name + "_comp"],
+                                      err_msg=name)
+
+
+def test_relabel_oracle_against_a_per_vertex_loop(orc):
+    """The numpy restatement of the -l modes against a plain loop that builds
+    each mode's order vertex by vertex."""
+    rng = np.random.default_rng(8)
+    V, E = 300, 2000
+    src = rng.integers(0, V, E)
+    dst = (rng.zipf(1.5, E) % V).astype(np.int64)
+    dout = [0] * V
+    din = [0] * V
+    for a, b in zip(src, dst):
+        dout[a] += 1
+        din[b] += 1
+    avg = E // V
+    for lmode in range(10):
+        deg = [dout[v] if lmode in (1, 4, 6, 8) else din[v] if lmode in (2, 5, 7, 9) else dout[v] + din[v]
+               for v in range(V)]
+        if lmode == 0:
+            order = list(range(V))
+        elif lmode in (1, 2, 3):
+            order = sorted(range(V), key=lambda v: (-deg[v], v))
+        elif lmode in (4, 5):
+            def group(d):
+                r = 2 * d // max(avg, 1)
+                return min(7, r.bit_length())
+            order = sorted(range(V), key=lambda v: (-group(deg[v]), v))
+        elif lmode in (6, 7):
+            hubs = sorted((v for v in range(V) if deg[v] > avg), key=lambda v: (-deg[v], v))
+            order = hubs + [v for v in range(V) if deg[v] <= avg]
+        else:
+            order = [v for v in range(V) if deg[v] > avg] + [v for v in range(V) if deg[v] <= avg]
+        want = np.empty(V, np.uint32)
+        want[np.array(order)] = np.arange(V, dtype=np.uint32)
+        np.testing.assert_array_equal(orc.relabel_order(src, dst, V, lmode), want, err_msg=f"mode {lmode}")
