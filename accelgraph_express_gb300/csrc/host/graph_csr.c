@@ -101,6 +101,12 @@ struct EdgeList *readEdgeListsbin(const char *fname, int weighted)
         fclose(f);
         return NULL;
     }
+    if ((size_t)bytes / rec > 0xffffffffull)
+    {
+        fprintf(stderr, "readEdgeListsbin: %s: more than 2^32-1 edges\n", fname);
+        fclose(f);
+        return NULL;
+    }
     uint32_t n = (uint32_t)((size_t)bytes / rec);
     struct EdgeList *e = newEdgeList(n, 0, weighted);
     uint32_t *buf = (uint32_t *)xmalloc((size_t)bytes + 16);
@@ -134,23 +140,42 @@ struct EdgeList *readEdgeListsText(const char *fname, int weighted)
         fprintf(stderr, "readEdgeListsText: cannot open %s: %s\n", fname, strerror(errno));
         return NULL;
     }
-    uint32_t cap = 1024, n = 0;
+    /* one edge per line: "src dst" or "src dst weight"; lines that do not
+     * start with two numbers (comments, headers, blank lines) are skipped */
+    size_t cap = 1024;
+    uint32_t n = 0;
     uint32_t *s = (uint32_t *)malloc(cap * 4), *d = (uint32_t *)malloc(cap * 4);
     float *w = weighted ? (float *)malloc(cap * 4) : NULL;
+    int ok = s && d && (!weighted || w);
     char line[512];
-    while (fgets(line, sizeof line, f))
+    while (ok && fgets(line, sizeof line, f))
     {
         unsigned long a, b;
         double c = 1.0;
         int got = sscanf(line, "%lu %lu %lf", &a, &b, &c);
         if (got < 2)
             continue;
+        if (n == 0xffffffffu)
+        {
+            fprintf(stderr, "readEdgeListsText: %s: more than 2^32-1 edges\n", fname);
+            ok = 0;
+            break;
+        }
         if (n == cap)
         {
             cap *= 2;
-            s = (uint32_t *)realloc(s, cap * 4);
-            d = (uint32_t *)realloc(d, cap * 4);
-            if (w) w = (float *)realloc(w, cap * 4);
+            uint32_t *s2 = (uint32_t *)realloc(s, cap * 4);
+            if (s2) s = s2;
+            uint32_t *d2 = (uint32_t *)realloc(d, cap * 4);
+            if (d2) d = d2;
+            float *w2 = w ? (float *)realloc(w, cap * 4) : NULL;
+            if (w2) w = w2;
+            if (!s2 || !d2 || (weighted && !w2))
+            {
+                fprintf(stderr, "readEdgeListsText: %s: out of memory\n", fname);
+                ok = 0;
+                break;
+            }
         }
         s[n] = (uint32_t)a;
         d[n] = (uint32_t)b;
@@ -158,7 +183,7 @@ struct EdgeList *readEdgeListsText(const char *fname, int weighted)
         n++;
     }
     fclose(f);
-    struct EdgeList *e = newEdgeList(n, 0, weighted);
+    struct EdgeList *e = ok ? newEdgeList(n, 0, weighted) : NULL;
     if (e)
     {
         memcpy(e->edges_array_src, s, (size_t)n * 4);

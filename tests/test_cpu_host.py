@@ -213,3 +213,36 @@ def test_cc_host_helpers_and_verify(gg, orc):
         assert L.connectedComponentsVerifyGraphCSR(st, g.ptr) == 0
     finally:
         L.freeCCStats(st)
+
+
+def test_text_loader_skips_comments_and_defaults_weights(gg, tmp_path):
+    """Text edge lists: comment and header lines are skipped, a missing
+    weight column reads as 1, and more edges than the first buffer holds
+    (1024) are kept in order."""
+    lines = ["# a comment", "% a header", ""]
+    rng = np.random.default_rng(1)
+    src = rng.integers(0, 500, 3000)
+    dst = rng.integers(0, 500, 3000)
+    for k, (a, b) in enumerate(zip(src, dst)):
+        lines.append(f"{a} {b} {k % 7 + 1}" if k % 2 else f"{a} {b}")
+    (tmp_path / "g.txt").write_text("\n".join(lines) + "\n")
+    L = gg.lib()
+    el = L.readEdgeListsText(str(tmp_path / "g.txt").encode(), 1)
+    assert el
+    try:
+        e = el.contents
+        assert e.num_edges == 3000 and e.num_vertices == int(max(src.max(), dst.max())) + 1
+        got_s = np.ctypeslib.as_array(e.edges_array_src, (3000,))
+        got_w = np.ctypeslib.as_array(e.edges_array_weight, (3000,))
+        np.testing.assert_array_equal(got_s, src.astype(np.uint32))
+        want_w = np.array([(k % 7 + 1) if k % 2 else 1 for k in range(3000)], np.float32)
+        np.testing.assert_array_equal(got_w, want_w)
+    finally:
+        L.freeEdgeList(el)
+
+
+def test_binary_loader_rejects_truncated_files(gg, tmp_path):
+    np.arange(7, dtype=np.uint32).tofile(tmp_path / "odd.bin")  # 28 bytes: not whole (src, dst) pairs
+    assert not gg.lib().readEdgeListsbin(str(tmp_path / "odd.bin").encode(), 0)
+    np.arange(8, dtype=np.uint32).tofile(tmp_path / "odd.wbin")  # 32 bytes: not whole triples
+    assert not gg.lib().readEdgeListsbin(str(tmp_path / "odd.wbin").encode(), 1)
