@@ -246,3 +246,19 @@ def test_binary_loader_rejects_truncated_files(gg, tmp_path):
     assert not gg.lib().readEdgeListsbin(str(tmp_path / "odd.bin").encode(), 0)
     np.arange(8, dtype=np.uint32).tofile(tmp_path / "odd.wbin")  # 32 bytes: not whole triples
     assert not gg.lib().readEdgeListsbin(str(tmp_path / "odd.wbin").encode(), 1)
+
+
+def test_every_header_compiles_alone_as_c(tmp_path):
+    """Each public header is self-contained C (a reference-side caller can
+    include any one of them first), with no warnings."""
+    import subprocess
+
+    inc = os.path.join(ROOT, "include")
+    for h in sorted(os.listdir(inc)):
+        if not h.endswith(".h"):
+            continue
+        src = tmp_path / "inc.c"
+        src.write_text(f'#include "{h}"\nint main(void) {{ return 0; }}\n')
+        r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", "-I", inc, "-c", str(src), "-o",
+                            str(tmp_path / "inc.o")], capture_output=True, text=True)
+        assert r.returncode == 0, (h, r.stderr)
