@@ -144,7 +144,11 @@ typedef struct gg_pr_params
 } gg_pr_params;
 
 /* Run the whole call (initialisation, every iteration, normalisation) as
- * one CUDA graph launch; per-launch timing (profile) is not available then. */
+ * one CUDA graph launch; per-launch timing (profile) is not available then.
+ * The instantiated graph stays with the mapping: a later call with the same
+ * parameters relaunches it, unless device memory of the mapping has been
+ * freed since (another algorithm regrowing a shared work buffer), in which
+ * case it is captured again. */
 #define GG_PR_CUDA_GRAPH 0x1u
 /* The pull gather of the FP32/BF16/FP16 modes serves the contributions of
  * the 16K vertices with the most out-edges from a shared-memory table (built
