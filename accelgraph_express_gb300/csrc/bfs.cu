@@ -11,11 +11,15 @@
  *         vertices above TD_HEAVY out-edges go to k_td_heavy, which spreads
  *         their edges over the whole grid
  *   k_bu  bottom-up step (BFS.c:752-803): one warp per 32-vertex bitmap word;
- *         each unvisited lane checks its first in-neighbours alone, longer
- *         lists are scanned by the whole warp 32 at a time with a ballot, so
- *         the parent is the first in-CSC neighbour in the frontier as in the
- *         reference; the warp owns its words of the next-frontier and visited
- *         bitmaps and writes them without atomics
+ *         each unvisited lane checks its first 4 in-neighbours alone, the
+ *         lanes still searching then scan the rest of their lists together,
+ *         32 candidates per round with a ballot, so the parent is the first
+ *         in-CSC neighbour in the frontier as in the reference; the warp owns
+ *         its words of the next-frontier and visited bitmaps and writes them
+ *         without atomics
+ *   k_bfs_init  parents, distances, the visited bitmap (vertices without
+ *         in-edges start visited), the source, and the device loop's
+ *         control block and first bitmap cleared, in one pass
  *   k_compact  bitmap -> queue (block-wide scan, one atomic per block pass)
  * Step counters are added and read once per block, not per warp: atomics
  * and loads of one address from every warp queue at one L2 slice.
