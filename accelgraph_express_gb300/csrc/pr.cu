@@ -21,6 +21,12 @@
  *
  * Storage: contributions in FP32, BF16 or FP16 (FP32 accumulation), or in
  * the fixed-point / quantised integer formats summed exactly in 64 bits.
+ *
+ * From 1M vertices the FP pull gather reads the contributions of the
+ * vertices with the most out-edges from a shared-memory table
+ * (k_pr_pull_hot, table built by hot.cu).  With GG_PR_CUDA_GRAPH the whole
+ * call is captured once into a CUDA graph kept on the mapping and relaunched
+ * by later calls with the same parameters.
  */
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
