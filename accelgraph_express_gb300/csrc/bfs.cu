@@ -908,6 +908,7 @@ extern "C" gg_status gg_bfs_device_results(const gg_graph *g, const int32_t **pa
 extern "C" gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parents, uint32_t *distances,
                             gg_bfs_result *r, void *stream)
 {
+    GgRange range("gg_bfs");
     if (!g || !p) return gg_fail(GG_ERR_INVALID, "NULL argument");
     if (p->mode > 4) return gg_fail(GG_ERR_INVALID, "unknown BFS mode");
     if (p->source >= g->V) return gg_fail(GG_ERR_INVALID, "source out of range");

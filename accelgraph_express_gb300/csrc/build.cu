@@ -456,6 +456,7 @@ gg_status build_csc_from_csr(gg_graph *g, SortBufs &B, uint32_t **off, uint32_t 
 gg_status gg_build_arrays(gg_graph *g, const uint32_t *src, const uint32_t *dst, const float *w, uint32_t what,
                           cudaStream_t s)
 {
+    GgRange range("gg_build_csr");
     const uint32_t V = g->V, E = g->E;
     if (V == 0) return gg_fail(GG_ERR_INVALID, "a graph needs at least one vertex");
     /* weights given and asked for; without given weights a _W request gets
@@ -695,6 +696,7 @@ struct Scratch
 gg_status gg_relabel_device(gg_graph *g, uint32_t V, uint64_t E, const uint32_t *src, const uint32_t *dst,
                             uint32_t mode, uint64_t seed, uint32_t *label, cudaStream_t s)
 {
+    GgRange range("gg_relabel");
     if (mode > 10) return gg_fail(GG_ERR_INVALID, "relabelling mode must be 0..10 (11 takes labels from the caller)");
     Scratch degs(g), keys(g), tmp(g), counts(g), sums(g), flag(g);
     GG_CHECK(degs.alloc((size_t)V * 8 + 64));

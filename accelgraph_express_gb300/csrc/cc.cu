@@ -287,6 +287,7 @@ gg_status until_stable(Cc &C, uint32_t max_iterations, bool with_compress, uint3
 
 extern "C" gg_status gg_cc(gg_graph *g, const gg_cc_params *p, uint32_t *components, gg_cc_result *r, void *stream)
 {
+    GgRange range("gg_cc");
     if (!g || !p) return gg_fail(GG_ERR_INVALID, "NULL argument");
     if (p->algorithm > 2) return gg_fail(GG_ERR_INVALID, "unknown connected-components algorithm");
     if (!g->out_off) return gg_fail(GG_ERR_INVALID, "connected components need GG_MAP_OUT");

@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <cstdint>
 #include <cstddef>
 #include <string>
@@ -144,6 +145,16 @@ gg_status gg_hot_prepare(gg_graph *g, cudaStream_t s, uint32_t cap);
 cudaStream_t gg_stream(gg_graph *g, void *user_stream);
 /* host wait on all work queued on `s`, bounded by the wait limit */
 gg_status gg_wait(cudaStream_t s);
+
+/* an NVTX range for the lifetime of a scope: each entry point is one named
+ * range in Nsight timelines (a no-op while no tool is attached) */
+struct GgRange
+{
+    explicit GgRange(const char *name) { nvtxRangePushA(name); }
+    ~GgRange() { nvtxRangePop(); }
+    GgRange(const GgRange &) = delete;
+    GgRange &operator=(const GgRange &) = delete;
+};
 /* host -> device copy; pageable sources go through page-locked staging
  * filled by all host threads (returns with the copy queued on s) */
 gg_status gg_copy_h2d(void *dst, const void *src, size_t bytes, cudaStream_t s);

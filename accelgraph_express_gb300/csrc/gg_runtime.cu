@@ -478,6 +478,7 @@ gg_status gg_graph_new(uint32_t V, uint32_t E, gg_graph **out)
 
 extern "C" gg_status gg_graph_map(const struct GraphCSR *graph, uint32_t what, void *stream, gg_graph **out)
 {
+    GgRange range("gg_graph_map");
     if (!out) return gg_fail(GG_ERR_INVALID, "out is NULL");
     *out = nullptr;
     if (!graph) return gg_fail(GG_ERR_INVALID, "graph is NULL");

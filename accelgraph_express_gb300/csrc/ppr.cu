@@ -360,6 +360,7 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
 extern "C" gg_status gg_ppr(gg_graph *g, const gg_ppr_params *p, const uint32_t *seed_off, const uint32_t *seeds,
                             float *ranks, gg_ppr_result *r, void *stream)
 {
+    GgRange range("gg_ppr");
     if (!g || !p || !seed_off) return gg_fail(GG_ERR_INVALID, "NULL argument");
     const uint32_t K = p->num_vectors;
     if (K < 1 || K > 64) return gg_fail(GG_ERR_INVALID, "num_vectors must be 1..64");

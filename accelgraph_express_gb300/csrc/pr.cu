@@ -896,6 +896,7 @@ gg_status pagerank_enqueue(Run &R, const gg_pr_params *p, IterRec *rec, float *r
 gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_result *r, void *stream,
                         uint32_t ngraphs, const uint32_t *h_voff)
 {
+    GgRange range(ngraphs ? "gg_pagerank_batch" : "gg_pagerank");
     if (!g || !p) return gg_fail(GG_ERR_INVALID, "NULL argument");
     if (p->mode > 13) return gg_fail(GG_ERR_INVALID, "unknown PageRank mode");
     if (p->storage > 2) return gg_fail(GG_ERR_INVALID, "unknown storage");

@@ -315,6 +315,7 @@ gg_status spmv_fp(gg_graph *g, const gg_spmv_params *p, const float *x_dev, floa
 extern "C" gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *x, float *x_out, float *y,
                              gg_spmv_result *r, void *stream)
 {
+    GgRange range("gg_spmv");
     if (!g || !p) return gg_fail(GG_ERR_INVALID, "NULL argument");
     if (p->mode > 3) return gg_fail(GG_ERR_INVALID, "unknown SpMV mode");
     if (p->storage > 2) return gg_fail(GG_ERR_INVALID, "unknown storage");
