@@ -27,7 +27,10 @@ def fixture_edges():
 
 def special_edges():
     """Edge cases: a hub whose in- and out-lists span many merge-path tiles,
-    isolated vertices, self loops, duplicates, a chain, a single edge."""
+    isolated vertices, self loops, duplicates, a chain, a single edge, a
+    directed ring (4096 levels from any source, every contribution equal:
+    direction-optimised BFS drains its edge budget one edge per level and
+    turns bottom-up near the end), and a graph without edges."""
     rng = np.random.default_rng(7)
     V = 5000
     hub_in = np.stack([rng.integers(0, V, 9000), np.zeros(9000, np.int64)], 1)      # in-degree 9000 at 0
@@ -41,4 +44,6 @@ def special_edges():
         "single": (np.array([0], np.uint32), np.array([1], np.uint32), None, 2),
         "star_out": (np.zeros(4000, np.uint32), np.arange(1, 4001, dtype=np.uint32), None, 4001),
         "star_in": (np.arange(1, 4001, dtype=np.uint32), np.zeros(4000, np.uint32), None, 4001),
+        "ring": (np.arange(4096, dtype=np.uint32), (np.arange(1, 4097) % 4096).astype(np.uint32), None, 4096),
+        "no_edges": (np.zeros(0, np.uint32), np.zeros(0, np.uint32), None, 64),
     }

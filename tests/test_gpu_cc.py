@@ -94,6 +94,16 @@ def test_cc_named_entry_points(gpu):
         np.testing.assert_array_equal(comp, gold, err_msg=fn)
 
 
+@pytest.mark.parametrize("algorithm", ["sv", "afforest", "weakly"])
+def test_cc_no_edges(gpu, algorithm):
+    """Every vertex is its own component."""
+    g = gpu.Graph.from_edges(np.zeros(0, np.uint32), np.zeros(0, np.uint32), num_vertices=100)
+    dg = gpu.DeviceGraph(g, gpu.MAP_OUT | gpu.MAP_IN)
+    comp, r = dg.cc(algorithm)
+    np.testing.assert_array_equal(comp, np.arange(100, dtype=np.uint32))
+    assert r["components"] == 100
+
+
 def test_cc_invalid(gpu):
     g, _ = _graph(gpu, "rmat10")
     dg = gpu.DeviceGraph(g, gpu.MAP_IN)
