@@ -3,7 +3,8 @@
 Run in a tree where the reference snapshot is mounted (default
 /root/reference, or $ACCELGRAPH_REFERENCE):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # everything
+    python tests/golden/make_golden.py ring hubs  # only the golden files of those graphs
 
 It writes
   fixtures.npz  the reference's fixture graphs (04_test_graphs/TEST/*), as
@@ -11,8 +12,9 @@ It writes
   golden_*.npz  outputs of the reference's own pageRank.c / BFS.c / SPMV.c,
                 compiled from the reference sources by oracle/build_ref.sh
                 (FPGA-offloaded loops replaced by the compute-unit emulation
-                in oracle/ref_shim/ref_capi_emu.c), on those fixtures and on
-                small seeded R-MAT graphs, run with one OpenMP thread.
+                in oracle/ref_shim/ref_capi_emu.c), on those fixtures, on
+                small seeded R-MAT graphs and on the edge-case graphs of
+                tests/graphs.py (special_edges), run with one OpenMP thread.
 The GPU machine has no reference tree; the tests read these files there.
 """
 import os
@@ -25,6 +27,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from oracle import oracle_ctypes as O  # noqa: E402
+
+sys.path.insert(0, os.path.dirname(HERE))
+from graphs import special_edges  # noqa: E402
 
 REF = os.environ.get("ACCELGRAPH_REFERENCE", "/root/reference")
 TEST = os.path.join(REF, "04_test_graphs", "TEST")
@@ -52,7 +57,7 @@ def sources(V):
     return sorted({0, 1, V // 2, V - 1})
 
 
-def main():
+def main(only):
     if O.ref_lib() is None:
         sys.exit("the reference could not be built (is the reference tree mounted?)")
     fx = {}
@@ -64,11 +69,16 @@ def main():
             fx[name + "_w"] = w
         V = int(max(s.max(), d.max())) + 1
         graphs[name] = O.Csr(V, s, d, w)
-    np.savez_compressed(os.path.join(HERE, "fixtures.npz"), **fx)
+    if not only:
+        np.savez_compressed(os.path.join(HERE, "fixtures.npz"), **fx)
     for name, (scale, ef) in RMAT.items():
         graphs[name] = O.rmat_csr(scale, ef, weighted=True, symmetric=name.endswith("u"))
+    for name, (s, d, w, V) in special_edges().items():
+        graphs[name] = O.Csr(V, s, d, w)
 
     for name, g in graphs.items():
+        if only and name not in only:
+            continue
         out = {"V": np.uint32(g.V), "E": np.uint32(g.E)}
         for mode in range(14):
             r, info = O.ref_pagerank(g, mode, PR_ITERS, PR_EPS)
@@ -96,4 +106,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(set(sys.argv[1:]))

@@ -6,9 +6,10 @@ import os
 import numpy as np
 import pytest
 
-from graphs import GOLDEN, fixture_edges
+from graphs import GOLDEN, fixture_edges, special_edges
 
-NAMES = ["graphbrew", "test", "v51_e1021", "v300_e2730", "rmat8", "rmat10", "rmat12u"]
+SPECIAL = ["hubs", "single", "star_out", "star_in", "ring", "no_edges"]
+NAMES = ["graphbrew", "test", "v51_e1021", "v300_e2730", "rmat8", "rmat10", "rmat12u"] + SPECIAL
 RMAT = {"rmat8": (8, 8, False), "rmat10": (10, 16, False), "rmat12u": (12, 8, True)}
 
 
@@ -17,6 +18,9 @@ def _graph(orc, name, weighted=True):
         s, e, sym = RMAT[name]
         src, dst, w = orc.rmat_edges(s, e, weighted=weighted, symmetric=sym)
         return orc.Csr(1 << s, src, dst, w)
+    if name in SPECIAL:
+        src, dst, w, V = special_edges()[name]
+        return orc.Csr(V, src, dst, w if weighted else None)
     src, dst, w = fixture_edges()[name]
     V = int(max(src.max(), dst.max())) + 1
     return orc.Csr(V, src, dst, w if weighted else None)

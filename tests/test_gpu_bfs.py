@@ -61,7 +61,8 @@ def test_bfs_modes_vs_oracle(graphs, dgs, orc, mode):
                 assert np.array_equal(np.where(levels >= 0, levels, 0), dist), tag
 
 
-@pytest.mark.parametrize("name", ["graphbrew", "test", "v51_e1021", "v300_e2730", "rmat8", "rmat10", "rmat12u"])
+@pytest.mark.parametrize("name", ["graphbrew", "test", "v51_e1021", "v300_e2730", "rmat8", "rmat10", "rmat12u",
+                                  "hubs", "single", "star_out", "star_in", "ring", "no_edges"])
 def test_bfs_vs_reference_golden(graphs, dgs, name):
     """Against the reference's own BFS.c (tests/golden)."""
     z = np.load(os.path.join(GOLDEN, f"golden_{name}.npz"))

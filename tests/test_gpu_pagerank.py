@@ -83,7 +83,8 @@ def test_pagerank_modes_vs_oracle(graphs, dgs, orc, mode):
             assert abs(res["error_total"] - info["error_total"]) <= 1e-9 * max(info["error_total"], 1e-12) + 1e-15
 
 
-@pytest.mark.parametrize("name", ["graphbrew", "test", "v51_e1021", "v300_e2730", "rmat8", "rmat10", "rmat12u"])
+@pytest.mark.parametrize("name", ["graphbrew", "test", "v51_e1021", "v300_e2730", "rmat8", "rmat10", "rmat12u",
+                                  "hubs", "single", "star_out", "star_in", "ring", "no_edges"])
 def test_pagerank_vs_reference_golden(graphs, dgs, orc, name):
     """Against outputs of the reference's own pageRank.c (tests/golden)."""
     z = np.load(os.path.join(GOLDEN, f"golden_{name}.npz"))
