@@ -80,28 +80,60 @@ void compressNodes(uint32_t num_vertices, uint32_t *components)
     }
 }
 
-/* counts[label] = component size; labels = ids by descending count, ties
- * by ascending id (a counting sort on the count) */
-static void fill_counts(struct CCStats *s)
+/* The arrays the reference's printCCStats leaves (connectedComponents.c:
+ * 168-200), which its CSR algorithms call on return (:463, :621, :716):
+ * counts[label] = size of that component, then the (count, id) pairs sorted
+ * by ascending count with the ids in labels, so the largest component ends
+ * at index V - 1.  The reference sorts with OpenGraph's
+ * radixSortEdgesByDegree (absent): restated as a stable counting sort on
+ * the count, ties in ascending id.  Each call starts again from the
+ * component array, so a second call gives the same arrays.  Returns the
+ * number of components. */
+static uint32_t fill_counts(struct CCStats *s)
 {
     const uint32_t V = s->num_vertices;
-    memset(s->counts, 0, (size_t)V * 4);
-    for (uint32_t v = 0; v < V; v++)
-        s->counts[s->components[v]]++;
+    uint32_t *size = (uint32_t *)calloc((size_t)V + 1, 4);
     uint32_t *start = (uint32_t *)calloc((size_t)V + 2, 4);
-    if (!start) return;
-    for (uint32_t v = 0; v < V; v++)
-        start[V - s->counts[v]]++; /* key V - count: ascending key = descending count */
-    uint32_t run = 0;
-    for (uint32_t k = 0; k <= V; k++)
+    if (!size || !start)
     {
-        const uint32_t c = start[k];
-        start[k] = run;
-        run += c;
+        free(size);
+        free(start);
+        return 0;
     }
     for (uint32_t v = 0; v < V; v++)
-        s->labels[start[V - s->counts[v]]++] = v;
+        if (s->components[v] < V) size[s->components[v]]++;
+    uint32_t n = 0;
+    for (uint32_t v = 0; v < V; v++)
+    {
+        n += size[v] != 0;
+        start[size[v] + 1]++;
+    }
+    for (uint32_t k = 0; k <= V; k++) /* start[k] = ids whose count is below k */
+        start[k + 1] += start[k];
+    for (uint32_t v = 0; v < V; v++)
+    {
+        const uint32_t pos = start[size[v]]++;
+        s->counts[pos] = size[v];
+        s->labels[pos] = v;
+    }
+    free(size);
     free(start);
+    return n;
+}
+
+/* the reference's table: the five largest components from the end of the
+ * sorted arrays, then the component count (connectedComponents.c:201-215) */
+static void print_top(const struct CCStats *s, uint32_t components)
+{
+    const uint32_t V = s->num_vertices;
+    printf(" -----------------------------------------------------\n");
+    printf("| %-21s | %-27s | \n", "Top Clusters", "Count");
+    printf(" -----------------------------------------------------\n");
+    for (uint32_t k = 0; k < 5 && k < V; k++)
+        printf("| %-21u | %-27u | \n", s->labels[V - 1 - k], s->counts[V - 1 - k]);
+    printf(" -----------------------------------------------------\n");
+    printf("| %-21s | %-27u | \n", "Num Components", components);
+    printf(" -----------------------------------------------------\n");
 }
 
 static struct CCStats *cc_run(struct Arguments *arguments, struct GraphCSR *graph, uint32_t algorithm)
@@ -140,7 +172,7 @@ static struct CCStats *cc_run(struct Arguments *arguments, struct GraphCSR *grap
     }
     stats->iterations = r.iterations;
     stats->time_total = gg_seconds() - t0;
-    fill_counts(stats);
+    const uint32_t ncomp = fill_counts(stats);
     if (gpu_options()->verbose)
     {
         static const char *names[] = {"Shiloach-Vishkin", "Afforest", "Weakly"};
@@ -151,7 +183,7 @@ static struct CCStats *cc_run(struct Arguments *arguments, struct GraphCSR *grap
         printf(" -----------------------------------------------------\n");
         printf("| %-15u | %-15u | %-15f | \n", stats->iterations, r.components, stats->time_total);
         printf(" -----------------------------------------------------\n");
-        printCCStats(stats);
+        print_top(stats, ncomp);
     }
     return stats;
 }
@@ -185,18 +217,7 @@ struct CCStats *connectedComponentsWeaklyGraphCSR(struct Arguments *arguments, s
 void printCCStats(struct CCStats *stats)
 {
     if (!stats) return;
-    const uint32_t V = stats->num_vertices;
-    uint32_t n = 0;
-    for (uint32_t v = 0; v < V; v++)
-        n += stats->counts[v] != 0;
-    printf(" -----------------------------------------------------\n");
-    printf("| %-21s | %-27s | \n", "Top Clusters", "Count");
-    printf(" -----------------------------------------------------\n");
-    for (uint32_t i = 0; i < 5 && i < n; i++)
-        printf("| %-21u | %-27u | \n", stats->labels[i], stats->counts[stats->labels[i]]);
-    printf(" -----------------------------------------------------\n");
-    printf("| %-21s | %-27u | \n", "Num Components", n);
-    printf(" -----------------------------------------------------\n");
+    print_top(stats, fill_counts(stats));
 }
 
 void printComponents(struct CCStats *stats)

@@ -18,10 +18,14 @@
  * the Afforest final link uses the out-edges only; otherwise it also links
  * the in-edges (the reference's DIRECTED build, :538-576).
  *
- * Stats: components (V labels), counts[label] = size of that component
- * (0 for ids that are no label), labels = the vertex ids ordered by
- * descending count, ties by ascending id, so labels[0] is the largest
- * component's label (printCCStats, :168-216, prints the top five).
+ * Stats: components (V labels); counts and labels as the reference's
+ * printCCStats leaves them (:168-200; its CSR algorithms call it on return,
+ * :463, :621, :716): the component sizes sorted ascending in counts, with
+ * the label of each in labels at the same index (ids that label no
+ * component have count 0 and come first; ties in ascending id), so
+ * labels[V-1] is the largest component's label and counts[V-1] its size.
+ * printCCStats recomputes both from components and prints the five
+ * largest.
  */
 
 #include <stdint.h>
@@ -64,7 +68,10 @@ struct CCStats *connectedComponentsShiloachVishkinGraphCSR(struct Arguments *arg
 struct CCStats *connectedComponentsWeaklyGraphCSR(struct Arguments *arguments, struct GraphCSR *graph);
 /* On the host (connectedComponents.c:722-832): every component is closed
  * under the graph's edges in both directions, and labels name a member of
- * their component.  Returns 1 (pass) or 0. */
+ * their component.  Returns 1 (pass) or 0.  The reference's version starts
+ * its flag at 1, clears it on an edge between two labels and prints PASS
+ * when it ends at 0, so it reports a correct labelling as FAIL; this one
+ * returns 1 for a correct labelling. */
 uint32_t connectedComponentsVerifyGraphCSR(struct CCStats *stats, struct GraphCSR *graph);
 
 #ifdef __cplusplus

@@ -215,6 +215,40 @@ def test_cc_host_helpers_and_verify(gg, orc):
         L.freeCCStats(st)
 
 
+def test_cc_stats_arrays_as_the_reference_leaves_them(gg, orc, capfd):
+    """printCCStats (the reference fills counts and labels there): sizes
+    sorted ascending with the label of each beside it, ties by ascending id,
+    the largest component last; a second call gives the same arrays; the
+    table lists the largest component first."""
+    import ctypes as C
+
+    rng = np.random.default_rng(9)
+    V = 700
+    s = rng.integers(0, V, 500).astype(np.uint32)
+    d = rng.integers(0, V, 500).astype(np.uint32)
+    g = gg.Graph.from_edges(s, d, num_vertices=V)
+    a = g.arrays()
+    gold = orc.cc_min_label(orc.Csr.from_arrays(V, g.E, a["out_off"], a["out_adj"], a["in_off"], a["in_adj"]))
+    size = np.bincount(gold, minlength=V).astype(np.uint32)
+    order = np.argsort(size, kind="stable").astype(np.uint32)
+    L = gg.lib()
+    st = L.newCCStatsGraphCSR(g.ptr)
+    try:
+        C.memmove(st.contents.components, gold.ctypes.data, V * 4)
+        for _ in range(2):
+            L.printCCStats(st)
+            counts = np.ctypeslib.as_array(st.contents.counts, (V,)).copy()
+            labels = np.ctypeslib.as_array(st.contents.labels, (V,)).copy()
+            np.testing.assert_array_equal(labels, order)
+            np.testing.assert_array_equal(counts, size[order])
+        C.CDLL(None).fflush(None)  # the table went through C stdio
+        out = capfd.readouterr().out
+        assert f"| {int(order[-1]):<21} | {int(size.max()):<27} |" in out
+        assert f"| {'Num Components':<21} | {int((size > 0).sum()):<27} |" in out
+    finally:
+        L.freeCCStats(st)
+
+
 def test_text_loader_skips_comments_and_defaults_weights(gg, tmp_path):
     """Text edge lists: comment and header lines are skipped, a missing
     weight column reads as 1, and more edges than the first buffer holds
