@@ -158,7 +158,8 @@ static struct CCStats *cc_run(struct Arguments *arguments, struct GraphCSR *grap
     p.algorithm = algorithm;
     p.neighbor_rounds = stats->neighbor_rounds;
     /* connectedComponents.c:475-479: 1024 samples, V / 2 on small graphs */
-    p.samples = V < 1024 ? (V / 2 ? V / 2 : 1) : 1024;
+    const uint32_t samples = V < 1024 ? V / 2 : 1024;
+    p.samples = samples ? samples : 1;
     p.use_in_edges = symmetric ? 0 : 1;
     p.seed = CC_SEED;
     gg_cc_result r;
@@ -170,6 +171,12 @@ static struct CCStats *cc_run(struct Arguments *arguments, struct GraphCSR *grap
         freeCCStats(stats);
         return NULL;
     }
+    /* the reference's Afforest draws its samples from the caller's
+     * generator (sampleFrequentNode, :293-302, called at :535); the device
+     * draws its own, and the caller's generator advances by the same count */
+    if (algorithm == GG_CC_AFFOREST)
+        for (uint32_t i = 0; i < samples; i++)
+            generateRandInt(&arguments->mt19937var);
     stats->iterations = r.iterations;
     stats->time_total = gg_seconds() - t0;
     const uint32_t ncomp = fill_counts(stats);

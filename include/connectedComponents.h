@@ -16,7 +16,10 @@
  * propagation rounds (Afforest: neighbor_rounds), which depends on the order
  * of concurrent updates, as in the reference.  With arguments->symmetric set
  * the Afforest final link uses the out-edges only; otherwise it also links
- * the in-edges (the reference's DIRECTED build, :538-576).
+ * the in-edges (the reference's DIRECTED build, :538-576).  Afforest
+ * advances arguments->mt19937var by its sample count (1024, or V / 2 below
+ * 1024 vertices), as the reference's host sampling does (:293-302, :535);
+ * the samples themselves are drawn on the device.
  *
  * Stats: components (V labels); counts and labels as the reference's
  * printCCStats leaves them (:168-200; its CSR algorithms call it on return,

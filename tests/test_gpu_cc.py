@@ -5,6 +5,8 @@ weakly connected components), through gg_cc and the reference's drop-in
 entry points."""
 import os
 
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -79,6 +81,13 @@ def test_cc_dropin(gpu, pushpull):
         args.pushpull = pushpull
         comp, counts, labels, info, ok = gpu.cc_csr(g, args, verify=True)
         np.testing.assert_array_equal(comp, gold, err_msg=name)
+        # Afforest (pushpull 1 and the default) advances the caller's
+        # generator by its sample count, as the reference's sampling does
+        fresh = gpu.default_arguments()
+        draws = (1024 if g.V >= 1024 else g.V // 2) if pushpull in (1, 3) else 0
+        for _ in range(draws):
+            gpu.lib().generateRandInt(C.byref(fresh.mt19937var))
+        assert bytes(fresh.mt19937var) == bytes(args.mt19937var), name
         size = np.bincount(gold, minlength=g.V).astype(np.uint32)
         order = np.argsort(size, kind="stable")
         np.testing.assert_array_equal(labels, order.astype(np.uint32), err_msg=name)
