@@ -13,8 +13,9 @@
  * 1 Afforest, 2 weakly connected components, anything else Afforest.
  * Every algorithm labels each vertex with the smallest vertex id of its
  * weakly connected component; `iterations` is the number of hook or
- * propagation rounds (Afforest: neighbor_rounds), which depends on the order
- * of concurrent updates, as in the reference.  With arguments->symmetric set
+ * propagation rounds, which depends on the order of concurrent updates, as
+ * in the reference; Afforest leaves it 0 as the reference's does (its table
+ * reports neighbor_rounds instead).  With arguments->symmetric set
  * the Afforest final link uses the out-edges only; otherwise it also links
  * the in-edges (the reference's DIRECTED build, :538-576).  Afforest
  * advances arguments->mt19937var by its sample count (1024, or V / 2 below

@@ -94,6 +94,10 @@ def test_cc_dropin(gpu, pushpull):
         np.testing.assert_array_equal(counts, size[order], err_msg=name)
         assert ok == 1
         assert info["neighbor_rounds"] == 2
+        if pushpull in (1, 3):
+            assert info["iterations"] == 0  # the reference's Afforest never counts them
+        else:
+            assert info["iterations"] >= 1
 
 
 def test_cc_named_entry_points(gpu):
