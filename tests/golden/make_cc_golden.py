@@ -1,8 +1,9 @@
 """Golden connected-component labels for tests/golden/golden_cc.npz.
 
-The reference has no outputs to pin connected components against (its CSR
-stats constructor, connectedComponents.c:52-60, leaves the label arrays
-unset), so the labels come from an independent implementation:
+The reference's connectedComponents.c cannot be compiled without Judy
+arrays (Judy.h), OpenGraph's sort and the FPGA's Shiloach-Vishkin unit, none
+of which are available, so the labels come from an independent
+implementation:
 scipy.sparse.csgraph.connected_components with connection="weak", turned
 into the labelling every reference algorithm converges to -- the smallest
 vertex id of each weakly connected component.
