@@ -18,14 +18,14 @@ mkdir -p "$OUT"
 CC="${CC:-gcc}"
 FLAGS="-O2 -fPIC -std=gnu11 -ffp-contract=off -fopenmp -w"
 INCS="-I$HERE/ref_shim -I$INC/config -I$INC/algorithms/capi -I$INC/capi_utils"
-for f in pageRank BFS SPMV; do
+for f in pageRank BFS SPMV connectedComponents; do
     $CC $FLAGS $INCS -c "$SRC/$f.c" -o "$OUT/$f.o"
 done
 for f in ref_utils ref_capi_emu ref_harness; do
     $CC $FLAGS $INCS -c "$HERE/ref_shim/$f.c" -o "$OUT/$f.o"
 done
 $CC -shared -fopenmp -Wl,--no-undefined -o "$OUT/libref.so" \
-    "$OUT/pageRank.o" "$OUT/BFS.o" "$OUT/SPMV.o" \
+    "$OUT/pageRank.o" "$OUT/BFS.o" "$OUT/SPMV.o" "$OUT/connectedComponents.o" \
     "$OUT/ref_utils.o" "$OUT/ref_capi_emu.o" "$OUT/ref_harness.o" -lm
 rm -f "$OUT"/*.o
 echo "built $OUT/libref.so"

@@ -13,6 +13,8 @@ struct ArrayQueue *newArrayQueue(uint32_t size);
 void freeArrayQueue(struct ArrayQueue *q);
 void resetArrayQueue(struct ArrayQueue *q);
 void enArrayQueue(struct ArrayQueue *q, uint32_t k);
+void enArrayQueueWithBitmap(struct ArrayQueue *q, uint32_t k);
+void softResetArrayQueue(struct ArrayQueue *q);
 uint32_t deArrayQueue(struct ArrayQueue *q);
 void slideWindowArrayQueue(struct ArrayQueue *q);
 uint32_t sizeArrayQueue(struct ArrayQueue *q);

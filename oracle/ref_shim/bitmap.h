@@ -1,6 +1,7 @@
 #ifndef SHIM_BITMAP_H
 #define SHIM_BITMAP_H
 #include <stdint.h>
+#define kBitsPerWord 32 /* bits per bitarray word */
 struct Bitmap { uint32_t size; uint32_t numSetBits; uint32_t *bitarray; };
 struct Bitmap *newBitmap(uint32_t size);
 void freeBitmap(struct Bitmap *b);

@@ -13,7 +13,14 @@
 #include "pageRank.h"
 #include "BFS.h"
 #include "SPMV.h"
+#include "connectedComponents.h"
+#include "Judy.h"
 #include "ref_emu.h"
+
+/* the reference's sample table (connectedComponents.c:44); only its
+ * Afforest frees it, so the harness frees it after every call: a later
+ * call on a smaller graph would otherwise index counts with old keys */
+extern Pvoid_t JArray;
 
 static int g_quiet = 1;
 void ref_set_quiet(int q) { g_quiet = q; }
@@ -152,6 +159,41 @@ int ref_spmv(int mode, uint32_t V, uint32_t E, const uint32_t *out_off, const ui
     memcpy(x, s->vector_input, (size_t)V * sizeof(float));
     memcpy(y, s->vector_output, (size_t)V * sizeof(float));
     freeSPMVStats(s);
+    release(&o);
+    return 0;
+}
+
+/* connected components through the reference's connectedComponentsGraphCSR:
+ * mode (pushpull) 1 Afforest, 2 weakly.  Its Shiloach-Vishkin runs on the
+ * FPGA, whose connected-components unit is not emulated, so mode 0 is
+ * refused.  The generator starts from the reference CLI's seed (27491095);
+ * its state after the call (624 words, then the index) is copied out. */
+int ref_cc(int mode, uint32_t V, uint32_t E, const uint32_t *out_off, const uint32_t *out_adj,
+           const uint32_t *in_off, const uint32_t *in_adj, uint32_t *components, uint32_t *counts,
+           uint32_t *labels, uint32_t *iterations, uint32_t *neighbor_rounds, uint32_t *mt_out)
+{
+    if (mode != 1 && mode != 2) return -1;
+    omp_set_num_threads(1);
+    owned o;
+    build(&o, V, E, out_off, out_adj, NULL, in_off, in_adj, NULL);
+    struct Arguments a;
+    args_init(&a, (uint32_t)mode, 0, 0.0, 0);
+    initializeMersenneState(&a.mt19937var, 27491095u);
+    ref_emu_cu_kind = REF_CU_NONE;
+    int saved = quiet_begin();
+    struct CCStats *s = connectedComponentsGraphCSR(&a, &o.g);
+    quiet_end(saved);
+    Word_t bytes;
+    JSLFA(bytes, JArray);
+    (void)bytes;
+    memcpy(components, s->components, (size_t)V * sizeof(uint32_t));
+    memcpy(counts, s->counts, (size_t)V * sizeof(uint32_t));
+    memcpy(labels, s->labels, (size_t)V * sizeof(uint32_t));
+    *iterations = s->iterations;
+    *neighbor_rounds = s->neighbor_rounds;
+    memcpy(mt_out, a.mt19937var.mt, sizeof(a.mt19937var.mt));
+    mt_out[624] = (uint32_t)a.mt19937var.mti;
+    freeCCStats(s);
     release(&o);
     return 0;
 }

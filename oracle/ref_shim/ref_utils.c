@@ -1,11 +1,13 @@
 /* This project's implementations of the OpenGraph utilities the reference's
- * CSR algorithm files call (Bitmap, ArrayQueue, Grid stubs).  Test
- * infrastructure only. */
+ * CSR algorithm files call (Bitmap, ArrayQueue, MT19937, the degree sort,
+ * Grid stubs).  Test infrastructure only. */
 #include <stdlib.h>
 #include <string.h>
 #include "bitmap.h"
 #include "arrayQueue.h"
 #include "graphGrid.h"
+#include "mt19937.h"
+#include "reorder.h"
 
 struct Bitmap *newBitmap(uint32_t size)
 {
@@ -88,6 +90,79 @@ void bitmapToArrayQueueDualOrder(struct Bitmap *b, struct ArrayQueue *q, struct 
     for (uint32_t v = 0; v < b->size; v++)
         if (getBit(b, v)) q->queue[q->tail_next++] = labels[v];
     slideWindowArrayQueue(q);
+}
+
+void enArrayQueueWithBitmap(struct ArrayQueue *q, uint32_t k)
+{
+    enArrayQueue(q, k);
+    setBit(q->q_bitmap, k);
+}
+
+/* the window only; the membership bitmap is kept */
+void softResetArrayQueue(struct ArrayQueue *q) { q->head = q->tail = q->tail_next = 0; }
+
+/* MT19937 (Matsumoto and Nishimura, ACM TOMACS 8(1), 1998): the 32-bit
+ * generator with its published initialisation and tempering constants */
+void initializeMersenneState(mt19937state *s, uint32_t seed)
+{
+    s->mt[0] = seed;
+    for (int i = 1; i < 624; i++)
+        s->mt[i] = 1812433253u * (s->mt[i - 1] ^ (s->mt[i - 1] >> 30)) + (uint32_t)i;
+    s->mti = 624;
+}
+
+uint32_t generateRandInt(mt19937state *s)
+{
+    if (s->mti >= 624)
+    {
+        for (int k = 0; k < 624; k++)
+        {
+            const uint32_t y = (s->mt[k] & 0x80000000u) | (s->mt[(k + 1) % 624] & 0x7fffffffu);
+            s->mt[k] = s->mt[(k + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+        }
+        s->mti = 0;
+    }
+    uint32_t y = s->mt[s->mti++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return y;
+}
+
+/* stable sort of the (degree, id) pairs by ascending degree (a counting
+ * sort: equal degrees keep their order), both arrays rewritten in place */
+uint32_t *radixSortEdgesByDegree(uint32_t *degrees, uint32_t *edges, uint32_t n)
+{
+    uint32_t maxd = 0;
+    for (uint32_t i = 0; i < n; i++)
+        if (degrees[i] > maxd) maxd = degrees[i];
+    uint32_t *start = (uint32_t *)calloc((size_t)maxd + 2, sizeof(uint32_t));
+    uint32_t *d2 = (uint32_t *)malloc((size_t)n * sizeof(uint32_t) + 4);
+    uint32_t *e2 = (uint32_t *)malloc((size_t)n * sizeof(uint32_t) + 4);
+    if (!start || !d2 || !e2)
+    {
+        free(start);
+        free(d2);
+        free(e2);
+        return edges;
+    }
+    for (uint32_t i = 0; i < n; i++)
+        start[degrees[i] + 1]++;
+    for (uint32_t k = 0; k <= maxd; k++)
+        start[k + 1] += start[k];
+    for (uint32_t i = 0; i < n; i++)
+    {
+        const uint32_t pos = start[degrees[i]]++;
+        d2[pos] = degrees[i];
+        e2[pos] = edges[i];
+    }
+    memcpy(degrees, d2, (size_t)n * sizeof(uint32_t));
+    memcpy(edges, e2, (size_t)n * sizeof(uint32_t));
+    free(start);
+    free(d2);
+    free(e2);
+    return edges;
 }
 
 /* Grid helpers: only referenced by the Grid variants, which are not run. */

@@ -1,9 +1,8 @@
 """Golden connected-component labels for tests/golden/golden_cc.npz.
 
-The reference's connectedComponents.c cannot be compiled without Judy
-arrays (Judy.h), OpenGraph's sort and the FPGA's Shiloach-Vishkin unit, none
-of which are available, so the labels come from an independent
-implementation:
+The labels come from an independent implementation (the reference's own
+Afforest and weakly variants give a second set, in golden_<graph>.npz from
+make_golden.py; its Shiloach-Vishkin runs on the FPGA and is not emulated):
 scipy.sparse.csgraph.connected_components with connection="weak", turned
 into the labelling every reference algorithm converges to -- the smallest
 vertex id of each weakly connected component.

@@ -9,7 +9,9 @@ Run in a tree where the reference snapshot is mounted (default
 It writes
   fixtures.npz  the reference's fixture graphs (04_test_graphs/TEST/*), as
                 uint32 edge arrays (weights from the .wbin files), and
-  golden_*.npz  outputs of the reference's own pageRank.c / BFS.c / SPMV.c,
+  golden_*.npz  outputs of the reference's own pageRank.c / BFS.c / SPMV.c /
+                connectedComponents.c (Afforest and weakly; Judy arrays
+                from the stand-in oracle/ref_shim/Judy.h),
                 compiled from the reference sources by oracle/build_ref.sh
                 (FPGA-offloaded loops replaced by the compute-unit emulation
                 in oracle/ref_shim/ref_capi_emu.c), on those fixtures, on
@@ -101,6 +103,15 @@ def main(only):
             x, y = O.ref_spmv(gu, mode, SPMV_ITERS)
             out[f"spmv{mode}_x"] = x
             out[f"spmv{mode}_y"] = y
+        # connectedComponents.c through connectedComponentsGraphCSR: 1
+        # Afforest, 2 weakly (its Shiloach-Vishkin runs on the FPGA)
+        for mode in (1, 2):
+            comp, counts, labels, info = O.ref_cc(g, mode)
+            out[f"cc{mode}_components"] = comp
+            out[f"cc{mode}_counts"] = counts
+            out[f"cc{mode}_labels"] = labels
+            out[f"cc{mode}_iterations"] = np.uint32(info["iterations"])
+            out[f"cc{mode}_mt"] = info["mt"]
         np.savez_compressed(os.path.join(HERE, f"golden_{name}.npz"), **out)
         print("wrote", name, g.V, g.E)
 

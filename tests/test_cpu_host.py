@@ -249,6 +249,25 @@ def test_cc_stats_arrays_as_the_reference_leaves_them(gg, orc, capfd):
         L.freeCCStats(st)
 
 
+def test_generator_state_as_the_reference_leaves_it(gg):
+    """The drop-in's MT19937 from the reference CLI's seed, advanced by the
+    reference Afforest's 1024 samples, is the generator state the
+    reference's own connectedComponents.c left (golden, R-MAT-10); its
+    weakly variant draws nothing."""
+    import ctypes as C
+    import os
+
+    from graphs import GOLDEN
+
+    z = np.load(os.path.join(GOLDEN, "golden_rmat10.npz"))
+    a = gg.default_arguments()
+    for _ in range(1024):
+        gg.lib().generateRandInt(C.byref(a.mt19937var))
+    np.testing.assert_array_equal(np.frombuffer(bytes(a.mt19937var), np.uint32), z["cc1_mt"])
+    b = gg.default_arguments()
+    np.testing.assert_array_equal(np.frombuffer(bytes(b.mt19937var), np.uint32), z["cc2_mt"])
+
+
 def test_text_loader_skips_comments_and_defaults_weights(gg, tmp_path):
     """Text edge lists: comment and header lines are skipped, a missing
     weight column reads as 1, and more edges than the first buffer holds

@@ -64,6 +64,24 @@ def test_oracle_spmv_matches_reference_golden(orc, name):
     assert not z["spmv2_y"].any()
 
 
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_cc_matches_reference_golden(orc, name):
+    """The reference's own connectedComponents.c (Afforest and weakly, run
+    by tests/golden/make_golden.py): its labels are the oracle's, and its
+    stats arrays are the component sizes sorted ascending with the label of
+    each beside it (ties in ascending id); its Afforest counts no
+    iterations."""
+    z = np.load(os.path.join(GOLDEN, f"golden_{name}.npz"))
+    want = orc.cc_min_label(_graph(orc, name))
+    size = np.bincount(want, minlength=len(want)).astype(np.uint32)
+    order = np.argsort(size, kind="stable").astype(np.uint32)
+    for mode in (1, 2):
+        np.testing.assert_array_equal(z[f"cc{mode}_components"], want, err_msg=f"{name} {mode}")
+        np.testing.assert_array_equal(z[f"cc{mode}_labels"], order, err_msg=f"{name} {mode}")
+        np.testing.assert_array_equal(z[f"cc{mode}_counts"], size[order], err_msg=f"{name} {mode}")
+    assert int(z["cc1_iterations"]) == 0
+
+
 def test_oracle_vs_reference_live(orc):
     """Fresh random graphs through the reference's compiled code."""
     if orc.ref_lib() is None:

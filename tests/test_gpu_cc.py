@@ -10,7 +10,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from graphs import GOLDEN
+from graphs import GOLDEN, fixture_edges, special_edges
 
 pytestmark = pytest.mark.gpu
 
@@ -98,6 +98,47 @@ def test_cc_dropin(gpu, pushpull):
             assert info["iterations"] == 0  # the reference's Afforest never counts them
         else:
             assert info["iterations"] >= 1
+
+
+REF_NAMES = ["graphbrew", "test", "v51_e1021", "v300_e2730", "rmat8", "rmat10", "rmat12u",
+             "hubs", "single", "star_out", "star_in", "ring", "no_edges"]
+REF_RMAT = {"rmat8": (8, 8, False), "rmat10": (10, 16, False), "rmat12u": (12, 8, True)}
+
+
+def _ref_graph(gpu, name):
+    if name in REF_RMAT:
+        s, e, sym = REF_RMAT[name]
+        return gpu.Graph.rmat(s, e, weighted=True, symmetric=sym)
+    special = special_edges()
+    if name in special:
+        s, d, w, V = special[name]
+        return gpu.Graph.from_edges(s, d, w, num_vertices=V)
+    s, d, w = fixture_edges()[name]
+    return gpu.Graph.from_edges(s, d, w)
+
+
+@pytest.mark.parametrize("name", REF_NAMES)
+def test_cc_dropin_vs_reference_golden(gpu, name):
+    """Against outputs of the reference's own connectedComponents.c
+    (tests/golden/make_golden.py): for Afforest (pushpull 1) and weakly (2)
+    the drop-in leaves the same components, counts and labels, Afforest's
+    iteration count, and the caller's generator in the same state."""
+    gpu.set_gpu_options(keep_resident=False, verbose=False)
+    z = np.load(os.path.join(GOLDEN, f"golden_{name}.npz"))
+    g = _ref_graph(gpu, name)
+    assert int(z["V"]) == g.V and int(z["E"]) == g.E
+    for pushpull in (1, 2):
+        args = gpu.default_arguments()
+        args.pushpull = pushpull
+        comp, counts, labels, info = gpu.cc_csr(g, args)
+        tag = f"{name} pushpull {pushpull}"
+        np.testing.assert_array_equal(comp, z[f"cc{pushpull}_components"], err_msg=tag)
+        np.testing.assert_array_equal(counts, z[f"cc{pushpull}_counts"], err_msg=tag)
+        np.testing.assert_array_equal(labels, z[f"cc{pushpull}_labels"], err_msg=tag)
+        if pushpull == 1:
+            assert info["iterations"] == int(z["cc1_iterations"]), tag
+        np.testing.assert_array_equal(np.frombuffer(bytes(args.mt19937var), np.uint32), z[f"cc{pushpull}_mt"],
+                                      err_msg=tag)
 
 
 def test_cc_named_entry_points(gpu):
