@@ -105,6 +105,10 @@ def test_oracle_vs_reference_live(orc):
             np.testing.assert_array_equal(d, rd)
             np.testing.assert_array_equal(p, rp)
             assert i1["processed_nodes"] == i2["processed_nodes"] and i1["iteration"] == i2["iteration"]
+        want = orc.cc_min_label(g)
+        for mode in (1, 2):
+            comp, _, _, _ = orc.ref_cc(g, mode)
+            np.testing.assert_array_equal(comp, want)
 
 
 def test_oracle_fp64_close_to_fp32(orc):
