@@ -103,7 +103,7 @@ def ref_lib():
         R.ref_spmv.argtypes = [C.c_int, C.c_uint32, C.c_uint32, u32p, u32p, C.c_void_p, u32p, u32p,
                                C.c_void_p, C.c_uint32, f32p, f32p]
         R.ref_cc.argtypes = [C.c_int, C.c_uint32, C.c_uint32, u32p, u32p, u32p, u32p, u32p, u32p, u32p,
-                             C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), u32p]
+                             C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), u32p, C.POINTER(C.c_uint32)]
         R.ref_set_quiet.argtypes = [C.c_int]
         _REF = R
     return _REF
@@ -368,7 +368,8 @@ def ref_spmv(g: Csr, mode=0, iterations=1):
 def ref_cc(g: Csr, mode=1):
     """The reference's connectedComponentsGraphCSR (1 Afforest, 2 weakly):
     components, counts, labels, {iterations, neighbor_rounds, mt: the
-    generator state after the call (624 words, then the index)}."""
+    generator state after the call (624 words, then the index), verify: what
+    the reference's connectedComponentsVerifyGraphCSR returns for it}."""
     R = ref_lib()
     comp = np.empty(g.V, np.uint32)
     counts = np.empty(g.V, np.uint32)
@@ -376,11 +377,13 @@ def ref_cc(g: Csr, mode=1):
     it = C.c_uint32()
     nr = C.c_uint32()
     mt = np.empty(625, np.uint32)
+    ver = C.c_uint32()
     rc = R.ref_cc(mode, g.V, g.E, g.out_off, g.out_adj, g.in_off, g.in_adj, comp, counts, labels,
-                  C.byref(it), C.byref(nr), mt)
+                  C.byref(it), C.byref(nr), mt, C.byref(ver))
     if rc != 0:
         raise ValueError(f"ref_cc mode {mode}")
-    return comp, counts, labels, {"iterations": it.value, "neighbor_rounds": nr.value, "mt": mt}
+    return comp, counts, labels, {"iterations": it.value, "neighbor_rounds": nr.value, "mt": mt,
+                                  "verify": ver.value}
 
 
 # ---------------------------------------------------------------------------

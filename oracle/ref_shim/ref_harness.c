@@ -167,10 +167,13 @@ int ref_spmv(int mode, uint32_t V, uint32_t E, const uint32_t *out_off, const ui
  * mode (pushpull) 1 Afforest, 2 weakly.  Its Shiloach-Vishkin runs on the
  * FPGA, whose connected-components unit is not emulated, so mode 0 is
  * refused.  The generator starts from the reference CLI's seed (27491095);
- * its state after the call (624 words, then the index) is copied out. */
+ * its state after the call (624 words, then the index) is copied out, and
+ * so is what the reference's connectedComponentsVerifyGraphCSR returns for
+ * the result. */
 int ref_cc(int mode, uint32_t V, uint32_t E, const uint32_t *out_off, const uint32_t *out_adj,
            const uint32_t *in_off, const uint32_t *in_adj, uint32_t *components, uint32_t *counts,
-           uint32_t *labels, uint32_t *iterations, uint32_t *neighbor_rounds, uint32_t *mt_out)
+           uint32_t *labels, uint32_t *iterations, uint32_t *neighbor_rounds, uint32_t *mt_out,
+           uint32_t *verify_out)
 {
     if (mode != 1 && mode != 2) return -1;
     omp_set_num_threads(1);
@@ -182,6 +185,7 @@ int ref_cc(int mode, uint32_t V, uint32_t E, const uint32_t *out_off, const uint
     ref_emu_cu_kind = REF_CU_NONE;
     int saved = quiet_begin();
     struct CCStats *s = connectedComponentsGraphCSR(&a, &o.g);
+    *verify_out = connectedComponentsVerifyGraphCSR(s, &o.g);
     quiet_end(saved);
     Word_t bytes;
     JSLFA(bytes, JArray);

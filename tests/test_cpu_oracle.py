@@ -107,8 +107,11 @@ def test_oracle_vs_reference_live(orc):
             assert i1["processed_nodes"] == i2["processed_nodes"] and i1["iteration"] == i2["iteration"]
         want = orc.cc_min_label(g)
         for mode in (1, 2):
-            comp, _, _, _ = orc.ref_cc(g, mode)
+            comp, _, _, info = orc.ref_cc(g, mode)
             np.testing.assert_array_equal(comp, want)
+            # the reference's verify inverts its own flag: a correct
+            # labelling reads FAIL (connectedComponents.c:722-832)
+            assert info["verify"] == 0
 
 
 def test_oracle_fp64_close_to_fp32(orc):
