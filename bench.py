@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--edge-factor", type=int, default=16)
     p.add_argument("--no-extras", action="store_true", help="skip the BF16/BFS/SpMV side measurements")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    p.add_argument("--leg", choices=["c1", "bfs", "ppr", "batch", "serve", "csr", "cc", "relabel"],
+    p.add_argument("--leg", choices=["c1", "bfs", "ppr", "batch", "serve", "csr", "cc", "relabel", "gather"],
                    help="run one side measurement alone and print its JSON (for profiling)")
     return p.parse_args()
 
@@ -238,7 +238,8 @@ def run_leg(leg):
     fn = {"c1": lambda: c1_extras(gg, torch), "bfs": lambda: bfs_extras(gg, torch, peak),
           "ppr": lambda: ppr_extras(gg, torch, peak), "batch": lambda: batch_extras(gg, torch, peak),
           "serve": lambda: serving_extras(gg), "csr": lambda: csr_build_extras(gg, torch, peak),
-          "cc": lambda: cc_extras(gg, torch, peak), "relabel": lambda: relabel_extras(gg, torch, peak)}[leg]
+          "cc": lambda: cc_extras(gg, torch, peak), "relabel": lambda: relabel_extras(gg, torch, peak),
+          "gather": lambda: {"metric": "random 4-byte gathers", "unit": "G/s", **gg.gather_ceiling()}}[leg]
     print(json.dumps({"leg": leg, **fn()}), flush=True)
 
 

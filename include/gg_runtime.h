@@ -363,6 +363,27 @@ gg_status gg_ppr(gg_graph *g, const gg_ppr_params *p, const uint32_t *seed_off, 
  * valid until the next call on `g`. */
 const float *gg_ppr_device_ranks(const gg_graph *g, uint32_t *stride);
 
+/* ---- gather ceilings --------------------------------------------------------- */
+
+/* Random 4-byte gathers per second (G/s) from hashed indices, every thread
+ * summing 4096 values: from the shared memory of 8-CTA clusters (184 KB per
+ * CTA, `clusters` of them resident on `cluster_sms` SMs), from each CTA's
+ * own shared memory, and from global memory through L2 over a 1.5 MB and a
+ * 64 MB array.  The pull gathers read one random value per in-edge, so these
+ * rates are the ceilings of their on-chip tables and of their L2 traffic.
+ * Allocates 64 MB for the call. */
+typedef struct gg_gather_rates
+{
+    double cluster_smem_gps;
+    double own_smem_gps;
+    double l2_small_gps;
+    double l2_large_gps;
+    uint32_t clusters;
+    uint32_t cluster_sms;
+} gg_gather_rates;
+
+gg_status gg_gather_ceiling(gg_gather_rates *rates, void *stream);
+
 /* ---- drop-in side options ---------------------------------------------------- */
 
 /*
