@@ -80,6 +80,42 @@ void compressNodes(uint32_t num_vertices, uint32_t *components)
     }
 }
 
+static int cmp_u32(const void *a, const void *b)
+{
+    const uint32_t x = *(const uint32_t *)a, y = *(const uint32_t *)b;
+    return x < y ? -1 : x > y;
+}
+
+/* connectedComponents.c:293-334: draws num_samples vertices with the
+ * caller's generator (generateRandInt % num_vertices) and returns the label
+ * seen most often among their components, ties to the smallest label (the
+ * reference walks its sample table in ascending label order and keeps the
+ * first maximum).  0 when nothing is sampled. */
+uint32_t sampleFrequentNode(mt19937state *mt19937var, uint32_t num_vertices, uint32_t num_samples,
+                            uint32_t *components)
+{
+    if (!mt19937var || !components || num_vertices == 0 || num_samples == 0) return 0;
+    uint32_t *seen = (uint32_t *)malloc((size_t)num_samples * sizeof(uint32_t));
+    if (!seen) return 0;
+    for (uint32_t i = 0; i < num_samples; i++)
+        seen[i] = components[generateRandInt(mt19937var) % num_vertices];
+    qsort(seen, num_samples, sizeof(uint32_t), cmp_u32);
+    uint32_t best = 0, best_count = 0;
+    for (uint32_t i = 0; i < num_samples;)
+    {
+        uint32_t j = i;
+        while (j < num_samples && seen[j] == seen[i]) j++;
+        if (j - i > best_count)
+        {
+            best_count = j - i;
+            best = seen[i];
+        }
+        i = j;
+    }
+    free(seen);
+    return best;
+}
+
 /* The arrays the reference's printCCStats leaves (connectedComponents.c:
  * 168-200), which its CSR algorithms call on return (:463, :621, :716):
  * counts[label] = size of that component, then the (count, id) pairs sorted

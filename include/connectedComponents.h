@@ -5,8 +5,9 @@
  * Connected components on CSR: the reference's public API for this kernel
  * (02_capi_graph/include/algorithms/capi/connectedComponents.h:21-66),
  * implemented on one GB300 GPU.  Only the CSR members exist; the Grid and
- * list members are not part of the drop-in, nor are the Judy-array sampling
- * helpers (addSample, sampleFrequentNode: the GPU samples on the device).
+ * list members are not part of the drop-in, nor is the Judy-array helper
+ * addSample (the GPU samples on the device; sampleFrequentNode is kept as
+ * a host function).
  *
  * connectedComponentsGraphCSR dispatches on arguments->pushpull as the
  * reference does (connectedComponents.c:337-360): 0 Shiloach-Vishkin,
@@ -65,6 +66,11 @@ void printComponents(struct CCStats *stats);
 uint32_t atomicMin(uint32_t *oldValue, uint32_t newValue);
 void linkNodes(uint32_t u, uint32_t v, uint32_t *components);
 void compressNodes(uint32_t num_vertices, uint32_t *components);
+/* :293-334: the most frequent component label among num_samples vertices
+ * drawn with the caller's generator (generateRandInt % num_vertices), ties
+ * to the smallest label; advances the generator by num_samples draws. */
+uint32_t sampleFrequentNode(mt19937state *mt19937var, uint32_t num_vertices, uint32_t num_samples,
+                            uint32_t *components);
 
 struct CCStats *connectedComponentsGraphCSR(struct Arguments *arguments, struct GraphCSR *graph);
 struct CCStats *connectedComponentsAfforestGraphCSR(struct Arguments *arguments, struct GraphCSR *graph);

@@ -163,6 +163,15 @@ int ref_spmv(int mode, uint32_t V, uint32_t E, const uint32_t *out_off, const ui
     return 0;
 }
 
+/* frees the reference's sample table after a direct call of its
+ * sampleFrequentNode, which leaves its keys there */
+void ref_cc_reset(void)
+{
+    Word_t bytes;
+    JSLFA(bytes, JArray);
+    (void)bytes;
+}
+
 /* connected components through the reference's connectedComponentsGraphCSR:
  * mode (pushpull) 1 Afforest, 2 weakly.  Its Shiloach-Vishkin runs on the
  * FPGA, whose connected-components unit is not emulated, so mode 0 is

@@ -38,6 +38,40 @@ def test_library_exports_every_declared_function(gg):
     assert not missing, missing
 
 
+def test_reference_headers_csr_entry_points_are_exported(gg):
+    """Where the reference tree is mounted: every function its four
+    algorithm headers declare is exported by the library, except the members
+    for other graph layouts (Grid, AdjArrayList, AdjLinkedList), the BFS
+    DualOrder variants and their helpers, the Judy sampling helper addSample
+    (sampling runs on the device), bottomUpStepGraphCSRCAPI (its arguments
+    are the FPGA's status and handle, the layer the GPU runtime replaces)
+    and pageRankCompare (declared by the reference, defined nowhere in
+    it)."""
+    import importlib.util
+
+    from graphs import GOLDEN
+
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    hdrs = os.path.join(mg.REF, "02_capi_graph", "include", "algorithms", "capi")
+    if not os.path.isdir(hdrs):
+        pytest.skip("reference tree not mounted here")
+    other_layout = re.compile(r"Grid|AdjArrayList|AdjLinkedList|DualOrder")
+    decl = re.compile(r"^[A-Za-z_][\w \*]*?[ \*](\w+)\s*\(")
+    want = set()
+    for h in ("pageRank.h", "BFS.h", "SPMV.h", "connectedComponents.h"):
+        for line in open(os.path.join(hdrs, h)):
+            m = decl.match(line)
+            if m and not other_layout.search(line) and m.group(1) not in ("addSample", "bottomUpStepGraphCSRCAPI",
+                                                                              "pageRankCompare"):
+                want.add(m.group(1))
+    assert len(want) > 40, sorted(want)
+    L = gg.lib()
+    missing = [n for n in sorted(want) if not hasattr(L, n)]
+    assert not missing, missing
+
+
 def test_struct_sizes_match_c_layout(gg, tmp_path):
     """The ctypes mirror has the C compiler's layout of every drop-in struct."""
     structs = {"Arguments": gg.Arguments, "GraphCSR": gg.GraphCSR, "EdgeList": gg.EdgeList,

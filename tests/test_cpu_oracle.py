@@ -82,6 +82,29 @@ def test_oracle_cc_matches_reference_golden(orc, name):
     assert int(z["cc1_iterations"]) == 0
 
 
+def test_sample_frequent_node_as_the_reference(gg, orc):
+    """The drop-in's sampleFrequentNode against the reference's own
+    (connectedComponents.c:293-334): same label, ties to the smallest, and
+    the caller's generator left in the same state."""
+    import ctypes as C
+
+    R = orc.ref_lib()
+    if R is None:
+        pytest.skip("reference tree not mounted here")
+    L = gg.lib()
+    rng = np.random.default_rng(3)
+    cases = [(1000, 500, rng.integers(0, 7, 1000)), (5000, 1024, rng.integers(0, 5000, 5000)),
+             (16, 64, np.arange(16)), (9, 3, np.arange(9))]
+    for V, S, comp in cases:
+        comp = np.ascontiguousarray(comp, np.uint32)
+        a, b = gg.default_arguments(), gg.default_arguments()
+        got = L.sampleFrequentNode(C.byref(a.mt19937var), V, S, comp.ctypes.data_as(C.c_void_p))
+        want = R.sampleFrequentNode(C.byref(b.mt19937var), V, S, comp.ctypes.data_as(C.c_void_p))
+        R.ref_cc_reset()
+        assert got == want, (V, S, got, want)
+        assert bytes(a.mt19937var) == bytes(b.mt19937var), (V, S)
+
+
 def test_oracle_vs_reference_live(orc):
     """Fresh random graphs through the reference's compiled code."""
     if orc.ref_lib() is None:
