@@ -38,6 +38,18 @@ def test_library_exports_every_declared_function(gg):
     assert not missing, missing
 
 
+def _reference_root():
+    """The reference snapshot's root, as tests/golden/make_golden.py names
+    it, or None where it is not mounted."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden",
+                                                  os.path.join(ROOT, "tests", "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    return mg.REF if os.path.isdir(os.path.join(mg.REF, "02_capi_graph")) else None
+
+
 def test_reference_headers_csr_entry_points_are_exported(gg):
     """Where the reference tree is mounted: every function its four
     algorithm headers declare is exported by the library, except the members
@@ -47,16 +59,10 @@ def test_reference_headers_csr_entry_points_are_exported(gg):
     are the FPGA's status and handle, the layer the GPU runtime replaces)
     and pageRankCompare (declared by the reference, defined nowhere in
     it)."""
-    import importlib.util
-
-    from graphs import GOLDEN
-
-    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
-    mg = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(mg)
-    hdrs = os.path.join(mg.REF, "02_capi_graph", "include", "algorithms", "capi")
-    if not os.path.isdir(hdrs):
+    ref = _reference_root()
+    if ref is None:
         pytest.skip("reference tree not mounted here")
+    hdrs = os.path.join(ref, "02_capi_graph", "include", "algorithms", "capi")
     other_layout = re.compile(r"Grid|AdjArrayList|AdjLinkedList|DualOrder")
     decl = re.compile(r"^[A-Za-z_][\w \*]*?[ \*](\w+)\s*\(")
     want = set()
@@ -70,6 +76,41 @@ def test_reference_headers_csr_entry_points_are_exported(gg):
     L = gg.lib()
     missing = [n for n in sorted(want) if not hasattr(L, n)]
     assert not missing, missing
+
+
+def test_struct_layouts_match_the_reference_headers(gg, tmp_path):
+    """Where the reference tree is mounted: struct Arguments and the four
+    stats structs have the reference's size and every field's offset (one
+    probe compiled against the reference's headers, with the oracle's
+    stand-ins for its absent OpenGraph headers, and against include/)."""
+    import subprocess
+
+    ref = _reference_root()
+    if ref is None:
+        pytest.skip("reference tree not mounted here")
+    structs = {"Arguments": gg.Arguments, "PageRankStats": gg.PageRankStats, "BFSStats": gg.BFSStats,
+               "SPMVStats": gg.SPMVStats, "CCStats": gg.CCStats}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "graphConfig.h"', '#include "pageRank.h"',
+             '#include "BFS.h"', '#include "SPMV.h"', '#include "connectedComponents.h"', "int main(void)", "{"]
+    for name, cls in structs.items():
+        lines.append(f'    printf("{name} %zu\\n", sizeof(struct {name}));')
+        for field, _ in cls._fields_:
+            lines.append(f'    printf("{name}.{field} %zu\\n", offsetof(struct {name}, {field}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+
+    def run(incs, tag):
+        exe = tmp_path / f"layout_{tag}"
+        subprocess.check_call(["gcc", "-std=gnu11", "-w", *incs, str(src), "-o", str(exe)])
+        return subprocess.check_output([str(exe)], text=True)
+
+    inc = os.path.join(ref, "02_capi_graph", "include")
+    theirs = run(["-I" + os.path.join(ROOT, "oracle", "ref_shim"), "-I" + os.path.join(inc, "config"),
+                  "-I" + os.path.join(inc, "algorithms", "capi"), "-I" + os.path.join(inc, "capi_utils")], "ref")
+    ours = run(["-I" + os.path.join(ROOT, "include")], "ours")
+    assert len(theirs.splitlines()) > 60
+    assert ours == theirs
 
 
 def test_struct_sizes_match_c_layout(gg, tmp_path):
