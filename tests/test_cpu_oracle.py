@@ -105,6 +105,53 @@ def test_sample_frequent_node_as_the_reference(gg, orc):
         assert bytes(a.mt19937var) == bytes(b.mt19937var), (V, S)
 
 
+def test_host_helpers_as_the_reference(gg, orc):
+    """The drop-in's host helpers against the reference's own, on the same
+    inputs in one thread: the atomic adds and set of pageRank.c:188-252 and
+    the minimum, link and compress of connectedComponents.c:233-283."""
+    import ctypes as C
+
+    R = orc.ref_lib()
+    if R is None:
+        pytest.skip("reference tree not mounted here")
+    L = gg.lib()
+    for lib in (L, R):
+        lib.addAtomicFloat.argtypes = [C.POINTER(C.c_float), C.c_float]
+        lib.addAtomicDouble.argtypes = [C.POINTER(C.c_double), C.c_double]
+        lib.addAtomicFixedPoint.argtypes = [C.POINTER(C.c_uint64), C.c_uint64]
+        lib.setAtomic.argtypes = [C.POINTER(C.c_uint64), C.c_uint64]
+        lib.atomicMin.argtypes = [C.POINTER(C.c_uint32), C.c_uint32]
+        lib.atomicMin.restype = C.c_uint32
+        lib.linkNodes.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p]
+        lib.compressNodes.argtypes = [C.c_uint32, C.c_void_p]
+    rng = np.random.default_rng(8)
+    vals = rng.random(200)
+    f = [C.c_float(0.125), C.c_float(0.125)]
+    d = [C.c_double(0.125), C.c_double(0.125)]
+    u = [C.c_uint64(3), C.c_uint64(3)]
+    for v in vals:
+        for k, lib in enumerate((L, R)):
+            lib.addAtomicFloat(C.byref(f[k]), float(v))
+            lib.addAtomicDouble(C.byref(d[k]), float(v))
+            lib.addAtomicFixedPoint(C.byref(u[k]), int(v * 2**32))
+    assert f[0].value == f[1].value and d[0].value == d[1].value and u[0].value == u[1].value
+    for k, lib in enumerate((L, R)):
+        lib.setAtomic(C.byref(u[k]), 12345)
+    assert u[0].value == u[1].value == 12345
+    for x, y in ((10, 3), (10, 12), (5, 5), (0, 7)):
+        a, b = C.c_uint32(x), C.c_uint32(x)
+        assert L.atomicMin(C.byref(a), y) == R.atomicMin(C.byref(b), y) and a.value == b.value
+    V = 700
+    src = rng.integers(0, V, 900)
+    dst = rng.integers(0, V, 900)
+    comps = [np.arange(V, dtype=np.uint32), np.arange(V, dtype=np.uint32)]
+    for k, lib in enumerate((L, R)):
+        for x, y in zip(src, dst):
+            lib.linkNodes(int(x), int(y), comps[k].ctypes.data)
+        lib.compressNodes(V, comps[k].ctypes.data)
+    np.testing.assert_array_equal(comps[0], comps[1])
+
+
 def test_oracle_vs_reference_live(orc):
     """Fresh random graphs through the reference's compiled code."""
     if orc.ref_lib() is None:
