@@ -31,3 +31,16 @@ def test_reference_arm_prints_the_contract_line():
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_algorithmic_bytes_match_the_stated_figures():
+    """The byte counts behind roofline.achieved: one PageRank pull iteration
+    (4E + 4(V+1) + (12+2s)V) and one gather launch (4E + 4(V+1) + sV + 4V) at
+    the R-MAT-24 and R-MAT-16 workloads, FP32."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.pr_bytes(1 << 24, 1 << 28, 4) == 1_476_395_012
+    assert bench.pr_bytes(1 << 16, 1 << 20, 4) == 5_767_172
+    assert bench.pr_gather_bytes(1 << 24, 1 << 28, 4) == 1_275_068_420
+    assert bench.pr_bytes(1 << 24, 1 << 28, 2) == 1_409_286_148
