@@ -36,7 +36,8 @@ def test_reference_arm_prints_the_contract_line():
 def test_algorithmic_bytes_match_the_stated_figures():
     """The byte counts behind roofline.achieved: one PageRank pull iteration
     (4E + 4(V+1) + (12+2s)V) and one gather launch (4E + 4(V+1) + sV + 4V) at
-    the R-MAT-24 and R-MAT-16 workloads, FP32."""
+    the R-MAT-24 and R-MAT-16 workloads, FP32, and the R-MAT-24 iteration
+    with BF16 contributions."""
     sys.path.insert(0, ROOT)
     import bench
 
