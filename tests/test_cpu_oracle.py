@@ -152,6 +152,39 @@ def test_host_helpers_as_the_reference(gg, orc):
     np.testing.assert_array_equal(comps[0], comps[1])
 
 
+def test_print_cc_stats_fills_as_the_reference(gg, orc, capfd):
+    """The same labelling through the reference's own printCCStats and the
+    drop-in's: the same counts and labels arrays (both structs start as the
+    reference's constructor leaves them: counts 0, labels the identity)."""
+    import ctypes as C
+
+    R = orc.ref_lib()
+    if R is None:
+        pytest.skip("reference tree not mounted here")
+    L = gg.lib()
+    rng = np.random.default_rng(12)
+    for V in (1, 9, 500, 4000):
+        comp = np.minimum.accumulate(rng.integers(0, V, V)).astype(np.uint32)  # labels that are vertex ids
+        comp = np.where(rng.random(V) < 0.5, comp, np.arange(V, dtype=np.uint32)).astype(np.uint32)
+        out = []
+        for lib in (R, L):
+            c = comp.copy()
+            counts = np.zeros(V, np.uint32)
+            labels = np.arange(V, dtype=np.uint32)
+            st = gg.CCStats()
+            st.num_vertices = V
+            st.components = c.ctypes.data_as(C.POINTER(C.c_uint32))
+            st.counts = counts.ctypes.data_as(C.POINTER(C.c_uint32))
+            st.labels = labels.ctypes.data_as(C.POINTER(C.c_uint32))
+            lib.printCCStats(C.byref(st))
+            out.append((counts, labels))
+        R.ref_cc_reset()
+        np.testing.assert_array_equal(out[0][0], out[1][0], err_msg=f"counts V={V}")
+        np.testing.assert_array_equal(out[0][1], out[1][1], err_msg=f"labels V={V}")
+    C.CDLL(None).fflush(None)
+    capfd.readouterr()
+
+
 def test_oracle_vs_reference_live(orc):
     """Fresh random graphs through the reference's compiled code."""
     if orc.ref_lib() is None:
