@@ -59,60 +59,70 @@ def sources(V):
     return sorted({0, 1, V // 2, V - 1})
 
 
-def main(only):
-    if O.ref_lib() is None:
-        sys.exit("the reference could not be built (is the reference tree mounted?)")
+def graphs():
+    """(graphs by name, the fixture edge arrays for fixtures.npz)."""
     fx = {}
-    graphs = {}
+    out = {}
     for name, (rel, weighted) in FIXTURES.items():
         s, d, w = load(rel, weighted)
         fx[name + "_src"], fx[name + "_dst"] = s, d
         if w is not None:
             fx[name + "_w"] = w
         V = int(max(s.max(), d.max())) + 1
-        graphs[name] = O.Csr(V, s, d, w)
+        out[name] = O.Csr(V, s, d, w)
+    for name, (scale, ef) in RMAT.items():
+        out[name] = O.rmat_csr(scale, ef, weighted=True, symmetric=name.endswith("u"))
+    for name, (s, d, w, V) in special_edges().items():
+        out[name] = O.Csr(V, s, d, w)
+    return out, fx
+
+
+def golden(g):
+    """The contents of one golden_<graph>.npz: the reference's own outputs on g."""
+    out = {"V": np.uint32(g.V), "E": np.uint32(g.E)}
+    for mode in range(14):
+        r, info = O.ref_pagerank(g, mode, PR_ITERS, PR_EPS)
+        out[f"pr{mode}_ranks"] = r
+        out[f"pr{mode}_iters"] = np.uint32(info["iterations"])
+        out[f"pr{mode}_err"] = np.float64(info["error_total"])
+    srcs = sources(g.V)
+    out["bfs_sources"] = np.array(srcs, np.int32)
+    for mode in range(5):
+        for s in srcs:
+            p, d, info = O.ref_bfs(g, mode, s)
+            out[f"bfs{mode}_{s}_parents"] = p
+            out[f"bfs{mode}_{s}_dist"] = d
+            out[f"bfs{mode}_{s}_processed"] = np.uint32(info["processed_nodes"])
+            out[f"bfs{mode}_{s}_iteration"] = np.uint32(info["iteration"])
+    # the reference is built WEIGHTED 0 (graphConfig.h:7): its SpMV uses
+    # the constant weight 0.0001f, so its golden runs on the unweighted view
+    gu = O.Csr.from_arrays(g.V, g.E, g.out_off, g.out_adj, g.in_off, g.in_adj)
+    for mode in range(4):
+        x, y = O.ref_spmv(gu, mode, SPMV_ITERS)
+        out[f"spmv{mode}_x"] = x
+        out[f"spmv{mode}_y"] = y
+    # connectedComponents.c through connectedComponentsGraphCSR: 1
+    # Afforest, 2 weakly (its Shiloach-Vishkin runs on the FPGA)
+    for mode in (1, 2):
+        comp, counts, labels, info = O.ref_cc(g, mode)
+        out[f"cc{mode}_components"] = comp
+        out[f"cc{mode}_counts"] = counts
+        out[f"cc{mode}_labels"] = labels
+        out[f"cc{mode}_iterations"] = np.uint32(info["iterations"])
+        out[f"cc{mode}_mt"] = info["mt"]
+    return out
+
+
+def main(only):
+    if O.ref_lib() is None:
+        sys.exit("the reference could not be built (is the reference tree mounted?)")
+    gs, fx = graphs()
     if not only:
         np.savez_compressed(os.path.join(HERE, "fixtures.npz"), **fx)
-    for name, (scale, ef) in RMAT.items():
-        graphs[name] = O.rmat_csr(scale, ef, weighted=True, symmetric=name.endswith("u"))
-    for name, (s, d, w, V) in special_edges().items():
-        graphs[name] = O.Csr(V, s, d, w)
-
-    for name, g in graphs.items():
+    for name, g in gs.items():
         if only and name not in only:
             continue
-        out = {"V": np.uint32(g.V), "E": np.uint32(g.E)}
-        for mode in range(14):
-            r, info = O.ref_pagerank(g, mode, PR_ITERS, PR_EPS)
-            out[f"pr{mode}_ranks"] = r
-            out[f"pr{mode}_iters"] = np.uint32(info["iterations"])
-            out[f"pr{mode}_err"] = np.float64(info["error_total"])
-        srcs = sources(g.V)
-        out["bfs_sources"] = np.array(srcs, np.int32)
-        for mode in range(5):
-            for s in srcs:
-                p, d, info = O.ref_bfs(g, mode, s)
-                out[f"bfs{mode}_{s}_parents"] = p
-                out[f"bfs{mode}_{s}_dist"] = d
-                out[f"bfs{mode}_{s}_processed"] = np.uint32(info["processed_nodes"])
-                out[f"bfs{mode}_{s}_iteration"] = np.uint32(info["iteration"])
-        # the reference is built WEIGHTED 0 (graphConfig.h:7): its SpMV uses
-        # the constant weight 0.0001f, so its golden runs on the unweighted view
-        gu = O.Csr.from_arrays(g.V, g.E, g.out_off, g.out_adj, g.in_off, g.in_adj)
-        for mode in range(4):
-            x, y = O.ref_spmv(gu, mode, SPMV_ITERS)
-            out[f"spmv{mode}_x"] = x
-            out[f"spmv{mode}_y"] = y
-        # connectedComponents.c through connectedComponentsGraphCSR: 1
-        # Afforest, 2 weakly (its Shiloach-Vishkin runs on the FPGA)
-        for mode in (1, 2):
-            comp, counts, labels, info = O.ref_cc(g, mode)
-            out[f"cc{mode}_components"] = comp
-            out[f"cc{mode}_counts"] = counts
-            out[f"cc{mode}_labels"] = labels
-            out[f"cc{mode}_iterations"] = np.uint32(info["iterations"])
-            out[f"cc{mode}_mt"] = info["mt"]
-        np.savez_compressed(os.path.join(HERE, f"golden_{name}.npz"), **out)
+        np.savez_compressed(os.path.join(HERE, f"golden_{name}.npz"), **golden(g))
         print("wrote", name, g.V, g.E)
 
 

@@ -185,6 +185,35 @@ def test_print_cc_stats_fills_as_the_reference(gg, orc, capfd):
     capfd.readouterr()
 
 
+def test_golden_files_reproduce_from_the_reference(orc):
+    """Where the reference tree is mounted: every golden_<graph>.npz and
+    fixtures.npz is exactly what tests/golden/make_golden.py computes from
+    the reference's own code now (same keys, bit-identical arrays)."""
+    import importlib.util
+
+    if orc.ref_lib() is None:
+        pytest.skip("reference tree not mounted here")
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    if not os.path.isdir(mg.TEST):
+        pytest.skip("reference fixtures not mounted here")
+    gs, fx = mg.graphs()
+    z = np.load(os.path.join(GOLDEN, "fixtures.npz"))
+    assert sorted(z.files) == sorted(fx)
+    for k in fx:
+        np.testing.assert_array_equal(z[k], fx[k], err_msg=k)
+    assert sorted(gs) == sorted(NAMES)
+    for name, g in gs.items():
+        want = mg.golden(g)
+        z = np.load(os.path.join(GOLDEN, f"golden_{name}.npz"))
+        assert sorted(z.files) == sorted(want), name
+        for k, v in want.items():
+            a, b = np.asarray(z[k]), np.asarray(v)
+            assert a.dtype == b.dtype and a.shape == b.shape, (name, k)
+            assert a.tobytes() == b.tobytes(), (name, k)
+
+
 def test_oracle_vs_reference_live(orc):
     """Fresh random graphs through the reference's compiled code."""
     if orc.ref_lib() is None:
