@@ -121,11 +121,6 @@ class CcResult(C.Structure):
 CC_ALGORITHMS = {"sv": 0, "afforest": 1, "weakly": 2}
 
 
-class GatherRates(C.Structure):
-    _fields_ = [("cluster_smem_gps", C.c_double), ("own_smem_gps", C.c_double), ("l2_small_gps", C.c_double),
-                ("l2_large_gps", C.c_double), ("clusters", C.c_uint32), ("cluster_sms", C.c_uint32)]
-
-
 class PrParams(C.Structure):
     _fields_ = [("mode", C.c_uint32), ("storage", C.c_uint32), ("max_iterations", C.c_uint32),
                 ("init_one_over_n", C.c_uint32), ("epsilon", C.c_double), ("damp", C.c_float),
@@ -302,7 +297,6 @@ def lib() -> C.CDLL:
         L.connectedComponentsVerifyGraphCSR.argtypes = [P(CCStats), P(GraphCSR)]
         L.connectedComponentsVerifyGraphCSR.restype = C.c_uint32
         L.gg_cc.argtypes = [C.c_void_p, P(CcParams), C.c_void_p, P(CcResult), C.c_void_p]
-        L.gg_gather_ceiling.argtypes = [P(GatherRates), C.c_void_p]
         L.freePageRankStats.argtypes = [P(PageRankStats)]
         L.freeBFSStats.argtypes = [P(BFSStats)]
         L.freeSPMVStats.argtypes = [P(SPMVStats)]
@@ -341,15 +335,6 @@ def _check(st, what):
 
 def device_init(device: int = 0):
     _check(lib().gg_device_init(device), "gg_device_init")
-
-
-def gather_ceiling() -> dict:
-    """gg_gather_ceiling: random 4-byte gathers per second (G/s) from a
-    cluster's shared memory, a CTA's own shared memory, and L2 (1.5 MB and
-    64 MB arrays)."""
-    r = GatherRates()
-    _check(lib().gg_gather_ceiling(C.byref(r), None), "gg_gather_ceiling")
-    return {k: getattr(r, k) for k, _ in GatherRates._fields_}
 
 
 def _np(ptr, n, dtype):

@@ -17,7 +17,6 @@
 #include <cuda_fp16.h>
 
 #include <cstring>
-#include <mutex>
 #include <string>
 #include <vector>
 
@@ -436,11 +435,14 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[GG_NOALLOC_SCRA
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void *g_noalloc_addr[kMaxDevices];
-
 size_t noalloc_coord_bytes(uint32_t ntiles) { return (((size_t)ntiles + 1) * sizeof(uint2) + 255) / 256 * 256; }
+
+/* [a, a + an) and [b, b + bn) share a byte */
+bool noalloc_overlap(const void *a, size_t an, const void *b, size_t bn)
+{
+    const uintptr_t pa = (uintptr_t)a, pb = (uintptr_t)b;
+    return an && bn && pa < pb + bn && pb < pa + an;
+}
 
 } // namespace
 
@@ -472,22 +474,20 @@ extern "C" gg_status gg_spmv_pull_noalloc(uint32_t V, uint32_t E, const uint32_t
         return gg_fail(GG_ERR_INVALID, "gg_spmv_pull_noalloc: V + E = " + std::to_string(items) +
                                            " exceeds the scratch limit of " + std::to_string(max_items) +
                                            " (4 MiB of tile scratch); use gg_spmv");
-    int dev = 0;
-    GG_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return gg_fail(GG_ERR_INVALID, "device index beyond the scratch table");
+    /* y is written while the others are read (x through the read-only
+     * path): an overlap would silently corrupt the product */
+    const size_t vb = (size_t)V * sizeof(float), eb = (size_t)E * sizeof(float);
+    if (noalloc_overlap(y, vb, x, vb) || noalloc_overlap(y, vb, w, eb) || noalloc_overlap(y, vb, in_src, eb) ||
+        noalloc_overlap(y, vb, in_off, vb + sizeof(uint32_t)))
+        return gg_fail(GG_ERR_INVALID, "gg_spmv_pull_noalloc: y overlaps x, w, in_off or in_src");
+    /* The host-side name of the array is not a device address: ask the
+     * runtime for it on every call, in the context current now.  A cached
+     * address would go stale when the context it came from is reset or when
+     * the caller switches to another context of the same device; the lookup
+     * is host-side and queues no work.  The first call in a context loads the
+     * library's kernels into it. */
     void *base = nullptr;
-    {
-        /* once per device, with that device current: the host-side name of
-         * the array is not a device address, so ask the runtime for it */
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_addr[dev])
-        {
-            void *p = nullptr;
-            GG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-            g_noalloc_addr[dev] = p;
-        }
-        base = g_noalloc_addr[dev];
-    }
+    GG_CUDA(cudaGetSymbolAddress(&base, g_noalloc_scratch));
     const uint32_t ntiles = (uint32_t)((items + GG_TILE_ITEMS - 1) / GG_TILE_ITEMS);
     uint2 *coord = (uint2 *)base;
     cudaStream_t s = (cudaStream_t)stream;

@@ -23,9 +23,10 @@ extras     BF16/FP16 PageRank, SpMV pull, BFS (R-MAT-22 undirected, 64
 cpu_baseline  the oracle's OpenMP restatement of the reference's pull loop
            (pageRank.c:1026-1085 with the gather as at :2890-2906) on all host
            cores, on a bounded number of iterations of the same graph.
---impl reference  times that CPU implementation alone, one iteration per
-           step (the reference's own code needs its absent OpenGraph library,
-           so the restatement stands in for it).
+--impl reference  times that CPU implementation alone on the same graph
+           (built by the oracle), 30 iterations per step as this arm's step
+           (the reference's own code needs its absent OpenGraph library and
+           FPGA, so the restatement stands in for it).
 With N > 1 GPUs every rank runs an independent replica (no collective on the
 data path); value sums all ranks' edges over the slowest rank's time.
 """
@@ -54,7 +55,7 @@ def parse():
     p.add_argument("--edge-factor", type=int, default=16)
     p.add_argument("--no-extras", action="store_true", help="skip the BF16/BFS/SpMV side measurements")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    p.add_argument("--leg", choices=["c1", "bfs", "ppr", "batch", "serve", "csr", "cc", "relabel", "gather"],
+    p.add_argument("--leg", choices=["c1", "bfs", "ppr", "batch", "serve", "csr", "cc", "relabel"],
                    help="run one side measurement alone and print its JSON (for profiling)")
     return p.parse_args()
 
@@ -161,31 +162,46 @@ def cpu_pagerank(graph, O, iters, threads):
 
 
 def run_reference(a, world, rank):
-    """The reference arm: the CPU implementation of the path on host cores."""
+    """The reference arm: the CPU implementation of the path on the host's
+    cores, on this arm's own workload and config.  The graph comes from the
+    oracle's R-MAT generator and CSR build (the same edges and arrays as the
+    product's builder gives; nothing of the product is imported), and every
+    step runs the full 30 pull iterations of the GPU arm's step with the
+    oracle's OpenMP restatement of the reference's pull loop (pageRank.c:
+    1026-1085, gather as at :2890-2906).  The reference's own compiled code
+    needs its absent OpenGraph library and its FPGA; the restatement is
+    bit-exact with that code compiled against stand-ins where the reference
+    tree is mounted."""
     if rank != 0:
         return
-    import accelgraph_express_gb300 as gg
     from oracle import oracle_ctypes as O
 
     threads = os.cpu_count() or 1
-    graph = gg.Graph.rmat(a.scale, a.edge_factor, seed=SEED)
-    V, E = graph.V, graph.E
+    t0 = time.perf_counter()
+    o = O.rmat_csr(a.scale, a.edge_factor, seed=SEED)
+    build_s = time.perf_counter() - t0
+    V, E = o.V, o.E
     times = []
     for i in range(a.warmup + a.steps):
-        _, _, dt, _ = cpu_pagerank(graph, O, 1, threads)
+        t0 = time.perf_counter()
+        O.pagerank(o, 0, ITERS, 0.0, nthreads=threads)
+        dt = time.perf_counter() - t0
         if i >= a.warmup:
             times.append(dt)
     t = sum(times)
-    value = E * len(times) / t / 1e9
+    value = E * ITERS * len(times) / t / 1e9
     line = {
         "impl": "reference", "metric": f"PageRank pull GTEPS, R-MAT-{a.scale} FP32", "value": value,
         "unit": "GTEPS", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": 1e3 * t / len(times), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": f"synthetic R-MAT scale {a.scale}, edge factor {a.edge_factor}, seed {SEED}",
+        "dtype": "f32",
+        "data": f"synthetic R-MAT scale {a.scale}, edge factor {a.edge_factor}, seed {SEED}, no label permutation",
         "config": {"workload": f"pagerank_pull_rmat{a.scale}", "vertices": V, "edges": E,
-                   "iterations_per_step": 1, "threads": threads},
+                   "iterations_per_step": ITERS, "epsilon": 0.0, "storage": "f32", "threads": threads,
+                   "graph_build_s": round(build_s, 2)},
         "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
-                         "sample": f"1 PageRank pull iteration over R-MAT-{a.scale} per step"},
+                         "sample": f"{ITERS} PageRank pull iterations over R-MAT-{a.scale} per step, "
+                                   f"{a.steps} steps"},
         "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -238,8 +254,7 @@ def run_leg(leg):
     fn = {"c1": lambda: c1_extras(gg, torch), "bfs": lambda: bfs_extras(gg, torch, peak),
           "ppr": lambda: ppr_extras(gg, torch, peak), "batch": lambda: batch_extras(gg, torch, peak),
           "serve": lambda: serving_extras(gg), "csr": lambda: csr_build_extras(gg, torch, peak),
-          "cc": lambda: cc_extras(gg, torch, peak), "relabel": lambda: relabel_extras(gg, torch, peak),
-          "gather": lambda: {"metric": "random 4-byte gathers", "unit": "G/s", **gg.gather_ceiling()}}[leg]
+          "cc": lambda: cc_extras(gg, torch, peak), "relabel": lambda: relabel_extras(gg, torch, peak)}[leg]
     print(json.dumps({"leg": leg, **fn()}), flush=True)
 
 
@@ -562,7 +577,7 @@ def serving_extras(gg, scale=23, n=1500, rate=150.0):
         else:
             qs.append(("bfs", int(nz[rng.integers(0, len(nz))])))
     gaps = rng.exponential(1.0 / rate, n)
-    sample = {0, 1, 2, 3, 5, 8, 13, 21, 34}
+    sample = set(range(0, n, max(1, n // 48)))  # every 31st query of 1500: 49 sampled
     srv = gg.Server(dg, max_ppr_batch=64, ppr_iterations=20, ppr_storage="f32")
     srv.take(srv.submit_ppr([0]))      # warm-up: work buffers, tiles
     srv.take(srv.submit_bfs(int(nz[0])))
@@ -594,15 +609,16 @@ def serving_extras(gg, scale=23, n=1500, rate=150.0):
     alone_ok, acc_ok = True, True
     a = g.arrays()
     o = O.Csr.from_arrays(V, g.E, a["out_off"], a["out_adj"], a["in_off"], a["in_adj"])
-    l1_checked = 0
+    l1_checked, l1_max = 0, 0.0
     for i in sorted(sample):
         kind, arg = qs[i]
         res, _ = srv.take(srv.submit_ppr(arg) if kind == "ppr" else srv.submit_bfs(arg))
         if kind == "ppr":
             alone_ok &= bool(np.array_equal(res, kept[i]))
-            if l1_checked < 1:
-                acc_ok &= bool(np.abs(kept[i] - O.ppr_f64_multi(o, arg, 20, float(np.float32(0.85)))).sum() <= 1e-6)
-                l1_checked += 1
+            l1 = float(np.abs(kept[i] - O.ppr_f64_multi(o, arg, 20, float(np.float32(0.85)))).sum())
+            l1_max = max(l1_max, l1)
+            acc_ok &= l1 <= 1e-6
+            l1_checked += 1
         else:
             alone_ok &= bool(np.array_equal(res[1], kept[i][1]))
             _, rd, _ = O.bfs(o, 2, arg)
@@ -617,6 +633,7 @@ def serving_extras(gg, scale=23, n=1500, rate=150.0):
            "achieved_qps": n / span, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
            "ppr_batch_mean": float(np.mean([x["batch_size"] for x in infos if x["kind"] == 0])),
            "alone_equals_mixed": alone_ok, "sampled_results_match_oracle": acc_ok,
+           "sampled": len(sample), "ppr_checked_vs_fp64": l1_checked, "ppr_l1_vs_fp64_max": l1_max,
            "all_ok": all(x["status"] == 0 for x in infos)}
     for k, name in ((0, "ppr"), (1, "bfs")):
         sel = lat[kinds == k]
@@ -657,23 +674,34 @@ def bfs_extras(gg, torch, peak, scale=22):
         # reached vertex, visited + next bitmaps per bottom-up step
         bytes_all.append(8.0 * r["edges_examined"] + 8.0 * int(reached.sum()) + r["bottom_up_steps"] * V / 4.0)
         bu += r["bottom_up_steps"]
-    # levels of one search against the oracle (bit-exact)
+    # every search against the oracle's direction-optimising BFS (the
+    # reference's BFS.c:525-803 restated): levels, processed vertices and
+    # edges examined bit-exact; the oracle's OpenMP run is the CPU baseline
     v = g.views()
     out_off = np.append(v["out_edges_idx"], np.uint32(E))
     in_off = np.append(v["in_edges_idx"], np.uint32(E))
     o = O.Csr.from_arrays(V, E, out_off, v["out_adj"], in_off, v["in_adj"])
-    t0 = time.perf_counter()
-    _, rd, info = O.bfs(o, 2, srcs[0], nthreads=os.cpu_count() or 1)
-    cpu_s = time.perf_counter() - t0
-    _, dist0, _ = dg.bfs(srcs[0], "do")
+    threads = os.cpu_count() or 1
+    match, counts_match, cpu_teps = 0, 0, []
+    for s in srcs:
+        t0 = time.perf_counter()
+        _, rd, info = O.bfs(o, 2, s, nthreads=threads)
+        cpu_s = time.perf_counter() - t0
+        _, dist, r = dg.bfs(s, "do")
+        match += int(np.array_equal(dist, rd))
+        counts_match += int(r["processed_nodes"] == info["processed_nodes"]
+                            and r["edges_examined"] == info["edges_examined"])
+        reached = (rd > 0) | (np.arange(V) == s)
+        cpu_teps.append(float(deg[reached].astype(np.int64).sum()) / 2.0 / cpu_s)
     hm = len(teps) / sum(1.0 / t for t in teps)
     out = {"graph": f"R-MAT-{scale} undirected, V={V}, E={E} directed", "sources": len(srcs),
            "gteps_harmonic": hm / 1e9, "ms_mean": float(np.mean(ms_all)),
            "alg_gbs_mean": float(np.mean([b / (m / 1e3) for b, m in zip(bytes_all, ms_all)]) / 1e9),
            "hbm_frac_mean": float(np.mean([b / (m / 1e3) for b, m in zip(bytes_all, ms_all)]) / 1e9 / peak),
            "bottom_up_steps_mean": bu / len(srcs),
-           "levels_match_oracle": bool(np.array_equal(dist0, rd)),
-           "cpu_baseline_gteps": float(deg[(rd > 0) | (np.arange(V) == srcs[0])].astype(np.int64).sum()) / 2.0 / cpu_s / 1e9}
+           "levels_match_oracle": f"{match}/{len(srcs)}",
+           "processed_and_edges_examined_match_oracle": f"{counts_match}/{len(srcs)}",
+           "cpu_baseline_gteps": len(cpu_teps) / sum(1.0 / t for t in cpu_teps) / 1e9, "cpu_cores": threads}
     dg.free()
     g.free()
     return out

@@ -312,14 +312,20 @@ gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *x, float *x
  * or a process whose device memory is reserved up front.  All arrays are the
  * caller's DEVICE pointers: in_off (V+1 offsets of the inverse CSR, with
  * in_off[V] = E), in_src (E in-neighbours), w (E FP32 weights), x (V), y (V,
- * overwritten).  The call allocates nothing: its scratch is a 4 MiB array
+ * overwritten).  in_off must be non-decreasing with in_off[V] = E: the
+ * kernels trust it, and other offsets are undefined behaviour (reads past
+ * in_src and w).  y must not overlap x, w, in_off or in_src (GG_ERR_INVALID
+ * when it does).  The call allocates nothing: its scratch is a 4 MiB array
  * inside the library that every GPU loading the library holds until the
  * process exits, so V + E must not exceed gg_spmv_pull_noalloc_max_items()
- * (GG_ERR_INVALID otherwise).  The first call on a device looks up the
- * array's device address; make that first call before any stream capture.
- * Calls share the one array: calls whose work overlaps on the GPU (other
- * streams, other host threads) race and must be serialised by the caller.
- * Work is queued on `stream` and not waited for.
+ * (GG_ERR_INVALID otherwise).  Every call looks up the array's device
+ * address in the context current at the call (a context that was reset or
+ * replaced gets the new address); the first call in a context also loads
+ * the library's kernels into it, so make that first call before any stream
+ * capture.  Calls share the one array: calls whose work overlaps on the GPU
+ * (other streams, other host threads) race and must be serialised by the
+ * caller.  Work is queued on `stream` (NULL: the legacy default stream) and
+ * not waited for.
  */
 gg_status gg_spmv_pull_noalloc(uint32_t V, uint32_t E, const uint32_t *in_off, const uint32_t *in_src,
                                const float *w, const float *x, float *y, void *stream);
@@ -362,27 +368,6 @@ gg_status gg_ppr(gg_graph *g, const gg_ppr_params *p, const uint32_t *seed_off, 
 /* Device pointer to the last gg_ppr's ranks (V rows of *stride floats),
  * valid until the next call on `g`. */
 const float *gg_ppr_device_ranks(const gg_graph *g, uint32_t *stride);
-
-/* ---- gather ceilings --------------------------------------------------------- */
-
-/* Random 4-byte gathers per second (G/s) from hashed indices, every thread
- * summing 4096 values: from the shared memory of 8-CTA clusters (184 KB per
- * CTA, `clusters` of them resident on `cluster_sms` SMs), from each CTA's
- * own shared memory, and from global memory through L2 over a 1.5 MB and a
- * 64 MB array.  The pull gathers read one random value per in-edge, so these
- * rates are the ceilings of their on-chip tables and of their L2 traffic.
- * Allocates 64 MB for the call. */
-typedef struct gg_gather_rates
-{
-    double cluster_smem_gps;
-    double own_smem_gps;
-    double l2_small_gps;
-    double l2_large_gps;
-    uint32_t clusters;
-    uint32_t cluster_sms;
-} gg_gather_rates;
-
-gg_status gg_gather_ceiling(gg_gather_rates *rates, void *stream);
 
 /* ---- drop-in side options ---------------------------------------------------- */
 

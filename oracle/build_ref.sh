@@ -1,12 +1,13 @@
 #!/bin/sh
 # Compile the reference's own CSR algorithm files, where they lie in the
 # reference tree, against the stand-in headers in oracle/ref_shim/, into
-# oracle/_ref/libref.so.  The reference tree is only present where the
-# reference snapshot is mounted; elsewhere this script does nothing and the
-# tests that need libref.so are skipped.  Test infrastructure only.
+# oracle/_ref/libref.so.  The reference tree is $ACCELGRAPH_REFERENCE, or a
+# snapshot checked out beside this repository (../reference); where neither
+# exists this script does nothing and the tests that need libref.so are
+# skipped.  Test infrastructure only.
 set -e
-REF="${ACCELGRAPH_REFERENCE:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${ACCELGRAPH_REFERENCE:-$HERE/../../reference}"
 OUT="$HERE/_ref"
 SRC="$REF/02_capi_graph/src/algorithms/capi"
 INC="$REF/02_capi_graph/include"

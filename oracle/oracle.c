@@ -32,6 +32,9 @@ void orc_rmat_edges(uint32_t scale, double a, double b, double c, uint64_t seed,
                     uint64_t first, uint64_t count, uint32_t *src, uint32_t *dst)
 {
     const double t1 = a, t2 = a + b, t3 = a + b + c;
+    /* every edge is a function of its index alone: any schedule gives the
+     * same list */
+#pragma omp parallel for schedule(static)
     for (uint64_t k = 0; k < count; k++)
     {
         uint64_t i = first + k;
@@ -53,6 +56,7 @@ void orc_rmat_edges(uint32_t scale, double a, double b, double c, uint64_t seed,
 
 void orc_rmat_weights(uint64_t seed, uint64_t first, uint64_t count, float *w)
 {
+#pragma omp parallel for schedule(static)
     for (uint64_t k = 0; k < count; k++)
     {
         uint64_t r = orc_splitmix64(seed + (first + k + 1) * PHI);
@@ -60,44 +64,106 @@ void orc_rmat_weights(uint64_t seed, uint64_t first, uint64_t count, float *w)
     }
 }
 
-/* Stable counting sort of `perm_in` (or the identity when NULL) by key[]. */
-static void counting_sort(uint32_t V, uint32_t E, const uint32_t *key, const uint32_t *perm_in,
-                          uint32_t *perm_out, uint32_t *off)
+/* Stable LSD radix sort of (key, val) pairs on the low `bits` bits of key,
+ * 8 bits per pass, OpenMP: each thread histograms and scatters its own
+ * contiguous chunk, chunks in thread order, so equal digits keep their input
+ * order (stable) whatever the thread count.  The result ends in key/val. */
+static void radix_sort_pairs(uint64_t *key, uint32_t *val, size_t n, int bits)
 {
-    memset(off, 0, (size_t)(V + 1) * sizeof(uint32_t));
-    for (uint32_t e = 0; e < E; e++)
-        off[key[e] + 1]++;
-    for (uint32_t v = 0; v < V; v++)
-        off[v + 1] += off[v];
-    uint32_t *cursor = (uint32_t *)malloc((size_t)V * sizeof(uint32_t) + 4);
-    memcpy(cursor, off, (size_t)V * sizeof(uint32_t));
-    for (uint32_t i = 0; i < E; i++)
+    uint64_t *k2 = (uint64_t *)malloc(n * sizeof(uint64_t) + 8);
+    uint32_t *v2 = (uint32_t *)malloc(n * sizeof(uint32_t) + 4);
+    int nt = 1;
+#ifdef _OPENMP
+    nt = omp_get_max_threads();
+#endif
+    size_t *cnt = (size_t *)malloc((size_t)nt * 256 * sizeof(size_t));
+    uint64_t *ka = key, *kb = k2;
+    uint32_t *va = val, *vb = v2;
+    for (int shift = 0; shift < bits; shift += 8)
     {
-        uint32_t e = perm_in ? perm_in[i] : i;
-        perm_out[cursor[key[e]]++] = e;
+#pragma omp parallel num_threads(nt)
+        {
+            int t = 0;
+#ifdef _OPENMP
+            t = omp_get_thread_num();
+#endif
+            const size_t lo = n * (size_t)t / (size_t)nt, hi = n * (size_t)(t + 1) / (size_t)nt;
+            size_t *c = cnt + (size_t)t * 256;
+            memset(c, 0, 256 * sizeof(size_t));
+            for (size_t i = lo; i < hi; i++)
+                c[(ka[i] >> shift) & 255]++;
+#pragma omp barrier
+#pragma omp single
+            {
+                size_t run = 0;
+                for (int d = 0; d < 256; d++)
+                    for (int u = 0; u < nt; u++)
+                    {
+                        size_t x = cnt[(size_t)u * 256 + d];
+                        cnt[(size_t)u * 256 + d] = run;
+                        run += x;
+                    }
+            }
+            for (size_t i = lo; i < hi; i++)
+            {
+                size_t at = c[(ka[i] >> shift) & 255]++;
+                kb[at] = ka[i];
+                vb[at] = va[i];
+            }
+        }
+        uint64_t *kt = ka; ka = kb; kb = kt;
+        uint32_t *vt = va; va = vb; vb = vt;
     }
-    free(cursor);
+    if (ka != key)
+    {
+        memcpy(key, ka, n * sizeof(uint64_t));
+        memcpy(val, va, n * sizeof(uint32_t));
+    }
+    free(cnt);
+    free(k2);
+    free(v2);
 }
 
+/* CSR (by_dst = 0) or inverse CSR (by_dst = 1) of an edge list: rows by the
+ * primary endpoint, each row's neighbours ascending, duplicates (and their
+ * weights) in input order -- the order of a stable sort by the neighbour
+ * followed by a stable sort by the row, done here as one stable radix sort
+ * of (row << b | neighbour). */
 void orc_build_csr(uint32_t V, uint32_t E, const uint32_t *src, const uint32_t *dst, const float *w,
                    int by_dst, uint32_t *off, uint32_t *adj, float *adj_w)
 {
     const uint32_t *primary = by_dst ? dst : src;
     const uint32_t *secondary = by_dst ? src : dst;
-    uint32_t *p1 = (uint32_t *)malloc((size_t)E * sizeof(uint32_t) + 4);
-    uint32_t *p2 = (uint32_t *)malloc((size_t)E * sizeof(uint32_t) + 4);
-    uint32_t *tmp_off = (uint32_t *)malloc((size_t)(V + 1) * sizeof(uint32_t));
-    counting_sort(V, E, secondary, NULL, p1, tmp_off);
-    counting_sort(V, E, primary, p1, p2, off);
+    int b = 1;
+    while (b < 32 && ((uint64_t)1 << b) < (uint64_t)V)
+        b++;
+    uint64_t *key = (uint64_t *)malloc((size_t)E * sizeof(uint64_t) + 8);
+    uint32_t *idx = (uint32_t *)malloc((size_t)E * sizeof(uint32_t) + 4);
+#pragma omp parallel for schedule(static)
     for (uint32_t i = 0; i < E; i++)
     {
-        adj[i] = secondary[p2[i]];
-        if (adj_w)
-            adj_w[i] = w ? w[p2[i]] : 0.0001f;
+        key[i] = ((uint64_t)primary[i] << b) | secondary[i];
+        idx[i] = i;
     }
-    free(p1);
-    free(p2);
-    free(tmp_off);
+    radix_sort_pairs(key, idx, E, 2 * b);
+    const uint64_t mask = ((uint64_t)1 << b) - 1;
+    /* off[v] = first position whose row is >= v */
+#pragma omp parallel for schedule(static)
+    for (uint32_t i = 0; i < E; i++)
+    {
+        const uint32_t r = (uint32_t)(key[i] >> b);
+        const uint32_t prev = i ? (uint32_t)(key[i - 1] >> b) + 1 : 0;
+        for (uint32_t v = prev; v <= r; v++)
+            off[v] = i;
+        adj[i] = (uint32_t)(key[i] & mask);
+        if (adj_w)
+            adj_w[i] = w ? w[idx[i]] : 0.0001f;
+    }
+    const uint32_t last = E ? (uint32_t)(key[E - 1] >> b) + 1 : 0;
+    for (uint32_t v = last; v <= V; v++)
+        off[v] = E;
+    free(key);
+    free(idx);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -527,13 +593,16 @@ void orc_ppr_f64_multi(const orc_csr *g, const uint32_t *seeds, uint32_t nseeds,
     double *tele = (double *)calloc((size_t)V + 1, sizeof(double));
     for (uint32_t i = 0; i < nseeds; i++) tele[seeds[i]] += 1.0 / (double)nseeds;
     for (uint32_t v = 0; v < V; v++) ranks[v] = tele[v];
+    /* per-vertex sums run in CSC order whatever the thread count */
     for (uint32_t it = 0; it < iterations; it++)
     {
+#pragma omp parallel for schedule(static)
         for (uint32_t v = 0; v < V; v++)
         {
             uint32_t d = out_degree(g, v);
             contrib[v] = d ? ranks[v] / d : 0.0;
         }
+#pragma omp parallel for schedule(dynamic, 1024)
         for (uint32_t v = 0; v < V; v++)
         {
             double s = 0.0;
@@ -965,6 +1034,7 @@ int orc_spmv(const orc_csr *g, int mode, uint32_t iterations, const float *x_in,
 
 void orc_spmv_f64(const orc_csr *g, const float *x, double *y)
 {
+#pragma omp parallel for schedule(dynamic, 1024)
     for (uint32_t v = 0; v < g->V; v++)
     {
         double s = 0.0;

@@ -1,7 +1,7 @@
 """Generate the golden vectors under tests/golden/ from the reference itself.
 
-Run in a tree where the reference snapshot is mounted (default
-/root/reference, or $ACCELGRAPH_REFERENCE):
+Run where the reference snapshot is available: $ACCELGRAPH_REFERENCE, or a
+checkout beside this repository (../reference):
 
     python tests/golden/make_golden.py            # everything
     python tests/golden/make_golden.py ring hubs  # only the golden files of those graphs
@@ -33,7 +33,7 @@ from oracle import oracle_ctypes as O  # noqa: E402
 sys.path.insert(0, os.path.dirname(HERE))
 from graphs import special_edges  # noqa: E402
 
-REF = os.environ.get("ACCELGRAPH_REFERENCE", "/root/reference")
+REF = os.environ.get("ACCELGRAPH_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 TEST = os.path.join(REF, "04_test_graphs", "TEST")
 
 FIXTURES = {

@@ -33,6 +33,22 @@ def test_reference_arm_prints_the_contract_line():
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
 
 
+def test_reference_arm_runs_the_same_config_without_the_product():
+    """The reference arm times the GPU arm's step (30 iterations) and never
+    imports or loads the product library: it builds its graph with the
+    oracle."""
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--scale', '9', '--steps', '1', "
+            "'--warmup', '0']; runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "assert 'accelgraph_express_gb300' not in sys.modules; "
+            "assert 'libaccelgraph_gb300' not in maps, 'product library loaded'")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads([x for x in out.stdout.splitlines() if x.startswith("{")][0])
+    assert line["config"]["iterations_per_step"] == 30 and line["config"]["epsilon"] == 0.0
+    assert line["config"]["workload"] == "pagerank_pull_rmat9"
+
+
 def test_algorithmic_bytes_match_the_stated_figures():
     """The byte counts behind roofline.achieved: one PageRank pull iteration
     (4E + 4(V+1) + (12+2s)V) and one gather launch (4E + 4(V+1) + sV + 4V) at

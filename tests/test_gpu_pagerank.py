@@ -12,8 +12,12 @@ Tolerances (stated here, used below):
   * mode 5 (push, 8-bit quantised scatter with FP32 atomics): L1 within
     5e-3 relative of the oracle (a rounding difference can move a quantised
     value by one level);
-  * data-driven push / pull-push (7, 8) are racy in the reference itself;
-    GPU ranks are compared to the FP64 fixed point with L1 <= 5e-2 relative;
+  * data-driven push / pull-push (7, 8) move residuals asynchronously (the
+    reference's OpenMP loop races on them; the GPU takes each residual with
+    an atomic exchange), so their ranks depend on the order of updates.
+    Against the FP64 fixed point (200 iterations), the GPU must be at least
+    as accurate as the oracle's race-free serial run of the same algorithm
+    (one thread), by the rule of tests/fpcheck.py;
   * BF16 / FP16 contribution storage vs the FP64 oracle: L1 relative error
     <= 2e-2 (BF16) and <= 3e-3 (FP16), reported as measured in the bench.
 """
@@ -71,9 +75,9 @@ def test_pagerank_modes_vs_oracle(graphs, dgs, orc, mode):
         ranks, res = dgs[name].pagerank(mode, iterations=20, epsilon=1e-4)
         ref, info = orc.pagerank(o, mode, 20, 1e-4)
         if mode in (7, 8):
-            ex = orc.pagerank_f64(o, 60)
-            l1 = np.abs(ranks - ex).sum() / max(np.abs(ex).sum(), 1e-30)
-            assert l1 <= 5e-2, (name, l1)
+            fixed_point = orc.pagerank_f64(o, 200)
+            serial, _ = orc.pagerank(o, mode, 20, 1e-4, nthreads=1)
+            assert_fp_as_accurate(ranks, serial, fixed_point, f"graph {name} mode {mode}")
             continue
         try:
             _cmp(mode, ranks, res, ref, info, orc, o)
