@@ -19,8 +19,13 @@
  * atomics into next[], then a vertex pass does the update.
  * Data-driven (modes 6, 7, 8): worklist variants (pageRank.c:2810-3300).
  *
- * Storage: contributions in FP32, BF16 or FP16 (FP32 accumulation), or in
- * the fixed-point / quantised integer formats summed exactly in 64 bits.
+ * Storage: contributions in FP32, or in the fixed-point / quantised integer
+ * formats summed exactly in 64 bits, or 16-bit BF16 / FP16 with an FP32
+ * correction pass: the gathered 16-bit values are per-iteration deltas of
+ * each vertex's contribution, and the vertex pass keeps the FP32 running
+ * sums and the FP32 value of everything stored so far, so every iteration
+ * stores the rounding of (contribution - stored so far) and no rounding
+ * error accumulates (k_pr_update_delta).
  *
  * From 1M vertices the FP pull gather reads the contributions of the
  * vertices with the most out-edges from a shared-memory table
@@ -47,7 +52,9 @@ struct IterRec
 {
     double err;
     uint32_t active;
-    uint32_t maxbits;  /* max contribution (float bits) for the quantised modes */
+    uint32_t maxbits;  /* max contribution (float bits) for the quantised modes; max |delta| for BF16/FP16 */
+    float qinv;        /* BF16/FP16: 1 / the scale this iteration's stored deltas were written with */
+    uint32_t pad;
 };
 
 /* ---- contribution formats --------------------------------------------------- */
@@ -483,6 +490,106 @@ __global__ void k_pr_update(PrCommon c, typename Fmt<K>::Acc *sums, typename Fmt
     if (threadIdx.x == 0) c.reduce(err, act);
 }
 
+/* ---- BF16 / FP16 storage with the FP32 correction pass ------------------------- */
+
+/* FP16 deltas are stored multiplied by a power of two chosen from the
+ * largest |delta| of the previous iteration, which lands at 2^13 .. 2^14
+ * (deltas may grow 4x before FP16's 65504 saturates; a saturated or
+ * underflowed part stays in the next delta).  Returns the exponent. */
+__device__ __forceinline__ int f16_scale_exp(uint32_t maxbits)
+{
+    const int be = (int)((maxbits >> 23) & 0xffu);
+    if (be == 0) return 0; /* zero (or subnormal) deltas: scale 1 */
+    int k = 13 - (be - 127);
+    return k < -120 ? -120 : (k > 120 ? 120 : k);
+}
+__device__ __forceinline__ float pow2f(int k) { return __uint_as_float((uint32_t)(127 + k) << 23); }
+
+/* store delta d (FP32) in format K with scale 2^k; returns the value the
+ * gather will see, unscaled (exact: a power-of-two product) */
+template <int K>
+__device__ __forceinline__ float store_delta(float d, int k, typename Fmt<K>::CT *q)
+{
+    if constexpr (K == K_BF16)
+    {
+        const __nv_bfloat16 b = __float2bfloat16_rn(d);
+        *q = b;
+        return __bfloat162float(b);
+    }
+    else
+    {
+        float x = __fmul_rn(d, pow2f(k));
+        x = fminf(fmaxf(x, -65504.0f), 65504.0f);
+        const __half h = __float2half_rn(x);
+        *q = h;
+        return __fmul_rn(__half2float(h), pow2f(-k));
+    }
+}
+
+/* initial state: rank = init, nothing stored yet, so the first delta is the
+ * whole first contribution; FP16's first scale comes from `init`, the
+ * largest contribution there is (out-degrees are >= 1) */
+template <int K>
+__global__ void k_pr_init_delta(float *__restrict__ rank, const uint32_t *__restrict__ outdeg, uint32_t V, float init,
+                                typename Fmt<K>::CT *qout, float *__restrict__ S, float *__restrict__ chat, IterRec *rec)
+{
+    const int k = K == K_F16 ? f16_scale_exp(__float_as_uint(init)) : 0;
+    uint32_t tmax = 0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    {
+        rank[v] = init;
+        const float c = contrib_of(init, outdeg[v]);
+        S[v] = 0.0f;
+        chat[v] = store_delta<K>(c, k, &qout[v]);
+        tmax = max(tmax, __float_as_uint(c));
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) rec[0].qinv = pow2f(-k);
+    block_max_bits<256>(tmax, &rec[0].maxbits);
+}
+
+/* The FP32 correction pass: the vertex update (pageRank.c:1055-1069, fused
+ * with the contribution pass :1026-1033) for 16-bit storage.  dsum[v] is
+ * the gathered (pull) or scattered (push) sum of the in-neighbours' stored
+ * deltas; S[v] is the FP32 sum of everything gathered so far (the sum of
+ * the in-neighbours' stored contributions), chat[v] the FP32 value of
+ * everything v has stored so far.  rank' = 0.15 + 0.85 * S, the next stored
+ * delta is round16(contrib' - chat): what one iteration's rounding lost is
+ * sent in the next, so the ranks carry only the rounding of the last delta,
+ * which shrinks as the iteration converges. */
+template <int K>
+__global__ void k_pr_update_delta(PrCommon c, float *dsum, float *__restrict__ S, float *__restrict__ chat,
+                                  typename Fmt<K>::CT *__restrict__ qout)
+{
+    if (c.skip()) return;
+    double err = 0.0;
+    uint32_t act = 0, tmax = 0;
+    const float in_inv = c.rec[c.it].qinv;
+    const int k = K == K_F16 ? f16_scale_exp(c.rec[c.it].maxbits) : 0;
+    float *__restrict__ rank = c.rank;
+    const uint32_t *__restrict__ outdeg = c.outdeg;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < c.V; v += gridDim.x * blockDim.x)
+    {
+        const float ds = dsum[v];
+        clear_after_read(&dsum[v], ds);
+        const float s = __fadd_rn(S[v], __fmul_rn(ds, in_inv));
+        S[v] = s;
+        const float pr = rank[v];
+        const float nr = __fadd_rn(c.base, __fmul_rn(c.damp, s));
+        rank[v] = nr;
+        const float e = fabsf(__fsub_rn(nr, pr));
+        err += (double)e;
+        if (e >= c.eps_f) act++;
+        const float ch = chat[v];
+        const float d = __fsub_rn(contrib_of(nr, outdeg[v]), ch);
+        chat[v] = __fadd_rn(ch, store_delta<K>(d, k, &qout[v]));
+        tmax = max(tmax, __float_as_uint(fabsf(d)));
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) c.rec[c.it + 1].qinv = pow2f(-k);
+    block_max_bits<256>(tmax, &c.rec[c.it + 1].maxbits);
+    block_sum2<256>(err, act);
+    if (threadIdx.x == 0) c.reduce(err, act);
+}
+
 /* ---- data-driven variants (pageRank.c:2810-3300) -------------------------------- */
 
 __global__ void k_dd_contrib(const float *__restrict__ rank, const uint32_t *__restrict__ outdeg, float *cf, uint32_t V,
@@ -675,9 +782,20 @@ gg_status run_pull(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
     GG_CHECK(gg_work(g, 5, ((size_t)V + 16) * sizeof(Acc), &sums));
     GG_CUDA(cudaMemsetAsync(sums, 0, ((size_t)V + 16) * sizeof(Acc), R.s));
     CT *cb[2] = {(CT *)c0, (CT *)c1};
+    /* 16-bit storage: FP32 running sums and stored-so-far values */
+    constexpr bool delta = K == K_BF16 || K == K_F16;
+    void *Sb = nullptr, *chb = nullptr;
+    if (delta)
+    {
+        GG_CHECK(gg_work(g, 28, ((size_t)V + 16) * 4, &Sb));
+        GG_CHECK(gg_work(g, 29, ((size_t)V + 16) * 4, &chb));
+    }
 
-    k_pr_init<K><<<grid_v(V), 256, 0, R.s>>>(rank, g->out_deg, V, init, Fmt<K>::quant ? nullptr : cb[0],
-                                               (float *)cf, rec);
+    if constexpr (delta)
+        k_pr_init_delta<K><<<grid_v(V), 256, 0, R.s>>>(rank, g->out_deg, V, init, cb[0], (float *)Sb, (float *)chb, rec);
+    else
+        k_pr_init<K><<<grid_v(V), 256, 0, R.s>>>(rank, g->out_deg, V, init, Fmt<K>::quant ? nullptr : cb[0],
+                                                   (float *)cf, rec);
     R.launches++;
     for (uint32_t it = 0; it < iters; it++)
     {
@@ -702,7 +820,11 @@ gg_status run_pull(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
         PrCommon c;
         c.rank = rank; c.outdeg = g->out_deg; c.V = V; c.base = base; c.damp = R.p->damp;
         c.eps_f = R.eps_f; c.eps_fl = R.eps_fl; c.rec = rec; c.it = it;
-        k_pr_update<K><<<grid_v(V), 256, 0, R.s>>>(c, (Acc *)sums, cb[(it + 1) & 1], (float *)cf);
+        if constexpr (delta)
+            k_pr_update_delta<K><<<grid_v(V), 256, 0, R.s>>>(c, (float *)sums, (float *)Sb, (float *)chb,
+                                                             cb[(it + 1) & 1]);
+        else
+            k_pr_update<K><<<grid_v(V), 256, 0, R.s>>>(c, (Acc *)sums, cb[(it + 1) & 1], (float *)cf);
         R.launches += 2;
         R.gather_launches++;
     }
@@ -729,8 +851,19 @@ gg_status run_push(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
         GG_CHECK(gg_work(g, 6, ((size_t)iters + 2) * 4, &zeros));
     }
     constexpr int KI = (K == K_Q8Z ? K_Q8 : K);
+    /* 16-bit storage: the scatter moves stored deltas (k_pr_update_delta) */
+    constexpr bool delta = K == K_BF16 || K == K_F16;
+    void *Sb = nullptr, *chb = nullptr;
+    if (delta)
+    {
+        GG_CHECK(gg_work(g, 28, ((size_t)V + 16) * 4, &Sb));
+        GG_CHECK(gg_work(g, 29, ((size_t)V + 16) * 4, &chb));
+    }
     if constexpr (K == K_Q8Z)
         k_pr_init<K_Q8><<<grid_v(V), 256, 0, R.s>>>(rank, g->out_deg, V, init, nullptr, (float *)cf, rec);
+    else if constexpr (delta)
+        k_pr_init_delta<K><<<grid_v(V), 256, 0, R.s>>>(rank, g->out_deg, V, init, (CT *)c0, (float *)Sb, (float *)chb,
+                                                         rec);
     else
         k_pr_init<K><<<grid_v(V), 256, 0, R.s>>>(rank, g->out_deg, V, init, (CT *)c0, nullptr, rec);
     R.launches++;
@@ -769,6 +902,8 @@ gg_status run_push(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
             k_pr_update<K_FX64><<<grid_v(V), 256, 0, R.s>>>(c, (unsigned long long *)nx, (unsigned long long *)c0, nullptr);
         else if constexpr (K == K_Q8Z)
             k_pr_update<K_Q8Z><<<grid_v(V), 256, 0, R.s>>>(c, (float *)nx, nullptr, (float *)cf);
+        else if constexpr (delta)
+            k_pr_update_delta<K><<<grid_v(V), 256, 0, R.s>>>(c, (float *)nx, (float *)Sb, (float *)chb, (CT *)c0);
         else
             k_pr_update<K><<<grid_v(V), 256, 0, R.s>>>(c, (float *)nx, (CT *)c0, nullptr);
         R.launches++;

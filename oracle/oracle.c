@@ -548,6 +548,91 @@ int orc_pagerank(const orc_csr *g, int mode, uint32_t iterations, double epsilon
     return 0;
 }
 
+/* Data-driven push (mode 7) and pull-push (mode 8) in the synchronous
+ * order: every worklist vertex takes the residual it held when the
+ * iteration began, and pull-push reads the ranks of that moment; pushes go
+ * to the residuals in vertex order (which fixes the activation tests).  The
+ * reference's OpenMP loop (pageRank.c:3049-3090) lies between this order
+ * and the sequential one of orc_pagerank, as does a GPU run of the same
+ * loop, whose vertices take their residuals with atomic exchanges at any
+ * point of the iteration.  ranks: V floats out, divided by V. */
+void orc_pagerank_dd_sync(const orc_csr *g, int mode, uint32_t iterations, double epsilon, float *ranks)
+{
+    const uint32_t V = g->V;
+    const float damp = 0.85f, base = 1.0f - damp;
+    float *resid = (float *)calloc((size_t)V + 1, sizeof(float));
+    float *taken = (float *)calloc((size_t)V + 1, sizeof(float));
+    float *old_rank = (float *)calloc((size_t)V + 1, sizeof(float));
+    uint8_t *wl_curr = (uint8_t *)calloc((size_t)V + 1, 1);
+    uint8_t *wl_next = (uint8_t *)calloc((size_t)V + 1, 1);
+    for (uint32_t v = 0; v < V; v++)
+    {
+        ranks[v] = base;
+        float r = 0.0f;
+        for (uint32_t j = g->in_off[v]; j < g->in_off[v + 1]; j++)
+        {
+            uint32_t du = out_degree(g, g->in_adj[j]);
+            if (du)
+                r += 1.0f / (float)du;
+        }
+        resid[v] = (1.0f - damp) * damp * r;
+        wl_curr[v] = 1;
+    }
+    for (uint32_t it = 0; it < iterations; it++)
+    {
+        uint32_t active = 0;
+        for (uint32_t v = 0; v < V; v++)
+        {
+            old_rank[v] = ranks[v];
+            taken[v] = 0.0f;
+            if (wl_curr[v])
+            {
+                taken[v] = resid[v];
+                resid[v] = 0.0f;
+            }
+        }
+        for (uint32_t v = 0; v < V; v++)
+        {
+            if (!wl_curr[v])
+                continue;
+            if (mode == 7)
+                ranks[v] = taken[v] + old_rank[v];
+            else
+            {
+                float in_pr = 0.0f;
+                for (uint32_t j = g->in_off[v]; j < g->in_off[v + 1]; j++)
+                {
+                    uint32_t u = g->in_adj[j];
+                    in_pr += old_rank[u] / (float)out_degree(g, u);
+                }
+                ranks[v] = base + (damp * in_pr);
+            }
+            uint32_t deg = out_degree(g, v);
+            float delta = damp * (taken[v] / deg);
+            for (uint32_t j = g->out_off[v]; j < g->out_off[v + 1]; j++)
+            {
+                uint32_t u = g->out_adj[j];
+                float prev = resid[u];
+                resid[u] += delta;
+                if ((fabs(prev + delta) >= epsilon) && (prev <= epsilon))
+                {
+                    active++;
+                    if (mode == 8)
+                        resid[u] += delta;
+                    wl_next[u] = 1;
+                }
+            }
+        }
+        uint8_t *t = wl_curr; wl_curr = wl_next; wl_next = t;
+        memset(wl_next, 0, V);
+        if (active == 0)
+            break;
+    }
+    for (uint32_t v = 0; v < V; v++)
+        ranks[v] = ranks[v] / (float)V;
+    free(resid); free(taken); free(old_rank); free(wl_curr); free(wl_next);
+}
+
 void orc_pagerank_f64(const orc_csr *g, uint32_t executed, int init_one_over_n, double *ranks)
 {
     const uint32_t V = g->V;

@@ -98,6 +98,11 @@ typedef struct orc_pr_out
 int orc_pagerank(const orc_csr *g, int mode, uint32_t iterations, double epsilon,
                  int init_one_over_n, float *ranks, orc_pr_out *out, int nthreads);
 
+/* Data-driven push (7) / pull-push (8) in the synchronous order (every
+ * vertex takes the residual it held when the iteration began); the other
+ * end of the range of schedules from orc_pagerank's sequential one. */
+void orc_pagerank_dd_sync(const orc_csr *g, int mode, uint32_t iterations, double epsilon, float *ranks);
+
 /* FP64 power iteration, same formulation, exactly `executed` iterations,
  * summing in-edges in CSC order.  ranks: V doubles out. */
 void orc_pagerank_f64(const orc_csr *g, uint32_t executed, int init_one_over_n, double *ranks);

@@ -64,6 +64,7 @@ def lib():
         L.orc_pagerank.argtypes = [C.POINTER(OrcCsr), C.c_int, C.c_uint32, C.c_double, C.c_int,
                                    f32p, C.POINTER(OrcPrOut), C.c_int]
         L.orc_pagerank.restype = C.c_int
+        L.orc_pagerank_dd_sync.argtypes = [C.POINTER(OrcCsr), C.c_int, C.c_uint32, C.c_double, f32p]
         L.orc_pagerank_f64.argtypes = [C.POINTER(OrcCsr), C.c_uint32, C.c_int, f64p]
         L.orc_ppr_f64.argtypes = [C.POINTER(OrcCsr), C.c_uint32, C.c_uint32, C.c_double, f64p]
         L.orc_ppr_f64_multi.argtypes = [C.POINTER(OrcCsr), u32p, C.c_uint32, C.c_uint32, C.c_double, f64p]
@@ -202,6 +203,14 @@ def pagerank(g: Csr, mode=0, iterations=20, epsilon=1e-4, init_one_over_n=False,
     return ranks, {"iterations": out.iterations, "active": out.active,
                    "error_total": out.error_total, "rank_sum": out.rank_sum,
                    "executed": out.executed}
+
+
+def pagerank_dd_sync(g: Csr, mode, iterations=20, epsilon=1e-4):
+    """Data-driven push (7) / pull-push (8) in the synchronous order."""
+    ranks = np.empty(g.V, np.float32)
+    cs = g.c()
+    lib().orc_pagerank_dd_sync(C.byref(cs), mode, iterations, epsilon, ranks)
+    return ranks
 
 
 def pagerank_f64(g: Csr, executed, init_one_over_n=False):

@@ -15,11 +15,21 @@ Tolerances (stated here, used below):
   * data-driven push / pull-push (7, 8) move residuals asynchronously (the
     reference's OpenMP loop races on them; the GPU takes each residual with
     an atomic exchange), so their ranks depend on the order of updates.
+    The oracle runs the two ends of the range of orders: sequential (every
+    push seen by later vertices of the same iteration) and synchronous
+    (every vertex takes the residual it held when the iteration began).
     Against the FP64 fixed point (200 iterations), the GPU must be at least
-    as accurate as the oracle's race-free serial run of the same algorithm
-    (one thread), by the rule of tests/fpcheck.py;
-  * BF16 / FP16 contribution storage vs the FP64 oracle: L1 relative error
-    <= 2e-2 (BF16) and <= 3e-3 (FP16), reported as measured in the bench.
+    as accurate as the less accurate of the two, by the rule of
+    tests/fpcheck.py;
+  * BF16 / FP16 storage with the FP32 correction pass (the gather reads
+    16-bit deltas, the vertex pass keeps FP32 sums and what was stored so
+    far): relative L1 vs the FP64 oracle after 30 iterations <= 5e-6 on the
+    R-MAT graphs (a CPU simulation of the same arithmetic gives 1.2e-6 to
+    2.0e-6 for BF16 and 1.4e-7 to 4.1e-7 for FP16 there; the bar on R-MAT-24
+    is 1e-6 absolute, measured in the bench).  On the hub graph, whose
+    deltas shrink only by the damping factor per iteration and span ten
+    orders of magnitude: BF16 <= 1e-4 (simulated 2.1e-5); FP16, whose one
+    scale per iteration must cover that span, <= 3e-3 (simulated 1.1e-3).
 """
 import os
 
@@ -77,7 +87,10 @@ def test_pagerank_modes_vs_oracle(graphs, dgs, orc, mode):
         if mode in (7, 8):
             fixed_point = orc.pagerank_f64(o, 200)
             serial, _ = orc.pagerank(o, mode, 20, 1e-4, nthreads=1)
-            assert_fp_as_accurate(ranks, serial, fixed_point, f"graph {name} mode {mode}")
+            sync = orc.pagerank_dd_sync(o, mode, 20, 1e-4)
+            err = lambda x: float(np.abs(x.astype(np.float64) - fixed_point).sum())  # noqa: E731
+            worse = serial if err(serial) >= err(sync) else sync
+            assert_fp_as_accurate(ranks, worse, fixed_point, f"graph {name} mode {mode}")
             continue
         try:
             _cmp(mode, ranks, res, ref, info, orc, o)
@@ -106,16 +119,37 @@ def test_pagerank_vs_reference_golden(graphs, dgs, orc, name):
             raise AssertionError(f"graph {name} mode {mode}: {e}") from None
 
 
-@pytest.mark.parametrize("storage,tol", [("bf16", 2e-2), ("f16", 3e-3)])
+LOW_PRECISION_TOL = {("bf16", "rmat10"): 5e-6, ("bf16", "rmat16"): 5e-6, ("bf16", "hubs"): 1e-4,
+                     ("f16", "rmat10"): 5e-6, ("f16", "rmat16"): 5e-6, ("f16", "hubs"): 3e-3}
+
+
+@pytest.mark.parametrize("storage", ["bf16", "f16"])
 @pytest.mark.parametrize("mode", ["pull", "push"])
-def test_pagerank_low_precision_storage(graphs, dgs, orc, storage, tol, mode):
+def test_pagerank_low_precision_storage(graphs, dgs, orc, storage, mode):
     for name in ["rmat10", "rmat16", "hubs"]:
         g, o = graphs[name]
         ranks, res = dgs[name].pagerank(mode, storage=storage, iterations=30, epsilon=0.0)
         ex = orc.pagerank_f64(o, 30)
         l1 = np.abs(ranks - ex).sum() / np.abs(ex).sum()
-        assert l1 <= tol, (name, storage, l1)
+        assert l1 <= LOW_PRECISION_TOL[storage, name], (name, storage, l1)
         assert res["iterations"] == 30
+
+
+def test_pagerank_bf16_hot_table_and_epsilon(graphs, dgs, orc):
+    """BF16 with the correction pass through the hot-vertex table, and with
+    an epsilon stop: the stop rule reads the FP32 ranks, so the iteration
+    count is the FP32 run's (within one, for a vertex on the threshold), and
+    the ranks stay within the R-MAT bound."""
+    g, o = graphs["rmat16"]
+    ex = orc.pagerank_f64(o, 30)
+    hot, res = dgs["rmat16"].pagerank("pull", storage="bf16", iterations=30, epsilon=0.0, hot=True)
+    assert res["hot_table"] == 1
+    assert np.abs(hot - ex).sum() / np.abs(ex).sum() <= 5e-6
+    _, res32 = dgs["rmat16"].pagerank("pull", iterations=20, epsilon=1e-4)
+    r16, res16 = dgs["rmat16"].pagerank("pull", storage="bf16", iterations=20, epsilon=1e-4)
+    assert abs(res16["iterations"] - res32["iterations"]) <= 1
+    ex = orc.pagerank_f64(o, res16["iterations"] + (1 if res16["active"] == 0 else 0))
+    assert np.abs(r16 - ex).sum() / np.abs(ex).sum() <= 5e-6
 
 
 def test_pagerank_one_over_n_formulation(graphs, dgs, orc):
