@@ -254,6 +254,16 @@ def lib() -> C.CDLL:
                                         C.c_void_p]
         L.graphCSRFromEdgeList.argtypes = [P(EdgeList)]
         L.graphCSRFromEdgeList.restype = P(GraphCSR)
+        L.writeEdgeListsText.argtypes = [P(EdgeList), C.c_char_p]
+        L.writeEdgeListsbin.argtypes = [P(EdgeList), C.c_char_p]
+        L.writeGraphCSRbin.argtypes = [P(GraphCSR), C.c_char_p]
+        L.readGraphCSRbin.argtypes = [C.c_char_p]
+        L.readGraphCSRbin.restype = P(GraphCSR)
+        L.edgeListFromGraphCSR.argtypes = [P(GraphCSR)]
+        L.edgeListFromGraphCSR.restype = P(EdgeList)
+        L.graphCSRFromFile.argtypes = [C.c_char_p, C.c_uint32, C.c_int]
+        L.graphCSRFromFile.restype = P(GraphCSR)
+        L.writeSerializedGraphDataStructure.argtypes = [P(Arguments)]
         L.graphCSRFromEdgeListDevice.argtypes = [P(EdgeList)]
         L.graphCSRFromEdgeListDevice.restype = P(GraphCSR)
         L.graphCSRFromEdgeListRelabelDevice.argtypes = [P(EdgeList), C.c_uint32, C.c_uint64]
@@ -432,14 +442,29 @@ class Graph:
             L.freeEdgeList(el)
 
     @classmethod
-    def from_file(cls, path, weighted=False):
-        L = lib()
-        fn = L.readEdgeListsbin if path.endswith("bin") else L.readEdgeListsText
-        el = fn(path.encode(), int(weighted))
-        if not el:
+    def from_file(cls, path, weighted=False, fmt=None):
+        """fmt: the reference's -z code (0 text edge list, 1 binary edge
+        list, 2 graphCSR binary); by default from the extension (.csr: 2,
+        .bin / .wbin: 1, else 0)."""
+        if fmt is None:
+            fmt = 2 if path.endswith(".csr") else 1 if path.endswith("bin") else 0
+        g = lib().graphCSRFromFile(path.encode(), fmt, int(weighted))
+        if not g:
             raise GgError(f"cannot read {path}")
+        return cls(g)
+
+    def save(self, path):
+        """Write the graphCSR binary file (the -c 2 format)."""
+        if lib().writeGraphCSRbin(self.ptr, path.encode()) != 0:
+            raise GgError(f"cannot write {path}")
+
+    def save_edges(self, path, binary=True):
+        """Write the edges in CSR order as a binary (.bin / .wbin) or text edge list."""
+        L = lib()
+        el = L.edgeListFromGraphCSR(self.ptr)
         try:
-            return cls(L.graphCSRFromEdgeList(el))
+            if (L.writeEdgeListsbin if binary else L.writeEdgeListsText)(el, path.encode()) != 0:
+                raise GgError(f"cannot write {path}")
         finally:
             L.freeEdgeList(el)
 

@@ -14,6 +14,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <errno.h>
+#include <math.h>
 #include <omp.h>
 
 #include "graphCSR.h"
@@ -648,4 +649,267 @@ void graphCSRFree(struct GraphCSR *g)
     free_edges(g->sorted_edges_array);
     free_edges(g->inverse_sorted_edges_array);
     free(g);
+}
+
+/* ---- serialisation: the reference's -z / -c / -x formats ------------------------
+ * (02_capi_graph/src/main/accel-graph.c:51 -z, :115-128 -c, :339-341 -x).
+ * Text and binary edge lists are the 04_test_graphs formats; the graphCSR
+ * binary layout is OpenGraph's and that code is absent, so this one is the
+ * project's own: a header, then every array of the GraphCSR in a fixed
+ * order, so a read gives back a graph whose arrays equal the written ones. */
+
+static int write_all(FILE *f, const void *p, size_t n) { return n == 0 || fwrite(p, 1, n, f) == n; }
+static int read_all(FILE *f, void *p, size_t n) { return n == 0 || fread(p, 1, n, f) == n; }
+
+int writeEdgeListsText(const struct EdgeList *e, const char *fname)
+{
+    FILE *f = e ? fopen(fname, "w") : NULL;
+    if (!f)
+    {
+        fprintf(stderr, "writeEdgeListsText: cannot open %s: %s\n", fname, e ? strerror(errno) : "no edge list");
+        return -1;
+    }
+    int ok = 1;
+    for (uint32_t i = 0; ok && i < e->num_edges; i++)
+    {
+        if (e->edges_array_weight)
+            ok = fprintf(f, "%u %u %.9g\n", e->edges_array_src[i], e->edges_array_dest[i],
+                         (double)e->edges_array_weight[i]) > 0;
+        else
+            ok = fprintf(f, "%u %u\n", e->edges_array_src[i], e->edges_array_dest[i]) > 0;
+    }
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) fprintf(stderr, "writeEdgeListsText: %s: write failed\n", fname);
+    return ok ? 0 : -1;
+}
+
+int writeEdgeListsbin(const struct EdgeList *e, const char *fname)
+{
+    FILE *f = e ? fopen(fname, "wb") : NULL;
+    if (!f)
+    {
+        fprintf(stderr, "writeEdgeListsbin: cannot open %s: %s\n", fname, e ? strerror(errno) : "no edge list");
+        return -1;
+    }
+    const int weighted = e->edges_array_weight != NULL;
+    const uint32_t k = weighted ? 3 : 2, chunk = 1u << 16;
+    uint32_t *buf = (uint32_t *)xmalloc((size_t)chunk * k * 4);
+    int ok = buf != NULL;
+    for (uint32_t i0 = 0; ok && i0 < e->num_edges; i0 += chunk)
+    {
+        const uint32_t n = e->num_edges - i0 < chunk ? e->num_edges - i0 : chunk;
+        for (uint32_t j = 0; j < n; j++)
+        {
+            buf[(size_t)j * k] = e->edges_array_src[i0 + j];
+            buf[(size_t)j * k + 1] = e->edges_array_dest[i0 + j];
+            /* the weight word is an integer, as readEdgeListsbin reads it */
+            if (weighted) buf[(size_t)j * k + 2] = (uint32_t)lrintf(e->edges_array_weight[i0 + j]);
+        }
+        ok = write_all(f, buf, (size_t)n * k * 4);
+    }
+    free(buf);
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) fprintf(stderr, "writeEdgeListsbin: %s: write failed\n", fname);
+    return ok ? 0 : -1;
+}
+
+#define GG_CSR_MAGIC "AGXCSR1"
+
+struct csr_file_header
+{
+    char magic[8];
+    uint32_t num_vertices, num_edges, weighted, avg_degree;
+    float max_weight;
+    uint32_t reserved[3];
+};
+
+/* the arrays of a GraphCSR in file order: (pointer, element count) */
+static int csr_arrays(const struct GraphCSR *g, void **ptr, size_t *n)
+{
+    const size_t V = g->num_vertices, E = g->num_edges;
+    int k = 0;
+    const struct Vertex *vx[2] = {g->vertices, g->inverse_vertices};
+    for (int d = 0; d < 2; d++)
+    {
+        ptr[k] = vx[d]->out_degree; n[k++] = V;
+        ptr[k] = vx[d]->in_degree; n[k++] = V;
+        ptr[k] = vx[d]->edges_idx; n[k++] = V;
+    }
+    const struct EdgeList *el[2] = {g->sorted_edges_array, g->inverse_sorted_edges_array};
+    for (int d = 0; d < 2; d++)
+    {
+        ptr[k] = el[d]->edges_array_src; n[k++] = E;
+        ptr[k] = el[d]->edges_array_dest; n[k++] = E;
+        ptr[k] = el[d]->edges_array_weight; n[k++] = el[d]->edges_array_weight ? E : 0;
+        ptr[k] = el[d]->label_array; n[k++] = V;
+        ptr[k] = el[d]->inverse_label_array; n[k++] = V;
+    }
+    return k;
+}
+
+int writeGraphCSRbin(const struct GraphCSR *g, const char *fname)
+{
+    FILE *f = g ? fopen(fname, "wb") : NULL;
+    if (!f)
+    {
+        fprintf(stderr, "writeGraphCSRbin: cannot open %s: %s\n", fname, g ? strerror(errno) : "no graph");
+        return -1;
+    }
+    struct csr_file_header h;
+    memset(&h, 0, sizeof h);
+    memcpy(h.magic, GG_CSR_MAGIC, 8);
+    h.num_vertices = g->num_vertices;
+    h.num_edges = g->num_edges;
+    h.weighted = g->sorted_edges_array->edges_array_weight != NULL;
+    h.avg_degree = g->avg_degree;
+    h.max_weight = g->max_weight;
+    void *ptr[16];
+    size_t n[16];
+    const int na = csr_arrays(g, ptr, n);
+    int ok = write_all(f, &h, sizeof h);
+    for (int i = 0; ok && i < na; i++)
+        ok = write_all(f, ptr[i], n[i] * 4);
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) fprintf(stderr, "writeGraphCSRbin: %s: write failed\n", fname);
+    return ok ? 0 : -1;
+}
+
+struct GraphCSR *readGraphCSRbin(const char *fname)
+{
+    FILE *f = fopen(fname, "rb");
+    if (!f)
+    {
+        fprintf(stderr, "readGraphCSRbin: cannot open %s: %s\n", fname, strerror(errno));
+        return NULL;
+    }
+    struct csr_file_header h;
+    if (!read_all(f, &h, sizeof h) || memcmp(h.magic, GG_CSR_MAGIC, 8) != 0)
+    {
+        fprintf(stderr, "readGraphCSRbin: %s: not a graphCSR binary file\n", fname);
+        fclose(f);
+        return NULL;
+    }
+    fseek(f, 0, SEEK_END);
+    const long bytes = ftell(f);
+    const uint64_t want = sizeof h + 4ull * (10ull * h.num_vertices + 4ull * h.num_edges +
+                                             (h.weighted ? 2ull * h.num_edges : 0ull));
+    if (bytes < 0 || (uint64_t)bytes != want)
+    {
+        fprintf(stderr, "readGraphCSRbin: %s: size %ld, expected %llu\n", fname, bytes, (unsigned long long)want);
+        fclose(f);
+        return NULL;
+    }
+    fseek(f, (long)sizeof h, SEEK_SET);
+    struct GraphCSR *g = alloc_graph(h.num_vertices, h.num_edges, h.weighted != 0, h.max_weight);
+    int ok = g != NULL;
+    for (int d = 0; ok && d < 2; d++)
+    {
+        struct EdgeList *el = d ? g->inverse_sorted_edges_array : g->sorted_edges_array;
+        el->label_array = (uint32_t *)xmalloc((size_t)h.num_vertices * 4 + 64);
+        el->inverse_label_array = (uint32_t *)xmalloc((size_t)h.num_vertices * 4 + 64);
+        el->max_weight = h.max_weight;
+        ok = el->label_array && el->inverse_label_array;
+    }
+    void *ptr[16];
+    size_t n[16];
+    const int na = ok ? csr_arrays(g, ptr, n) : 0;
+    for (int i = 0; ok && i < na; i++)
+        ok = read_all(f, ptr[i], n[i] * 4);
+    fclose(f);
+    if (!ok)
+    {
+        fprintf(stderr, "readGraphCSRbin: %s: read failed\n", fname);
+        graphCSRFree(g);
+        return NULL;
+    }
+    g->avg_degree = h.avg_degree;
+    /* page-lock the arrays the GPU path uploads, as the builds do */
+    const size_t V = h.num_vertices, E = h.num_edges;
+    gg_host_pin(g->vertices->out_degree, V * 4);
+    gg_host_pin(g->vertices->edges_idx, V * 4);
+    gg_host_pin(g->inverse_vertices->edges_idx, V * 4);
+    gg_host_pin(g->sorted_edges_array->edges_array_dest, E * 4);
+    gg_host_pin(g->inverse_sorted_edges_array->edges_array_dest, E * 4);
+    if (h.weighted)
+    {
+        gg_host_pin(g->sorted_edges_array->edges_array_weight, E * 4);
+        gg_host_pin(g->inverse_sorted_edges_array->edges_array_weight, E * 4);
+    }
+    return g;
+}
+
+struct EdgeList *edgeListFromGraphCSR(const struct GraphCSR *g)
+{
+    if (!g)
+        return NULL;
+    const struct EdgeList *s = g->sorted_edges_array;
+    struct EdgeList *e = newEdgeList(g->num_edges, g->num_vertices, s->edges_array_weight != NULL);
+    if (!e)
+        return NULL;
+    /* edges in CSR order, as original ids (through the inverse labels) */
+    for (uint32_t i = 0; i < g->num_edges; i++)
+    {
+        e->edges_array_src[i] = s->inverse_label_array[s->edges_array_src[i]];
+        e->edges_array_dest[i] = s->inverse_label_array[s->edges_array_dest[i]];
+        if (e->edges_array_weight) e->edges_array_weight[i] = s->edges_array_weight[i];
+    }
+    e->num_vertices = g->num_vertices;
+    e->max_weight = g->max_weight;
+    return e;
+}
+
+struct GraphCSR *graphCSRFromFile(const char *fname, uint32_t format, int weighted)
+{
+    if (format == 2)
+        return readGraphCSRbin(fname);
+    struct EdgeList *e = format == 0 ? readEdgeListsText(fname, weighted) : readEdgeListsbin(fname, weighted);
+    if (!e)
+        return NULL;
+    struct GraphCSR *g = graphCSRFromEdgeList(e);
+    freeEdgeList(e);
+    return g;
+}
+
+void writeSerializedGraphDataStructure(struct Arguments *arguments)
+{
+    if (!arguments || !arguments->fnameb)
+    {
+        fprintf(stderr, "writeSerializedGraphDataStructure: no input file (-f)\n");
+        return;
+    }
+    const char *in = arguments->fnameb;
+    const uint32_t from = arguments->fnameb_format, to = arguments->convert_format;
+    const int weighted = arguments->weighted != 0;
+    const char *ext = to == 0 ? ".txt" : to == 1 ? (weighted ? ".wbin" : ".bin") : ".csr";
+    size_t len = strlen(in) + strlen(ext) + 1;
+    char *out = (char *)malloc(len);
+    if (!out)
+        return;
+    snprintf(out, len, "%s%s", in, ext);
+    int rc = -1;
+    if (to == 2)
+    {
+        struct GraphCSR *g = graphCSRFromFile(in, from, weighted);
+        if (g) rc = writeGraphCSRbin(g, out);
+        graphCSRFree(g);
+    }
+    else
+    {
+        struct EdgeList *e = NULL;
+        if (from == 2)
+        {
+            struct GraphCSR *g = readGraphCSRbin(in);
+            e = edgeListFromGraphCSR(g);
+            graphCSRFree(g);
+        }
+        else
+            e = from == 0 ? readEdgeListsText(in, weighted) : readEdgeListsbin(in, weighted);
+        if (e) rc = to == 0 ? writeEdgeListsText(e, out) : writeEdgeListsbin(e, out);
+        freeEdgeList(e);
+    }
+    if (rc == 0)
+        printf("| %-51s | \n| %-51s | \n", "serialised", out);
+    else
+        fprintf(stderr, "writeSerializedGraphDataStructure: %s -> %s failed\n", in, out);
+    free(out);
 }

@@ -140,6 +140,35 @@ struct GraphCSR *graphCSRFromEdgeListDevice(const struct EdgeList *edgeList);
 struct GraphCSR *graphCSRFromEdgeListRelabelDevice(const struct EdgeList *edgeList, uint32_t lmode, uint64_t seed);
 void graphCSRFree(struct GraphCSR *graph);
 
+/* ---- serialisation ----------------------------------------------------------
+ * The reference's file options (02_capi_graph/src/main/accel-graph.c): -z
+ * picks the input format (:51: 0 text edge list, 1 binary edge list,
+ * 2 graphCSR binary), -c the output format of -x serialisation (:115-128,
+ * same codes), and -x writes the converted file instead of running an
+ * algorithm (:339-341).  The graphCSR binary layout is OpenGraph's, whose
+ * code is absent; this one is the project's own: a 32-byte header (magic
+ * "AGXCSR1", V, E, weighted, avg_degree, max_weight), then the uint32/float
+ * arrays of both Vertex structs (out_degree, in_degree, edges_idx) and both
+ * sorted edge lists (src, dest, weight if weighted, label_array,
+ * inverse_label_array), forward direction first.  Every function returns 0
+ * (or a pointer) on success and -1 (or NULL) with a message on stderr. */
+int writeEdgeListsText(const struct EdgeList *edgeList, const char *fname);
+/* uint32 pairs, or triples when weighted; the weight word holds the weight
+ * rounded to an integer, as the reference's .wbin files and
+ * readEdgeListsbin have it. */
+int writeEdgeListsbin(const struct EdgeList *edgeList, const char *fname);
+int writeGraphCSRbin(const struct GraphCSR *graph, const char *fname);
+struct GraphCSR *readGraphCSRbin(const char *fname);
+/* The edges of a CSR, in CSR order, under their original ids. */
+struct EdgeList *edgeListFromGraphCSR(const struct GraphCSR *graph);
+/* Load a graph in format 0 (text), 1 (binary edge list) or 2 (graphCSR
+ * binary): the -f / -z pair. */
+struct GraphCSR *graphCSRFromFile(const char *fname, uint32_t format, int weighted);
+/* -x: read arguments->fnameb in arguments->fnameb_format and write it in
+ * arguments->convert_format (weighted when arguments->weighted) to
+ * fnameb + ".txt", ".bin" / ".wbin" or ".csr" (accel-graph.c:341). */
+void writeSerializedGraphDataStructure(struct Arguments *arguments);
+
 #ifdef __cplusplus
 }
 #endif
