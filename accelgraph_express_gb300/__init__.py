@@ -168,7 +168,7 @@ class PprParams(C.Structure):
 
 class PprResult(C.Structure):
     _fields_ = [("gather_ms", C.c_float), ("gather_launches", C.c_uint32), ("launches", C.c_uint32),
-                ("padded_vectors", C.c_uint32)]
+                ("padded_vectors", C.c_uint32), ("persistent", C.c_uint32)]
 
 
 class ServerParams(C.Structure):
@@ -227,6 +227,7 @@ def lib() -> C.CDLL:
         L.gg_spmv.argtypes = [C.c_void_p, P(SpmvParams), C.c_void_p, C.c_void_p, C.c_void_p, P(SpmvResult),
                               C.c_void_p]
         L.gg_set_wait_timeout_ms.argtypes = [C.c_uint32]
+        L.gg_set_barrier_limit_us.argtypes = [C.c_uint32]
         L.gg_ppr.argtypes = [C.c_void_p, P(PprParams), C.c_void_p, C.c_void_p, C.c_void_p, P(PprResult), C.c_void_p]
         L.gg_ppr_device_ranks.argtypes = [C.c_void_p, P(C.c_uint32)]
         L.gg_ppr_device_ranks.restype = C.c_void_p

@@ -523,7 +523,6 @@ __global__ void k_queue_to_bitmap(const uint32_t *__restrict__ q, uint32_t qlen,
  * lines, so the spinning blocks of one group do not queue behind the
  * arrivals or the other groups at one L2 slice */
 constexpr size_t CTL_BYTES = 8192;
-constexpr unsigned int BAR_GROUPS = 16;
 
 struct DoOut
 {
@@ -540,70 +539,15 @@ struct DoArgs
     Counters *c;  /* three slots */
     uint4 *heavy;
     char *ctl;
+    unsigned long long bar_limit_ns; /* device-side wait limit of the grid barrier */
     uint32_t V, words, E, src, alpha, beta;
 };
 
-__device__ __forceinline__ unsigned long long global_ns()
+/* the grid barrier (gg_device.cuh) over the control block, failures
+ * recorded in DoOut::err */
+__device__ __forceinline__ bool grid_barrier(char *ctl, unsigned long long limit_ns, unsigned int &gen)
 {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-/* grid-wide barrier over co-resident blocks (cooperative launch), two
- * levels: blocks arrive at their group's counter, the last of a group at the
- * root, and the last at the root releases every group.  A wait gives up
- * after 2 s and records the failure in DoOut::err; the block then reports
- * false and leaves, and the others give up at their next barrier. */
-constexpr unsigned long long BAR_LIMIT_NS = 2000000000ull;
-
-__device__ __forceinline__ bool grid_barrier(char *ctl, unsigned int &gen)
-{
-    __shared__ unsigned int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0)
-    {
-        unsigned int *root = (unsigned int *)(ctl + 512);
-        const unsigned int G = gridDim.x < BAR_GROUPS ? gridDim.x : BAR_GROUPS;
-        const unsigned int grp = blockIdx.x % G;
-        const unsigned int gsize = (gridDim.x - grp + G - 1) / G;
-        unsigned int *count = (unsigned int *)(ctl + 1024 + 128 * grp);
-        unsigned int *rel = (unsigned int *)(ctl + 4096 + 128 * grp);
-        const unsigned int target = gen + 1;
-        bool released = false, ok = true;
-        __threadfence();
-        if (atomicAdd(count, 1u) == gsize - 1)
-        {
-            atomicExch(count, 0u);
-            __threadfence();
-            if (atomicAdd(root, 1u) == G - 1)
-            {
-                atomicExch(root, 0u);
-                __threadfence();
-                for (unsigned int k = 0; k < G; k++) atomicExch((unsigned int *)(ctl + 4096 + 128 * k), target);
-                released = true;
-            }
-        }
-        if (!released)
-        {
-            const unsigned long long t0 = global_ns();
-            while (*(volatile unsigned int *)rel != target)
-            {
-                if (global_ns() - t0 > BAR_LIMIT_NS)
-                {
-                    atomicExch(&((DoOut *)(ctl + 256))->err, 1u);
-                    ok = false;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        __threadfence();
-        s_ok = ok ? 1u : 0u;
-    }
-    __syncthreads();
-    gen++;
-    return s_ok != 0u;
+    return gg::grid_barrier(ctl, &((DoOut *)(ctl + 256))->err, limit_ns, gen);
 }
 
 /* one read of a counter slot per block, shared with its threads */
@@ -660,7 +604,7 @@ __global__ void __launch_bounds__(256, 6) k_bfs_do(DoArgs a)
             /* queue -> bitmap (bm[bcur] is clear: the host cleared it and
              * every compaction clears what it reads) */
             q2bm_body(a.q[qcur], qlen, a.bm[bcur]);
-            if (!(ok = grid_barrier(a.ctl, gen))) break;
+            if (!(ok = grid_barrier(a.ctl, a.bar_limit_ns, gen))) break;
             nf = qlen;
             do
             {
@@ -669,7 +613,7 @@ __global__ void __launch_bounds__(256, 6) k_bfs_do(DoArgs a)
                 clear_slot(a.c + (s + 1) % 3);
                 bu_body(a.in_off, a.in_adj, a.parents, a.dist, 1, level + 1, a.bm[bcur], a.bm[bcur ^ 1], a.visited,
                         a.V, a.words, cs);
-                if (!(ok = grid_barrier(a.ctl, gen))) break;
+                if (!(ok = grid_barrier(a.ctl, a.bar_limit_ns, gen))) break;
                 const Counters k = read_counters_block(cs);
                 nf = k.nf;
                 edges += k.edges;
@@ -683,7 +627,7 @@ __global__ void __launch_bounds__(256, 6) k_bfs_do(DoArgs a)
             Counters *cs = a.c + s % 3;
             clear_slot(a.c + (s + 1) % 3);
             compact_body(a.bm[bcur], a.words, a.q[qcur], cs, true);
-            if (!(ok = grid_barrier(a.ctl, gen))) break;
+            if (!(ok = grid_barrier(a.ctl, a.bar_limit_ns, gen))) break;
             qlen = read_counters_block(cs).qlen;
             s++;
             mf = 1;
@@ -695,14 +639,14 @@ __global__ void __launch_bounds__(256, 6) k_bfs_do(DoArgs a)
             clear_slot(a.c + (s + 1) % 3);
             td_body(a.q[qcur], qlen, a.out_off, a.out_adj, a.parents, a.dist, level + 1, a.visited, a.q[qcur ^ 1],
                     nullptr, cs, a.heavy);
-            if (!(ok = grid_barrier(a.ctl, gen))) break;
+            if (!(ok = grid_barrier(a.ctl, a.bar_limit_ns, gen))) break;
             /* the deferred high-degree vertices, when there are any (every
              * block reads the same final count, so all skip together) */
             if (read_counters_block(cs).nheavy)
             {
                 td_heavy_body(a.heavy, a.out_adj, a.parents, a.dist, level + 1, a.visited, a.q[qcur ^ 1], nullptr,
                               cs);
-                if (!(ok = grid_barrier(a.ctl, gen))) break;
+                if (!(ok = grid_barrier(a.ctl, a.bar_limit_ns, gen))) break;
             }
             const Counters k = read_counters_block(cs);
             mf = k.mf;
@@ -840,7 +784,7 @@ gg_status bfs_setup(Bfs &B, gg_graph *g, void *stream, int profile)
     GG_CHECK(gg_work(g, 6, wb, &p)); B.visited = (uint32_t *)p;
     GG_CHECK(gg_work(g, 7, CTL_BYTES, &p)); B.c = (Counters *)p;
     GG_CHECK(gg_pinned(g, 256, &p)); B.h = (Counters *)p;
-    static_assert(3 * sizeof(Counters) <= 256 && sizeof(DoOut) <= 256 && 4096 + 128 * BAR_GROUPS <= CTL_BYTES,
+    static_assert(3 * sizeof(Counters) <= 256 && sizeof(DoOut) <= 256 && GG_BAR_BYTES <= CTL_BYTES,
                   "control layout");
     GG_CHECK(gg_work(g, 8, (size_t)TD_MAX_HEAVY * sizeof(uint4), &p)); B.heavy = (uint4 *)p;
     return GG_OK;
@@ -870,6 +814,7 @@ gg_status do_search(Bfs &B, const gg_bfs_params *p)
     a.c = (Counters *)ctl;
     a.heavy = B.heavy;
     a.ctl = ctl;
+    a.bar_limit_ns = gg_barrier_limit_ns();
     a.V = B.V;
     a.words = B.words;
     a.E = g->E;

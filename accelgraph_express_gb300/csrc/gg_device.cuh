@@ -561,4 +561,76 @@ __device__ __forceinline__ void warp_push(const uint32_t *__restrict__ off, cons
     }
 }
 
+/*
+ * Grid-wide barrier over the co-resident blocks of a cooperative launch, on
+ * a control block `ctl` of GG_BAR_BYTES zeroed before the launch: the root
+ * counter at 512, per group of blocks an arrival counter at 1024 + 128 g and
+ * a release word at 4096 + 128 g (separate 128-byte lines, so the spinning
+ * blocks of one group do not queue behind the arrivals or the other groups
+ * at one L2 slice).  Two levels: blocks arrive at their group's counter, the
+ * last of a group at the root, and the last at the root releases every
+ * group.  A wait gives up after limit_ns (globaltimer) and sets *err; the
+ * block then reports false and the caller leaves, so the other blocks give
+ * up at their next barrier and the launch ends with *err set, the context
+ * intact.  Bytes 0..511 of ctl are the caller's.
+ */
+constexpr unsigned int GG_BAR_GROUPS = 16;
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool grid_barrier(char *ctl, unsigned int *err, unsigned long long limit_ns,
+                                             unsigned int &gen)
+{
+    __shared__ unsigned int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        unsigned int *root = (unsigned int *)(ctl + 512);
+        const unsigned int G = gridDim.x < GG_BAR_GROUPS ? gridDim.x : GG_BAR_GROUPS;
+        const unsigned int grp = blockIdx.x % G;
+        const unsigned int gsize = (gridDim.x - grp + G - 1) / G;
+        unsigned int *count = (unsigned int *)(ctl + 1024 + 128 * grp);
+        unsigned int *rel = (unsigned int *)(ctl + 4096 + 128 * grp);
+        const unsigned int target = gen + 1;
+        bool released = false, ok = true;
+        __threadfence();
+        if (atomicAdd(count, 1u) == gsize - 1)
+        {
+            atomicExch(count, 0u);
+            __threadfence();
+            if (atomicAdd(root, 1u) == G - 1)
+            {
+                atomicExch(root, 0u);
+                __threadfence();
+                for (unsigned int k = 0; k < G; k++) atomicExch((unsigned int *)(ctl + 4096 + 128 * k), target);
+                released = true;
+            }
+        }
+        if (!released)
+        {
+            const unsigned long long t0 = global_ns();
+            while (*(volatile unsigned int *)rel != target)
+            {
+                if (global_ns() - t0 > limit_ns)
+                {
+                    atomicExch(err, 1u);
+                    ok = false;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        s_ok = ok ? 1u : 0u;
+    }
+    __syncthreads();
+    gen++;
+    return s_ok != 0u;
+}
+
 } // namespace gg

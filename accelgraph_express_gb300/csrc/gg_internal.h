@@ -188,6 +188,11 @@ int gg_persistent_grid(const void *kernel, uint32_t ntiles, int ctas_per_sm = 0)
  * thousand sectors); more hide more latency. */
 #define GG_PULL_CTAS_PER_SM 5
 
+/* control block bytes of gg::grid_barrier (gg_device.cuh) */
+#define GG_BAR_BYTES (4096 + 128 * 16)
+/* device-side wait limit of the grid barriers, in ns (gg_set_barrier_limit_us) */
+unsigned long long gg_barrier_limit_ns();
+
 /* Hot-vertex table of the pull gather (hot.cu): up to GG_HOT_ENTRIES
  * vertices with the most out-edges are read from a shared-memory table of
  * GG_HOT_TABLE_BYTES (as many entries as the stored value type fits: 8K FP32,

@@ -67,6 +67,15 @@ extern "C" const char *gg_last_error(void) { return t_last_error.c_str(); }
 
 extern "C" void gg_set_wait_timeout_ms(uint32_t ms) { g_wait_timeout_ms.store(ms ? ms : 120000); }
 
+static std::atomic<unsigned long long> g_barrier_limit_ns{2000000000ull};
+
+extern "C" void gg_set_barrier_limit_us(uint32_t us)
+{
+    g_barrier_limit_ns.store(us ? (unsigned long long)us * 1000ull : 2000000000ull);
+}
+
+unsigned long long gg_barrier_limit_ns() { return g_barrier_limit_ns.load(); }
+
 int gg_sm_count() { return g_sm_count > 0 ? g_sm_count : 152; }
 
 int gg_persistent_grid(const void *kernel, uint32_t ntiles, int ctas_per_sm)

@@ -51,6 +51,13 @@ template <> struct PairIO<float>
         asm volatile("ld.global.nc.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
         return v;
     }
+    /* through L2 only: contributions rewritten inside the persistent launch */
+    static __device__ __forceinline__ Raw load_cg(const float *p)
+    {
+        float2 v;
+        asm volatile("ld.global.cg.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+        return v;
+    }
     static __device__ __forceinline__ float2 unpack(Raw r) { return r; }
     static __device__ __forceinline__ void store(float *p, float a, float b)
     {
@@ -63,6 +70,12 @@ template <> struct PairIO<__nv_bfloat16>
     static __device__ __forceinline__ Raw load(const __nv_bfloat16 *p)
     {
         return ldg_val(reinterpret_cast<const uint32_t *>(p));
+    }
+    static __device__ __forceinline__ Raw load_cg(const __nv_bfloat16 *p)
+    {
+        uint32_t v;
+        asm volatile("ld.global.cg.u32 %0, [%1];" : "=r"(v) : "l"(p));
+        return v;
     }
     /* element 2i is the low half of the word (little-endian), BF16 -> FP32 is exact */
     static __device__ __forceinline__ float2 unpack(Raw r)
@@ -120,9 +133,12 @@ __device__ __forceinline__ void ppr_slot(float *slots, uint32_t tile, float s0, 
     *reinterpret_cast<float2 *>(slots + (size_t)tile * KP + 2 * gl) = make_float2(s0, s1);
 }
 
-/* one group of KP/2 lanes per tile; U edges' lines in flight per batch */
-template <int KP, class CT, int U>
-__global__ void __launch_bounds__(256) k_ppr_pull(PprArgs<CT> a)
+/* one group of KP/2 lanes per tile; U edges' lines in flight per batch;
+ * COHERENT: contributions read through L2 only (they are rewritten inside
+ * the launch by the persistent kernel; the read-only path may keep stale
+ * lines from an earlier iteration) */
+template <int KP, class CT, int U, bool COHERENT>
+__device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
 {
     constexpr uint32_t LPE = KP / 2;
     static_assert(U <= (int)LPE, "one id load per batch");
@@ -182,7 +198,9 @@ __global__ void __launch_bounds__(256) k_ppr_pull(PprArgs<CT> a)
             for (int i = 0; i < U; i++)
             {
                 const uint32_t u = __shfl_sync(gmask, myid, i, LPE);
-                if ((uint32_t)i < nb) v[i] = PairIO<CT>::load(a.cin + (size_t)u * KP + 2 * gl);
+                if ((uint32_t)i < nb)
+                    v[i] = COHERENT ? PairIO<CT>::load_cg(a.cin + (size_t)u * KP + 2 * gl)
+                                    : PairIO<CT>::load(a.cin + (size_t)u * KP + 2 * gl);
             }
             const uint32_t en = e + U;
             myid = 0;
@@ -211,11 +229,17 @@ __global__ void __launch_bounds__(256) k_ppr_pull(PprArgs<CT> a)
     }
 }
 
+template <int KP, class CT, int U>
+__global__ void __launch_bounds__(256) k_ppr_pull(PprArgs<CT> a)
+{
+    ppr_gather_tiles<KP, CT, U, false>(a);
+}
+
 /* finish the rows spanning tiles: the row that begins in tile t and is
  * still open at t's end (row coord[t+1].x) sums tail[t], the tails of the
  * tiles it crosses and the head of the tile where it ends, in tile order */
 template <int KP, class CT>
-__global__ void __launch_bounds__(256) k_ppr_fixup(PprArgs<CT> a)
+__device__ __forceinline__ void ppr_fixup_tiles(const PprArgs<CT> &a)
 {
     constexpr uint32_t LPE = KP / 2, B = 8;
     const uint32_t lane = threadIdx.x & 31, gl = lane % LPE;
@@ -247,6 +271,47 @@ __global__ void __launch_bounds__(256) k_ppr_fixup(PprArgs<CT> a)
         tot.x += h.x;
         tot.y += h.y;
         ppr_finish<KP, CT>(a, r, tot.x, tot.y, a.seed_idx[r], a.outdeg[r], gl);
+    }
+}
+
+template <int KP, class CT>
+__global__ void __launch_bounds__(256) k_ppr_fixup(PprArgs<CT> a)
+{
+    ppr_fixup_tiles<KP, CT>(a);
+}
+
+/* every iteration in one cooperative launch: gather, grid barrier, fix-up
+ * of the spanning rows, grid barrier.  The control block (GG_BAR_BYTES,
+ * zeroed before the launch) holds the barrier; a barrier wait that runs out
+ * sets *err and the launch ends (gg_set_barrier_limit_us). */
+template <class CT>
+struct PprLoop
+{
+    CT *cb0, *cb1;
+    float *rank;
+    uint32_t iterations;
+    char *ctl;
+    unsigned int *err;
+    unsigned long long limit_ns;
+};
+
+/* as many resident CTAs as the per-iteration gather gets (FP32: 3, BF16: 4
+ * per SM) */
+template <class CT> constexpr int ppr_persist_ctas() { return sizeof(CT) == 2 ? 4 : 3; }
+
+template <int KP, class CT, int U>
+__global__ void __launch_bounds__(256, ppr_persist_ctas<CT>()) k_ppr_persist(PprArgs<CT> a, PprLoop<CT> L)
+{
+    unsigned int gen = 0;
+    for (uint32_t it = 0; it < L.iterations; it++)
+    {
+        a.cin = (it & 1) ? L.cb1 : L.cb0;
+        a.cout = (it & 1) ? L.cb0 : L.cb1;
+        a.rank = it + 1 == L.iterations ? L.rank : nullptr;
+        ppr_gather_tiles<KP, CT, U, true>(a);
+        if (!grid_barrier(L.ctl, L.err, L.limit_ns, gen)) return;
+        ppr_fixup_tiles<KP, CT>(a);
+        if (it + 1 < L.iterations && !grid_barrier(L.ctl, L.err, L.limit_ns, gen)) return;
     }
 }
 
@@ -294,7 +359,7 @@ int occupancy_grid(K kernel, int threads, size_t work_groups, int lanes_per_grou
 template <int KP, class CT>
 gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const uint32_t *d_seedv, const float *d_init,
                   const float *d_tele, uint32_t *d_seed_idx, float *d_rank, cudaStream_t s, gg_ppr_result &res,
-                  std::vector<cudaEvent_t> &evs)
+                  std::vector<cudaEvent_t> &evs, void **ctl_out)
 {
     constexpr int LPE = KP / 2;
     constexpr int U = LPE < 16 ? LPE : 16;
@@ -325,6 +390,31 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
     a.head = (float *)slots;
     a.tail = (float *)slots + (size_t)t.ntiles * KP;
     CT *cb[2] = {(CT *)c0, (CT *)c1};
+    if (!p->profile)
+    {
+        /* all iterations in one cooperative launch: every block resident */
+        int per_sm = 0;
+        GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ppr_persist<KP, CT, U>, 256, 0));
+        if (per_sm < 1) return gg_fail(GG_ERR_CUDA, "k_ppr_persist cannot be resident");
+        const size_t groups_per_block = 256 / LPE;
+        const size_t need = ((size_t)t.ntiles + groups_per_block - 1) / groups_per_block;
+        const size_t cap = (size_t)gg_sm_count() * (size_t)per_sm;
+        const int grid = (int)(need < cap ? (need ? need : 1) : cap);
+        void *ctl;
+        GG_CHECK(gg_work(g, 30, GG_BAR_BYTES, &ctl));
+        GG_CUDA(cudaMemsetAsync(ctl, 0, GG_BAR_BYTES, s));
+        PprLoop<CT> L;
+        L.cb0 = cb[0]; L.cb1 = cb[1]; L.rank = d_rank; L.iterations = p->iterations;
+        L.ctl = (char *)ctl; L.err = (unsigned int *)ctl; L.limit_ns = gg_barrier_limit_ns();
+        void *args[] = {&a, &L};
+        GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_ppr_persist<KP, CT, U>, dim3(grid), dim3(256), args, 0, s));
+        res.launches++;
+        res.gather_launches = p->iterations;
+        res.persistent = 1;
+        *ctl_out = ctl;
+        GG_CUDA(cudaGetLastError());
+        return GG_OK;
+    }
     const int grid = occupancy_grid(k_ppr_pull<KP, CT, U>, 256, t.ntiles, LPE);
     const int fgrid = occupancy_grid(k_ppr_fixup<KP, CT>, 256, t.ntiles, LPE);
     for (uint32_t it = 0; it < p->iterations; it++)
@@ -414,11 +504,12 @@ extern "C" gg_status gg_ppr(gg_graph *g, const gg_ppr_params *p, const uint32_t 
             GG_CUDA(cudaMemcpyAsync(d_tab, tables.data(), tables.size() * sizeof(float), cudaMemcpyHostToDevice, s));
         }
         std::vector<cudaEvent_t> evs;
+        void *ctl = nullptr;
         const float *d_init = (const float *)d_tab, *d_tele = (const float *)d_tab + (size_t)nv * KP;
         gg_status st;
 #define GG_PPR_RUN(KPV, CTV)                                                                                          \
     run_ppr<KPV, CTV>(g, p, nv, (const uint32_t *)d_seedv, d_init, d_tele, (uint32_t *)d_idx, (float *)d_rank, s,     \
-                      res, evs)
+                      res, evs, &ctl)
         if (p->storage == GG_STORE_BF16)
             st = KP == 16 ? GG_PPR_RUN(16, __nv_bfloat16) : KP == 32 ? GG_PPR_RUN(32, __nv_bfloat16) : GG_PPR_RUN(64, __nv_bfloat16);
         else
@@ -428,7 +519,14 @@ extern "C" gg_status gg_ppr(gg_graph *g, const gg_ppr_params *p, const uint32_t 
         if (ranks)
             GG_CUDA(cudaMemcpy2DAsync(ranks, (size_t)K * sizeof(float), d_rank, (size_t)KP * sizeof(float),
                                       (size_t)K * sizeof(float), V, cudaMemcpyDeviceToHost, s));
+        uint32_t *h_err = nullptr;
+        if (ctl)
+        {
+            GG_CHECK(gg_pinned(g, 64, (void **)&h_err));
+            GG_CUDA(cudaMemcpyAsync(h_err, ctl, 4, cudaMemcpyDeviceToHost, s));
+        }
         GG_CHECK(gg_wait(s));
+        if (h_err && *h_err) return gg_fail(GG_ERR_KERNEL, "batched PageRank grid barrier timed out");
         for (size_t i = 0; i + 1 < evs.size(); i += 2) res.gather_ms += gg_event_ms(evs[i], evs[i + 1]);
         g->ppr_ranks = (const float *)d_rank;
         g->ppr_stride = KP;

@@ -557,8 +557,8 @@ __global__ void k_pr_init_delta(float *__restrict__ rank, const uint32_t *__rest
  * sent in the next, so the ranks carry only the rounding of the last delta,
  * which shrinks as the iteration converges. */
 template <int K>
-__global__ void k_pr_update_delta(PrCommon c, float *dsum, float *__restrict__ S, float *__restrict__ chat,
-                                  typename Fmt<K>::CT *__restrict__ qout)
+__global__ void k_pr_update_delta(PrCommon c, float init, float *__restrict__ dsum, float *__restrict__ S,
+                                  float *__restrict__ chat, typename Fmt<K>::CT *__restrict__ qout)
 {
     if (c.skip()) return;
     double err = 0.0;
@@ -571,9 +571,13 @@ __global__ void k_pr_update_delta(PrCommon c, float *dsum, float *__restrict__ S
     {
         const float ds = dsum[v];
         clear_after_read(&dsum[v], ds);
-        const float s = __fadd_rn(S[v], __fmul_rn(ds, in_inv));
+        const float s_old = S[v];
+        const float s = __fadd_rn(s_old, __fmul_rn(ds, in_inv));
         S[v] = s;
-        const float pr = rank[v];
+        /* the rank the previous pass wrote, recomputed from its sum (the same
+         * two roundings), so the rank array is only written: a store to a
+         * sector whose read is still in flight stalls */
+        const float pr = c.it == 0 ? init : __fadd_rn(c.base, __fmul_rn(c.damp, s_old));
         const float nr = __fadd_rn(c.base, __fmul_rn(c.damp, s));
         rank[v] = nr;
         const float e = fabsf(__fsub_rn(nr, pr));
@@ -821,7 +825,7 @@ gg_status run_pull(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
         c.rank = rank; c.outdeg = g->out_deg; c.V = V; c.base = base; c.damp = R.p->damp;
         c.eps_f = R.eps_f; c.eps_fl = R.eps_fl; c.rec = rec; c.it = it;
         if constexpr (delta)
-            k_pr_update_delta<K><<<grid_v(V), 256, 0, R.s>>>(c, (float *)sums, (float *)Sb, (float *)chb,
+            k_pr_update_delta<K><<<grid_v(V), 256, 0, R.s>>>(c, init, (float *)sums, (float *)Sb, (float *)chb,
                                                              cb[(it + 1) & 1]);
         else
             k_pr_update<K><<<grid_v(V), 256, 0, R.s>>>(c, (Acc *)sums, cb[(it + 1) & 1], (float *)cf);
@@ -903,7 +907,7 @@ gg_status run_push(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
         else if constexpr (K == K_Q8Z)
             k_pr_update<K_Q8Z><<<grid_v(V), 256, 0, R.s>>>(c, (float *)nx, nullptr, (float *)cf);
         else if constexpr (delta)
-            k_pr_update_delta<K><<<grid_v(V), 256, 0, R.s>>>(c, (float *)nx, (float *)Sb, (float *)chb, (CT *)c0);
+            k_pr_update_delta<K><<<grid_v(V), 256, 0, R.s>>>(c, init, (float *)nx, (float *)Sb, (float *)chb, (CT *)c0);
         else
             k_pr_update<K><<<grid_v(V), 256, 0, R.s>>>(c, (float *)nx, (CT *)c0, nullptr);
         R.launches++;

@@ -55,7 +55,7 @@ def parse():
     p.add_argument("--edge-factor", type=int, default=16)
     p.add_argument("--no-extras", action="store_true", help="skip the BF16/BFS/SpMV side measurements")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    p.add_argument("--leg", choices=["c1", "bfs", "ppr", "batch", "serve", "csr", "cc", "relabel"],
+    p.add_argument("--leg", choices=["pr", "c1", "bfs", "ppr", "batch", "serve", "csr", "cc", "relabel"],
                    help="run one side measurement alone and print its JSON (for profiling)")
     return p.parse_args()
 
@@ -251,7 +251,14 @@ def run_leg(leg):
 
     gg.device_init(0)
     peak, _ = load_peaks()
-    fn = {"c1": lambda: c1_extras(gg, torch), "bfs": lambda: bfs_extras(gg, torch, peak),
+    def pr():
+        g = gg.Graph.rmat(24, 16, seed=SEED)
+        dg = gg.DeviceGraph(g, gg.MAP_IN)
+        r = pr_storage_extras(gg, g, dg, g.V, g.E, torch.cuda.current_stream().cuda_stream, torch, peak)
+        dg.free()
+        return r
+
+    fn = {"pr": pr, "c1": lambda: c1_extras(gg, torch), "bfs": lambda: bfs_extras(gg, torch, peak),
           "ppr": lambda: ppr_extras(gg, torch, peak), "batch": lambda: batch_extras(gg, torch, peak),
           "serve": lambda: serving_extras(gg), "csr": lambda: csr_build_extras(gg, torch, peak),
           "cc": lambda: cc_extras(gg, torch, peak), "relabel": lambda: relabel_extras(gg, torch, peak)}[leg]
@@ -922,6 +929,26 @@ def extras(gg, graph, dg, V, E, sptr, torch, peak):
     import numpy as np
     from oracle import oracle_ctypes as O
 
+    out = pr_storage_extras(gg, graph, dg, V, E, sptr, torch, peak)
+    out["c1_rmat16"] = c1_extras(gg, torch)
+    out.update(spmv_extras(gg, graph, V, E, sptr, torch, peak))
+    dg.free()
+    out["bfs_do"] = bfs_extras(gg, torch, peak)
+    out["ppr_batched"] = ppr_extras(gg, torch, peak)
+    out["many_graphs"] = batch_extras(gg, torch, peak)
+    out["serving"] = serving_extras(gg)
+    out["csr_build"] = csr_build_extras(gg, torch, peak)
+    out["connected_components"] = cc_extras(gg, torch, peak)
+    return out
+
+
+def pr_storage_extras(gg, graph, dg, V, E, sptr, torch, peak):
+    """PageRank pull in FP32 and in BF16 / FP16 storage with the FP32
+    correction pass, 30 iterations: GTEPS, gather roofline, L1 / L-inf vs the
+    FP64 oracle."""
+    import numpy as np
+    from oracle import oracle_ctypes as O
+
     out = {}
     v = graph.views()
     out_off = np.append(v["out_edges_idx"], np.uint32(E))
@@ -955,15 +982,6 @@ def extras(gg, graph, dg, V, E, sptr, torch, peak):
             "iteration_hbm_frac": pr_bytes(V, E, s) / (ms / ITERS / 1e3) / 1e9 / peak,
             "l1_vs_fp64": l1, "linf_vs_fp64": linf, "l1_relative": l1 / float(np.abs(exact).sum())}
     out["fp64_oracle_s"] = round(f64_s, 2)
-    out["c1_rmat16"] = c1_extras(gg, torch)
-    out.update(spmv_extras(gg, graph, V, E, sptr, torch, peak))
-    dg.free()
-    out["bfs_do"] = bfs_extras(gg, torch, peak)
-    out["ppr_batched"] = ppr_extras(gg, torch, peak)
-    out["many_graphs"] = batch_extras(gg, torch, peak)
-    out["serving"] = serving_extras(gg)
-    out["csr_build"] = csr_build_extras(gg, torch, peak)
-    out["connected_components"] = cc_extras(gg, torch, peak)
     return out
 
 

@@ -70,6 +70,14 @@ const char *gg_last_error(void);
 /* Upper bound, in milliseconds, of every host wait on device work
  * (default 120000, env GG_WAIT_TIMEOUT_MS). */
 void gg_set_wait_timeout_ms(uint32_t ms);
+/* Upper bound, in microseconds, of each device-side wait of the grid
+ * barriers inside the single-launch kernels (direction-optimising BFS,
+ * batched personalised PageRank); default 2,000,000 (2 s), 0 restores it.
+ * A wait that runs out ends the launch early and the call returns
+ * GG_ERR_KERNEL with the context intact.  For diagnostics and tests of
+ * that path: at a few microseconds the barriers give up before the other
+ * blocks arrive. */
+void gg_set_barrier_limit_us(uint32_t us);
 
 /* Copy the arrays selected by `what` to HBM.  Offsets are padded so that
  * every array starts on a 256-byte boundary.  The host graph is only read. */
@@ -358,6 +366,7 @@ typedef struct gg_ppr_result
     uint32_t gather_launches;
     uint32_t launches;
     uint32_t padded_vectors;  /* vectors per vertex row on the device: 16, 32 or 64 */
+    uint32_t persistent;      /* 1: every iteration ran in one cooperative launch (profile off) */
 } gg_ppr_result;
 
 /* Seeds of vector k are seeds[seed_off[k] .. seed_off[k+1]) (host arrays,

@@ -117,3 +117,52 @@ def test_bfs_device_loop_matches_host_loop(graphs, dgs, mode):
             for k in ("processed_nodes", "levels", "top_down_steps", "bottom_up_steps", "edges_examined"):
                 assert r0[k] == r1[k], (tag, k, r0[k], r1[k])
             assert r0["launches"] == 2, (tag, r0["launches"])  # k_bfs_init and k_bfs_do
+
+
+def test_bfs_barrier_wait_runs_out_and_the_context_recovers(gpu, graphs, dgs, orc):
+    """The single-launch direction-optimising search waits at grid barriers
+    with a device-side limit.  At 1 us the blocks that reach a barrier first
+    give up while the others are still working: the search ends early and
+    gg_bfs reports a kernel error.  The next search, at the default limit,
+    is exact against the oracle on the same context."""
+    g, o = graphs["rmat16u"]
+    s = int(np.nonzero(np.diff(o.out_off.astype(np.int64)))[0][0])
+    L = gpu.lib()
+    L.gg_set_barrier_limit_us(1)
+    try:
+        with pytest.raises(gpu.GgError, match="timed out"):
+            dgs["rmat16u"].bfs(s, "do")
+    finally:
+        L.gg_set_barrier_limit_us(0)
+    _, dist, res = dgs["rmat16u"].bfs(s, "do")
+    _, rd, info = orc.bfs(o, 2, s)
+    np.testing.assert_array_equal(dist, rd)
+    assert res["edges_examined"] == info["edges_examined"]
+
+
+def test_host_wait_limit_returns_timeout_and_work_completes(gpu, graphs, dgs, orc):
+    """Every host wait on device work polls with a limit
+    (gg_set_wait_timeout_ms).  A 1 ms limit on a PageRank that runs longer
+    returns GG_ETIMEDOUT (5) instead of blocking; the queued work still
+    completes, and a call at the default limit is correct."""
+    import ctypes as C
+
+    L = gpu.lib()
+    big = gpu.Graph.rmat(20, 16)
+    d = gpu.DeviceGraph(big, gpu.MAP_IN)
+    d.pagerank("pull", iterations=2, epsilon=0.0)  # tiles and work buffers exist
+    p = gpu.PrParams(0, 0, 200, 0, 0.0, 0.85, 0, 0x2)  # 200 FP32 pull iterations, hot table off
+    r = gpu.PrResult()
+    L.gg_set_wait_timeout_ms(1)
+    try:
+        st = L.gg_pagerank(d.h, C.byref(p), None, C.byref(r), None)
+    finally:
+        L.gg_set_wait_timeout_ms(0)
+    assert st == 5, (st, L.gg_last_error())
+    g, o = graphs["rmat16"]
+    ranks, res = dgs["rmat16"].pagerank("pull", iterations=20, epsilon=1e-4)
+    ref, info = orc.pagerank(o, 0, 20, 1e-4)
+    assert res["iterations"] == info["iterations"]
+    d.pagerank("pull", iterations=2, epsilon=0.0)  # waits behind the 200 iterations
+    d.free()
+    big.free()

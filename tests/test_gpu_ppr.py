@@ -128,3 +128,41 @@ def test_ppr_rejects_bad_arguments(gpu, rg):
     with pytest.raises(gpu.GgError):
         dg.ppr([[0]], storage="f16")
     dg.free()
+
+
+def test_ppr_persistent_launch_equals_per_iteration_launches(gpu, rg):
+    """gg_ppr runs every iteration in one cooperative launch (grid barriers
+    between the gather and the fix-up of the rows spanning tiles); with
+    profile on it launches the two phases per iteration instead.  Same
+    arithmetic in the same order: bit-identical results."""
+    g, _ = rg
+    sets = seed_sets(g.V, 40, g.arrays()["out_degree"], np.random.default_rng(8))
+    dg = gpu.DeviceGraph(g, gpu.MAP_IN)
+    for storage in ("f32", "bf16"):
+        one, r1 = dg.ppr(sets, iterations=ITERS, storage=storage)
+        many, r2 = dg.ppr(sets, iterations=ITERS, storage=storage, profile=True)
+        assert r1["persistent"] == 1 and r1["launches"] <= 3
+        assert r2["persistent"] == 0 and r2["gather_launches"] == ITERS
+        np.testing.assert_array_equal(one, many)
+    dg.free()
+
+
+def test_ppr_barrier_wait_runs_out_and_the_context_recovers(gpu, rg):
+    """A grid-barrier wait limit of 1 us runs out while the blocks with
+    tiles are still gathering: the launch ends, gg_ppr reports a kernel
+    error, and the next call (default limit) gives the same ranks as
+    before, on the same context."""
+    g, _ = rg
+    sets = seed_sets(g.V, 16, g.arrays()["out_degree"], np.random.default_rng(9))
+    dg = gpu.DeviceGraph(g, gpu.MAP_IN)
+    good, _ = dg.ppr(sets, iterations=ITERS, storage="f32")
+    L = gpu.lib()
+    L.gg_set_barrier_limit_us(1)
+    try:
+        with pytest.raises(gpu.GgError, match="timed out"):
+            dg.ppr(sets, iterations=ITERS, storage="f32")
+    finally:
+        L.gg_set_barrier_limit_us(0)
+    again, _ = dg.ppr(sets, iterations=ITERS, storage="f32")
+    np.testing.assert_array_equal(again, good)
+    dg.free()
