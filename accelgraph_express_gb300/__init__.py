@@ -127,7 +127,7 @@ class PrParams(C.Structure):
                 ("profile", C.c_uint32), ("flags", C.c_uint32)]
 
 
-PR_CUDA_GRAPH, PR_HOT_OFF, PR_HOT_ON = 0x1, 0x2, 0x4
+PR_CUDA_GRAPH, PR_HOT_OFF, PR_HOT_ON, PR_BATCH_UNION = 0x1, 0x2, 0x4, 0x8
 
 
 def _pr_flags(cuda_graph, hot):
@@ -228,6 +228,8 @@ def lib() -> C.CDLL:
                               C.c_void_p]
         L.gg_set_wait_timeout_ms.argtypes = [C.c_uint32]
         L.gg_set_barrier_limit_us.argtypes = [C.c_uint32]
+        L.gg_pagerank_batch_iterations.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+        L.gg_pagerank_batch_config.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
         L.gg_ppr.argtypes = [C.c_void_p, P(PprParams), C.c_void_p, C.c_void_p, C.c_void_p, P(PprResult), C.c_void_p]
         L.gg_ppr_device_ranks.argtypes = [C.c_void_p, P(C.c_uint32)]
         L.gg_ppr_device_ranks.restype = C.c_void_p
@@ -617,18 +619,28 @@ class DeviceGraph:
         return ranks, {k: getattr(r, k) for k, _ in PrResult._fields_}
 
     def pagerank_batch(self, vertex_off, mode="pull", storage="f32", iterations=20, epsilon=1e-4, damp=0.85,
-                       profile=False, copy_out=True, stream=None, cuda_graph=False, hot=None):
+                       profile=False, copy_out=True, stream=None, cuda_graph=False, hot=None, union=False):
         """PageRank of a union of graphs (vertex ranges vertex_off[i] ..
-        vertex_off[i+1]); each vertex normalised by its own graph's size."""
+        vertex_off[i+1]); each vertex normalised by its own graph's size.
+        FP32 pull runs the many-graphs kernel unless union=True."""
         voff = np.ascontiguousarray(vertex_off, np.uint32)
         p = PrParams(PR_MODES[mode] if isinstance(mode, str) else mode, STORE[storage], iterations, 0, epsilon,
-                     damp, int(profile), _pr_flags(cuda_graph, hot))
+                     damp, int(profile), _pr_flags(cuda_graph, hot) | (PR_BATCH_UNION if union else 0))
         r = PrResult()
         ranks = np.empty(self.graph.V, np.float32) if copy_out else None
         _check(lib().gg_pagerank_batch(self.h, C.byref(p), len(voff) - 1, voff.ctypes.data,
                                        None if ranks is None else ranks.ctypes.data, C.byref(r), stream),
                "gg_pagerank_batch")
         return ranks, {k: getattr(r, k) for k, _ in PrResult._fields_}
+
+    def batch_iterations(self, ngraphs):
+        """Per-graph iteration counts of the last many-graphs run."""
+        out = np.empty(ngraphs, np.uint32)
+        _check(lib().gg_pagerank_batch_iterations(self.h, ngraphs, out.ctypes.data), "gg_pagerank_batch_iterations")
+        return out
+
+    def batch_config(self, ipt=7, warps=16, smem_vmax=4096):
+        _check(lib().gg_pagerank_batch_config(self.h, ipt, warps, smem_vmax), "gg_pagerank_batch_config")
 
     def bfs(self, source, mode="do", profile=False, copy_out=True, stream=None):
         p = BfsParams(BFS_MODES[mode] if isinstance(mode, str) else mode, source, 15, 18, int(profile))

@@ -879,6 +879,7 @@ extern "C" gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parent
     uint32_t outdeg_src = 0;
     if (!device_loop)
     {
+        GG_CHECK(gg_wait(B.s)); /* bounded, before a copy to pageable memory */
         GG_CUDA(cudaMemcpyAsync(&outdeg_src, g->out_deg + src, 4, cudaMemcpyDeviceToHost, B.s));
         GG_CHECK(gg_wait(B.s));
     }

@@ -516,6 +516,7 @@ gg_status gg_build_arrays(gg_graph *g, const uint32_t *src, const uint32_t *dst,
             g->out_adj = nullptr;
         }
         unsigned int flags[2] = {0u, 0u};
+        if ((st = gg_wait(s)) != GG_OK) break; /* bounded, before a copy to pageable memory */
         if (cudaMemcpyAsync(flags, bad, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         {
             st = gg_fail(GG_ERR_CUDA, "cudaMemcpyAsync");
@@ -530,6 +531,7 @@ gg_status gg_build_arrays(gg_graph *g, const uint32_t *src, const uint32_t *dst,
             cudaMemsetAsync(mx, 0, 4, s);
             k_max_weight<<<grid_for(E, 256), 256, 0, s>>>(w, E, mx);
             unsigned int bits = 0;
+            if ((st = gg_wait(s)) != GG_OK) break;
             cudaMemcpyAsync(&bits, mx, 4, cudaMemcpyDeviceToHost, s);
             if ((st = gg_wait(s)) == GG_OK) memcpy(&g->max_weight, &bits, 4);
         }
@@ -711,6 +713,7 @@ gg_status gg_relabel_device(gg_graph *g, uint32_t V, uint64_t E, const uint32_t 
     k_degree_max<<<grid_for(V, 256), 256, 0, s>>>(dout, din, V, mode, dmax_d);
     GG_CUDA(cudaGetLastError());
     unsigned long long hf[2] = {0, 0};
+    GG_CHECK(gg_wait(s)); /* bounded, before a copy to pageable memory */
     GG_CUDA(cudaMemcpyAsync(hf, flag.p, 16, cudaMemcpyDeviceToHost, s));
     GG_CHECK(gg_wait(s));
     if (hf[0] & 0xffffffffull) return gg_fail(GG_ERR_INVALID, "edge list has a vertex id >= num_vertices");
@@ -753,6 +756,7 @@ gg_status gg_check_permutation(gg_graph *g, const uint32_t *label, uint32_t V, c
     k_perm_hits<<<grid_for(V, 256), 256, 0, s>>>(label, V, (uint32_t *)hits.p, (uint32_t *)flag.p);
     GG_CUDA(cudaGetLastError());
     uint32_t bad = 0;
+    GG_CHECK(gg_wait(s)); /* bounded, before a copy to pageable memory */
     GG_CUDA(cudaMemcpyAsync(&bad, flag.p, 4, cudaMemcpyDeviceToHost, s));
     GG_CHECK(gg_wait(s));
     if (bad) return gg_fail(GG_ERR_INVALID, "label array is not a permutation of 0..V-1");

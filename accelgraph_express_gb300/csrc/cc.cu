@@ -351,6 +351,7 @@ extern "C" gg_status gg_cc(gg_graph *g, const gg_cc_params *p, uint32_t *compone
             k_cc_sample<<<grid_for(ns), 256, 0, C.s>>>(C.comp, V, p->seed, ns, (uint32_t *)sp);
             C.launches++;
             std::vector<uint32_t> smp(ns);
+            GG_CHECK(gg_wait(C.s)); /* bounded, before a copy to pageable memory */
             GG_CUDA(cudaMemcpyAsync(smp.data(), sp, (size_t)ns * 4, cudaMemcpyDeviceToHost, C.s));
             GG_CHECK(gg_wait(C.s));
             std::sort(smp.begin(), smp.end());

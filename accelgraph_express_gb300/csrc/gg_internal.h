@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <cstddef>
 #include <string>
+#include <vector>
 
 #include "gg_runtime.h"
 
@@ -39,6 +40,27 @@ struct gg_buf
 {
     void *ptr = nullptr;
     size_t bytes = 0;
+};
+
+/* Configuration of the many-graphs PageRank kernel (graphs.cu): tile items
+ * per lane (5, 7 or 9), warps per CTA, and the bin threshold: graphs of at
+ * most smem_vmax vertices keep contributions and sums in shared memory. */
+struct gg_graphs_config
+{
+    uint32_t ipt = 7, warps = 16, smem_vmax = 4096;
+};
+
+/* The many-graphs run's preparation, cached on the mapping for the graph
+ * boundaries it was made for: per-graph tile coordinates and the size order
+ * (one device allocation at coord: voff, cbase, order, then the tiles). */
+struct gg_graphs_state
+{
+    uint32_t ngraphs = 0, items = 0;
+    std::vector<uint32_t> h_voff;
+    void *coord = nullptr;
+    size_t bytes = 0;
+    const uint32_t *voff = nullptr, *cbase = nullptr, *order = nullptr;
+    uint2 *tiles = nullptr;
 };
 
 struct gg_graph
@@ -102,6 +124,12 @@ struct gg_graph
     uint32_t ev_count = 0;
     size_t device_bytes = 0;
     const float *last_ranks = nullptr;
+    /* the last many-graphs run: preparation and per-graph iteration counts */
+    gg_graphs_state graphs;
+    const uint32_t *graphs_iters = nullptr;
+    uint32_t graphs_n = 0;
+    /* the many-graphs configuration in force (default, set, or tuned) */
+    gg_graphs_config graphs_cfg;
 };
 
 /* error state */
@@ -205,6 +233,16 @@ unsigned long long gg_barrier_limit_ns();
 #define GG_HOT_TABLE_BYTES 32768u
 #define GG_HOT_WARPS 32
 #define GG_HOT_IPT 7
+/* many-graphs PageRank (graphs.cu): tile coordinates and size order for the
+ * graph boundaries h_voff (cached on the mapping), and the one launch */
+gg_status gg_graphs_prepare(gg_graph *g, uint32_t ngraphs, const uint32_t *h_voff, uint32_t items, cudaStream_t s);
+gg_status gg_graphs_launch(gg_graph *g, const gg_graphs_config &cfg, uint32_t ngraphs, const gg_pr_params *p,
+                           float eps_f, float *rank, uint32_t *counter, uint32_t *iters, uint32_t *active, double *err,
+                           cudaStream_t s);
+size_t gg_graphs_tile_items(const gg_graphs_config &cfg);
+/* the configuration a many-graphs run on g uses */
+gg_graphs_config gg_graphs_choice(gg_graph *g, uint32_t ngraphs);
+
 /* smallest float f with (double)f >= x, and largest float f with (double)f <= x */
 float gg_float_ceil(double x);
 float gg_float_floor(double x);

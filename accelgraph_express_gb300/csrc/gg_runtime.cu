@@ -326,6 +326,9 @@ gg_status gg_copy_h2d(void *dst, const void *src, size_t bytes, cudaStream_t s)
 
 gg_status gg_copy_d2h(void *dst, const void *src, size_t bytes, cudaStream_t s)
 {
+    /* a copy to pageable memory blocks the host until the stream's earlier
+     * work is done: wait for that work with the bounded poll first */
+    if (!host_pinned(dst)) GG_CHECK(gg_wait(s));
     if (bytes < ((size_t)4 << 20) || host_pinned(dst))
     {
         GG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
@@ -595,6 +598,7 @@ extern "C" gg_status gg_relabel_order(const struct EdgeList *edges, uint32_t lmo
     if (st == GG_OK) st = upload(g, (void **)&dd, edges->edges_array_dest, (size_t)E * 4, (size_t)E * 4 + 16, s);
     if (st == GG_OK) st = gg_dev_alloc(g, (void **)&dl, (size_t)V * 4 + 16);
     if (st == GG_OK) st = gg_relabel_device(g, V, E, ds, dd, lmode, seed, dl, s);
+    if (st == GG_OK) st = gg_wait(s);
     if (st == GG_OK && cudaMemcpyAsync(label_array, dl, (size_t)V * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         st = gg_fail(GG_ERR_CUDA, "cudaMemcpyAsync");
     if (st == GG_OK) st = gg_wait(s);
@@ -631,6 +635,7 @@ extern "C" gg_status gg_graph_download(const gg_graph *gc, uint32_t *out_idx, ui
     } parts[] = {{out_idx, g->out_off, vb, "out-CSR"}, {out_adj, g->out_adj, eb, "out-CSR"},
                  {out_w, g->out_w, eb, "out-edge weights"}, {in_idx, g->in_off, vb, "CSC"},
                  {in_adj, g->in_adj, eb, "CSC"}, {in_w, g->in_w, eb, "in-edge weights"}};
+    GG_CHECK(gg_wait(s)); /* bounded, before copies to pageable memory */
     for (const Part &p : parts)
     {
         if (!p.host) continue;
@@ -710,6 +715,7 @@ extern "C" gg_status gg_graph_unmap(gg_graph *g)
     gg_dev_free(g, g->hot_list, (size_t)GG_HOT_ENTRIES * 4);
     free_tiles(g, g->hot_tiles);
     for (auto &b : g->work) gg_dev_free(g, b.ptr, b.bytes);
+    gg_dev_free(g, g->graphs.coord, g->graphs.bytes);
     if (g->pinned) cudaFreeHost(g->pinned);
     if (g->pr_exec) cudaGraphExecDestroy(g->pr_exec);
     for (uint32_t i = 0; i < g->ev_count; i++) cudaEventDestroy(g->ev_pool[i]);

@@ -108,6 +108,7 @@ gg_status gg_hot_prepare(gg_graph *g, cudaStream_t s, uint32_t cap)
     k_deg_hist<<<gg_sm_count() * 2, 256, 0, s>>>(g->out_deg, V, (uint32_t *)hist);
     GG_CUDA(cudaGetLastError());
     std::vector<uint32_t> h(65536);
+    GG_CHECK(gg_wait(s)); /* bounded, before a copy to pageable memory */
     GG_CUDA(cudaMemcpyAsync(h.data(), hist, 65536 * 4, cudaMemcpyDeviceToHost, s));
     GG_CHECK(gg_wait(s));
     /* threshold: the degree T with fewer than H vertices above it */
@@ -127,6 +128,7 @@ gg_status gg_hot_prepare(gg_graph *g, cudaStream_t s, uint32_t cap)
     k_hot_encode<<<grid, 256, 0, s>>>(g->in_adj, E, (const uint32_t *)slot_of, g->hot_adj);
     GG_CUDA(cudaGetLastError());
     std::vector<uint32_t> c(4);
+    GG_CHECK(gg_wait(s));
     GG_CUDA(cudaMemcpyAsync(c.data(), cnt, 16, cudaMemcpyDeviceToHost, s));
     GG_CHECK(gg_wait(s));
     g->hot_n = T > 0 ? (c[0] + (c[1] < H - above ? c[1] : H - above)) : c[0];

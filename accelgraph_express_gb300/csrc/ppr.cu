@@ -516,6 +516,7 @@ extern "C" gg_status gg_ppr(gg_graph *g, const gg_ppr_params *p, const uint32_t 
             st = KP == 16 ? GG_PPR_RUN(16, float) : KP == 32 ? GG_PPR_RUN(32, float) : GG_PPR_RUN(64, float);
 #undef GG_PPR_RUN
         if (st != GG_OK) return st;
+        GG_CHECK(gg_wait(s)); /* bounded, before a copy to pageable memory */
         if (ranks)
             GG_CUDA(cudaMemcpy2DAsync(ranks, (size_t)K * sizeof(float), d_rank, (size_t)KP * sizeof(float),
                                       (size_t)K * sizeof(float), V, cudaMemcpyDeviceToHost, s));

@@ -37,6 +37,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -1029,6 +1030,69 @@ gg_status pagerank_enqueue(Run &R, const gg_pr_params *p, IterRec *rec, float *r
 }
 
 
+/* many graphs, one CTA per graph, every iteration in one launch (graphs.cu):
+ * FP32 pull; per-graph stop; the result reports the largest iteration count
+ * and the sum of the active counts of graphs that ran out of iterations */
+gg_status graphs_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_result *r, void *stream,
+                      uint32_t ngraphs, const uint32_t *h_voff)
+{
+    cudaStream_t s = gg_stream(g, stream);
+    const uint32_t V = g->V;
+    const gg_graphs_config cfg = gg_graphs_choice(g, ngraphs);
+    GG_CHECK(gg_graphs_prepare(g, ngraphs, h_voff, (uint32_t)gg_graphs_tile_items(cfg), s));
+    void *rank_v, *stat, *sum_v;
+    GG_CHECK(gg_work(g, 0, ((size_t)V + 16) * 4, &rank_v));
+    GG_CHECK(gg_work(g, 23, 64 + (size_t)ngraphs * 16, &stat));
+    GG_CHECK(gg_work(g, 10, 64, &sum_v));
+    uint32_t *counter = (uint32_t *)stat;
+    uint32_t *iters = (uint32_t *)((char *)stat + 64);
+    uint32_t *active = iters + ngraphs;
+    double *err = (double *)(active + ngraphs + (ngraphs & 1));
+    GG_CUDA(cudaMemsetAsync(sum_v, 0, 64, s));
+    /* vertices outside every graph keep rank 0 */
+    if (h_voff[0] > 0 || h_voff[ngraphs] < V) GG_CUDA(cudaMemsetAsync(rank_v, 0, (size_t)V * 4, s));
+    gg_pr_result res;
+    memset(&res, 0, sizeof(res));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (p->profile)
+    {
+        GG_CHECK(gg_event_at(g, 0, &e0));
+        GG_CHECK(gg_event_at(g, 1, &e1));
+        GG_CUDA(cudaEventRecord(e0, s));
+    }
+    GG_CHECK(gg_graphs_launch(g, cfg, ngraphs, p, gg_float_ceil(p->epsilon), (float *)rank_v, counter, iters, active,
+                              err, s));
+    if (p->profile) GG_CUDA(cudaEventRecord(e1, s));
+    k_pr_finalize<<<grid_v(V), 256, 0, s>>>((float *)rank_v, V, 0, (double *)sum_v);
+    GG_CUDA(cudaGetLastError());
+    std::vector<uint32_t> h_it(2 * (size_t)ngraphs);
+    std::vector<double> h_err(ngraphs);
+    double sum = 0.0;
+    /* a bounded wait first: a copy to pageable memory would block until the
+     * launch ends, however long that is */
+    GG_CHECK(gg_wait(s));
+    GG_CUDA(cudaMemcpyAsync(h_it.data(), iters, (size_t)ngraphs * 8, cudaMemcpyDeviceToHost, s));
+    GG_CUDA(cudaMemcpyAsync(h_err.data(), err, (size_t)ngraphs * 8, cudaMemcpyDeviceToHost, s));
+    GG_CUDA(cudaMemcpyAsync(&sum, sum_v, 8, cudaMemcpyDeviceToHost, s));
+    if (ranks && V) GG_CHECK(gg_copy_d2h(ranks, rank_v, (size_t)V * 4, s));
+    GG_CHECK(gg_wait(s));
+    for (uint32_t i = 0; i < ngraphs; i++)
+    {
+        res.iterations = std::max(res.iterations, h_it[i]);
+        if (h_it[i] >= p->max_iterations) res.active += h_it[ngraphs + i];
+        res.error_total = std::max(res.error_total, h_err[i]);
+    }
+    res.rank_sum = sum;
+    res.launches = 2;
+    res.gather_launches = 1;
+    if (p->profile) res.gather_ms = gg_event_ms(e0, e1);
+    g->last_ranks = (const float *)rank_v;
+    g->graphs_iters = iters;
+    g->graphs_n = ngraphs;
+    if (r) *r = res;
+    return GG_OK;
+}
+
 /* one PageRank run; with ngraphs > 0 the mapping is the union of ngraphs
  * graphs (vertex ranges h_voff[g] .. h_voff[g+1]) and the final
  * normalisation divides each vertex by its own graph's vertex count */
@@ -1039,6 +1103,11 @@ gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_
     if (!g || !p) return gg_fail(GG_ERR_INVALID, "NULL argument");
     if (p->mode > 13) return gg_fail(GG_ERR_INVALID, "unknown PageRank mode");
     if (p->storage > 2) return gg_fail(GG_ERR_INVALID, "unknown storage");
+    if (ngraphs && p->mode == GG_PR_PULL && p->storage == GG_STORE_F32 && !(p->flags & GG_PR_BATCH_UNION))
+    {
+        if (!g->in_off || !g->out_deg) return gg_fail(GG_ERR_INVALID, "pull PageRank needs GG_MAP_IN");
+        return graphs_impl(g, p, ranks, r, stream, ngraphs, h_voff);
+    }
     const int pull = !(p->mode == GG_PR_PUSH || p->mode == GG_PR_PUSH_FX64 || p->mode == GG_PR_PUSH_Q ||
                        p->mode == GG_PR_DD_PUSH || p->mode == GG_PR_DD_PULLPUSH);
     if (pull && !g->in_off) return gg_fail(GG_ERR_INVALID, "pull PageRank needs GG_MAP_IN");
@@ -1146,6 +1215,9 @@ gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_
 
     std::vector<IterRec> h(iters + 2);
     double sum = 0.0;
+    /* a bounded wait first: a copy to pageable memory would block until the
+     * iterations end, however long that is */
+    GG_CHECK(gg_wait(R.s));
     GG_CUDA(cudaMemcpyAsync(h.data(), rec, ((size_t)iters + 2) * sizeof(IterRec), cudaMemcpyDeviceToHost, R.s));
     GG_CUDA(cudaMemcpyAsync(&sum, sum_v, sizeof(double), cudaMemcpyDeviceToHost, R.s));
     if (ranks && V) GG_CHECK(gg_copy_d2h(ranks, rank, (size_t)V * 4, R.s));

@@ -403,6 +403,7 @@ extern "C" gg_status gg_spmv(gg_graph *g, const gg_spmv_params *p, const float *
         GG_CUDA(cudaGetLastError());
     }
     double checksum = 0.0;
+    GG_CHECK(gg_wait(s)); /* bounded, before a copy to pageable memory */
     GG_CUDA(cudaMemcpyAsync(&checksum, chk, 8, cudaMemcpyDeviceToHost, s));
     if (y && V) GG_CHECK(gg_copy_d2h(y, yv, (size_t)V * 4, s));
     if (x_out && V) GG_CHECK(gg_copy_d2h(x_out, xf, (size_t)V * 4, s));

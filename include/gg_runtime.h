@@ -164,6 +164,11 @@ typedef struct gg_pr_params
  * vertices up; HOT_OFF never, HOT_ON on any graph.  Results are the same. */
 #define GG_PR_HOT_OFF 0x2u
 #define GG_PR_HOT_ON 0x4u
+/* gg_pagerank_batch: run the ordinary pull over the union of the graphs
+ * (every graph iterates until all have converged) instead of the
+ * many-graphs kernel (FP32 pull: one CTA per graph, each graph with its own
+ * stop, every iteration in one launch). */
+#define GG_PR_BATCH_UNION 0x8u
 
 typedef struct gg_pr_result
 {
@@ -185,13 +190,28 @@ gg_status gg_pagerank(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_re
 const float *gg_pagerank_device_ranks(const gg_graph *g);
 /* PageRank over a mapping that is the union of `ngraphs` graphs occupying
  * vertex ranges vertex_off[i] .. vertex_off[i+1] (host array, ngraphs+1
- * entries, from 0 to V; no counterpart in the reference): the iterations of
- * gg_pagerank over the union, then each vertex divided by its own graph's
- * vertex count, so with no edges between the ranges every graph gets its own
- * PageRank.  The reference formulation only (init_one_over_n = 0); the stop
- * rule and error_total are over the union. */
+ * entries, from 0 to V; no counterpart in the reference), every graph
+ * ranked as if alone (each vertex divided by its own graph's vertex count).
+ * The reference formulation only (init_one_over_n = 0).
+ * FP32 pull: the many-graphs kernel, one launch for every graph and every
+ * iteration; one CTA per graph (largest first), small graphs' contributions
+ * in shared memory (gg_pagerank_batch_config / gg_autotune pick the bin
+ * threshold and tile shape); every graph stops on its own (iteration counts
+ * from gg_pagerank_batch_iterations); the result carries the largest count,
+ * the largest error_total and the active vertices of graphs that ran out.
+ * The edges must stay inside their graph's range (GG_ERR_INVALID otherwise).
+ * Other modes, or GG_PR_BATCH_UNION: the iterations of gg_pagerank over the
+ * union, the stop rule and error_total over the union. */
 gg_status gg_pagerank_batch(gg_graph *g, const gg_pr_params *p, uint32_t ngraphs, const uint32_t *vertex_off,
                             float *ranks, gg_pr_result *r, void *stream);
+/* Per-graph iteration counts (the reference's convention) of the last
+ * many-graphs run of gg_pagerank_batch on g, which had `ngraphs` graphs. */
+gg_status gg_pagerank_batch_iterations(const gg_graph *g, uint32_t ngraphs, uint32_t *iterations);
+/* Shape of the many-graphs kernel on g: merge items per lane of its tiles
+ * (5, 7 or 9), warps per CTA (1..32), and the bin threshold: graphs of at
+ * most smem_vmax vertices keep contributions and sums in shared memory (0:
+ * none).  Default 7, 16, 4096; gg_autotune picks one per mapping. */
+gg_status gg_pagerank_batch_config(gg_graph *g, uint32_t ipt, uint32_t warps, uint32_t smem_vmax);
 
 /* ---- BFS -------------------------------------------------------------------- */
 

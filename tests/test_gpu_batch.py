@@ -91,3 +91,58 @@ def test_cuda_graph_cache_reuse_and_invalidation(gpu):
     e, _ = dg.pagerank("pull", iterations=20, epsilon=1e-4, storage="bf16", cuda_graph=True)
     e_plain, _ = dg.pagerank("pull", iterations=20, epsilon=1e-4, storage="bf16")
     np.testing.assert_allclose(e, e_plain, rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("cfg", [(7, 16, 4096), (7, 16, 0), (5, 8, 200), (9, 32, 512), (7, 4, 64)])
+def test_many_graphs_kernel_per_graph_stop(gpu, orc, batch, cfg):
+    """The many-graphs kernel (one CTA per graph, every iteration in one
+    launch) with an epsilon stop: every graph stops on its own, after the
+    iterations of the reference's loop on that graph alone, and its ranks
+    pass the floating-point rule against the FP64 oracle.  The shapes cover
+    every graph in shared memory, none, and a mix (bins at 64, 200 and 512
+    vertices), with 5, 7 and 9 items per lane and 4 to 32 warps."""
+    g, voff = batch
+    dg = gpu.DeviceGraph(g, gpu.MAP_IN)
+    dg.batch_config(*cfg)
+    ranks, res = dg.pagerank_batch(voff, iterations=20, epsilon=1e-4)
+    its = dg.batch_iterations(len(SCALES))
+    dg.free()
+    assert res["launches"] == 2 and res["gather_launches"] == 1
+    for i, sc in enumerate(SCALES):
+        o = orc.rmat_csr(sc, 8, seed=SEED0 + i)
+        ref, info = orc.pagerank(o, 0, 20, 1e-4)
+        assert its[i] == info["iterations"], (i, its[i], info["iterations"])
+        ex = orc.pagerank_f64(o, info["executed"])
+        assert_fp_as_accurate(ranks[voff[i]:voff[i + 1]], ref, ex, f"graph {i} (scale {sc}) cfg {cfg}")
+    assert res["iterations"] == int(its.max())
+
+
+def test_many_graphs_kernel_matches_union_run(gpu, batch):
+    """With epsilon 0 every graph runs all iterations either way: the
+    many-graphs kernel and the union pull agree to FP32 rounding."""
+    g, voff = batch
+    dg = gpu.DeviceGraph(g, gpu.MAP_IN)
+    a, _ = dg.pagerank_batch(voff, iterations=20, epsilon=0.0)
+    b, rb = dg.pagerank_batch(voff, iterations=20, epsilon=0.0, union=True)
+    dg.free()
+    assert rb["gather_launches"] == 20
+    np.testing.assert_allclose(a, b, rtol=2e-6, atol=0)
+
+
+def test_many_graphs_kernel_rejects_edges_across_graphs(gpu, batch):
+    """The kernel reads a small graph's contributions by local index, so a
+    vertex_off that cuts a graph in two (edges cross the boundary) is
+    refused, and the other shape configurations are checked on input."""
+    g, voff = batch
+    dg = gpu.DeviceGraph(g, gpu.MAP_IN)
+    bad = voff.copy()
+    bad[3] = (voff[3] + voff[4]) // 2   # splits graph 3
+    with pytest.raises(gpu.GgError, match="cross"):
+        dg.pagerank_batch(bad, iterations=5, epsilon=0.0)
+    with pytest.raises(gpu.GgError):
+        dg.batch_config(ipt=6)
+    with pytest.raises(gpu.GgError):
+        dg.batch_config(warps=32, smem_vmax=1 << 20)
+    ok, _ = dg.pagerank_batch(voff, iterations=5, epsilon=0.0)  # the right boundaries still work
+    assert np.isfinite(ok).all()
+    dg.free()
