@@ -201,6 +201,36 @@ BFS_MODES = {"pull": 0, "push": 1, "do": 2, "push_bitmap": 3, "do_bitmap": 4}
 SPMV_MODES = {"pull": 0, "push": 1, "pull_fx": 2, "push_fx": 3}
 
 
+class TuneParams(C.Structure):
+    _fields_ = [("families", C.c_uint32), ("storage", C.c_uint32), ("reps", C.c_uint32), ("ngraphs", C.c_uint32),
+                ("vertex_off", C.c_void_p)]
+
+
+class TuneChoice(C.Structure):
+    _fields_ = [("family", C.c_uint32), ("params", C.c_uint32 * 4), ("default_ms", C.c_float),
+                ("tuned_ms", C.c_float), ("candidates", C.c_uint32)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("choice", TuneChoice * 5), ("n", C.c_uint32)]
+
+
+TUNE_PR, TUNE_SPMV, TUNE_BFS, TUNE_PPR, TUNE_BATCH = 0x1, 0x2, 0x4, 0x8, 0x10
+TUNE_NAMES = {TUNE_PR: "pr", TUNE_SPMV: "spmv", TUNE_BFS: "bfs", TUNE_PPR: "ppr", TUNE_BATCH: "batch"}
+
+
+def tune_save(path):
+    _check(lib().gg_tune_save(path.encode()), "gg_tune_save")
+
+
+def tune_load(path):
+    _check(lib().gg_tune_load(path.encode()), "gg_tune_load")
+
+
+def tune_reset():
+    _check(lib().gg_tune_reset(), "gg_tune_reset")
+
+
 class GgError(RuntimeError):
     pass
 
@@ -229,7 +259,11 @@ def lib() -> C.CDLL:
         L.gg_set_wait_timeout_ms.argtypes = [C.c_uint32]
         L.gg_set_barrier_limit_us.argtypes = [C.c_uint32]
         L.gg_pagerank_batch_iterations.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
-        L.gg_pagerank_batch_config.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.gg_autotune.argtypes = [C.c_void_p, P(TuneParams), P(TuneResult), C.c_void_p]
+        L.gg_tune_save.argtypes = [C.c_char_p]
+        L.gg_tune_load.argtypes = [C.c_char_p]
+        L.gg_tune_get.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+        L.gg_pagerank_batch_config.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]
         L.gg_ppr.argtypes = [C.c_void_p, P(PprParams), C.c_void_p, C.c_void_p, C.c_void_p, P(PprResult), C.c_void_p]
         L.gg_ppr_device_ranks.argtypes = [C.c_void_p, P(C.c_uint32)]
         L.gg_ppr_device_ranks.restype = C.c_void_p
@@ -633,14 +667,36 @@ class DeviceGraph:
                "gg_pagerank_batch")
         return ranks, {k: getattr(r, k) for k, _ in PrResult._fields_}
 
+    def autotune(self, families=TUNE_PR, storage="f32", reps=3, vertex_off=None, stream=None):
+        """gg_autotune: time candidate launch shapes on this mapping and keep
+        the fastest; returns {family name: {params, default_ms, tuned_ms,
+        candidates}}."""
+        voff = None if vertex_off is None else np.ascontiguousarray(vertex_off, np.uint32)
+        p = TuneParams(families, STORE[storage], reps, 0 if voff is None else len(voff) - 1,
+                       None if voff is None else voff.ctypes.data)
+        r = TuneResult()
+        _check(lib().gg_autotune(self.h, C.byref(p), C.byref(r), stream), "gg_autotune")
+        out = {}
+        for i in range(r.n):
+            c = r.choice[i]
+            out[TUNE_NAMES[c.family]] = {"params": list(c.params), "default_ms": c.default_ms,
+                                         "tuned_ms": c.tuned_ms, "candidates": c.candidates}
+        return out
+
+    def tuned(self, family):
+        """The launch shape this mapping uses now for one GG_TUNE_* family."""
+        out = (C.c_uint32 * 4)()
+        _check(lib().gg_tune_get(self.h, family, out), "gg_tune_get")
+        return list(out)
+
     def batch_iterations(self, ngraphs):
         """Per-graph iteration counts of the last many-graphs run."""
         out = np.empty(ngraphs, np.uint32)
         _check(lib().gg_pagerank_batch_iterations(self.h, ngraphs, out.ctypes.data), "gg_pagerank_batch_iterations")
         return out
 
-    def batch_config(self, ipt=7, warps=16, smem_vmax=4096):
-        _check(lib().gg_pagerank_batch_config(self.h, ipt, warps, smem_vmax), "gg_pagerank_batch_config")
+    def batch_config(self, ipt=7, warps=16, smem_vmax=4096, ctas_per_sm=2):
+        _check(lib().gg_pagerank_batch_config(self.h, ipt, warps, smem_vmax, ctas_per_sm), "gg_pagerank_batch_config")
 
     def bfs(self, source, mode="do", profile=False, copy_out=True, stream=None):
         p = BfsParams(BFS_MODES[mode] if isinstance(mode, str) else mode, source, 15, 18, int(profile))

@@ -8,7 +8,7 @@
  *   k_td  top-down step (BFS.c:688-750): one warp per frontier vertex, lanes
  *         over its out-edges, CAS claim of parents[u], warp-aggregated
  *         enqueue (ballot + popc + one atomic per warp), mf += -old parent;
- *         vertices above TD_HEAVY out-edges go to k_td_heavy, which spreads
+ *         vertices above the heavy threshold go to k_td_heavy, which spreads
  *         their edges over the whole grid
  *   k_bu  bottom-up step (BFS.c:752-803): one warp per 32-vertex bitmap word;
  *         each unvisited lane checks its first 4 in-neighbours alone, the
@@ -183,15 +183,15 @@ __device__ __forceinline__ void td_enqueue(bool claimed, uint32_t u, uint32_t la
     }
 }
 
-/* frontier vertices with more out-edges than this go to k_td_heavy, at most
+/* frontier vertices with more out-edges than `heavy_thr` (64 by default,
+ * the tuned value per mapping otherwise) go to k_td_heavy, at most
  * TD_MAX_HEAVY of them per step (further ones stay with their warp) */
-#define TD_HEAVY 64u
 #define TD_MAX_HEAVY 4096u
 
 __device__ __forceinline__ void td_body(const uint32_t *q, uint32_t qlen,
                                         const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
                                         int32_t *parents, uint32_t *dist, uint32_t newdist, uint32_t *visited,
-                                        uint32_t *nq, uint32_t *nbm, Counters *c, uint4 *heavy)
+                                        uint32_t *nq, uint32_t *nbm, Counters *c, uint4 *heavy, uint32_t heavy_thr)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -203,7 +203,7 @@ __device__ __forceinline__ void td_body(const uint32_t *q, uint32_t qlen,
         const uint32_t v = q[i];
         const uint32_t s = off[v], e = off[v + 1];
         if (lane == 0) edges += e - s;
-        if (e - s > TD_HEAVY)
+        if (e - s > heavy_thr)
         {
             uint32_t slot = 0;
             if (lane == 0) slot = atomicAdd(&c->nheavy, 1u);
@@ -480,9 +480,10 @@ __device__ __forceinline__ void q2bm_body(const uint32_t *q, uint32_t qlen, uint
 __global__ void __launch_bounds__(256) k_td(const uint32_t *__restrict__ q, uint32_t qlen,
                                             const uint32_t *__restrict__ off, const uint32_t *__restrict__ adj,
                                             int32_t *parents, uint32_t *dist, uint32_t newdist, uint32_t *visited,
-                                            uint32_t *nq, uint32_t *nbm, Counters *c, uint4 *heavy)
+                                            uint32_t *nq, uint32_t *nbm, Counters *c, uint4 *heavy,
+                                            uint32_t heavy_thr)
 {
-    td_body(q, qlen, off, adj, parents, dist, newdist, visited, nq, nbm, c, heavy);
+    td_body(q, qlen, off, adj, parents, dist, newdist, visited, nq, nbm, c, heavy, heavy_thr);
 }
 __global__ void __launch_bounds__(256) k_td_heavy(const uint4 *__restrict__ heavy, const uint32_t *__restrict__ adj,
                                                   int32_t *parents, uint32_t *dist, uint32_t newdist,
@@ -540,7 +541,7 @@ struct DoArgs
     uint4 *heavy;
     char *ctl;
     unsigned long long bar_limit_ns; /* device-side wait limit of the grid barrier */
-    uint32_t V, words, E, src, alpha, beta;
+    uint32_t V, words, E, src, alpha, beta, heavy_thr;
 };
 
 /* the grid barrier (gg_device.cuh) over the control block, failures
@@ -638,7 +639,7 @@ __global__ void __launch_bounds__(256, 6) k_bfs_do(DoArgs a)
             Counters *cs = a.c + s % 3;
             clear_slot(a.c + (s + 1) % 3);
             td_body(a.q[qcur], qlen, a.out_off, a.out_adj, a.parents, a.dist, level + 1, a.visited, a.q[qcur ^ 1],
-                    nullptr, cs, a.heavy);
+                    nullptr, cs, a.heavy, a.heavy_thr);
             if (!(ok = grid_barrier(a.ctl, a.bar_limit_ns, gen))) break;
             /* the deferred high-degree vertices, when there are any (every
              * block reads the same final count, so all skip together) */
@@ -721,7 +722,8 @@ gg_status td_step(Bfs &B, const uint32_t *q, uint32_t qlen, uint32_t *nq, uint32
     if (qlen)
     {
         k_td<<<cap_blocks((uint64_t)qlen * 32), 256, 0, B.s>>>(q, qlen, B.g->out_off, B.g->out_adj, B.parents, B.dist,
-                                                                newdist, B.visited, nq, nbm, B.c, B.heavy);
+                                                                newdist, B.visited, nq, nbm, B.c, B.heavy,
+                                                                B.g->bfs_heavy);
         k_td_heavy<<<gg_sm_count() * 8, 256, 0, B.s>>>(B.heavy, B.g->out_adj, B.parents, B.dist, newdist, B.visited,
                                                        nq, nbm, B.c);
         B.launches += 2;
@@ -815,6 +817,7 @@ gg_status do_search(Bfs &B, const gg_bfs_params *p)
     a.heavy = B.heavy;
     a.ctl = ctl;
     a.bar_limit_ns = gg_barrier_limit_ns();
+    a.heavy_thr = g->bfs_heavy;
     a.V = B.V;
     a.words = B.words;
     a.E = g->E;
@@ -865,6 +868,7 @@ extern "C" gg_status gg_bfs(gg_graph *g, const gg_bfs_params *p, int32_t *parent
 
     Bfs B;
     GG_CHECK(bfs_setup(B, g, stream, p->profile));
+    gg_tune_lookup(g, B.s);
     const uint32_t V = B.V, src = p->source;
     const bool device_loop = (p->mode == GG_BFS_DO || p->mode == GG_BFS_DO_BITMAP) && !p->profile;
     /* the device loop's control block and first bitmap are cleared by the

@@ -42,12 +42,22 @@ struct gg_buf
     size_t bytes = 0;
 };
 
+/* Launch shape of an FP pull gather (PageRank, SpMV): the default, set by
+ * gg_autotune, or found in the tuning cache for a graph like this one. */
+struct gg_pull_shape
+{
+    uint32_t hot = 2;        /* hot-vertex table: 0 off, 1 on, 2 by size (from 1M vertices) */
+    uint32_t ctas = 5;       /* plain kernel: resident CTAs per SM (GG_PULL_CTAS_PER_SM) */
+    uint32_t hot_warps = 32; /* hot kernel: warps of its one CTA per SM (GG_HOT_WARPS) */
+};
+
 /* Configuration of the many-graphs PageRank kernel (graphs.cu): tile items
  * per lane (5, 7 or 9), warps per CTA, and the bin threshold: graphs of at
  * most smem_vmax vertices keep contributions and sums in shared memory. */
 struct gg_graphs_config
 {
     uint32_t ipt = 7, warps = 16, smem_vmax = 4096;
+    uint32_t ctas = 2; /* resident CTAs per SM: the shared-memory carve-out holds just these, the rest is L1 */
 };
 
 /* The many-graphs run's preparation, cached on the mapping for the graph
@@ -130,6 +140,13 @@ struct gg_graph
     uint32_t graphs_n = 0;
     /* the many-graphs configuration in force (default, set, or tuned) */
     gg_graphs_config graphs_cfg;
+    /* tuned launch shapes (tune.cu): the pull gathers, the BFS heavy-vertex
+     * threshold, the batched PPR tile; tuned = bit per family */
+    gg_pull_shape pr_shape, spmv_shape;
+    uint32_t bfs_heavy = 64;
+    uint32_t ppr_tile = 512, ppr_tiles_items = 0;
+    uint32_t tuned = 0;
+    bool tune_looked_up = false;
 };
 
 /* error state */
@@ -242,6 +259,9 @@ gg_status gg_graphs_launch(gg_graph *g, const gg_graphs_config &cfg, uint32_t ng
 size_t gg_graphs_tile_items(const gg_graphs_config &cfg);
 /* the configuration a many-graphs run on g uses */
 gg_graphs_config gg_graphs_choice(gg_graph *g, uint32_t ngraphs);
+/* tuning (tune.cu): apply the process's tuning cache to g once (the shapes
+ * tuned earlier for a graph of the same size class on this GPU) */
+void gg_tune_lookup(gg_graph *g, cudaStream_t s);
 
 /* smallest float f with (double)f >= x, and largest float f with (double)f <= x */
 float gg_float_ceil(double x);

@@ -80,16 +80,36 @@ int gg_sm_count() { return g_sm_count > 0 ? g_sm_count : 152; }
 
 int gg_persistent_grid(const void *kernel, uint32_t ntiles, int ctas_per_sm)
 {
+    /* per (kernel, requested CTAs per SM): the resident CTAs per SM and the
+     * carve-out that holds them; the carve-out is a kernel attribute, so it
+     * is set again whenever a kernel is launched with another request than
+     * the one last applied to it */
+    struct Shape
+    {
+        const void *kernel;
+        int ctas, bps, pct;
+    };
+    struct Applied
+    {
+        const void *kernel;
+        int pct;
+    };
     static std::mutex mu;
-    static const void *keys[64];
-    static int vals[64];
-    static int n = 0;
-    int bps = 0;
+    static Shape shapes[128];
+    static Applied applied[64];
+    static int nshapes = 0, napplied = 0;
+    int bps = 0, pct = 0;
     {
         std::lock_guard<std::mutex> lk(mu);
-        for (int i = 0; i < n; i++)
-            if (keys[i] == kernel) bps = vals[i];
-        if (!bps)
+        int found = -1;
+        for (int i = 0; i < nshapes; i++)
+            if (shapes[i].kernel == kernel && shapes[i].ctas == ctas_per_sm) found = i;
+        if (found >= 0)
+        {
+            bps = shapes[found].bps;
+            pct = shapes[found].pct;
+        }
+        else
         {
             cudaError_t e = cudaSuccess;
             if (ctas_per_sm > 0)
@@ -104,7 +124,7 @@ int gg_persistent_grid(const void *kernel, uint32_t ntiles, int ctas_per_sm)
                 if (e == cudaSuccess && smem_sm > 0)
                 {
                     const double need = (double)ctas_per_sm * (double)(fa.sharedSizeBytes + 1024);
-                    int pct = (int)ceil(100.0 * need / (double)smem_sm);
+                    pct = (int)ceil(100.0 * need / (double)smem_sm);
                     pct = pct < 1 ? 1 : (pct > 100 ? 100 : pct);
                     e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
                 }
@@ -114,16 +134,31 @@ int gg_persistent_grid(const void *kernel, uint32_t ntiles, int ctas_per_sm)
             {
                 cudaGetLastError();
                 bps = 1;
+                pct = 0;
             }
             if (ctas_per_sm > 0 && bps > ctas_per_sm) bps = ctas_per_sm;
             if (getenv("GG_DEBUG"))
                 fprintf(stderr, "gg: kernel %p: %d CTAs of %d threads per SM (%s)\n", kernel, bps, GG_TILE_NT,
                         cudaGetErrorString(e));
-            if (n < 64)
+            if (nshapes < 128) shapes[nshapes++] = Shape{kernel, ctas_per_sm, bps, pct};
+        }
+        /* the carve-out applied to this kernel last */
+        if (pct > 0)
+        {
+            int a = -1;
+            for (int i = 0; i < napplied; i++)
+                if (applied[i].kernel == kernel) a = i;
+            if (a < 0 && napplied < 64)
             {
-                keys[n] = kernel;
-                vals[n] = bps;
-                n++;
+                a = napplied++;
+                applied[a] = Applied{kernel, 0};
+            }
+            if (a >= 0 && applied[a].pct != pct)
+            {
+                if (cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct) == cudaSuccess)
+                    applied[a].pct = pct;
+                else
+                    cudaGetLastError();
             }
         }
     }
@@ -661,6 +696,14 @@ extern "C" gg_status gg_graph_share(const gg_graph *src, gg_graph **out)
     g->out_off = src->out_off; g->out_adj = src->out_adj; g->out_w = src->out_w;
     g->in_off = src->in_off; g->in_adj = src->in_adj; g->in_w = src->in_w;
     g->out_deg = src->out_deg;
+    /* the launch shapes tuned for the graph */
+    g->pr_shape = src->pr_shape;
+    g->spmv_shape = src->spmv_shape;
+    g->bfs_heavy = src->bfs_heavy;
+    g->ppr_tile = src->ppr_tile;
+    g->graphs_cfg = src->graphs_cfg;
+    g->tuned = src->tuned;
+    g->tune_looked_up = src->tune_looked_up;
     cudaError_t e = cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess)
     {

@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -347,9 +348,26 @@ gg_status gg_graphs_launch(gg_graph *g, const gg_graphs_config &cfg, uint32_t ng
     }
     if (smem + 1024 > 227 * 1024) return gg_fail(GG_ERR_INVALID, "many-graphs configuration exceeds shared memory");
     GG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    /* carve-out: just the shared memory of cfg.ctas CTAs (1 KB reserved
+     * each, plus the static part), so the rest of the SM's array stays L1
+     * for the gathers' lines in flight */
+    int dev = 0, smem_sm = 0;
+    GG_CUDA(cudaGetDevice(&dev));
+    GG_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    cudaFuncAttributes fa;
+    GG_CUDA(cudaFuncGetAttributes(&fa, fn));
+    const uint32_t want = cfg.ctas ? cfg.ctas : 1;
+    if (smem_sm > 0)
+    {
+        const double need = (double)want * (double)(smem + fa.sharedSizeBytes + 1024);
+        int pct = (int)ceil(100.0 * need / (double)smem_sm);
+        pct = pct < 1 ? 1 : (pct > 100 ? 100 : pct);
+        GG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+    }
     int per_sm = 0;
     GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)(warps * 32), smem));
     if (per_sm < 1) return gg_fail(GG_ERR_INVALID, "many-graphs configuration cannot be resident");
+    if ((uint32_t)per_sm > want) per_sm = (int)want;
     const uint32_t grid = std::min<uint32_t>((uint32_t)gg_sm_count() * (uint32_t)per_sm, ngraphs);
     void *args[] = {&a};
     GG_CUDA(cudaLaunchKernel(fn, dim3(grid ? grid : 1), dim3(warps * 32), args, smem, s));
@@ -358,7 +376,6 @@ gg_status gg_graphs_launch(gg_graph *g, const gg_graphs_config &cfg, uint32_t ng
 
 size_t gg_graphs_tile_items(const gg_graphs_config &cfg) { return (size_t)32 * (cfg.ipt == 5 || cfg.ipt == 9 ? cfg.ipt : 7); }
 
-gg_graphs_config gg_graphs_choice(gg_graph *g, uint32_t) { return g->graphs_cfg; }
 
 extern "C" gg_status gg_pagerank_batch_iterations(const gg_graph *g, uint32_t ngraphs, uint32_t *iterations)
 {
@@ -369,15 +386,18 @@ extern "C" gg_status gg_pagerank_batch_iterations(const gg_graph *g, uint32_t ng
     return GG_OK;
 }
 
-extern "C" gg_status gg_pagerank_batch_config(gg_graph *g, uint32_t ipt, uint32_t warps, uint32_t smem_vmax)
+extern "C" gg_status gg_pagerank_batch_config(gg_graph *g, uint32_t ipt, uint32_t warps, uint32_t smem_vmax,
+                                              uint32_t ctas_per_sm)
 {
     if (!g) return gg_fail(GG_ERR_INVALID, "NULL graph");
     if (ipt != 5 && ipt != 7 && ipt != 9) return gg_fail(GG_ERR_INVALID, "ipt must be 5, 7 or 9");
     if (warps < 1 || warps > 32) return gg_fail(GG_ERR_INVALID, "warps must be 1..32");
+    if (ctas_per_sm < 1 || ctas_per_sm * warps > 64) return gg_fail(GG_ERR_INVALID, "ctas_per_sm must be 1..64/warps");
     gg_graphs_config c;
     c.ipt = ipt;
     c.warps = warps;
     c.smem_vmax = smem_vmax;
+    c.ctas = ctas_per_sm;
     size_t smem = 0;
     switch (ipt)
     {
@@ -385,7 +405,9 @@ extern "C" gg_status gg_pagerank_batch_config(gg_graph *g, uint32_t ipt, uint32_
     case 9: smem = graphs_smem<9>(warps, smem_vmax); break;
     default: smem = graphs_smem<7>(warps, smem_vmax); break;
     }
-    if (smem + 1024 > 227 * 1024) return gg_fail(GG_ERR_INVALID, "configuration exceeds shared memory");
+    if (smem + 1024 > 227 * 1024 || ctas_per_sm * (smem + 2048) > 228 * 1024)
+        return gg_fail(GG_ERR_INVALID, "configuration exceeds shared memory");
     g->graphs_cfg = c;
+    g->tuned |= GG_TUNE_BATCH;
     return GG_OK;
 }

@@ -37,7 +37,6 @@ namespace {
 
 using namespace gg;
 
-constexpr uint32_t PPR_TILE = 512; /* merge items per tile */
 constexpr uint32_t NO_SEED = 0xffffffffu;
 
 /* two stored values per lane */
@@ -94,6 +93,7 @@ struct PprArgs
     const uint32_t *off, *adj, *outdeg, *seed_idx;
     const uint2 *coord;
     uint32_t ntiles, V, E;
+    uint32_t tile;     /* merge items per tile (512 by default, the tuned size per mapping otherwise) */
     const CT *cin;
     CT *cout;
     float *rank;       /* [V][KP], written when not null (last iteration) */
@@ -249,9 +249,9 @@ __device__ __forceinline__ void ppr_fixup_tiles(const PprArgs<CT> &a)
     {
         const uint32_t r = a.coord[t + 1].x;
         if (r >= a.V) continue;
-        if (((uint64_t)r + a.off[r]) / PPR_TILE != t) continue;
+        if (((uint64_t)r + a.off[r]) / a.tile != t) continue;
         /* the tile of the row's end item */
-        const uint32_t t_last = (uint32_t)(((uint64_t)r + a.off[r + 1]) / PPR_TILE);
+        const uint32_t t_last = (uint32_t)(((uint64_t)r + a.off[r + 1]) / a.tile);
         float2 tot = *reinterpret_cast<const float2 *>(a.tail + (size_t)t * KP + 2 * gl);
         for (uint32_t m = t + 1; m < t_last; m += B)
         {
@@ -365,13 +365,20 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
     constexpr int U = LPE < 16 ? LPE : 16;
     const uint32_t V = g->V;
     gg_tiles &t = g->ppr_tiles;
+    const uint32_t tile = g->ppr_tile;
+    if (t.coord && g->ppr_tiles_items != tile)
+    {
+        gg_dev_free(g, t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2));
+        t.coord = nullptr;
+    }
     if (!t.coord)
     {
-        const uint64_t nt = ((uint64_t)V + g->E + PPR_TILE - 1) / PPR_TILE;
+        const uint64_t nt = ((uint64_t)V + g->E + tile - 1) / tile;
         if (nt >= 0xffffffffull) return gg_fail(GG_ERR_INVALID, "graph too large for 32-bit tile ids");
         t.ntiles = (uint32_t)(nt ? nt : 1);
         GG_CHECK(gg_dev_alloc(g, (void **)&t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2)));
-        GG_CHECK(gg_launch_tile_coords(g->in_off, V, g->E, t.ntiles, t.coord, s, PPR_TILE));
+        GG_CHECK(gg_launch_tile_coords(g->in_off, V, g->E, t.ntiles, t.coord, s, tile));
+        g->ppr_tiles_items = tile;
         res.launches++;
     }
     void *c0, *c1, *slots;
@@ -385,7 +392,7 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
 
     PprArgs<CT> a;
     a.off = g->in_off; a.adj = g->in_adj; a.outdeg = g->out_deg; a.seed_idx = d_seed_idx;
-    a.coord = t.coord; a.ntiles = t.ntiles; a.V = V; a.E = g->E;
+    a.coord = t.coord; a.ntiles = t.ntiles; a.V = V; a.E = g->E; a.tile = tile;
     a.tele = d_tele; a.damp = p->damp;
     a.head = (float *)slots;
     a.tail = (float *)slots + (size_t)t.ntiles * KP;
@@ -468,6 +475,7 @@ extern "C" gg_status gg_ppr(gg_graph *g, const gg_ppr_params *p, const uint32_t 
         if (seeds[i] >= V) return gg_fail(GG_ERR_INVALID, "seed vertex out of range");
     const uint32_t KP = K <= 16 ? 16 : (K <= 32 ? 32 : 64);
     cudaStream_t s = gg_stream(g, stream);
+    gg_tune_lookup(g, s);
     gg_ppr_result res;
     memset(&res, 0, sizeof(res));
     res.padded_vectors = KP;

@@ -229,18 +229,19 @@ __host__ __device__ constexpr uint32_t hot_entries()
                : GG_HOT_ENTRIES;
 }
 template <int K>
-__host__ __device__ constexpr size_t hot_stage_bytes()
+__host__ __device__ constexpr size_t hot_stage_bytes(uint32_t warps)
 {
-    return (size_t)GG_HOT_WARPS * PullStage<GG_HOT_IPT, typename Fmt<K>::Acc>::BYTES;
+    return (size_t)warps * PullStage<GG_HOT_IPT, typename Fmt<K>::Acc>::BYTES;
 }
 template <int K>
-__host__ __device__ constexpr size_t hot_smem_bytes()
+__host__ __device__ constexpr size_t hot_smem_bytes(uint32_t warps)
 {
-    return hot_stage_bytes<K>() + ((size_t)hot_entries<K>() * sizeof(typename Fmt<K>::CT) + 15) / 16 * 16;
+    return hot_stage_bytes<K>(warps) + ((size_t)hot_entries<K>() * sizeof(typename Fmt<K>::CT) + 15) / 16 * 16;
 }
 
-/* one CTA of GG_HOT_WARPS warps per SM: the CTA fills the table with the
- * hot vertices' stored contributions, then its warps run the engine */
+/* one CTA per SM (up to GG_HOT_WARPS warps, the tuned count): the CTA fills
+ * the table with the hot vertices' stored contributions, then its warps run
+ * the engine */
 template <int K>
 __global__ void __launch_bounds__(GG_HOT_WARPS * 32, 1)
     k_pr_pull_hot(const uint32_t *__restrict__ off, const uint32_t *__restrict__ hot_adj,
@@ -251,35 +252,43 @@ __global__ void __launch_bounds__(GG_HOT_WARPS * 32, 1)
     typedef typename Fmt<K>::CT CT;
     extern __shared__ __align__(16) unsigned char gg_dyn[];
     if (it > 0 && rec[it - 1].active == 0u) return;
-    CT *s_hot = reinterpret_cast<CT *>(gg_dyn + hot_stage_bytes<K>());
+    CT *s_hot = reinterpret_cast<CT *>(gg_dyn + hot_stage_bytes<K>(blockDim.x >> 5));
     for (uint32_t i = threadIdx.x; i < hot_n; i += blockDim.x) s_hot[i] = cin[hot_list[i]];
     __syncthreads();
     warp_pull_sums_dyn<GG_HOT_IPT>(gg_dyn, off, hot_adj, V, coord, ntiles, sums, PrGatherHot<K>{cin, s_hot});
 }
 
-/* grid of k_pr_pull_hot<K>: one CTA per SM, the carve-out sized to its
- * shared memory (the rest of the array stays L1) */
+/* grid of k_pr_pull_hot<K> with `warps` warps: one CTA per SM, the
+ * carve-out sized to its shared memory (the rest of the array stays L1) */
 template <int K>
-int hot_grid(uint32_t ntiles)
+int hot_grid(uint32_t ntiles, uint32_t warps)
 {
     static int ok = -1;
+    static uint32_t applied = 0;
+    int dev = 0, smem_sm = 0;
     if (ok < 0)
     {
-        int dev = 0, smem_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-        const size_t need = hot_smem_bytes<K>();
-        cudaError_t e = cudaFuncSetAttribute(k_pr_pull_hot<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-        if (e == cudaSuccess && smem_sm > 0)
-        {
-            int pct = (int)ceil(100.0 * (double)(need + 1024) / (double)smem_sm);
-            e = cudaFuncSetAttribute(k_pr_pull_hot<K>, cudaFuncAttributePreferredSharedMemoryCarveout, pct > 100 ? 100 : pct);
-        }
+        const size_t most = hot_smem_bytes<K>(GG_HOT_WARPS);
+        cudaError_t e = cudaFuncSetAttribute(k_pr_pull_hot<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
         ok = e == cudaSuccess ? 1 : 0;
         if (!ok) cudaGetLastError();
     }
     if (!ok) return 0;
-    const uint32_t need = (ntiles + GG_HOT_WARPS - 1) / GG_HOT_WARPS;
+    if (applied != warps)
+    {
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        if (smem_sm > 0)
+        {
+            const int pct = (int)ceil(100.0 * (double)(hot_smem_bytes<K>(warps) + 1024) / (double)smem_sm);
+            if (cudaFuncSetAttribute(k_pr_pull_hot<K>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     pct > 100 ? 100 : pct) == cudaSuccess)
+                applied = warps;
+            else
+                cudaGetLastError();
+        }
+    }
+    const uint32_t need = (ntiles + warps - 1) / warps;
     const uint32_t cap = (uint32_t)gg_sm_count();
     return (int)(need < cap ? (need ? need : 1) : cap);
 }
@@ -751,6 +760,7 @@ struct Run
     const gg_pr_params *p;
     float eps_f = 0.0f, eps_fl = 0.0f;
     bool use_hot = false; /* pull gather through the hot-vertex table */
+    gg_pull_shape shape;  /* launch shape of the FP pull gather */
     uint32_t launches = 0;
     uint32_t gather_launches = 0;
     float gather_ms = 0.0f;
@@ -812,14 +822,15 @@ gg_status run_pull(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
         const CT *cin = Fmt<K>::quant ? cb[0] : cb[it & 1];
         GG_CHECK(timed_begin(R));
         int hg = 0;
+        const uint32_t hw = R.shape.hot_warps;
         if constexpr (sizeof(Acc) == 4)
-            if (R.use_hot && g->hot_cap == hot_entries<K>()) hg = hot_grid<K>(g->hot_tiles.ntiles);
+            if (R.use_hot && g->hot_cap == hot_entries<K>()) hg = hot_grid<K>(g->hot_tiles.ntiles, hw);
         if (hg)
-            k_pr_pull_hot<K><<<hg, GG_HOT_WARPS * 32, hot_smem_bytes<K>(), R.s>>>(
+            k_pr_pull_hot<K><<<hg, hw * 32, hot_smem_bytes<K>(hw), R.s>>>(
                 g->in_off, g->hot_adj, g->hot_tiles.coord, g->hot_tiles.ntiles, V, (Acc *)sums, cin, g->hot_list,
                 g->hot_n, rec, it);
         else
-            k_pr_pull<K><<<gg_persistent_grid((const void *)k_pr_pull<K>, t->ntiles, GG_PULL_CTAS_PER_SM), GG_TILE_NT, 0,
+            k_pr_pull<K><<<gg_persistent_grid((const void *)k_pr_pull<K>, t->ntiles, (int)R.shape.ctas), GG_TILE_NT, 0,
                            R.s>>>(g->in_off, g->in_adj, t->coord, t->ntiles, V, (Acc *)sums, PrGather<K>{cin}, rec, it);
         GG_CHECK(timed_end(R));
         PrCommon c;
@@ -1138,7 +1149,10 @@ gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_
 
     /* the hot-vertex table for the FP pull modes (prepared before any
      * capture: preparation reads back to the host) */
-    if (p->mode == GG_PR_PULL && !(p->flags & GG_PR_HOT_OFF) && ((p->flags & GG_PR_HOT_ON) || V >= (1u << 20)) &&
+    gg_tune_lookup(g, R.s);
+    R.shape = g->pr_shape;
+    const bool hot_default = R.shape.hot == 2 ? V >= (1u << 20) : R.shape.hot == 1;
+    if (p->mode == GG_PR_PULL && !(p->flags & GG_PR_HOT_OFF) && ((p->flags & GG_PR_HOT_ON) || hot_default) &&
         V < GG_HOT_FLAG && V > 0)
     {
         const uint32_t cap = GG_HOT_TABLE_BYTES / (p->storage == GG_STORE_F32 ? 4u : 2u);
@@ -1158,7 +1172,7 @@ gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_
     {
         struct Key
         {
-            uint32_t mode, storage, iters, init, flags, ngraphs, use_hot, V, E;
+            uint32_t mode, storage, iters, init, flags, ngraphs, use_hot, V, E, ctas, hot_warps;
             float damp;
             double eps;
         } key;
@@ -1166,6 +1180,7 @@ gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_
         memset(&key, 0, sizeof(key));
         key.mode = p->mode; key.storage = p->storage; key.iters = iters; key.init = p->init_one_over_n;
         key.flags = p->flags; key.ngraphs = ngraphs; key.use_hot = R.use_hot ? 1u : 0u; key.V = V; key.E = g->E;
+        key.ctas = R.shape.ctas; key.hot_warps = R.shape.hot_warps;
         key.damp = p->damp; key.eps = p->epsilon;
         if (g->pr_exec && g->pr_gen == g->mem_gen && memcmp(g->pr_key, &key, sizeof(key)) == 0)
         {

@@ -66,9 +66,9 @@ struct SpmvGatherHot
 };
 
 template <class T>
-__host__ __device__ constexpr size_t spmv_hot_stage_bytes()
+__host__ __device__ constexpr size_t spmv_hot_stage_bytes(uint32_t warps)
 {
-    return (size_t)GG_HOT_WARPS * PullStage<GG_HOT_IPT, float>::BYTES;
+    return (size_t)warps * PullStage<GG_HOT_IPT, float>::BYTES;
 }
 template <class T>
 __host__ __device__ constexpr uint32_t spmv_hot_entries()
@@ -76,9 +76,9 @@ __host__ __device__ constexpr uint32_t spmv_hot_entries()
     return GG_HOT_TABLE_BYTES / sizeof(T) < GG_HOT_ENTRIES ? (uint32_t)(GG_HOT_TABLE_BYTES / sizeof(T)) : GG_HOT_ENTRIES;
 }
 template <class T>
-__host__ __device__ constexpr size_t spmv_hot_smem_bytes()
+__host__ __device__ constexpr size_t spmv_hot_smem_bytes(uint32_t warps)
 {
-    return spmv_hot_stage_bytes<T>() + ((size_t)spmv_hot_entries<T>() * sizeof(T) + 15) / 16 * 16;
+    return spmv_hot_stage_bytes<T>(warps) + ((size_t)spmv_hot_entries<T>() * sizeof(T) + 15) / 16 * 16;
 }
 
 template <class T>
@@ -88,34 +88,42 @@ __global__ void __launch_bounds__(GG_HOT_WARPS * 32, 1)
                     const T *__restrict__ x, const uint32_t *__restrict__ hot_list, uint32_t hot_n)
 {
     extern __shared__ __align__(16) unsigned char gg_dyn[];
-    T *s_hot = reinterpret_cast<T *>(gg_dyn + spmv_hot_stage_bytes<T>());
+    T *s_hot = reinterpret_cast<T *>(gg_dyn + spmv_hot_stage_bytes<T>(blockDim.x >> 5));
     for (uint32_t i = threadIdx.x; i < hot_n; i += blockDim.x) s_hot[i] = x[hot_list[i]];
     __syncthreads();
     warp_pull_sums_dyn<GG_HOT_IPT>(gg_dyn, off, hot_adj, V, coord, ntiles, y, SpmvGatherHot<T>{w, x, s_hot});
 }
 
-/* one CTA of GG_HOT_WARPS warps per SM, carve-out sized to its shared memory */
+/* one CTA of `warps` warps per SM, carve-out sized to its shared memory */
 template <class T>
-int spmv_hot_grid(uint32_t ntiles)
+int spmv_hot_grid(uint32_t ntiles, uint32_t warps)
 {
     static int ok = -1;
+    static uint32_t applied = 0;
     if (ok < 0)
     {
-        int dev = 0, smem_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-        const size_t need = spmv_hot_smem_bytes<T>();
-        cudaError_t e = cudaFuncSetAttribute(k_spmv_pull_hot<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-        if (e == cudaSuccess && smem_sm > 0)
-        {
-            int pct = (int)ceil(100.0 * (double)(need + 1024) / (double)smem_sm);
-            e = cudaFuncSetAttribute(k_spmv_pull_hot<T>, cudaFuncAttributePreferredSharedMemoryCarveout, pct > 100 ? 100 : pct);
-        }
+        const size_t most = spmv_hot_smem_bytes<T>(GG_HOT_WARPS);
+        cudaError_t e = cudaFuncSetAttribute(k_spmv_pull_hot<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
         ok = e == cudaSuccess ? 1 : 0;
         if (!ok) cudaGetLastError();
     }
     if (!ok) return 0;
-    const uint32_t need = (ntiles + GG_HOT_WARPS - 1) / GG_HOT_WARPS;
+    if (applied != warps)
+    {
+        int dev = 0, smem_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        if (smem_sm > 0)
+        {
+            const int pct = (int)ceil(100.0 * (double)(spmv_hot_smem_bytes<T>(warps) + 1024) / (double)smem_sm);
+            if (cudaFuncSetAttribute(k_spmv_pull_hot<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     pct > 100 ? 100 : pct) == cudaSuccess)
+                applied = warps;
+            else
+                cudaGetLastError();
+        }
+    }
+    const uint32_t need = (ntiles + warps - 1) / warps;
     const uint32_t cap = (uint32_t)gg_sm_count();
     return (int)(need < cap ? (need ? need : 1) : cap);
 }
@@ -265,7 +273,10 @@ gg_status spmv_fp(gg_graph *g, const gg_spmv_params *p, const float *x_dev, floa
     const T *xv = sizeof(T) == 4 ? (const T *)xf : (const T *)xs;
     /* the hot-vertex table (as for the PageRank pull): by default from 1M vertices */
     bool use_hot = false;
-    if (pull && !(p->flags & GG_PR_HOT_OFF) && ((p->flags & GG_PR_HOT_ON) || V >= (1u << 20)) && V < GG_HOT_FLAG)
+    gg_tune_lookup(g, s);
+    const gg_pull_shape shape = g->spmv_shape;
+    const bool hot_default = shape.hot == 2 ? V >= (1u << 20) : shape.hot == 1;
+    if (pull && !(p->flags & GG_PR_HOT_OFF) && ((p->flags & GG_PR_HOT_ON) || hot_default) && V < GG_HOT_FLAG)
     {
         GG_CHECK(gg_hot_prepare(g, s, spmv_hot_entries<T>()));
         use_hot = g->hot_cap == spmv_hot_entries<T>();
@@ -284,12 +295,12 @@ gg_status spmv_fp(gg_graph *g, const gg_spmv_params *p, const float *x_dev, floa
             /* y is the row-sum array: zero, then the gather stores rows and
              * adds the partials of rows spanning tiles */
             GG_CUDA(cudaMemsetAsync(y, 0, (size_t)V * sizeof(float), s));
-            const int hg = use_hot ? spmv_hot_grid<T>(g->hot_tiles.ntiles) : 0;
+            const int hg = use_hot ? spmv_hot_grid<T>(g->hot_tiles.ntiles, shape.hot_warps) : 0;
             if (hg)
-                k_spmv_pull_hot<T><<<hg, GG_HOT_WARPS * 32, spmv_hot_smem_bytes<T>(), s>>>(
+                k_spmv_pull_hot<T><<<hg, shape.hot_warps * 32, spmv_hot_smem_bytes<T>(shape.hot_warps), s>>>(
                     g->in_off, g->hot_adj, g->hot_tiles.coord, g->hot_tiles.ntiles, V, y, w, xv, g->hot_list, g->hot_n);
             else
-                k_spmv_pull<T><<<gg_persistent_grid((const void *)k_spmv_pull<T>, t->ntiles, GG_PULL_CTAS_PER_SM),
+                k_spmv_pull<T><<<gg_persistent_grid((const void *)k_spmv_pull<T>, t->ntiles, (int)shape.ctas),
                                  GG_TILE_NT, 0, s>>>(g->in_off, g->in_adj, t->coord, t->ntiles, V, y, SpmvGather<T>{w, xv});
         }
         else

@@ -293,6 +293,9 @@ def main():
     dg = gg.DeviceGraph(graph, gg.MAP_IN)
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
+    # launch shape of the gather picked by the autotuner on this graph
+    # (setup, like the graph build; the default shape is one candidate)
+    tune = dg.autotune(gg.TUNE_PR, reps=3, stream=sptr).get("pr")
 
     def step(profile=True):
         _, r = dg.pagerank("pull", iterations=ITERS, epsilon=0.0, copy_out=False, profile=profile, stream=sptr)
@@ -368,7 +371,8 @@ def main():
         "config": {"workload": f"pagerank_pull_rmat{a.scale}", "vertices": V, "edges": E,
                    "iterations_per_step": ITERS, "epsilon": 0.0, "storage": "f32",
                    "l2": "inputs larger than L2 (4E = %.2f GB CSC ids per iteration)" % (4 * E / 1e9),
-                   "parallelism": f"replicas x{world}", "graph_build_s": round(t_build, 2)},
+                   "parallelism": f"replicas x{world}", "graph_build_s": round(t_build, 2),
+                   "gather_shape": tune},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": kernel, "alg_bytes_per_launch": alg,
                      "launch_ms": per_launch_ms, "peak_source": peak_kind, "iteration": iteration},
@@ -520,9 +524,16 @@ def splitmix_unit(seed):
 def batch_extras(gg, torch, peak, n=4096, iters=20):
     """Many small graphs in one run: n R-MAT graphs, graph i of scale
     round(10 + 7u) with u uniform from SplitMix64(seed+4+i) (V = 2^scale,
-    log-uniform between 2^10 and 2^17), edge factor 8, R-MAT seed seed+4+i;
-    their union is ranked by one pull PageRank of `iters` iterations launched
-    as a single CUDA graph, every vertex normalised by its own graph's size."""
+    log-uniform between 2^10 and 2^17), edge factor 8, R-MAT seed seed+4+i.
+    The many-graphs kernel ranks all of them, every iteration, in one launch
+    (one CTA per graph, largest first; graphs up to the bin threshold keep
+    their contributions in shared memory), in the configuration the
+    autotuner picks for this batch and in the default one; the union pull
+    (20 x 2 launches over the block-diagonal union, as one CUDA graph) is
+    timed beside it.  Roofline: the algorithm's per-iteration bytes summed
+    over the graphs.  Parity: the smallest, a middle and the largest graph
+    against the FP64 oracle; CPU baseline: the oracle's OpenMP pull on 64
+    graphs spread over the size range."""
     import numpy as np
     from oracle import oracle_ctypes as O
 
@@ -532,18 +543,43 @@ def batch_extras(gg, torch, peak, n=4096, iters=20):
     build_s = time.perf_counter() - t0
     V, E = g.V, g.E
     dg = gg.DeviceGraph(g, gg.MAP_IN)
-    for _ in range(2):
-        dg.pagerank_batch(voff, iterations=iters, epsilon=0.0, copy_out=False, cuda_graph=True)
-    torch.cuda.synchronize()
-    reps = 5
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(reps):
-        dg.pagerank_batch(voff, iterations=iters, epsilon=0.0, copy_out=False, cuda_graph=True)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / reps
-    ranks, _ = dg.pagerank_batch(voff, iterations=iters, epsilon=0.0, cuda_graph=True)
+
+    def timed(**kw):
+        for _ in range(2):
+            dg.pagerank_batch(voff, iterations=iters, epsilon=0.0, copy_out=False, **kw)
+        torch.cuda.synchronize()
+        reps = 5
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            _, r = dg.pagerank_batch(voff, iterations=iters, epsilon=0.0, copy_out=False, **kw)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, r
+
+    out = {"graphs": n, "vertices": V, "edges": E, "iterations": iters, "build_s": round(build_s, 1)}
+    alg = pr_bytes(V, E, 4)
+    runs = {}
+    dg.batch_config(7, 16, 4096, 2)
+    ms, r = timed()
+    runs["many_graphs_kernel_default_shape"] = {
+        "ms_per_run": ms, "gteps": E * iters / (ms / 1e3) / 1e9,
+        "iteration_hbm_frac": alg / (ms / iters / 1e3) / 1e9 / peak, "launches": r["launches"],
+        "shape": dg.tuned(gg.TUNE_BATCH)}
+    t0 = time.perf_counter()
+    tune = dg.autotune(gg.TUNE_BATCH, reps=2, vertex_off=voff)["batch"]
+    tune_s = time.perf_counter() - t0
+    ms, r = timed()
+    runs["many_graphs_kernel"] = {"ms_per_run": ms, "gteps": E * iters / (ms / 1e3) / 1e9,
+                                  "iteration_hbm_frac": alg / (ms / iters / 1e3) / 1e9 / peak,
+                                  "launches": r["launches"], "shape": dg.tuned(gg.TUNE_BATCH),
+                                  "autotune": tune, "autotune_s": round(tune_s, 1)}
+    ms, r = timed(union=True, cuda_graph=True)
+    runs["union_pull_cuda_graph"] = {"ms_per_run": ms, "gteps": E * iters / (ms / 1e3) / 1e9,
+                                     "iteration_hbm_frac": alg / (ms / iters / 1e3) / 1e9 / peak,
+                                     "launches": r["launches"]}
+    out.update(runs)
+    ranks, _ = dg.pagerank_batch(voff, iterations=iters, epsilon=0.0)
     dg.free()
     g.free()
     # parity on the smallest, a middle and the largest graph
@@ -554,10 +590,19 @@ def batch_extras(gg, torch, peak, n=4096, iters=20):
         ex = O.pagerank_f64(o, iters)
         part = ranks[voff[i]:voff[i + 1]]
         worst = max(worst, float(np.abs(part - ex).sum() / np.abs(ex).sum()))
-    return {"graphs": n, "vertices": V, "edges": E, "iterations": iters, "build_s": round(build_s, 1),
-            "ms_per_run": ms, "gteps": E * iters / (ms / 1e3) / 1e9,
-            "iteration_hbm_frac": pr_bytes(V, E, 4) / (ms / iters / 1e3) / 1e9 / peak,
-            "l1_relative_vs_fp64_max": worst, "launch": "one CUDA graph per run"}
+    out["l1_relative_vs_fp64_max"] = worst
+    # CPU baseline: 64 graphs spread over the sizes, the oracle's OpenMP pull
+    threads = os.cpu_count() or 1
+    cpu_e, cpu_s = 0, 0.0
+    for i in order[:: max(1, n // 64)][:64]:
+        o = O.rmat_csr(scales[int(i)], 8, seed=SEED + 4 + int(i))
+        t0 = time.perf_counter()
+        O.pagerank(o, 0, iters, 0.0, nthreads=threads)
+        cpu_s += time.perf_counter() - t0
+        cpu_e += o.E * iters
+    out["cpu_baseline"] = {"gteps": cpu_e / cpu_s / 1e9, "cores": threads, "kind": "port",
+                           "sample": "64 of the graphs, every 64th by size, 20 iterations each"}
+    return out
 
 
 def serving_extras(gg, scale=23, n=1500, rate=150.0):

@@ -208,10 +208,13 @@ gg_status gg_pagerank_batch(gg_graph *g, const gg_pr_params *p, uint32_t ngraphs
  * many-graphs run of gg_pagerank_batch on g, which had `ngraphs` graphs. */
 gg_status gg_pagerank_batch_iterations(const gg_graph *g, uint32_t ngraphs, uint32_t *iterations);
 /* Shape of the many-graphs kernel on g: merge items per lane of its tiles
- * (5, 7 or 9), warps per CTA (1..32), and the bin threshold: graphs of at
- * most smem_vmax vertices keep contributions and sums in shared memory (0:
- * none).  Default 7, 16, 4096; gg_autotune picks one per mapping. */
-gg_status gg_pagerank_batch_config(gg_graph *g, uint32_t ipt, uint32_t warps, uint32_t smem_vmax);
+ * (5, 7 or 9), warps per CTA (1..32), the bin threshold (graphs of at most
+ * smem_vmax vertices keep contributions and sums in shared memory; 0: none)
+ * and the resident CTAs per SM (the shared-memory carve-out holds just
+ * these; the rest of the SM's array is L1).  Default 7, 16, 4096, 2;
+ * gg_autotune picks one per mapping. */
+gg_status gg_pagerank_batch_config(gg_graph *g, uint32_t ipt, uint32_t warps, uint32_t smem_vmax,
+                                   uint32_t ctas_per_sm);
 
 /* ---- BFS -------------------------------------------------------------------- */
 
@@ -397,6 +400,64 @@ gg_status gg_ppr(gg_graph *g, const gg_ppr_params *p, const uint32_t *seed_off, 
 /* Device pointer to the last gg_ppr's ranks (V rows of *stride floats),
  * valid until the next call on `g`. */
 const float *gg_ppr_device_ranks(const gg_graph *g, uint32_t *stride);
+
+/* ---- autotuner ----------------------------------------------------------------
+ * No counterpart in the reference (its one run-time granularity knob is
+ * binSize, graphConfig.h:18).  gg_autotune times candidate launch shapes of
+ * the hot kernels on a mapping and keeps the fastest on it (the default
+ * shape is always a candidate); the picks are also remembered per graph
+ * class (size, mean degree, degree skew, SM count), so the first call on a
+ * later mapping of a graph of the same class starts with them, and
+ * gg_tune_save / gg_tune_load carry them to another process.
+ *   GG_TUNE_PR, GG_TUNE_SPMV  FP pull gather: hot-vertex table off with 3-8
+ *                             CTAs per SM, or on with 16/24/32 warps
+ *   GG_TUNE_BFS               top-down heavy-vertex threshold (32..1024)
+ *   GG_TUNE_PPR               batched personalised PageRank tile (256/512/1024)
+ *   GG_TUNE_BATCH             many-graphs kernel: shared-memory bin threshold,
+ *                             CTAs per SM, warps per CTA, items per lane
+ *                             (needs vertex_off)
+ */
+#define GG_TUNE_PR 0x1u
+#define GG_TUNE_SPMV 0x2u
+#define GG_TUNE_BFS 0x4u
+#define GG_TUNE_PPR 0x8u
+#define GG_TUNE_BATCH 0x10u
+
+typedef struct gg_tune_params
+{
+    uint32_t families;          /* GG_TUNE_* bits */
+    uint32_t storage;           /* gg_storage the PR / SpMV / PPR candidates run with */
+    uint32_t reps;              /* timed runs per candidate after one untimed run (0: 3) */
+    uint32_t ngraphs;           /* GG_TUNE_BATCH: graphs of the batch */
+    const uint32_t *vertex_off; /* GG_TUNE_BATCH: their vertex ranges (host, ngraphs + 1) */
+} gg_tune_params;
+
+typedef struct gg_tune_choice
+{
+    uint32_t family;      /* GG_TUNE_* */
+    uint32_t params[4];   /* PR/SPMV: hot (0/1), CTAs per SM, hot warps; BFS: threshold; PPR: tile;
+                             BATCH: items per lane, warps, bin threshold, CTAs per SM */
+    float default_ms;     /* median time of the default shape */
+    float tuned_ms;       /* median time of the pick */
+    uint32_t candidates;  /* shapes timed */
+} gg_tune_choice;
+
+typedef struct gg_tune_result
+{
+    gg_tune_choice choice[5];
+    uint32_t n;
+} gg_tune_result;
+
+gg_status gg_autotune(gg_graph *g, const gg_tune_params *p, gg_tune_result *r, void *stream);
+/* The remembered picks of this process, as text lines; load adds them. */
+gg_status gg_tune_save(const char *path);
+gg_status gg_tune_load(const char *path);
+/* Forget the remembered picks (mappings keep the shapes they have). */
+gg_status gg_tune_reset(void);
+/* The shape g uses now for one family (params as in gg_tune_choice; a
+ * mapping that has not run the family yet may still pick up a remembered
+ * shape on its first call). */
+gg_status gg_tune_get(const gg_graph *g, uint32_t family, uint32_t *params);
 
 /* ---- drop-in side options ---------------------------------------------------- */
 
