@@ -173,7 +173,7 @@ class PprResult(C.Structure):
 
 class ServerParams(C.Structure):
     _fields_ = [("max_ppr_batch", C.c_uint32), ("ppr_iterations", C.c_uint32), ("damp", C.c_float),
-                ("ppr_storage", C.c_uint32), ("mem_budget_bytes", C.c_uint64)]
+                ("ppr_storage", C.c_uint32), ("mem_budget_bytes", C.c_uint64), ("bfs_workers", C.c_uint32)]
 
 
 class QueryInfo(C.Structure):
@@ -782,17 +782,18 @@ def set_gpu_options(storage="f32", device=0, keep_resident=False, verbose=False)
 
 class Server:
     """Query server over a DeviceGraph mapped with MAP_IN | MAP_OUT
-    (include/gg_server.h): batched personalised PageRank and BFS queries,
-    results held on the device until taken."""
+    (include/gg_server.h): personalised PageRank queries in one continuous
+    batch, BFS queries on several workers, results held on the device until
+    taken."""
 
     QUERY_PPR, QUERY_BFS = 0, 1
 
     def __init__(self, dg, max_ppr_batch=64, ppr_iterations=20, damp=0.85, ppr_storage="f32",
-                 mem_budget_bytes=None):
+                 mem_budget_bytes=None, bfs_workers=2):
         self.dg = dg
         self.V = dg.graph.V
         budget = mem_budget_bytes if mem_budget_bytes is not None else 256 * 8 * self.V
-        p = ServerParams(max_ppr_batch, ppr_iterations, damp, STORE[ppr_storage], budget)
+        p = ServerParams(max_ppr_batch, ppr_iterations, damp, STORE[ppr_storage], budget, bfs_workers)
         self.h = C.c_void_p()
         _check(lib().gg_server_start(dg.h, C.byref(p), C.byref(self.h)), "gg_server_start")
 

@@ -263,6 +263,32 @@ gg_graphs_config gg_graphs_choice(gg_graph *g, uint32_t ngraphs);
  * tuned earlier for a graph of the same size class on this GPU) */
 void gg_tune_lookup(gg_graph *g, cudaStream_t s);
 
+/* One iteration of the batched personalised PageRank on caller-held state
+ * (ppr.cu; the server's continuous batch): the first kp (16/32/64) vectors
+ * of rows of rs values; vectors in rank_mask write their ranks, vectors in
+ * zero_mask store zero contributions (their slot is freed). */
+struct gg_ppr_round_args
+{
+    uint32_t kp = 16, rs = 64;
+    int bf16 = 0;
+    const void *cin = nullptr;
+    void *cout = nullptr;
+    float *rank = nullptr;
+    unsigned long long rank_mask = 0, zero_mask = 0;
+    const uint32_t *seed_idx = nullptr;
+    const float *tele = nullptr;
+    float *slots = nullptr;
+    float damp = 0.85f;
+};
+/* tiles and the two contribution buffers (zeroed) and the tile slots */
+gg_status gg_ppr_round_prepare(gg_graph *g, uint32_t rs, int bf16, void **cb0, void **cb1, float **slots,
+                               cudaStream_t s);
+/* seed indices of the seed vertices, and iteration-0 contributions of the
+ * vectors in `fresh` at them (their columns must be zero elsewhere) */
+gg_status gg_ppr_round_seed(gg_graph *g, uint32_t rs, int bf16, void *cin, const uint32_t *d_seedv, uint32_t nseedv,
+                            const float *d_init, uint32_t *d_seed_idx, unsigned long long fresh, cudaStream_t s);
+gg_status gg_ppr_round(gg_graph *g, const gg_ppr_round_args &r, cudaStream_t s);
+
 /* smallest float f with (double)f >= x, and largest float f with (double)f <= x */
 float gg_float_ceil(double x);
 float gg_float_floor(double x);

@@ -94,10 +94,14 @@ struct PprArgs
     const uint2 *coord;
     uint32_t ntiles, V, E;
     uint32_t tile;     /* merge items per tile (512 by default, the tuned size per mapping otherwise) */
+    uint32_t rs;       /* values per vertex row of cin / cout / rank / tele: KP, or more when
+                          only the first KP of a wider row are run (the server) */
     const CT *cin;
     CT *cout;
-    float *rank;       /* [V][KP], written when not null (last iteration) */
-    const float *tele; /* [nseeds][KP]: (1-d) c_k(v) / |S_k| of seed vertex i */
+    float *rank;       /* [V][rs]: ranks of the vectors in rank_mask are written here */
+    unsigned long long rank_mask; /* vectors whose ranks this iteration writes (their last) */
+    unsigned long long zero_mask; /* vectors whose contributions are stored as zero (a freed slot) */
+    const float *tele; /* [nseeds][rs]: (1-d) c_k(v) / |S_k| of seed vertex i */
     float *head;       /* [ntiles][KP]: partial of the row that ends in the tile but began before it */
     float *tail;       /* [ntiles][KP]: partial of the row left open at the tile's end */
     float damp;
@@ -111,7 +115,7 @@ __device__ __forceinline__ void ppr_finish(const PprArgs<CT> &a, uint32_t r, flo
     float r0 = __fmul_rn(a.damp, s0), r1 = __fmul_rn(a.damp, s1);
     if (si != NO_SEED)
     {
-        const float2 t = *reinterpret_cast<const float2 *>(a.tele + (size_t)si * KP + 2 * gl);
+        const float2 t = *reinterpret_cast<const float2 *>(a.tele + (size_t)si * a.rs + 2 * gl);
         r0 = __fadd_rn(t.x, r0);
         r1 = __fadd_rn(t.y, r1);
     }
@@ -122,9 +126,18 @@ __device__ __forceinline__ void ppr_finish(const PprArgs<CT> &a, uint32_t r, flo
         c0 = __fdiv_rn(r0, fd);
         c1 = __fdiv_rn(r1, fd);
     }
-    const size_t o = (size_t)r * KP + 2 * gl;
+    const uint32_t pair = (uint32_t)(a.zero_mask >> (2 * gl)) & 3u;
+    if (pair & 1u) c0 = 0.0f;
+    if (pair & 2u) c1 = 0.0f;
+    const size_t o = (size_t)r * a.rs + 2 * gl;
     PairIO<CT>::store(a.cout + o, c0, c1);
-    if (a.rank) *reinterpret_cast<float2 *>(a.rank + o) = make_float2(r0, r1);
+    const uint32_t want = (uint32_t)(a.rank_mask >> (2 * gl)) & 3u;
+    if (want == 3u)
+        *reinterpret_cast<float2 *>(a.rank + o) = make_float2(r0, r1);
+    else if (want == 1u)
+        a.rank[o] = r0;
+    else if (want == 2u)
+        a.rank[o + 1] = r1;
 }
 
 template <int KP>
@@ -199,8 +212,8 @@ __device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
             {
                 const uint32_t u = __shfl_sync(gmask, myid, i, LPE);
                 if ((uint32_t)i < nb)
-                    v[i] = COHERENT ? PairIO<CT>::load_cg(a.cin + (size_t)u * KP + 2 * gl)
-                                    : PairIO<CT>::load(a.cin + (size_t)u * KP + 2 * gl);
+                    v[i] = COHERENT ? PairIO<CT>::load_cg(a.cin + (size_t)u * a.rs + 2 * gl)
+                                    : PairIO<CT>::load(a.cin + (size_t)u * a.rs + 2 * gl);
             }
             const uint32_t en = e + U;
             myid = 0;
@@ -288,7 +301,6 @@ template <class CT>
 struct PprLoop
 {
     CT *cb0, *cb1;
-    float *rank;
     uint32_t iterations;
     char *ctl;
     unsigned int *err;
@@ -307,7 +319,7 @@ __global__ void __launch_bounds__(256, ppr_persist_ctas<CT>()) k_ppr_persist(Ppr
     {
         a.cin = (it & 1) ? L.cb1 : L.cb0;
         a.cout = (it & 1) ? L.cb0 : L.cb1;
-        a.rank = it + 1 == L.iterations ? L.rank : nullptr;
+        a.rank_mask = it + 1 == L.iterations ? ~0ull : 0ull;
         ppr_gather_tiles<KP, CT, U, true>(a);
         if (!grid_barrier(L.ctl, L.err, L.limit_ns, gen)) return;
         ppr_fixup_tiles<KP, CT>(a);
@@ -316,19 +328,25 @@ __global__ void __launch_bounds__(256, ppr_persist_ctas<CT>()) k_ppr_persist(Ppr
 }
 
 /* contributions of the seed vertices at iteration 0 (the rest is zero) */
-template <int KP, class CT>
+/* contributions of the seed vertices at iteration 0 (the rest is zero), and
+ * their seed indices; rows of rs values, of which vectors in `fresh` are
+ * written (all of them for gg_ppr; the newly admitted slots for the
+ * server, whose other columns hold running vectors) */
+template <class CT>
 __global__ void k_ppr_seed_init(const uint32_t *__restrict__ seed_vertex, uint32_t nseeds,
                                 const float *__restrict__ init, const uint32_t *__restrict__ outdeg, CT *cin,
-                                uint32_t *seed_idx)
+                                uint32_t *seed_idx, uint32_t rs, unsigned long long fresh)
 {
-    const uint64_t n = (uint64_t)nseeds * (KP / 2);
+    const uint64_t n = (uint64_t)nseeds * (rs / 2);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
     {
-        const uint32_t s = (uint32_t)(i / (KP / 2)), gl = (uint32_t)(i % (KP / 2));
+        const uint32_t s = (uint32_t)(i / (rs / 2)), gl = (uint32_t)(i % (rs / 2));
         const uint32_t v = seed_vertex[s];
         if (gl == 0) seed_idx[v] = s;
+        const uint32_t pair = (uint32_t)(fresh >> (2 * gl)) & 3u;
+        if (!pair) continue;
         const uint32_t deg = outdeg[v];
-        const float2 r = *reinterpret_cast<const float2 *>(init + (size_t)s * KP + 2 * gl);
+        const float2 r = *reinterpret_cast<const float2 *>(init + (size_t)s * rs + 2 * gl);
         float c0 = 0.0f, c1 = 0.0f;
         if (deg)
         {
@@ -336,7 +354,15 @@ __global__ void k_ppr_seed_init(const uint32_t *__restrict__ seed_vertex, uint32
             c0 = __fdiv_rn(r.x, fd);
             c1 = __fdiv_rn(r.y, fd);
         }
-        PairIO<CT>::store(cin + (size_t)v * KP + 2 * gl, c0, c1);
+        CT *dst = cin + (size_t)v * rs + 2 * gl;
+        if (pair == 3u)
+            PairIO<CT>::store(dst, c0, c1);
+        else
+        {
+            /* one of the pair: the other column belongs to a running vector */
+            if (pair & 1u) dst[0] = from_f32<CT>(c0);
+            if (pair & 2u) dst[1] = from_f32<CT>(c1);
+        }
     }
 }
 
@@ -387,12 +413,14 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
     GG_CHECK(gg_work(g, 18, (size_t)t.ntiles * KP * sizeof(float) * 2, &slots));
     GG_CUDA(cudaMemsetAsync(c0, 0, (size_t)V * KP * sizeof(CT), s));
     GG_CUDA(cudaMemsetAsync(d_seed_idx, 0xff, (size_t)V * sizeof(uint32_t), s));
-    k_ppr_seed_init<KP, CT><<<gg_sm_count() * 2, 256, 0, s>>>(d_seedv, nseedv, d_init, g->out_deg, (CT *)c0, d_seed_idx);
+    k_ppr_seed_init<CT><<<gg_sm_count() * 2, 256, 0, s>>>(d_seedv, nseedv, d_init, g->out_deg, (CT *)c0, d_seed_idx,
+                                                          KP, ~0ull);
     res.launches++;
 
     PprArgs<CT> a;
     a.off = g->in_off; a.adj = g->in_adj; a.outdeg = g->out_deg; a.seed_idx = d_seed_idx;
-    a.coord = t.coord; a.ntiles = t.ntiles; a.V = V; a.E = g->E; a.tile = tile;
+    a.coord = t.coord; a.ntiles = t.ntiles; a.V = V; a.E = g->E; a.tile = tile; a.rs = KP;
+    a.rank = d_rank; a.rank_mask = 0; a.zero_mask = 0;
     a.tele = d_tele; a.damp = p->damp;
     a.head = (float *)slots;
     a.tail = (float *)slots + (size_t)t.ntiles * KP;
@@ -411,7 +439,7 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
         GG_CHECK(gg_work(g, 30, GG_BAR_BYTES, &ctl));
         GG_CUDA(cudaMemsetAsync(ctl, 0, GG_BAR_BYTES, s));
         PprLoop<CT> L;
-        L.cb0 = cb[0]; L.cb1 = cb[1]; L.rank = d_rank; L.iterations = p->iterations;
+        L.cb0 = cb[0]; L.cb1 = cb[1]; L.iterations = p->iterations;
         L.ctl = (char *)ctl; L.err = (unsigned int *)ctl; L.limit_ns = gg_barrier_limit_ns();
         void *args[] = {&a, &L};
         GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_ppr_persist<KP, CT, U>, dim3(grid), dim3(256), args, 0, s));
@@ -428,7 +456,7 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
     {
         a.cin = cb[it & 1];
         a.cout = cb[(it + 1) & 1];
-        a.rank = it + 1 == p->iterations ? d_rank : nullptr;
+        a.rank_mask = it + 1 == p->iterations ? ~0ull : 0ull;
         if (p->profile)
         {
             cudaEvent_t e;
@@ -453,6 +481,86 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
 }
 
 } // namespace
+
+/* ---- one iteration on caller-held state (the server's continuous batch) ----- */
+
+namespace {
+
+template <int KP, class CT>
+gg_status round_run(gg_graph *g, const gg_ppr_round_args &r, cudaStream_t s)
+{
+    constexpr int LPE = KP / 2;
+    constexpr int U = LPE < 16 ? LPE : 16;
+    gg_tiles &t = g->ppr_tiles;
+    PprArgs<CT> a;
+    a.off = g->in_off; a.adj = g->in_adj; a.outdeg = g->out_deg; a.seed_idx = r.seed_idx;
+    a.coord = t.coord; a.ntiles = t.ntiles; a.V = g->V; a.E = g->E; a.tile = g->ppr_tiles_items; a.rs = r.rs;
+    a.cin = (const CT *)r.cin; a.cout = (CT *)r.cout; a.rank = r.rank;
+    a.rank_mask = r.rank_mask; a.zero_mask = r.zero_mask;
+    a.tele = r.tele; a.damp = r.damp;
+    a.head = r.slots;
+    a.tail = r.slots + (size_t)t.ntiles * KP;
+    const int grid = occupancy_grid(k_ppr_pull<KP, CT, U>, 256, t.ntiles, LPE);
+    const int fgrid = occupancy_grid(k_ppr_fixup<KP, CT>, 256, t.ntiles, LPE);
+    k_ppr_pull<KP, CT, U><<<grid, 256, 0, s>>>(a);
+    k_ppr_fixup<KP, CT><<<fgrid, 256, 0, s>>>(a);
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+}
+
+} // namespace
+
+gg_status gg_ppr_round_prepare(gg_graph *g, uint32_t rs, int bf16, void **cb0, void **cb1, float **slots,
+                               cudaStream_t s)
+{
+    gg_tiles &t = g->ppr_tiles;
+    const uint32_t tile = g->ppr_tile;
+    const uint32_t V = g->V;
+    if (t.coord && g->ppr_tiles_items != tile)
+    {
+        gg_dev_free(g, t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2));
+        t.coord = nullptr;
+    }
+    if (!t.coord)
+    {
+        const uint64_t nt = ((uint64_t)V + g->E + tile - 1) / tile;
+        if (nt >= 0xffffffffull) return gg_fail(GG_ERR_INVALID, "graph too large for 32-bit tile ids");
+        t.ntiles = (uint32_t)(nt ? nt : 1);
+        GG_CHECK(gg_dev_alloc(g, (void **)&t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2)));
+        GG_CHECK(gg_launch_tile_coords(g->in_off, V, g->E, t.ntiles, t.coord, s, tile));
+        g->ppr_tiles_items = tile;
+    }
+    const size_t cb = (size_t)V * rs * (bf16 ? 2 : 4);
+    GG_CHECK(gg_work(g, 16, cb, cb0));
+    GG_CHECK(gg_work(g, 17, cb, cb1));
+    GG_CHECK(gg_work(g, 18, (size_t)t.ntiles * rs * sizeof(float) * 2, (void **)slots));
+    GG_CUDA(cudaMemsetAsync(*cb0, 0, cb, s));
+    GG_CUDA(cudaMemsetAsync(*cb1, 0, cb, s));
+    return GG_OK;
+}
+
+gg_status gg_ppr_round_seed(gg_graph *g, uint32_t rs, int bf16, void *cin, const uint32_t *d_seedv, uint32_t nseedv,
+                            const float *d_init, uint32_t *d_seed_idx, unsigned long long fresh, cudaStream_t s)
+{
+    if (!nseedv) return GG_OK;
+    if (bf16)
+        k_ppr_seed_init<__nv_bfloat16><<<gg_sm_count() * 2, 256, 0, s>>>(d_seedv, nseedv, d_init, g->out_deg,
+                                                                         (__nv_bfloat16 *)cin, d_seed_idx, rs, fresh);
+    else
+        k_ppr_seed_init<float><<<gg_sm_count() * 2, 256, 0, s>>>(d_seedv, nseedv, d_init, g->out_deg, (float *)cin,
+                                                                 d_seed_idx, rs, fresh);
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+}
+
+gg_status gg_ppr_round(gg_graph *g, const gg_ppr_round_args &r, cudaStream_t s)
+{
+    if (r.bf16)
+        return r.kp == 16 ? round_run<16, __nv_bfloat16>(g, r, s)
+               : r.kp == 32 ? round_run<32, __nv_bfloat16>(g, r, s) : round_run<64, __nv_bfloat16>(g, r, s);
+    return r.kp == 16 ? round_run<16, float>(g, r, s) : r.kp == 32 ? round_run<32, float>(g, r, s)
+                                                                : round_run<64, float>(g, r, s);
+}
 
 extern "C" gg_status gg_ppr(gg_graph *g, const gg_ppr_params *p, const uint32_t *seed_off, const uint32_t *seeds,
                             float *ranks, gg_ppr_result *r, void *stream)

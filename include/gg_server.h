@@ -7,19 +7,25 @@
  * submit personalised-PageRank queries (a seed set) and BFS queries (a
  * source) from any thread; two worker threads drain them on the GPU:
  *
- *   PPR  waiting queries are batched, up to max_ppr_batch per launch, into
- *        one gg_ppr call (K vectors per gather), so a query's latency is the
- *        wait for the running batch plus one batched run;
- *   BFS  one direction-optimising gg_bfs per query, on a shared view of the
- *        graph with its own stream, so it overlaps the PPR batches.
+ *   PPR  continuous batching: one running batch of up to max_ppr_batch
+ *        vector slots (64 at most) advances every busy slot by one iteration
+ *        per round (one gather over the first 16, 32 or 64 slots, as the busy
+ *        ones need); between rounds waiting queries are admitted into free
+ *        slots and slots that ran all their iterations retire, so a query
+ *        waits at most one round before it starts, and its latency is about
+ *        its own iterations;
+ *   BFS  bfs_workers workers (default 2), each running one direction-
+ *        optimising gg_bfs per query on its own shared view of the graph
+ *        and stream, so searches overlap each other and the PPR rounds.
  *
  * Results stay in device memory until the client takes them.  Admission is
  * by a device-memory budget: a worker starts work only while the results
  * held (taken or not) plus the new ones fit mem_budget_bytes (PPR: 4V bytes
  * per query, BFS: 8V), so a client that does not take results slows the
  * server down instead of exhausting the GPU.  A query's result does not
- * depend on the queries batched or running with it (gg_ppr's vectors are
- * bit-identical alone or batched; BFS levels are exact).
+ * depend on the queries batched or running with it (a PPR vector is
+ * bit-identical to gg_ppr's for that seed set alone, whatever slots run
+ * beside it; BFS levels are exact).
  */
 
 #include <stdint.h>
@@ -40,6 +46,7 @@ typedef struct gg_server_params
     float damp;                 /* 0.85 */
     uint32_t ppr_storage;       /* GG_STORE_F32 or GG_STORE_BF16 */
     uint64_t mem_budget_bytes;  /* device bytes for results held; at least 8V */
+    uint32_t bfs_workers;       /* concurrent BFS workers, 0: 2 (at most 16) */
 } gg_server_params;
 
 enum { GG_QUERY_PPR = 0, GG_QUERY_BFS = 1 };
@@ -51,7 +58,7 @@ typedef struct gg_query_info
     double submit_s;            /* host steady-clock seconds */
     double start_s;             /* its run was launched */
     double done_s;              /* its result was complete in device memory */
-    uint32_t batch_size;        /* PPR: vectors in its launch */
+    uint32_t batch_size;        /* PPR: busy slots of the running batch when it was admitted */
     uint32_t bfs_levels;        /* BFS: frontier steps run */
     uint32_t bfs_reached;       /* BFS: vertices reached, source included */
 } gg_query_info;

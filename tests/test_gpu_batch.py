@@ -93,14 +93,15 @@ def test_cuda_graph_cache_reuse_and_invalidation(gpu):
     np.testing.assert_allclose(e, e_plain, rtol=1e-6, atol=0)
 
 
-@pytest.mark.parametrize("cfg", [(7, 16, 4096), (7, 16, 0), (5, 8, 200), (9, 32, 512), (7, 4, 64)])
+@pytest.mark.parametrize("cfg", [(7, 16, 4096, 2), (7, 16, 0, 2), (5, 8, 200, 4), (9, 32, 512, 1), (7, 4, 64, 3)])
 def test_many_graphs_kernel_per_graph_stop(gpu, orc, batch, cfg):
     """The many-graphs kernel (one CTA per graph, every iteration in one
     launch) with an epsilon stop: every graph stops on its own, after the
     iterations of the reference's loop on that graph alone, and its ranks
     pass the floating-point rule against the FP64 oracle.  The shapes cover
     every graph in shared memory, none, and a mix (bins at 64, 200 and 512
-    vertices), with 5, 7 and 9 items per lane and 4 to 32 warps."""
+    vertices), with 5, 7 and 9 items per lane, 4 to 32 warps and 1 to 4
+    resident CTAs per SM."""
     g, voff = batch
     dg = gpu.DeviceGraph(g, gpu.MAP_IN)
     dg.batch_config(*cfg)

@@ -103,3 +103,53 @@ def test_server_rejects_and_times_out(gpu, rg):
     with pytest.raises(gpu.GgError):
         gpu.Server(pull_only, ppr_iterations=5)   # BFS needs the out-CSR too
     pull_only.free()
+
+
+def test_server_ppr_equals_gg_ppr_alone(gpu, orc, rg):
+    """A PPR query run in the server's continuous batch, beside others
+    admitted and retired at other iterations, is bit-identical to gg_ppr on
+    that seed set alone (FP32 and BF16 storage)."""
+    g, o = rg
+    rng = np.random.default_rng(21)
+    sets = [[int(x) for x in rng.integers(0, g.V, int(rng.integers(1, 20)))] for _ in range(24)]
+    for storage in ("f32", "bf16"):
+        dg = gpu.DeviceGraph(g, gpu.MAP_IN | gpu.MAP_OUT)
+        srv = gpu.Server(dg, ppr_iterations=ITERS, ppr_storage=storage)
+        try:
+            got = []
+            tickets = []
+            for i, s in enumerate(sets):
+                tickets.append(srv.submit_ppr(s))
+                if i % 5 == 4:   # take some while others run: slots retire and refill
+                    got.append(srv.take(tickets.pop(0))[0])
+            got += [srv.take(t)[0] for t in tickets]
+        finally:
+            srv.stop()
+        for s, r in zip(sets, got):
+            alone, _ = dg.ppr([s], iterations=ITERS, storage=storage)
+            np.testing.assert_array_equal(r, alone[:, 0])
+        dg.free()
+
+
+def test_server_admits_between_iterations(gpu, orc):
+    """Continuous batching: a query submitted while another is running
+    starts before that one ends (at the next iteration boundary) instead of
+    waiting for it, and both are exact."""
+    import time
+
+    g, o = pair(gpu, orc, gpu.Graph.rmat(16, 16))
+    dg = gpu.DeviceGraph(g, gpu.MAP_IN | gpu.MAP_OUT)
+    srv = gpu.Server(dg, ppr_iterations=400, ppr_storage="f32")
+    try:
+        t1 = srv.submit_ppr([1, 2])
+        time.sleep(0.005)
+        t2 = srv.submit_ppr([3])
+        r1, i1 = srv.take(t1)
+        r2, i2 = srv.take(t2)
+    finally:
+        srv.stop()
+        dg.free()
+    assert i2["start_s"] < i1["done_s"], (i1, i2)
+    assert i2["batch_size"] == 2
+    for r, s in ((r1, [1, 2]), (r2, [3])):
+        assert np.abs(r - orc.ppr_f64_multi(o, s, 400, DAMP)).sum() <= 1e-5
