@@ -207,7 +207,7 @@ class TuneParams(C.Structure):
 
 
 class TuneChoice(C.Structure):
-    _fields_ = [("family", C.c_uint32), ("params", C.c_uint32 * 4), ("default_ms", C.c_float),
+    _fields_ = [("family", C.c_uint32), ("params", C.c_uint32 * 5), ("default_ms", C.c_float),
                 ("tuned_ms", C.c_float), ("candidates", C.c_uint32)]
 
 
@@ -263,6 +263,7 @@ def lib() -> C.CDLL:
         L.gg_tune_save.argtypes = [C.c_char_p]
         L.gg_tune_load.argtypes = [C.c_char_p]
         L.gg_tune_get.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+        L.gg_pagerank_batch_strategy.argtypes = [C.c_void_p, C.c_uint32]
         L.gg_pagerank_batch_config.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]
         L.gg_ppr.argtypes = [C.c_void_p, P(PprParams), C.c_void_p, C.c_void_p, C.c_void_p, P(PprResult), C.c_void_p]
         L.gg_ppr_device_ranks.argtypes = [C.c_void_p, P(C.c_uint32)]
@@ -685,7 +686,7 @@ class DeviceGraph:
 
     def tuned(self, family):
         """The launch shape this mapping uses now for one GG_TUNE_* family."""
-        out = (C.c_uint32 * 4)()
+        out = (C.c_uint32 * 5)()
         _check(lib().gg_tune_get(self.h, family, out), "gg_tune_get")
         return list(out)
 
@@ -695,8 +696,12 @@ class DeviceGraph:
         _check(lib().gg_pagerank_batch_iterations(self.h, ngraphs, out.ctypes.data), "gg_pagerank_batch_iterations")
         return out
 
-    def batch_config(self, ipt=7, warps=16, smem_vmax=4096, ctas_per_sm=2):
+    def batch_config(self, ipt=7, warps=16, smem_vmax=4096, ctas_per_sm=2, strategy=None):
+        """Shape of the many-graphs kernel; strategy 1 runs it, 2 the union
+        pull, 0 picks by mean graph size (None leaves it as it is)."""
         _check(lib().gg_pagerank_batch_config(self.h, ipt, warps, smem_vmax, ctas_per_sm), "gg_pagerank_batch_config")
+        if strategy is not None:
+            _check(lib().gg_pagerank_batch_strategy(self.h, strategy), "gg_pagerank_batch_strategy")
 
     def bfs(self, source, mode="do", profile=False, copy_out=True, stream=None):
         p = BfsParams(BFS_MODES[mode] if isinstance(mode, str) else mode, source, 15, 18, int(profile))

@@ -58,6 +58,10 @@ struct gg_graphs_config
 {
     uint32_t ipt = 7, warps = 16, smem_vmax = 4096;
     uint32_t ctas = 2; /* resident CTAs per SM: the shared-memory carve-out holds just these, the rest is L1 */
+    /* 0: by mean graph size (the many-graphs kernel up to 4096 vertices per
+     * graph on average, the union pull above), 1: the many-graphs kernel,
+     * 2: the union pull */
+    uint32_t strategy = 0;
 };
 
 /* The many-graphs run's preparation, cached on the mapping for the graph
@@ -269,7 +273,7 @@ void gg_tune_lookup(gg_graph *g, cudaStream_t s);
  * zero_mask store zero contributions (their slot is freed). */
 struct gg_ppr_round_args
 {
-    uint32_t kp = 16, rs = 64;
+    uint32_t kp = 16; /* rows hold 64 values */
     int bf16 = 0;
     const void *cin = nullptr;
     void *cout = nullptr;

@@ -407,7 +407,17 @@ extern "C" gg_status gg_pagerank_batch_config(gg_graph *g, uint32_t ipt, uint32_
     }
     if (smem + 1024 > 227 * 1024 || ctas_per_sm * (smem + 2048) > 228 * 1024)
         return gg_fail(GG_ERR_INVALID, "configuration exceeds shared memory");
+    c.strategy = g->graphs_cfg.strategy;
     g->graphs_cfg = c;
+    g->tuned |= GG_TUNE_BATCH;
+    return GG_OK;
+}
+
+extern "C" gg_status gg_pagerank_batch_strategy(gg_graph *g, uint32_t strategy)
+{
+    if (!g) return gg_fail(GG_ERR_INVALID, "NULL graph");
+    if (strategy > 2) return gg_fail(GG_ERR_INVALID, "strategy must be 0, 1 or 2");
+    g->graphs_cfg.strategy = strategy;
     g->tuned |= GG_TUNE_BATCH;
     return GG_OK;
 }

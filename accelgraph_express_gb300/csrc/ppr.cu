@@ -93,9 +93,7 @@ struct PprArgs
     const uint32_t *off, *adj, *outdeg, *seed_idx;
     const uint2 *coord;
     uint32_t ntiles, V, E;
-    uint32_t tile;     /* merge items per tile (512 by default, the tuned size per mapping otherwise) */
-    uint32_t rs;       /* values per vertex row of cin / cout / rank / tele: KP, or more when
-                          only the first KP of a wider row are run (the server) */
+    uint32_t tile_log2; /* merge items per tile, a power of two (512 by default, the tuned size otherwise) */
     const CT *cin;
     CT *cout;
     float *rank;       /* [V][rs]: ranks of the vectors in rank_mask are written here */
@@ -108,14 +106,16 @@ struct PprArgs
 };
 
 /* rank and contribution of row r from its (two-vector) sum */
-template <int KP, class CT>
+/* RS: values per vertex row of cin / cout / rank / tele -- KP, or 64 when
+ * only the first KP of wider rows are run (the server's continuous batch) */
+template <int KP, int RS, class CT>
 __device__ __forceinline__ void ppr_finish(const PprArgs<CT> &a, uint32_t r, float s0, float s1, uint32_t si,
                                            uint32_t deg, uint32_t gl)
 {
     float r0 = __fmul_rn(a.damp, s0), r1 = __fmul_rn(a.damp, s1);
     if (si != NO_SEED)
     {
-        const float2 t = *reinterpret_cast<const float2 *>(a.tele + (size_t)si * a.rs + 2 * gl);
+        const float2 t = *reinterpret_cast<const float2 *>(a.tele + (size_t)si * RS + 2 * gl);
         r0 = __fadd_rn(t.x, r0);
         r1 = __fadd_rn(t.y, r1);
     }
@@ -129,7 +129,7 @@ __device__ __forceinline__ void ppr_finish(const PprArgs<CT> &a, uint32_t r, flo
     const uint32_t pair = (uint32_t)(a.zero_mask >> (2 * gl)) & 3u;
     if (pair & 1u) c0 = 0.0f;
     if (pair & 2u) c1 = 0.0f;
-    const size_t o = (size_t)r * a.rs + 2 * gl;
+    const size_t o = (size_t)r * RS + 2 * gl;
     PairIO<CT>::store(a.cout + o, c0, c1);
     const uint32_t want = (uint32_t)(a.rank_mask >> (2 * gl)) & 3u;
     if (want == 3u)
@@ -150,7 +150,7 @@ __device__ __forceinline__ void ppr_slot(float *slots, uint32_t tile, float s0, 
  * COHERENT: contributions read through L2 only (they are rewritten inside
  * the launch by the persistent kernel; the read-only path may keep stale
  * lines from an earlier iteration) */
-template <int KP, class CT, int U, bool COHERENT>
+template <int KP, int RS, class CT, int U, bool COHERENT>
 __device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
 {
     constexpr uint32_t LPE = KP / 2;
@@ -192,7 +192,7 @@ __device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
             if (r == i0 && start0 < j0)
                 ppr_slot<KP>(a.head, tile, s0, s1, gl);
             else
-                ppr_finish<KP, CT>(a, r, s0, s1, si, deg, gl);
+                ppr_finish<KP, RS, CT>(a, r, s0, s1, si, deg, gl);
             s0 = 0.0f;
             s1 = 0.0f;
             r++;
@@ -212,8 +212,8 @@ __device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
             {
                 const uint32_t u = __shfl_sync(gmask, myid, i, LPE);
                 if ((uint32_t)i < nb)
-                    v[i] = COHERENT ? PairIO<CT>::load_cg(a.cin + (size_t)u * a.rs + 2 * gl)
-                                    : PairIO<CT>::load(a.cin + (size_t)u * a.rs + 2 * gl);
+                    v[i] = COHERENT ? PairIO<CT>::load_cg(a.cin + (size_t)u * RS + 2 * gl)
+                                    : PairIO<CT>::load(a.cin + (size_t)u * RS + 2 * gl);
             }
             const uint32_t en = e + U;
             myid = 0;
@@ -242,16 +242,16 @@ __device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
     }
 }
 
-template <int KP, class CT, int U>
+template <int KP, int RS, class CT, int U>
 __global__ void __launch_bounds__(256) k_ppr_pull(PprArgs<CT> a)
 {
-    ppr_gather_tiles<KP, CT, U, false>(a);
+    ppr_gather_tiles<KP, RS, CT, U, false>(a);
 }
 
 /* finish the rows spanning tiles: the row that begins in tile t and is
  * still open at t's end (row coord[t+1].x) sums tail[t], the tails of the
  * tiles it crosses and the head of the tile where it ends, in tile order */
-template <int KP, class CT>
+template <int KP, int RS, class CT>
 __device__ __forceinline__ void ppr_fixup_tiles(const PprArgs<CT> &a)
 {
     constexpr uint32_t LPE = KP / 2, B = 8;
@@ -262,9 +262,9 @@ __device__ __forceinline__ void ppr_fixup_tiles(const PprArgs<CT> &a)
     {
         const uint32_t r = a.coord[t + 1].x;
         if (r >= a.V) continue;
-        if (((uint64_t)r + a.off[r]) / a.tile != t) continue;
+        if ((((uint64_t)r + a.off[r]) >> a.tile_log2) != t) continue;
         /* the tile of the row's end item */
-        const uint32_t t_last = (uint32_t)(((uint64_t)r + a.off[r + 1]) / a.tile);
+        const uint32_t t_last = (uint32_t)(((uint64_t)r + a.off[r + 1]) >> a.tile_log2);
         float2 tot = *reinterpret_cast<const float2 *>(a.tail + (size_t)t * KP + 2 * gl);
         for (uint32_t m = t + 1; m < t_last; m += B)
         {
@@ -283,14 +283,14 @@ __device__ __forceinline__ void ppr_fixup_tiles(const PprArgs<CT> &a)
         const float2 h = *reinterpret_cast<const float2 *>(a.head + (size_t)t_last * KP + 2 * gl);
         tot.x += h.x;
         tot.y += h.y;
-        ppr_finish<KP, CT>(a, r, tot.x, tot.y, a.seed_idx[r], a.outdeg[r], gl);
+        ppr_finish<KP, RS, CT>(a, r, tot.x, tot.y, a.seed_idx[r], a.outdeg[r], gl);
     }
 }
 
-template <int KP, class CT>
+template <int KP, int RS, class CT>
 __global__ void __launch_bounds__(256) k_ppr_fixup(PprArgs<CT> a)
 {
-    ppr_fixup_tiles<KP, CT>(a);
+    ppr_fixup_tiles<KP, RS, CT>(a);
 }
 
 /* every iteration in one cooperative launch: gather, grid barrier, fix-up
@@ -320,9 +320,9 @@ __global__ void __launch_bounds__(256, ppr_persist_ctas<CT>()) k_ppr_persist(Ppr
         a.cin = (it & 1) ? L.cb1 : L.cb0;
         a.cout = (it & 1) ? L.cb0 : L.cb1;
         a.rank_mask = it + 1 == L.iterations ? ~0ull : 0ull;
-        ppr_gather_tiles<KP, CT, U, true>(a);
+        ppr_gather_tiles<KP, KP, CT, U, true>(a);
         if (!grid_barrier(L.ctl, L.err, L.limit_ns, gen)) return;
-        ppr_fixup_tiles<KP, CT>(a);
+        ppr_fixup_tiles<KP, KP, CT>(a);
         if (it + 1 < L.iterations && !grid_barrier(L.ctl, L.err, L.limit_ns, gen)) return;
     }
 }
@@ -419,7 +419,7 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
 
     PprArgs<CT> a;
     a.off = g->in_off; a.adj = g->in_adj; a.outdeg = g->out_deg; a.seed_idx = d_seed_idx;
-    a.coord = t.coord; a.ntiles = t.ntiles; a.V = V; a.E = g->E; a.tile = tile; a.rs = KP;
+    a.coord = t.coord; a.ntiles = t.ntiles; a.V = V; a.E = g->E; a.tile_log2 = (uint32_t)__builtin_ctz(tile);
     a.rank = d_rank; a.rank_mask = 0; a.zero_mask = 0;
     a.tele = d_tele; a.damp = p->damp;
     a.head = (float *)slots;
@@ -450,8 +450,8 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
         GG_CUDA(cudaGetLastError());
         return GG_OK;
     }
-    const int grid = occupancy_grid(k_ppr_pull<KP, CT, U>, 256, t.ntiles, LPE);
-    const int fgrid = occupancy_grid(k_ppr_fixup<KP, CT>, 256, t.ntiles, LPE);
+    const int grid = occupancy_grid(k_ppr_pull<KP, KP, CT, U>, 256, t.ntiles, LPE);
+    const int fgrid = occupancy_grid(k_ppr_fixup<KP, KP, CT>, 256, t.ntiles, LPE);
     for (uint32_t it = 0; it < p->iterations; it++)
     {
         a.cin = cb[it & 1];
@@ -464,7 +464,7 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
             GG_CUDA(cudaEventRecord(e, s));
             evs.push_back(e);
         }
-        k_ppr_pull<KP, CT, U><<<grid, 256, 0, s>>>(a);
+        k_ppr_pull<KP, KP, CT, U><<<grid, 256, 0, s>>>(a);
         if (p->profile)
         {
             cudaEvent_t e;
@@ -472,7 +472,7 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
             GG_CUDA(cudaEventRecord(e, s));
             evs.push_back(e);
         }
-        k_ppr_fixup<KP, CT><<<fgrid, 256, 0, s>>>(a);
+        k_ppr_fixup<KP, KP, CT><<<fgrid, 256, 0, s>>>(a);
         res.launches += 2;
         res.gather_launches++;
     }
@@ -494,16 +494,17 @@ gg_status round_run(gg_graph *g, const gg_ppr_round_args &r, cudaStream_t s)
     gg_tiles &t = g->ppr_tiles;
     PprArgs<CT> a;
     a.off = g->in_off; a.adj = g->in_adj; a.outdeg = g->out_deg; a.seed_idx = r.seed_idx;
-    a.coord = t.coord; a.ntiles = t.ntiles; a.V = g->V; a.E = g->E; a.tile = g->ppr_tiles_items; a.rs = r.rs;
+    a.coord = t.coord; a.ntiles = t.ntiles; a.V = g->V; a.E = g->E;
+    a.tile_log2 = (uint32_t)__builtin_ctz(g->ppr_tiles_items);
     a.cin = (const CT *)r.cin; a.cout = (CT *)r.cout; a.rank = r.rank;
     a.rank_mask = r.rank_mask; a.zero_mask = r.zero_mask;
     a.tele = r.tele; a.damp = r.damp;
     a.head = r.slots;
     a.tail = r.slots + (size_t)t.ntiles * KP;
-    const int grid = occupancy_grid(k_ppr_pull<KP, CT, U>, 256, t.ntiles, LPE);
-    const int fgrid = occupancy_grid(k_ppr_fixup<KP, CT>, 256, t.ntiles, LPE);
-    k_ppr_pull<KP, CT, U><<<grid, 256, 0, s>>>(a);
-    k_ppr_fixup<KP, CT><<<fgrid, 256, 0, s>>>(a);
+    const int grid = occupancy_grid(k_ppr_pull<KP, 64, CT, U>, 256, t.ntiles, LPE);
+    const int fgrid = occupancy_grid(k_ppr_fixup<KP, 64, CT>, 256, t.ntiles, LPE);
+    k_ppr_pull<KP, 64, CT, U><<<grid, 256, 0, s>>>(a);
+    k_ppr_fixup<KP, 64, CT><<<fgrid, 256, 0, s>>>(a);
     GG_CUDA(cudaGetLastError());
     return GG_OK;
 }

@@ -1117,7 +1117,9 @@ gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_
     if (ngraphs && p->mode == GG_PR_PULL && p->storage == GG_STORE_F32 && !(p->flags & GG_PR_BATCH_UNION))
     {
         if (!g->in_off || !g->out_deg) return gg_fail(GG_ERR_INVALID, "pull PageRank needs GG_MAP_IN");
-        return graphs_impl(g, p, ranks, r, stream, ngraphs, h_voff);
+        const gg_graphs_config cfg = gg_graphs_choice(g, ngraphs);
+        const bool per_graph = cfg.strategy == 1 || (cfg.strategy == 0 && g->V <= 4096ull * ngraphs);
+        if (per_graph) return graphs_impl(g, p, ranks, r, stream, ngraphs, h_voff);
     }
     const int pull = !(p->mode == GG_PR_PUSH || p->mode == GG_PR_PUSH_FX64 || p->mode == GG_PR_PUSH_Q ||
                        p->mode == GG_PR_DD_PUSH || p->mode == GG_PR_DD_PULLPUSH);

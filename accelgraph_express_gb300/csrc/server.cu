@@ -263,7 +263,6 @@ void gg_server::ppr_loop()
         const uint32_t top = cover ? 64 - (uint32_t)__builtin_clzll(cover) : 1;
         gg_ppr_round_args r;
         r.kp = top <= 16 ? 16 : top <= 32 ? 32 : 64;
-        r.rs = SLOTS;
         r.bf16 = bf16;
         r.cin = cb[parity];
         r.cout = cb[parity ^ 1];

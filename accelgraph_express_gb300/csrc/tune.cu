@@ -21,9 +21,10 @@
  *             time of eight searches from fixed sources;
  *   PPR       merge items per tile of the batched personalised PageRank
  *             (256, 512, 1024); measured: one K = 64 run of 5 iterations;
- *   BATCH     the many-graphs kernel: bin threshold (0, 1024, 2048, 4096,
- *             8192 vertices in shared memory), then resident CTAs per SM
- *             (1-4), then warps per CTA (8, 16, 32), then items per lane (5,
+ *   BATCH     the union pull against the many-graphs kernel, and the
+ *             kernel's shape: resident CTAs per SM x warps per CTA (2 x 16,
+ *             1 x 32, 1 x 16, 2 x 8, 4 x 8), then the bin threshold (0, 1024,
+ *             4096, 8192 vertices in shared memory), then items per lane (5,
  *             7, 9), each stage keeping the best of the one before
  *             (coordinate descent); measured: one run of the batch.
  * Every candidate runs once untimed, then `reps` timed runs; the median
@@ -60,7 +61,7 @@ struct Key
 
 struct Pick
 {
-    uint32_t v[4];
+    uint32_t v[5];
 };
 
 std::mutex g_mu;
@@ -322,75 +323,104 @@ gg_status tune_batch(gg_graph *g, uint32_t ngraphs, const uint32_t *voff, uint32
                      gg_tune_choice &c)
 {
     const gg_graphs_config keep = g->graphs_cfg;
-    gg_graphs_config cur; /* the default */
+    const uint32_t tuned_before = g->tuned;
     float best = INFINITY;
     uint32_t n = 0;
-    auto try_cfg = [&](const gg_graphs_config &x, bool *better) -> gg_status {
-        *better = false;
-        if (gg_pagerank_batch_config(g, x.ipt, x.warps, x.smem_vmax, x.ctas) != GG_OK) return GG_OK; /* does not fit */
-        gg_pr_params p = {GG_PR_PULL, GG_STORE_F32, 20, 0, 0.0, 0.85f, 0, 0};
-        float ms = INFINITY;
-        GG_CHECK(time_runs(g, s, reps, [&]() -> gg_status {
+    gg_pr_params p = {GG_PR_PULL, GG_STORE_F32, 20, 0, 0.0, 0.85f, 0, 0};
+    auto run_cfg = [&](const gg_graphs_config &x, float *ms) -> gg_status {
+        *ms = INFINITY;
+        if (x.strategy == 1 && gg_pagerank_batch_config(g, x.ipt, x.warps, x.smem_vmax, x.ctas) != GG_OK)
+        {
+            gg_last_error();
+            return GG_OK; /* does not fit */
+        }
+        g->graphs_cfg.strategy = x.strategy;
+        return time_runs(g, s, reps, [&]() -> gg_status {
             gg_pr_result r;
             return gg_pagerank_batch(g, &p, ngraphs, voff, nullptr, &r, s);
-        }, &ms));
+        }, ms);
+    };
+    gg_graphs_config bestc;
+    auto consider = [&](const gg_graphs_config &x) -> gg_status {
+        float ms;
+        GG_CHECK(run_cfg(x, &ms));
         if (n++ == 0) c.default_ms = ms;
         if (ms < best)
         {
             best = ms;
-            *better = true;
+            bestc = x;
         }
         return GG_OK;
     };
-    bool better;
-    gg_status st = try_cfg(cur, &better);
-    gg_graphs_config bestc = cur;
-    for (uint32_t vmax : {0u, 1024u, 2048u, 8192u})
+    /* the default first: the rule by mean graph size */
+    gg_graphs_config dflt;
+    dflt.strategy = g->V <= 4096ull * ngraphs ? 1u : 2u;
+    gg_status st = consider(dflt);
+    gg_graphs_config other = dflt;
+    other.strategy = dflt.strategy == 1 ? 2u : 1u;
+    if (st == GG_OK) st = consider(other);
+    /* the kernel's shape: CTAs x warps, then the bin, then items per lane */
+    gg_graphs_config base;
+    base.strategy = 1;
+    const uint32_t shapes[][2] = {{2, 16}, {1, 32}, {1, 16}, {2, 8}, {4, 8}};
+    gg_graphs_config kbest = base;
+    float kms = INFINITY;
+    auto stage = [&](const gg_graphs_config &x) -> gg_status {
+        float ms;
+        GG_CHECK(run_cfg(x, &ms));
+        n++;
+        if (ms < kms)
+        {
+            kms = ms;
+            kbest = x;
+        }
+        if (ms < best)
+        {
+            best = ms;
+            bestc = x;
+        }
+        return GG_OK;
+    };
+    for (const auto &sh : shapes)
     {
         if (st != GG_OK) break;
-        gg_graphs_config x = bestc;
+        gg_graphs_config x = base;
+        x.ctas = sh[0];
+        x.warps = sh[1];
+        st = stage(x);
+    }
+    const gg_graphs_config k1 = kbest;
+    for (uint32_t vmax : {0u, 1024u, 8192u})
+    {
+        if (st != GG_OK) break;
+        gg_graphs_config x = k1;
         x.smem_vmax = vmax;
-        st = try_cfg(x, &better);
-        if (better) bestc = x;
+        st = stage(x);
     }
-    const gg_graphs_config stage2 = bestc;
-    for (uint32_t ctas : {1u, 3u, 4u})
-    {
-        if (st != GG_OK) break;
-        gg_graphs_config x = stage2;
-        x.ctas = ctas;
-        st = try_cfg(x, &better);
-        if (better) bestc = x;
-    }
-    const gg_graphs_config stage2b = bestc;
-    for (uint32_t w : {8u, 32u})
-    {
-        if (st != GG_OK) break;
-        gg_graphs_config x = stage2b;
-        x.warps = w;
-        st = try_cfg(x, &better);
-        if (better) bestc = x;
-    }
-    const gg_graphs_config stage3 = bestc;
+    const gg_graphs_config k2 = kbest;
     for (uint32_t ipt : {5u, 9u})
     {
         if (st != GG_OK) break;
-        gg_graphs_config x = stage3;
+        gg_graphs_config x = k2;
         x.ipt = ipt;
-        st = try_cfg(x, &better);
-        if (better) bestc = x;
+        st = stage(x);
     }
     if (st != GG_OK)
     {
         g->graphs_cfg = keep;
+        g->tuned = tuned_before;
         return st;
     }
-    g->graphs_cfg = bestc;
+    /* the kernel's best shape is kept even when the union pull wins */
+    g->graphs_cfg = kbest;
+    g->graphs_cfg.strategy = bestc.strategy;
+    g->tuned |= GG_TUNE_BATCH;
     c.family = GG_TUNE_BATCH;
-    c.params[0] = bestc.ipt;
-    c.params[1] = bestc.warps;
-    c.params[2] = bestc.smem_vmax;
-    c.params[3] = bestc.ctas;
+    c.params[0] = kbest.ipt;
+    c.params[1] = kbest.warps;
+    c.params[2] = kbest.smem_vmax;
+    c.params[3] = kbest.ctas;
+    c.params[4] = bestc.strategy;
     c.tuned_ms = best;
     c.candidates = n;
     return GG_OK;
@@ -411,7 +441,11 @@ gg_graphs_config gg_graphs_choice(gg_graph *g, uint32_t ngraphs)
     k.family = GG_TUNE_BATCH;
     k.storage = 0;
     k.glog = ilog2((double)ngraphs);
-    if (recall(k, p) && gg_pagerank_batch_config(g, p.v[0], p.v[1], p.v[2], p.v[3]) != GG_OK) gg_last_error();
+    if (recall(k, p))
+    {
+        if (gg_pagerank_batch_config(g, p.v[0], p.v[1], p.v[2], p.v[3]) != GG_OK) gg_last_error();
+        g->graphs_cfg.strategy = p.v[4];
+    }
     return g->graphs_cfg;
 }
 
@@ -457,7 +491,7 @@ extern "C" gg_status gg_autotune(gg_graph *g, const gg_tune_params *p, gg_tune_r
         kk.family = c.family;
         kk.storage = storage;
         if (c.family == GG_TUNE_BATCH) kk.glog = ilog2((double)p->ngraphs);
-        remember(kk, Pick{{c.params[0], c.params[1], c.params[2], c.params[3]}});
+        remember(kk, Pick{{c.params[0], c.params[1], c.params[2], c.params[3], c.params[4]}});
         g->tuned |= c.family;
     };
     if ((p->families & GG_TUNE_PR) && g->in_off)
@@ -500,10 +534,11 @@ extern "C" gg_status gg_tune_save(const char *path)
     FILE *f = fopen(path, "w");
     if (!f) return gg_fail(GG_ERR_INVALID, std::string("cannot write ") + path);
     std::lock_guard<std::mutex> lk(g_mu);
-    fprintf(f, "# family storage log2V log2deg log2skew sms log2graphs : p0 p1 p2 p3\n");
+    fprintf(f, "# family storage log2V log2deg log2skew sms log2graphs : p0 p1 p2 p3 p4\n");
     for (const auto &e : g_cache)
-        fprintf(f, "%u %u %u %u %u %u %u : %u %u %u %u\n", e.first.family, e.first.storage, e.first.vlog, e.first.dlog,
-                e.first.slog, e.first.sms, e.first.glog, e.second.v[0], e.second.v[1], e.second.v[2], e.second.v[3]);
+        fprintf(f, "%u %u %u %u %u %u %u : %u %u %u %u %u\n", e.first.family, e.first.storage, e.first.vlog,
+                e.first.dlog, e.first.slog, e.first.sms, e.first.glog, e.second.v[0], e.second.v[1], e.second.v[2],
+                e.second.v[3], e.second.v[4]);
     const bool ok = fclose(f) == 0;
     return ok ? GG_OK : gg_fail(GG_ERR_INVALID, std::string("cannot write ") + path);
 }
@@ -520,8 +555,8 @@ extern "C" gg_status gg_tune_load(const char *path)
         Key k{};
         Pick p{};
         if (line[0] == '#') continue;
-        if (sscanf(line, "%u %u %u %u %u %u %u : %u %u %u %u", &k.family, &k.storage, &k.vlog, &k.dlog, &k.slog,
-                   &k.sms, &k.glog, &p.v[0], &p.v[1], &p.v[2], &p.v[3]) == 11)
+        if (sscanf(line, "%u %u %u %u %u %u %u : %u %u %u %u %u", &k.family, &k.storage, &k.vlog, &k.dlog, &k.slog,
+                   &k.sms, &k.glog, &p.v[0], &p.v[1], &p.v[2], &p.v[3], &p.v[4]) == 12)
         {
             remember(k, p);
             n++;
@@ -541,7 +576,7 @@ extern "C" gg_status gg_tune_reset(void)
 extern "C" gg_status gg_tune_get(const gg_graph *g, uint32_t family, uint32_t *params)
 {
     if (!g || !params) return gg_fail(GG_ERR_INVALID, "NULL argument");
-    memset(params, 0, 4 * sizeof(uint32_t));
+    memset(params, 0, 5 * sizeof(uint32_t));
     switch (family)
     {
     case GG_TUNE_PR: params[0] = g->pr_shape.hot; params[1] = g->pr_shape.ctas; params[2] = g->pr_shape.hot_warps; break;
@@ -551,7 +586,7 @@ extern "C" gg_status gg_tune_get(const gg_graph *g, uint32_t family, uint32_t *p
     case GG_TUNE_PPR: params[0] = g->ppr_tile; break;
     case GG_TUNE_BATCH:
         params[0] = g->graphs_cfg.ipt; params[1] = g->graphs_cfg.warps; params[2] = g->graphs_cfg.smem_vmax;
-        params[3] = g->graphs_cfg.ctas; break;
+        params[3] = g->graphs_cfg.ctas; params[4] = g->graphs_cfg.strategy; break;
     default: return gg_fail(GG_ERR_INVALID, "unknown tuning family");
     }
     return GG_OK;

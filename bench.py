@@ -560,7 +560,7 @@ def batch_extras(gg, torch, peak, n=4096, iters=20):
     out = {"graphs": n, "vertices": V, "edges": E, "iterations": iters, "build_s": round(build_s, 1)}
     alg = pr_bytes(V, E, 4)
     runs = {}
-    dg.batch_config(7, 16, 4096, 2)
+    dg.batch_config(7, 16, 4096, 2, strategy=1)
     ms, r = timed()
     runs["many_graphs_kernel_default_shape"] = {
         "ms_per_run": ms, "gteps": E * iters / (ms / 1e3) / 1e9,

@@ -200,8 +200,10 @@ const float *gg_pagerank_device_ranks(const gg_graph *g);
  * from gg_pagerank_batch_iterations); the result carries the largest count,
  * the largest error_total and the active vertices of graphs that ran out.
  * The edges must stay inside their graph's range (GG_ERR_INVALID otherwise).
- * Other modes, or GG_PR_BATCH_UNION: the iterations of gg_pagerank over the
- * union, the stop rule and error_total over the union. */
+ * Other modes, GG_PR_BATCH_UNION, or the union strategy (large mean graph
+ * size by default, gg_pagerank_batch_strategy, gg_autotune): the iterations
+ * of gg_pagerank over the union, the stop rule and error_total over the
+ * union. */
 gg_status gg_pagerank_batch(gg_graph *g, const gg_pr_params *p, uint32_t ngraphs, const uint32_t *vertex_off,
                             float *ranks, gg_pr_result *r, void *stream);
 /* Per-graph iteration counts (the reference's convention) of the last
@@ -215,6 +217,10 @@ gg_status gg_pagerank_batch_iterations(const gg_graph *g, uint32_t ngraphs, uint
  * gg_autotune picks one per mapping. */
 gg_status gg_pagerank_batch_config(gg_graph *g, uint32_t ipt, uint32_t warps, uint32_t smem_vmax,
                                    uint32_t ctas_per_sm);
+/* Which FP32 pull gg_pagerank_batch runs on g: 0 by the batch's mean graph
+ * size (the many-graphs kernel up to 4096 vertices per graph, the union
+ * pull above; the default), 1 the many-graphs kernel, 2 the union pull. */
+gg_status gg_pagerank_batch_strategy(gg_graph *g, uint32_t strategy);
 
 /* ---- BFS -------------------------------------------------------------------- */
 
@@ -413,9 +419,10 @@ const float *gg_ppr_device_ranks(const gg_graph *g, uint32_t *stride);
  *                             CTAs per SM, or on with 16/24/32 warps
  *   GG_TUNE_BFS               top-down heavy-vertex threshold (32..1024)
  *   GG_TUNE_PPR               batched personalised PageRank tile (256/512/1024)
- *   GG_TUNE_BATCH             many-graphs kernel: shared-memory bin threshold,
- *                             CTAs per SM, warps per CTA, items per lane
- *                             (needs vertex_off)
+ *   GG_TUNE_BATCH             many graphs: the union pull or the many-graphs
+ *                             kernel, and the kernel's shape (CTAs per SM and
+ *                             warps, shared-memory bin threshold, items per
+ *                             lane; needs vertex_off)
  */
 #define GG_TUNE_PR 0x1u
 #define GG_TUNE_SPMV 0x2u
@@ -435,8 +442,9 @@ typedef struct gg_tune_params
 typedef struct gg_tune_choice
 {
     uint32_t family;      /* GG_TUNE_* */
-    uint32_t params[4];   /* PR/SPMV: hot (0/1), CTAs per SM, hot warps; BFS: threshold; PPR: tile;
-                             BATCH: items per lane, warps, bin threshold, CTAs per SM */
+    uint32_t params[5];   /* PR/SPMV: hot (0/1), CTAs per SM, hot warps; BFS: threshold; PPR: tile;
+                             BATCH: items per lane, warps, bin threshold, CTAs per SM, strategy
+                             (1 the many-graphs kernel, 2 the union pull) */
     float default_ms;     /* median time of the default shape */
     float tuned_ms;       /* median time of the pick */
     uint32_t candidates;  /* shapes timed */

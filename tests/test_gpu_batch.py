@@ -104,7 +104,7 @@ def test_many_graphs_kernel_per_graph_stop(gpu, orc, batch, cfg):
     resident CTAs per SM."""
     g, voff = batch
     dg = gpu.DeviceGraph(g, gpu.MAP_IN)
-    dg.batch_config(*cfg)
+    dg.batch_config(*cfg, strategy=1)
     ranks, res = dg.pagerank_batch(voff, iterations=20, epsilon=1e-4)
     its = dg.batch_iterations(len(SCALES))
     dg.free()
@@ -123,7 +123,9 @@ def test_many_graphs_kernel_matches_union_run(gpu, batch):
     many-graphs kernel and the union pull agree to FP32 rounding."""
     g, voff = batch
     dg = gpu.DeviceGraph(g, gpu.MAP_IN)
-    a, _ = dg.pagerank_batch(voff, iterations=20, epsilon=0.0)
+    dg.batch_config(strategy=1)
+    a, ra = dg.pagerank_batch(voff, iterations=20, epsilon=0.0)
+    assert ra["gather_launches"] == 1
     b, rb = dg.pagerank_batch(voff, iterations=20, epsilon=0.0, union=True)
     dg.free()
     assert rb["gather_launches"] == 20

@@ -65,7 +65,7 @@ def test_remembered_shapes_reach_new_mappings_and_files(gpu, tmp_path):
     gpu.tune_reset()
     c = gpu.DeviceGraph(g, gpu.MAP_IN)
     c.pagerank("pull", iterations=1, epsilon=0.0, copy_out=False)
-    assert c.tuned(gpu.TUNE_PR) == [2, 5, 32, 0]  # the default, nothing remembered
+    assert c.tuned(gpu.TUNE_PR) == [2, 5, 32, 0, 0]  # the default, nothing remembered
     gpu.tune_load(path)
     d = gpu.DeviceGraph(g, gpu.MAP_IN)
     d.pagerank("pull", iterations=1, epsilon=0.0, copy_out=False)
@@ -108,10 +108,10 @@ def test_batch_tuning_picks_a_valid_shape(gpu, orc):
     g, voff = gpu.Graph.rmat_batch(scales, edge_factor=8, seed0=77)
     dg = gpu.DeviceGraph(g, gpu.MAP_IN)
     picks = dg.autotune(gpu.TUNE_BATCH, reps=2, vertex_off=voff)
-    ipt, warps, vmax, ctas = picks["batch"]["params"]
-    assert ipt in (5, 7, 9) and warps in (8, 16, 32) and ctas in (1, 2, 3, 4)
+    ipt, warps, vmax, ctas, strategy = picks["batch"]["params"]
+    assert ipt in (5, 7, 9) and warps in (8, 16, 32) and ctas in (1, 2, 4) and strategy in (1, 2)
     assert picks["batch"]["tuned_ms"] <= picks["batch"]["default_ms"]
-    assert dg.tuned(gpu.TUNE_BATCH) == [ipt, warps, vmax, ctas]
+    assert dg.tuned(gpu.TUNE_BATCH) == [ipt, warps, vmax, ctas, strategy]
     ranks, _ = dg.pagerank_batch(voff, iterations=20, epsilon=0.0)
     for i, sc in enumerate(scales):
         o = orc.rmat_csr(sc, 8, seed=77 + i)
