@@ -105,9 +105,31 @@ struct PprArgs
     float damp;
 };
 
-/* rank and contribution of row r from its (two-vector) sum */
-/* RS: values per vertex row of cin / cout / rank / tele -- KP, or 64 when
- * only the first KP of wider rows are run (the server's continuous batch) */
+/* the stores of a row end in an iteration where some vectors write their
+ * ranks or retire (rare: kept out of line so the unrolled edge loop, which
+ * inlines the row end at every edge of a batch, stays small; inlined, it
+ * cost the K = 64 gather 20% on R-MAT-22) */
+template <class CT>
+__device__ __noinline__ void ppr_store_masked(CT *cout, float *rank, unsigned long long rank_mask,
+                                              unsigned long long zero_mask, size_t o, float r0, float r1, float c0,
+                                              float c1, uint32_t gl)
+{
+    const uint32_t zero = (uint32_t)(zero_mask >> (2 * gl)) & 3u;
+    if (zero & 1u) c0 = 0.0f;
+    if (zero & 2u) c1 = 0.0f;
+    PairIO<CT>::store(cout + o, c0, c1);
+    const uint32_t want = (uint32_t)(rank_mask >> (2 * gl)) & 3u;
+    if (want == 3u)
+        *reinterpret_cast<float2 *>(rank + o) = make_float2(r0, r1);
+    else if (want == 1u)
+        rank[o] = r0;
+    else if (want == 2u)
+        rank[o + 1] = r1;
+}
+
+/* rank and contribution of row r from its (two-vector) sum.  RS: values per
+ * vertex row of cin / cout / rank / tele -- KP, or 64 when only the first KP
+ * of wider rows are run (the server's continuous batch) */
 template <int KP, int RS, class CT>
 __device__ __forceinline__ void ppr_finish(const PprArgs<CT> &a, uint32_t r, float s0, float s1, uint32_t si,
                                            uint32_t deg, uint32_t gl)
@@ -126,18 +148,11 @@ __device__ __forceinline__ void ppr_finish(const PprArgs<CT> &a, uint32_t r, flo
         c0 = __fdiv_rn(r0, fd);
         c1 = __fdiv_rn(r1, fd);
     }
-    const uint32_t pair = (uint32_t)(a.zero_mask >> (2 * gl)) & 3u;
-    if (pair & 1u) c0 = 0.0f;
-    if (pair & 2u) c1 = 0.0f;
     const size_t o = (size_t)r * RS + 2 * gl;
-    PairIO<CT>::store(a.cout + o, c0, c1);
-    const uint32_t want = (uint32_t)(a.rank_mask >> (2 * gl)) & 3u;
-    if (want == 3u)
-        *reinterpret_cast<float2 *>(a.rank + o) = make_float2(r0, r1);
-    else if (want == 1u)
-        a.rank[o] = r0;
-    else if (want == 2u)
-        a.rank[o + 1] = r1;
+    if ((a.rank_mask | a.zero_mask) == 0ull)
+        PairIO<CT>::store(a.cout + o, c0, c1);
+    else
+        ppr_store_masked<CT>(a.cout, a.rank, a.rank_mask, a.zero_mask, o, r0, r1, c0, c1, gl);
 }
 
 template <int KP>

@@ -57,6 +57,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--leg", choices=["pr", "c1", "bfs", "ppr", "batch", "serve", "csr", "cc", "relabel"],
                    help="run one side measurement alone and print its JSON (for profiling)")
+    p.add_argument("--leg-scale", type=int, help="R-MAT scale of the --leg graph (small cases for profiling)")
     return p.parse_args()
 
 
@@ -243,25 +244,29 @@ class Replicas:
         return self.world * units_per_rank / (slowest_ms / 1e3)
 
 
-def run_leg(leg):
-    """One side measurement alone, its JSON on stdout."""
+def run_leg(leg, scale=None):
+    """One side measurement alone, its JSON on stdout; `scale` shrinks the
+    leg's R-MAT graph (for profiling captures on a small case)."""
     import torch
 
     import accelgraph_express_gb300 as gg
 
     gg.device_init(0)
     peak, _ = load_peaks()
+    kw = {} if scale is None else {"scale": scale}
+
     def pr():
-        g = gg.Graph.rmat(24, 16, seed=SEED)
+        g = gg.Graph.rmat(scale or 24, 16, seed=SEED)
         dg = gg.DeviceGraph(g, gg.MAP_IN)
         r = pr_storage_extras(gg, g, dg, g.V, g.E, torch.cuda.current_stream().cuda_stream, torch, peak)
         dg.free()
         return r
 
-    fn = {"pr": pr, "c1": lambda: c1_extras(gg, torch), "bfs": lambda: bfs_extras(gg, torch, peak),
-          "ppr": lambda: ppr_extras(gg, torch, peak), "batch": lambda: batch_extras(gg, torch, peak),
-          "serve": lambda: serving_extras(gg), "csr": lambda: csr_build_extras(gg, torch, peak),
-          "cc": lambda: cc_extras(gg, torch, peak), "relabel": lambda: relabel_extras(gg, torch, peak)}[leg]
+    fn = {"pr": pr, "c1": lambda: c1_extras(gg, torch, peak=peak, **kw),
+          "bfs": lambda: bfs_extras(gg, torch, peak, **kw), "ppr": lambda: ppr_extras(gg, torch, peak, **kw),
+          "batch": lambda: batch_extras(gg, torch, peak), "serve": lambda: serving_extras(gg, **kw),
+          "csr": lambda: csr_build_extras(gg, torch, peak, **kw), "cc": lambda: cc_extras(gg, torch, peak),
+          "relabel": lambda: relabel_extras(gg, torch, peak, **kw)}[leg]
     print(json.dumps({"leg": leg, **fn()}), flush=True)
 
 
@@ -272,7 +277,7 @@ def main():
         run_reference(a, world, rank)
         return
     if a.leg:
-        run_leg(a.leg)
+        run_leg(a.leg, a.leg_scale)
         return
 
     import numpy as np
@@ -461,7 +466,7 @@ def ppr_extras(gg, torch, peak, scale=22, K=64, iters=20):
     return out
 
 
-def c1_extras(gg, torch, scale=16):
+def c1_extras(gg, torch, scale=16, peak=6660.9):
     """The CPU-runnable configuration: PageRank pull on R-MAT-16 (65,536
     vertices, 1,048,576 edges), epsilon 1e-4, at most 20 iterations, in the
     reference's formulation (start 0.15, divide by V at the end) and with
@@ -499,14 +504,40 @@ def c1_extras(gg, torch, scale=16):
         t0 = time.perf_counter()
         O.pagerank(o, 0, 20, 1e-4, init_one_over_n=one_over_n, nthreads=os.cpu_count() or 1)
         cpu_ms = (time.perf_counter() - t0) * 1e3
+        alg = pr_bytes(V, E, 4) * info["executed"]
         out[name] = {"iterations": r["iterations"], "iterations_reference_loop": info["iterations"],
-                     "ms_per_call": ms, "gteps": E * (info["executed"]) / (ms / 1e3) / 1e9,
+                     "iterations_executed": info["executed"], "ms_per_call": ms,
+                     "gteps": E * (info["executed"]) / (ms / 1e3) / 1e9,
+                     "roofline": {"alg_bytes_per_call": alg, "achieved_gbs": alg / (ms / 1e3) / 1e9,
+                                  "frac": alg / (ms / 1e3) / 1e9 / peak,
+                                  "note": "R-MAT-16's 5.8 MB per iteration stays in L2; the call is launch-bound"},
                      "ms_per_call_stream_launches": timed[False],
                      "gteps_stream_launches": E * (info["executed"]) / (timed[False] / 1e3) / 1e9,
                      "l1_vs_fp64": float(np.abs(ranks - ex).sum()), "linf_vs_fp64": float(np.abs(ranks - ex).max()),
                      "l1_reference_fp32_loop_vs_fp64": float(np.abs(ref - ex).sum()),
                      "cpu_gteps": E * info["executed"] / (cpu_ms / 1e3) / 1e9}
     dg.free()
+    # end to end through the drop-in entry point on host arrays (upload,
+    # 20 iterations at epsilon 1e-4, ranks back), as a C caller makes it
+    import ctypes as C
+    gg.set_gpu_options(storage="f32", device=0, keep_resident=False, verbose=False)
+    args = gg.default_arguments(iterations=20, epsilon=1e-4)
+    L = gg.lib()
+    for _ in range(3):
+        L.freePageRankStats(L.pageRankGraphCSR(C.byref(args), g.ptr))
+    reps = 20
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        st = L.pageRankGraphCSR(C.byref(args), g.ptr)
+        if not st:
+            raise gg.GgError("pageRankGraphCSR failed")
+        its = st.contents.iterations
+        L.freePageRankStats(st)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / reps
+    executed = out["reference_formulation"]["iterations_executed"]
+    out["e2e"] = {"ms_per_call": e2e_ms, "gteps": E * executed / (e2e_ms / 1e3) / 1e9, "iterations": its,
+                  "h2d_bytes_per_call": 4 * V + 4 + 4 * E + 4 * V, "d2h_bytes_per_call": 4 * V,
+                  "call": "pageRankGraphCSR + freePageRankStats"}
     g.free()
     return out
 
@@ -975,7 +1006,7 @@ def extras(gg, graph, dg, V, E, sptr, torch, peak):
     from oracle import oracle_ctypes as O
 
     out = pr_storage_extras(gg, graph, dg, V, E, sptr, torch, peak)
-    out["c1_rmat16"] = c1_extras(gg, torch)
+    out["c1_rmat16"] = c1_extras(gg, torch, peak=peak)
     out.update(spmv_extras(gg, graph, V, E, sptr, torch, peak))
     dg.free()
     out["bfs_do"] = bfs_extras(gg, torch, peak)
