@@ -57,7 +57,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--leg", choices=["pr", "c1", "bfs", "ppr", "batch", "serve", "csr", "cc", "relabel"],
                    help="run one side measurement alone and print its JSON (for profiling)")
-    p.add_argument("--leg-scale", type=int, help="R-MAT scale of the --leg graph (small cases for profiling)")
+    p.add_argument("--leg-scale", type=int,
+                   help="R-MAT scale of the --leg graph, or the number of graphs of --leg batch (small cases for profiling)")
     return p.parse_args()
 
 
@@ -264,7 +265,7 @@ def run_leg(leg, scale=None):
 
     fn = {"pr": pr, "c1": lambda: c1_extras(gg, torch, peak=peak, **kw),
           "bfs": lambda: bfs_extras(gg, torch, peak, **kw), "ppr": lambda: ppr_extras(gg, torch, peak, **kw),
-          "batch": lambda: batch_extras(gg, torch, peak), "serve": lambda: serving_extras(gg, **kw),
+          "batch": lambda: batch_extras(gg, torch, peak, **({} if scale is None else {"n": scale})), "serve": lambda: serving_extras(gg, **kw),
           "csr": lambda: csr_build_extras(gg, torch, peak, **kw), "cc": lambda: cc_extras(gg, torch, peak),
           "relabel": lambda: relabel_extras(gg, torch, peak, **kw)}[leg]
     print(json.dumps({"leg": leg, **fn()}), flush=True)
