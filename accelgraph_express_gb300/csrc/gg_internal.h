@@ -58,9 +58,9 @@ struct gg_graphs_config
 {
     uint32_t ipt = 7, warps = 16, smem_vmax = 4096;
     uint32_t ctas = 2; /* resident CTAs per SM: the shared-memory carve-out holds just these, the rest is L1 */
-    /* 0: by mean graph size (the many-graphs kernel up to 4096 vertices per
-     * graph on average, the union pull above), 1: the many-graphs kernel,
-     * 2: the union pull */
+    /* without an epsilon stop: 0 the union pull (default), 1 the
+     * many-graphs kernel, 2 the union pull (tuned); with one, always the
+     * many-graphs kernel */
     uint32_t strategy = 0;
 };
 

@@ -55,8 +55,11 @@ struct GraphsArgs
 };
 
 /* the in-neighbour's contribution: shared memory for small graphs, global
- * (plain loads: the values are rewritten inside the launch) otherwise;
- * `base` is offset by the graph's first vertex so it takes union ids */
+ * (plain loads: the values are rewritten inside the launch, by the same
+ * CTA) otherwise; `base` is offset by the graph's first vertex so it takes
+ * union ids.  One engine instance serves both through a generic pointer: a
+ * second instance for the global case made the kernel spill at its 64
+ * registers. */
 struct GraphsGather
 {
     typedef float Acc;
@@ -65,6 +68,89 @@ struct GraphsGather
     __device__ __forceinline__ Raw load(uint32_t, uint32_t u) const { return base[u]; }
     __device__ __forceinline__ Acc value(const Raw &r) const { return r; }
 };
+
+/* every iteration of one graph (vertices vb .. vb + Vg) by the whole CTA:
+ * the gather into sm, a CTA barrier, the vertex pass (two vertices per
+ * thread per step... 's residual and
+ * active count; returns the reference's iteration count */
+template <int IPT>
+__device__ __forceinline__ uint32_t graph_iterations(const GraphsArgs &a, unsigned char *stage, float *c, float *sm,
+                                                     uint32_t vb, uint32_t Vg, uint32_t cb, uint32_t ntiles,
+                                                     float base, double *err_out, uint32_t *act_out)
+{
+    typedef PullStage<IPT, float> S;
+    __shared__ double s_err[32];
+    __shared__ uint32_t s_act[32];
+    const uint32_t warps = blockDim.x >> 5, w = threadIdx.x >> 5;
+    uint32_t it = 0, act = 0;
+    double err = 0.0;
+    for (; it < a.iterations; it++)
+    {
+        warp_pull_sums_core<IPT>(reinterpret_cast<uint32_t *>(stage), reinterpret_cast<float *>(stage + S::OFF_BYTES),
+                                 reinterpret_cast<float *>(stage + S::OFF_BYTES + S::VAL_BYTES), w, warps, a.off,
+                                 a.adj, a.V, a.coord + cb, ntiles, sm - vb, GraphsGather{c - vb});
+        __syncthreads();
+        double e_sum = 0.0;
+        uint32_t n_act = 0;
+        constexpr uint32_t U = 2; /* measured: 4 was slower, and spills at IPT 9 */
+        for (uint32_t v0 = threadIdx.x; v0 < Vg; v0 += U * blockDim.x)
+        {
+            float sv[U], pr[U];
+            uint32_t dg[U];
+#pragma unroll
+            for (uint32_t k = 0; k < U; k++)
+            {
+                const uint32_t v = v0 + k * blockDim.x;
+                if (v < Vg)
+                {
+                    sv[k] = sm[v];
+                    pr[k] = a.rank[vb + v];
+                    dg[k] = __ldg(a.outdeg + vb + v);
+                }
+            }
+#pragma unroll
+            for (uint32_t k = 0; k < U; k++)
+            {
+                const uint32_t v = v0 + k * blockDim.x;
+                if (v < Vg)
+                {
+                    sm[v] = 0.0f;
+                    const float nr = __fadd_rn(base, __fmul_rn(a.damp, sv[k]));
+                    a.rank[vb + v] = nr;
+                    const float e = fabsf(__fsub_rn(nr, pr[k]));
+                    e_sum += (double)e;
+                    n_act += e >= a.eps_f ? 1u : 0u;
+                    c[v] = contrib_of_f(nr, dg[k]);
+                }
+            }
+        }
+        /* CTA sums of the residual and the active count */
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            e_sum += __shfl_down_sync(0xffffffffu, e_sum, o);
+            n_act += __shfl_down_sync(0xffffffffu, n_act, o);
+        }
+        if ((threadIdx.x & 31) == 0)
+        {
+            s_err[w] = e_sum;
+            s_act[w] = n_act;
+        }
+        __syncthreads();
+        err = 0.0;
+        act = 0;
+        for (uint32_t k = 0; k < warps; k++)
+        {
+            err += s_err[k];
+            act += s_act[k];
+        }
+        __syncthreads();
+        if (act == 0) break; /* pageRank.c:1073: the reference stops here */
+    }
+    *err_out = err;
+    *act_out = act;
+    return it < a.iterations ? it : a.iterations;
+}
 
 template <int IPT>
 __global__ void __launch_bounds__(1024, 1) k_pr_graphs(GraphsArgs a)
@@ -76,8 +162,6 @@ __global__ void __launch_bounds__(1024, 1) k_pr_graphs(GraphsArgs a)
     float *s_c = reinterpret_cast<float *>(gg_dyn + (size_t)warps * S::BYTES);
     float *s_sum = s_c + a.smem_vmax;
     __shared__ uint32_t s_g;
-    __shared__ double s_err[32];
-    __shared__ uint32_t s_act[32];
     for (;;)
     {
         if (threadIdx.x == 0) s_g = atomicAdd(a.counter, 1u);
@@ -102,59 +186,16 @@ __global__ void __launch_bounds__(1024, 1) k_pr_graphs(GraphsArgs a)
             sm[v] = 0.0f;
         }
         __syncthreads();
-        uint32_t it = 0, act = 0;
         double err = 0.0;
-        for (; it < a.iterations; it++)
-        {
-            warp_pull_sums_core<IPT>(reinterpret_cast<uint32_t *>(stage),
-                                     reinterpret_cast<float *>(stage + S::OFF_BYTES),
-                                     reinterpret_cast<float *>(stage + S::OFF_BYTES + S::VAL_BYTES), w, warps, a.off,
-                                     a.adj, a.V, a.coord + cb, ntiles, sm - vb, GraphsGather{c - vb});
-            __syncthreads();
-            double e_sum = 0.0;
-            uint32_t n_act = 0;
-            for (uint32_t v = threadIdx.x; v < Vg; v += blockDim.x)
-            {
-                const float s = sm[v];
-                sm[v] = 0.0f;
-                const float pr = a.rank[vb + v];
-                const float nr = __fadd_rn(base, __fmul_rn(a.damp, s));
-                a.rank[vb + v] = nr;
-                const float e = fabsf(__fsub_rn(nr, pr));
-                e_sum += (double)e;
-                n_act += e >= a.eps_f ? 1u : 0u;
-                c[v] = contrib_of_f(nr, a.outdeg[vb + v]);
-            }
-            /* CTA sums of the residual and the active count */
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-            {
-                e_sum += __shfl_down_sync(0xffffffffu, e_sum, o);
-                n_act += __shfl_down_sync(0xffffffffu, n_act, o);
-            }
-            if ((threadIdx.x & 31) == 0)
-            {
-                s_err[w] = e_sum;
-                s_act[w] = n_act;
-            }
-            __syncthreads();
-            err = 0.0;
-            act = 0;
-            for (uint32_t k = 0; k < warps; k++)
-            {
-                err += s_err[k];
-                act += s_act[k];
-            }
-            __syncthreads();
-            if (act == 0) break; /* pageRank.c:1073: the reference stops here */
-        }
+        uint32_t act = 0, its;
+        its = graph_iterations<IPT>(a, stage, c, sm, vb, Vg, cb, ntiles, base, &err, &act);
         /* pageRank.c:1080-1085 */
         if (!a.one_over_n)
             for (uint32_t v = threadIdx.x; v < Vg; v += blockDim.x)
                 a.rank[vb + v] = __fdiv_rn(a.rank[vb + v], fV);
         if (threadIdx.x == 0)
         {
-            a.iters_out[gi] = it < a.iterations ? it : a.iterations;
+            a.iters_out[gi] = its;
             a.active_out[gi] = act;
             a.err_out[gi] = Vg ? err / (double)Vg : 0.0;
         }

@@ -1117,9 +1117,13 @@ gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_
     if (ngraphs && p->mode == GG_PR_PULL && p->storage == GG_STORE_F32 && !(p->flags & GG_PR_BATCH_UNION))
     {
         if (!g->in_off || !g->out_deg) return gg_fail(GG_ERR_INVALID, "pull PageRank needs GG_MAP_IN");
+        /* an epsilon stop needs the many-graphs kernel (every graph stops on
+         * its own; the union stops when all have converged); without one
+         * every graph runs all iterations either way and the strategy
+         * decides: the union pull by default (faster on every R-MAT mix
+         * measured), the many-graphs kernel when set or tuned so */
         const gg_graphs_config cfg = gg_graphs_choice(g, ngraphs);
-        const bool per_graph = cfg.strategy == 1 || (cfg.strategy == 0 && g->V <= 4096ull * ngraphs);
-        if (per_graph) return graphs_impl(g, p, ranks, r, stream, ngraphs, h_voff);
+        if (p->epsilon > 0.0 || cfg.strategy == 1) return graphs_impl(g, p, ranks, r, stream, ngraphs, h_voff);
     }
     const int pull = !(p->mode == GG_PR_PUSH || p->mode == GG_PR_PUSH_FX64 || p->mode == GG_PR_PUSH_Q ||
                        p->mode == GG_PR_DD_PUSH || p->mode == GG_PR_DD_PULLPUSH);

@@ -21,9 +21,10 @@
  *             time of eight searches from fixed sources;
  *   PPR       merge items per tile of the batched personalised PageRank
  *             (256, 512, 1024); measured: one K = 64 run of 5 iterations;
- *   BATCH     the union pull against the many-graphs kernel, and the
+ *   BATCH     (runs without an epsilon stop) the union pull against the
+ *             many-graphs kernel, and the
  *             kernel's shape: resident CTAs per SM x warps per CTA (2 x 16,
- *             1 x 32, 1 x 16, 2 x 8, 4 x 8), then the bin threshold (0, 1024,
+ *             1 x 32, 1 x 16, 2 x 8, 4 x 8, 8 x 4), then the bin threshold (0, 1024,
  *             4096, 8192 vertices in shared memory), then items per lane (5,
  *             7, 9), each stage keeping the best of the one before
  *             (coordinate descent); measured: one run of the batch.
@@ -352,17 +353,17 @@ gg_status tune_batch(gg_graph *g, uint32_t ngraphs, const uint32_t *voff, uint32
         }
         return GG_OK;
     };
-    /* the default first: the rule by mean graph size */
+    /* the default first: the union pull; then the kernel's default shape */
     gg_graphs_config dflt;
-    dflt.strategy = g->V <= 4096ull * ngraphs ? 1u : 2u;
+    dflt.strategy = 2;
     gg_status st = consider(dflt);
     gg_graphs_config other = dflt;
-    other.strategy = dflt.strategy == 1 ? 2u : 1u;
+    other.strategy = 1;
     if (st == GG_OK) st = consider(other);
     /* the kernel's shape: CTAs x warps, then the bin, then items per lane */
     gg_graphs_config base;
     base.strategy = 1;
-    const uint32_t shapes[][2] = {{2, 16}, {1, 32}, {1, 16}, {2, 8}, {4, 8}};
+    const uint32_t shapes[][2] = {{2, 16}, {1, 32}, {1, 16}, {2, 8}, {4, 8}, {8, 4}};
     gg_graphs_config kbest = base;
     float kms = INFINITY;
     auto stage = [&](const gg_graphs_config &x) -> gg_status {

@@ -193,17 +193,18 @@ const float *gg_pagerank_device_ranks(const gg_graph *g);
  * entries, from 0 to V; no counterpart in the reference), every graph
  * ranked as if alone (each vertex divided by its own graph's vertex count).
  * The reference formulation only (init_one_over_n = 0).
- * FP32 pull: the many-graphs kernel, one launch for every graph and every
- * iteration; one CTA per graph (largest first), small graphs' contributions
- * in shared memory (gg_pagerank_batch_config / gg_autotune pick the bin
- * threshold and tile shape); every graph stops on its own (iteration counts
- * from gg_pagerank_batch_iterations); the result carries the largest count,
- * the largest error_total and the active vertices of graphs that ran out.
- * The edges must stay inside their graph's range (GG_ERR_INVALID otherwise).
- * Other modes, GG_PR_BATCH_UNION, or the union strategy (large mean graph
- * size by default, gg_pagerank_batch_strategy, gg_autotune): the iterations
- * of gg_pagerank over the union, the stop rule and error_total over the
- * union. */
+ * FP32 pull with an epsilon stop, or with the many-graphs strategy
+ * (gg_pagerank_batch_strategy, gg_autotune): the many-graphs kernel, one
+ * launch for every graph and every iteration; one CTA per graph (largest
+ * first), small graphs' contributions in shared memory
+ * (gg_pagerank_batch_config / gg_autotune pick the bin threshold and tile
+ * shape); every graph stops on its own (iteration counts from
+ * gg_pagerank_batch_iterations); the result carries the largest count, the
+ * largest error_total and the active vertices of graphs that ran out.  The
+ * edges must stay inside their graph's range (GG_ERR_INVALID otherwise).
+ * Otherwise (other modes, GG_PR_BATCH_UNION, FP32 without an epsilon stop
+ * by default): the iterations of gg_pagerank over the union, the stop rule
+ * and error_total over the union. */
 gg_status gg_pagerank_batch(gg_graph *g, const gg_pr_params *p, uint32_t ngraphs, const uint32_t *vertex_off,
                             float *ranks, gg_pr_result *r, void *stream);
 /* Per-graph iteration counts (the reference's convention) of the last
@@ -217,9 +218,11 @@ gg_status gg_pagerank_batch_iterations(const gg_graph *g, uint32_t ngraphs, uint
  * gg_autotune picks one per mapping. */
 gg_status gg_pagerank_batch_config(gg_graph *g, uint32_t ipt, uint32_t warps, uint32_t smem_vmax,
                                    uint32_t ctas_per_sm);
-/* Which FP32 pull gg_pagerank_batch runs on g: 0 by the batch's mean graph
- * size (the many-graphs kernel up to 4096 vertices per graph, the union
- * pull above; the default), 1 the many-graphs kernel, 2 the union pull. */
+/* Which FP32 pull gg_pagerank_batch runs on g when epsilon is 0 (every
+ * graph runs all iterations either way): 0 the union pull (the default;
+ * measured faster on R-MAT mixes), 1 the many-graphs kernel, 2 the union
+ * pull.  With an epsilon stop the many-graphs kernel always runs, so that
+ * every graph stops on its own. */
 gg_status gg_pagerank_batch_strategy(gg_graph *g, uint32_t strategy);
 
 /* ---- BFS -------------------------------------------------------------------- */

@@ -109,7 +109,7 @@ def test_batch_tuning_picks_a_valid_shape(gpu, orc):
     dg = gpu.DeviceGraph(g, gpu.MAP_IN)
     picks = dg.autotune(gpu.TUNE_BATCH, reps=2, vertex_off=voff)
     ipt, warps, vmax, ctas, strategy = picks["batch"]["params"]
-    assert ipt in (5, 7, 9) and warps in (8, 16, 32) and ctas in (1, 2, 4) and strategy in (1, 2)
+    assert ipt in (5, 7, 9) and warps in (4, 8, 16, 32) and ctas in (1, 2, 4, 8) and strategy in (1, 2)
     assert picks["batch"]["tuned_ms"] <= picks["batch"]["default_ms"]
     assert dg.tuned(gpu.TUNE_BATCH) == [ipt, warps, vmax, ctas, strategy]
     ranks, _ = dg.pagerank_batch(voff, iterations=20, epsilon=0.0)
