@@ -427,7 +427,8 @@ def ppr_extras(gg, torch, peak, scale=22, K=64, iters=20):
     """Batched personalised PageRank: K one-hot seed vectors (SplitMix64 from
     vertices with out-edges) over a directed R-MAT graph, one multi-vector
     pull gather per iteration; aggregate GTEPS = K*E*iters/t, roofline
-    against 4E + 8V + K*V*4s bytes per iteration, L1 vs FP64 for 4 vectors."""
+    against 4E + 8V + K*V*4s bytes per iteration, L1 vs FP64 for 4 vectors;
+    the CPU baseline runs the same vectors in FP32 on the host cores."""
     import numpy as np
     from oracle import oracle_ctypes as O
 
@@ -462,6 +463,14 @@ def ppr_extras(gg, torch, peak, scale=22, K=64, iters=20):
                         "gather_launch_ms": gms / reps,
                         "iteration_hbm_frac": alg / (ms / iters / 1e3) / 1e9 / peak,
                         "alg_bytes_per_iteration": alg, "l1_vs_fp64_max": l1}
+    # CPU baseline: the same K vectors in FP32, [V][K] rows, OpenMP over
+    # destination vertices on every host core; a bounded sample of 2 iterations
+    cpu_iters = 2
+    t0 = time.perf_counter()
+    O.ppr_f32_batch(o, sets, cpu_iters, float(np.float32(0.85)))
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"gteps": K * E * cpu_iters / cpu_s / 1e9, "cores": os.cpu_count(), "kind": "port",
+                           "sample": f"all {K} vectors, {cpu_iters} of the {iters} iterations, FP32"}
     dg.free()
     g.free()
     return out
@@ -643,7 +652,9 @@ def serving_extras(gg, scale=23, n=1500, rate=150.0):
     out-edges, on a directed R-MAT graph with CSR and CSC resident.  Reports
     latency percentiles (server clock, submit to result in device memory),
     throughput, PPR batch sizes, and checks sampled queries: PPR bit-identical
-    alone and within L1 1e-6 of FP64, BFS distances exact."""
+    alone and within L1 1e-6 of FP64, BFS distances exact.  The CPU baseline
+    is the per-query time of the same queries on the host cores, and the
+    query rate that implies for this mix."""
     import threading
     import numpy as np
     from oracle import oracle_ctypes as O
@@ -710,6 +721,19 @@ def serving_extras(gg, scale=23, n=1500, rate=150.0):
     srv.stop()
     dg.free()
     g.free()
+    # CPU baseline: three sampled PPR queries (FP32, 20 iterations) and three
+    # sampled BFS queries, each run alone on every host core
+    cpu = {"ppr": [], "bfs": []}
+    for i in sorted(sample):
+        kind, arg = qs[i]
+        if len(cpu[kind]) >= 3:
+            continue
+        t0 = time.perf_counter()
+        if kind == "ppr":
+            O.ppr_f32_batch(o, [list(arg)], 20, float(np.float32(0.85)))
+        else:
+            O.bfs(o, 2, arg, nthreads=os.cpu_count())
+        cpu[kind].append((time.perf_counter() - t0) * 1e3)
     lat = np.array([(x["done_s"] - x["submit_s"]) * 1e3 for x in infos])
     kinds = np.array([x["kind"] for x in infos])
     span = max(x["done_s"] for x in infos) - min(x["submit_s"] for x in infos)
@@ -719,6 +743,11 @@ def serving_extras(gg, scale=23, n=1500, rate=150.0):
            "alone_equals_mixed": alone_ok, "sampled_results_match_oracle": acc_ok,
            "sampled": len(sample), "ppr_checked_vs_fp64": l1_checked, "ppr_l1_vs_fp64_max": l1_max,
            "all_ok": all(x["status"] == 0 for x in infos)}
+    cp, cb = statistics.mean(cpu["ppr"] or [0.0]), statistics.mean(cpu["bfs"] or [0.0])
+    out["cpu_baseline"] = {"ppr_ms_per_query": cp, "bfs_ms_per_query": cb,
+                           "qps_capacity": 1e3 / (0.7 * cp + 0.3 * cb) if cp + cb > 0 else None,
+                           "cores": os.cpu_count(), "kind": "port",
+                           "sample": "3 sampled PPR and 3 sampled BFS queries, one at a time on all host cores"}
     for k, name in ((0, "ppr"), (1, "bfs")):
         sel = lat[kinds == k]
         if len(sel):

@@ -705,6 +705,61 @@ void orc_ppr_f64(const orc_csr *g, uint32_t seed, uint32_t iterations, double da
     orc_ppr_f64_multi(g, &seed, 1, iterations, damp, ranks);
 }
 
+/* K personalised PageRank vectors advanced together, FP32, the CPU timing
+ * baseline of the batched GPU form: ranks and contributions vertex-major
+ * ([V][K], one row of K values per vertex, so every in-edge reads one
+ * contiguous row), the per-vector arithmetic of orc_ppr_f64_multi in float
+ * (contribution = rank / outdeg, rank' = tele + damp * sum).  init[v*K + k]
+ * is vector k's starting rank (c_k(v)/|S_k|); the teleport is
+ * (1 - damp) * init.  OpenMP over destination vertices, nthreads threads
+ * (0: all). */
+void orc_ppr_f32_batch(const orc_csr *g, uint32_t K, const float *init, uint32_t iterations, float damp,
+                       int nthreads, float *ranks)
+{
+    const uint32_t V = g->V;
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+    float *contrib = (float *)malloc(((size_t)V * K + 1) * sizeof(float));
+    float *tele = (float *)malloc(((size_t)V * K + 1) * sizeof(float));
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (uint32_t v = 0; v < V; v++)
+        for (uint32_t k = 0; k < K; k++)
+        {
+            const size_t i = (size_t)v * K + k;
+            tele[i] = (1.0f - damp) * init[i];
+            ranks[i] = init[i];
+        }
+    for (uint32_t it = 0; it < iterations; it++)
+    {
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+        for (uint32_t v = 0; v < V; v++)
+        {
+            const uint32_t d = out_degree(g, v);
+            const float fd = (float)d;
+            for (uint32_t k = 0; k < K; k++)
+                contrib[(size_t)v * K + k] = d ? ranks[(size_t)v * K + k] / fd : 0.0f;
+        }
+#pragma omp parallel num_threads(nthreads)
+        {
+            float *s = (float *)malloc((size_t)K * sizeof(float));
+#pragma omp for schedule(dynamic, 1024)
+            for (uint32_t v = 0; v < V; v++)
+            {
+                for (uint32_t k = 0; k < K; k++) s[k] = 0.0f;
+                for (uint32_t j = g->in_off[v]; j < g->in_off[v + 1]; j++)
+                {
+                    const float *row = contrib + (size_t)g->in_adj[j] * K;
+                    for (uint32_t k = 0; k < K; k++) s[k] += row[k];
+                }
+                for (uint32_t k = 0; k < K; k++)
+                    ranks[(size_t)v * K + k] = tele[(size_t)v * K + k] + damp * s[k];
+            }
+            free(s);
+        }
+    }
+    free(tele);
+    free(contrib);
+}
+
 /* ------------------------------------------------------------------------ */
 /* BFS                                                                       */
 /* ------------------------------------------------------------------------ */

@@ -115,6 +115,11 @@ void orc_ppr_f64(const orc_csr *g, uint32_t seed, uint32_t iterations, double da
  * of the initial rank and of the (1-d) teleport. */
 void orc_ppr_f64_multi(const orc_csr *g, const uint32_t *seeds, uint32_t nseeds, uint32_t iterations, double damp,
                        double *ranks);
+/* K vectors together in FP32 ([V][K] rows; init[v*K + k] = vector k's
+ * starting rank, teleport (1-d) init), OpenMP over vertices (nthreads, 0:
+ * all): the CPU timing baseline of the batched GPU form. */
+void orc_ppr_f32_batch(const orc_csr *g, uint32_t K, const float *init, uint32_t iterations, float damp,
+                       int nthreads, float *ranks);
 
 /* ---- BFS ---------------------------------------------------------------- */
 

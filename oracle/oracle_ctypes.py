@@ -68,6 +68,7 @@ def lib():
         L.orc_pagerank_f64.argtypes = [C.POINTER(OrcCsr), C.c_uint32, C.c_int, f64p]
         L.orc_ppr_f64.argtypes = [C.POINTER(OrcCsr), C.c_uint32, C.c_uint32, C.c_double, f64p]
         L.orc_ppr_f64_multi.argtypes = [C.POINTER(OrcCsr), u32p, C.c_uint32, C.c_uint32, C.c_double, f64p]
+        L.orc_ppr_f32_batch.argtypes = [C.POINTER(OrcCsr), C.c_uint32, f32p, C.c_uint32, C.c_float, C.c_int, f32p]
         L.orc_bfs.argtypes = [C.POINTER(OrcCsr), C.c_int, C.c_int, i32p, u32p, C.POINTER(OrcBfsOut), C.c_int]
         L.orc_spmv.argtypes = [C.POINTER(OrcCsr), C.c_int, C.c_uint32, C.c_void_p, f32p, f32p,
                                C.POINTER(C.c_double), C.c_int]
@@ -233,6 +234,20 @@ def ppr_f64_multi(g: Csr, seeds, iterations, damp=0.85):
     r = np.empty(g.V, np.float64)
     cs = g.c()
     lib().orc_ppr_f64_multi(C.byref(cs), s, len(s), iterations, damp, r)
+    return r
+
+
+def ppr_f32_batch(g: Csr, sets, iterations, damp=0.85, nthreads=0):
+    """K seed sets advanced together in FP32 on the host cores ([V][K])."""
+    K = len(sets)
+    share = np.zeros((g.V, K), np.float64)
+    for k, s in enumerate(sets):
+        for v in s:
+            share[v, k] += 1.0 / len(s)
+    init = share.astype(np.float32)
+    r = np.empty((g.V, K), np.float32)
+    cs = g.c()
+    lib().orc_ppr_f32_batch(C.byref(cs), K, init, iterations, damp, nthreads, r)
     return r
 
 

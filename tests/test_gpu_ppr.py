@@ -79,9 +79,17 @@ def test_ppr_bf16_bound(gpu, orc, rg):
     ex = oracle_vectors(orc, o, sets)
     l1 = np.abs(ranks - ex).sum(0)
     mass = np.abs(ex).sum(0)
-    # BF16 keeps 8 significant bits per stored contribution (relative step
-    # 2^-8), summed in FP32: a vector's L1 error stays below 1% of its mass
-    assert (l1 <= 1e-2 * np.maximum(mass, 1e-30)).all(), (l1 / np.maximum(mass, 1e-30)).max()
+    # BF16 keeps 8 significant bits per stored contribution (rounding error
+    # up to 2^-9 relative), summed in FP32.  Each iteration's rounding is
+    # contracted by d per later iteration, so the error settles near
+    # 2^-9 / (1 - d) times the mass with random signs: a numpy restatement
+    # of this storage over 320 seed sets drawn as here on R-MAT-13 gives at
+    # most 4.1e-3 of a vector's mass (a small set concentrates its mass on
+    # few rows), and R-MAT-22 measures 3.0e-3.  Bound: 8e-3.  (Storing
+    # BF16 deltas with an FP32 stored-so-far value -- the PageRank correction
+    # pass -- only reaches ~1e-4 here: a PPR vector's change per iteration
+    # decays like d^t, so every iteration's rounding weighs the same.)
+    assert (l1 <= 8e-3 * np.maximum(mass, 1e-30)).all(), (l1 / np.maximum(mass, 1e-30)).max()
 
 
 def test_ppr_hub_rows_span_tiles(gpu, orc, hub):
