@@ -231,6 +231,23 @@ def tune_reset():
     _check(lib().gg_tune_reset(), "gg_tune_reset")
 
 
+HOST_COPY = {"auto": 0, "staged": 1, "driver": 2, "device": 3}
+
+
+def set_host_copy_mode(mode):
+    """How pageable host arrays are copied to the device (gg_set_host_copy_mode)."""
+    lib().gg_set_host_copy_mode(HOST_COPY[mode] if isinstance(mode, str) else int(mode))
+
+
+def device_cache_trim():
+    """Hand the library's cached device blocks back to CUDA."""
+    lib().gg_device_cache_trim()
+
+
+def device_cache_bytes():
+    return int(lib().gg_device_cache_bytes())
+
+
 class GgError(RuntimeError):
     pass
 
@@ -250,6 +267,10 @@ def lib() -> C.CDLL:
         L.gg_graph_unmap.argtypes = [C.c_void_p]
         L.gg_graph_device_bytes.argtypes = [C.c_void_p]
         L.gg_graph_device_bytes.restype = C.c_size_t
+        L.gg_device_cache_trim.argtypes = []
+        L.gg_device_cache_trim.restype = None
+        L.gg_device_cache_bytes.argtypes = []
+        L.gg_device_cache_bytes.restype = C.c_size_t
         L.gg_pagerank.argtypes = [C.c_void_p, P(PrParams), C.c_void_p, P(PrResult), C.c_void_p]
         L.gg_pagerank_device_ranks.argtypes = [C.c_void_p]
         L.gg_pagerank_device_ranks.restype = C.c_void_p
@@ -258,6 +279,9 @@ def lib() -> C.CDLL:
                               C.c_void_p]
         L.gg_set_wait_timeout_ms.argtypes = [C.c_uint32]
         L.gg_set_barrier_limit_us.argtypes = [C.c_uint32]
+        L.gg_set_host_copy_mode.argtypes = [C.c_uint32]
+        L.gg_set_host_copy_mode.restype = None
+        L.gg_host_copy_mode.restype = C.c_uint32
         L.gg_pagerank_batch_iterations.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
         L.gg_autotune.argtypes = [C.c_void_p, P(TuneParams), P(TuneResult), C.c_void_p]
         L.gg_tune_save.argtypes = [C.c_char_p]
@@ -323,6 +347,8 @@ def lib() -> C.CDLL:
                      "pageRankDataDrivenPushGraphCSR", "pageRankDataDrivenPullPushGraphCSR"]:
             getattr(L, name).argtypes = [P(Arguments), P(GraphCSR)]
             getattr(L, name).restype = P(PageRankStats)
+        L.newPageRankStatsGraphCSR.argtypes = [P(GraphCSR)]
+        L.newPageRankStatsGraphCSR.restype = P(PageRankStats)
         for name in ["breadthFirstSearchGraphCSR", "breadthFirstSearchPullGraphCSR",
                      "breadthFirstSearchPushGraphCSR", "breadthFirstSearchDirectionOptimizedGraphCSR",
                      "breadthFirstSearchPushBitmapGraphCSR",

@@ -204,12 +204,22 @@ struct GgRange
     GgRange(const GgRange &) = delete;
     GgRange &operator=(const GgRange &) = delete;
 };
-/* host -> device copy; pageable sources go through page-locked staging
- * filled by all host threads (returns with the copy queued on s) */
+/* host -> device copy (returns with the copy queued on s; the source must
+ * stay valid until s reaches it); pageable sources are read by a kernel
+ * where the device uses the host page tables, else go through page-locked
+ * staging filled by all host threads */
 gg_status gg_copy_h2d(void *dst, const void *src, size_t bytes, cudaStream_t s);
 /* device -> host copy, complete on return (waits for s); pageable
- * destinations are filled from page-locked staging by all host threads */
+ * destinations are written by the driver's copy where the device uses the
+ * host page tables, else filled from page-locked staging by all host
+ * threads */
 gg_status gg_copy_d2h(void *dst, const void *src, size_t bytes, cudaStream_t s);
+/* make a pageable destination of a coming device -> host copy resident (one
+ * store per page on all host threads; its contents become undefined), so
+ * the copy runs at the DMA rate; called while the device still computes the
+ * data, it overlaps that work.  A no-op for page-locked memory, below 4 MB,
+ * and where the device does not use the host page tables. */
+void gg_host_dst_prepare(void *dst, size_t bytes);
 /* tiles of the CSC (in = 1) or CSR (in = 0), computed on first use */
 gg_status gg_tiles_get(gg_graph *g, int in, cudaStream_t s, gg_tiles **out);
 /* bf16 (storage 1) / f16 (storage 2) copy of the in- or out-edge weights */

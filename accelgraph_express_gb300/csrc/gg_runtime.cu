@@ -11,6 +11,7 @@
 #include <cuda_fp16.h>
 
 #include <omp.h>
+#include <unistd.h>
 
 #include <atomic>
 #include <cmath>
@@ -21,6 +22,8 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <unordered_map>
+#include <vector>
 
 #include "gg_internal.h"
 
@@ -198,28 +201,161 @@ extern "C" gg_status gg_device_init(int device)
     return GG_OK;
 }
 
+/* ---- device memory ------------------------------------------------------
+ * Blocks the library frees are kept for reuse.  A mapping made and dropped
+ * on every call (the drop-in entry points on a host graph) would otherwise
+ * pay cudaMalloc and cudaFree for each of its arrays every time, about 1 ms
+ * per GB-sized array on this system.  A block enters the cache once the
+ * device is idle, the same point cudaFree's implicit synchronisation waited
+ * for, so no queued kernel can still read it when it is handed out again.
+ * A request takes the smallest cached block of its device that is at least
+ * as large and at most 1/8 larger.  The cache holds at most
+ * GG_DEVICE_CACHE_MB (default 16384) MB; the oldest blocks leave first.  An
+ * allocation that fails empties it and tries again, and
+ * gg_device_cache_trim() empties it on request. */
+namespace {
+struct CachedBlock
+{
+    void *ptr;
+    size_t bytes;
+    int device;
+    uint64_t seq;
+};
+std::mutex g_cache_mu;
+std::vector<CachedBlock> g_cache;
+std::unordered_map<void *, size_t> g_live; /* block -> its allocated size */
+size_t g_cache_bytes = 0;
+uint64_t g_cache_seq = 0;
+
+size_t cache_limit()
+{
+    static const size_t v = [] {
+        const char *e = getenv("GG_DEVICE_CACHE_MB");
+        return (size_t)(e ? strtoull(e, nullptr, 10) : 16384ull) << 20;
+    }();
+    return v;
+}
+
+/* the block of the cache's oldest entry leaves it (lock held) */
+void cache_evict_oldest()
+{
+    size_t k = 0;
+    for (size_t i = 1; i < g_cache.size(); i++)
+        if (g_cache[i].seq < g_cache[k].seq) k = i;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    if (g_cache[k].device != cur) cudaSetDevice(g_cache[k].device);
+    cudaFree(g_cache[k].ptr);
+    if (g_cache[k].device != cur) cudaSetDevice(cur);
+    g_cache_bytes -= g_cache[k].bytes;
+    g_cache[k] = g_cache.back();
+    g_cache.pop_back();
+}
+
+/* a freed block into the cache (the device is idle), or back to CUDA */
+void cache_put(void *p, size_t fallback_bytes)
+{
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    size_t bytes = fallback_bytes;
+    auto it = g_live.find(p);
+    if (it != g_live.end())
+    {
+        bytes = it->second;
+        g_live.erase(it);
+    }
+    const size_t limit = cache_limit();
+    if (bytes > limit)
+    {
+        cudaFree(p);
+        return;
+    }
+    while (!g_cache.empty() && g_cache_bytes + bytes > limit) cache_evict_oldest();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    g_cache.push_back(CachedBlock{p, bytes, dev, ++g_cache_seq});
+    g_cache_bytes += bytes;
+}
+
+/* free a block; device_idle: the caller has synchronised the device since
+ * the block was last used */
+void dev_release(gg_graph *g, void *p, size_t bytes, bool device_idle)
+{
+    if (!p) return;
+    g->mem_gen++;
+    const size_t b = align_up(bytes ? bytes : 256, 256);
+    g->device_bytes = g->device_bytes >= b ? g->device_bytes - b : 0;
+    if (!device_idle && cudaDeviceSynchronize() != cudaSuccess)
+    {
+        /* the context is in error: hand the block back to CUDA as before */
+        cudaGetLastError();
+        std::lock_guard<std::mutex> lock(g_cache_mu);
+        g_live.erase(p);
+        cudaFree(p);
+        return;
+    }
+    cache_put(p, b);
+}
+} // namespace
+
+extern "C" void gg_device_cache_trim(void)
+{
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    while (!g_cache.empty()) cache_evict_oldest();
+}
+
+extern "C" size_t gg_device_cache_bytes(void)
+{
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    return g_cache_bytes;
+}
+
 gg_status gg_dev_alloc(gg_graph *g, void **p, size_t bytes)
 {
     *p = nullptr;
-    if (bytes == 0) bytes = 256;
-    cudaError_t e = cudaMalloc(p, align_up(bytes, 256));
+    const size_t need = align_up(bytes ? bytes : 256, 256);
+    int dev = 0;
+    GG_CUDA(cudaGetDevice(&dev));
+    {
+        std::lock_guard<std::mutex> lock(g_cache_mu);
+        size_t best = g_cache.size();
+        for (size_t i = 0; i < g_cache.size(); i++)
+        {
+            const CachedBlock &c = g_cache[i];
+            if (c.device != dev || c.bytes < need || c.bytes > need + need / 8) continue;
+            if (best == g_cache.size() || c.bytes < g_cache[best].bytes) best = i;
+        }
+        if (best < g_cache.size())
+        {
+            *p = g_cache[best].ptr;
+            g_live[*p] = g_cache[best].bytes;
+            g_cache_bytes -= g_cache[best].bytes;
+            g_cache[best] = g_cache.back();
+            g_cache.pop_back();
+            g->device_bytes += need;
+            return GG_OK;
+        }
+    }
+    cudaError_t e = cudaMalloc(p, need);
+    if (e == cudaErrorMemoryAllocation)
+    {
+        cudaGetLastError();
+        gg_device_cache_trim();
+        e = cudaMalloc(p, need);
+    }
     if (e != cudaSuccess)
     {
         *p = nullptr;
         return gg_cuda_fail(e, "cudaMalloc");
     }
-    g->device_bytes += align_up(bytes, 256);
+    {
+        std::lock_guard<std::mutex> lock(g_cache_mu);
+        g_live[*p] = need;
+    }
+    g->device_bytes += need;
     return GG_OK;
 }
 
-void gg_dev_free(gg_graph *g, void *p, size_t bytes)
-{
-    if (!p) return;
-    g->mem_gen++;
-    cudaFree(p);
-    size_t b = align_up(bytes ? bytes : 256, 256);
-    g->device_bytes = g->device_bytes >= b ? g->device_bytes - b : 0;
-}
+void gg_dev_free(gg_graph *g, void *p, size_t bytes) { dev_release(g, p, bytes, false); }
 
 gg_status gg_work(gg_graph *g, int slot, size_t bytes, void **out)
 {
@@ -294,13 +430,74 @@ gg_status gg_wait(cudaStream_t s)
     return st;
 }
 
-/* ---- host -> device copies of pageable memory ---------------------------
- * A copy from pageable host memory goes through the driver's own staging,
- * whose rate varied several-fold between runs on this system.  Sources
- * that are not page-locked are copied instead in 32 MB chunks through two
- * page-locked buffers (kept for the process), each chunk filled by all host
- * threads while the previous chunk's DMA runs. */
+/* ---- copies between HBM and pageable host memory -------------------------
+ * Copies from pageable memory take one of three routes
+ * (gg_set_host_copy_mode).  Measured on a GB300 with a Grace host, a 2.1 GB
+ * pageable edge list built into a CSR (upload included) in a long-running
+ * process: the driver's own pageable copy 30.6-31.3 ms; a kernel reading
+ * the source in place through the host's page tables 29.7 ms once the
+ * driver had touched those pages, but 197-240 ms as the process's first
+ * access to them; through two page-locked 32 MB buffers, each filled by all
+ * host threads while the other's DMA runs, 42-45 ms; page-locking the
+ * source in place for one DMA (cudaHostRegister) 133 ms.  So where the GPU
+ * uses the host's page tables (cudaDevAttrPageableMemoryAccessUsesHostPage-
+ * Tables: Grace hosts) the default is the driver's copy, elsewhere the
+ * staging, whose rate does not depend on how the host backs the pages.
+ * Copies to pageable memory where the GPU uses the host's page tables are
+ * the driver's copy (~190 GB/s once the pages are resident:
+ * gg_host_dst_prepare makes them so), else go through the staging buffers. */
 namespace {
+int g_host_pt_device = -1;
+std::atomic<int> g_host_pt{-1};
+
+/* the current device reads pageable memory through the host page tables */
+bool host_page_tables()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return false;
+    }
+    int v = g_host_pt.load();
+    if (v < 0 || g_host_pt_device != dev)
+    {
+        int a = 0;
+        if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess)
+        {
+            cudaGetLastError();
+            a = 0;
+        }
+        g_host_pt_device = dev;
+        v = a ? 1 : 0;
+        g_host_pt.store(v);
+    }
+    return v == 1;
+}
+
+/* one write per host page of [p, p + n), on all host threads: pages never
+ * touched are faulted in here, in parallel, instead of one by one under the
+ * DMA (64 MB of fresh pages: 3.4 ms as a DMA target, 0.5 + 0.45 ms touched
+ * first); pages already resident cost one store each */
+void touch_pages(void *p, size_t n)
+{
+    static const size_t pg = [] {
+        const long v = sysconf(_SC_PAGESIZE);
+        return v > 0 ? (size_t)v : (size_t)4096;
+    }();
+    volatile unsigned char *b = (volatile unsigned char *)p;
+    const size_t pages = (n + pg - 1) / pg;
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < pages; i++) b[i * pg] = 0;
+    if (n) b[n - 1] = 0;
+}
+
+__global__ void k_copy_from_host(const uint4 *__restrict__ src, uint4 *__restrict__ dst, size_t n16)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
 constexpr size_t STAGE_BYTES = (size_t)32 << 20;
 std::mutex g_stage_mu;
 void *g_stage[2] = {nullptr, nullptr};
@@ -328,11 +525,45 @@ bool host_pinned(const void *p)
 }
 } // namespace
 
+static std::atomic<uint32_t> g_host_copy{0xffffffffu};
+
+extern "C" void gg_set_host_copy_mode(uint32_t mode)
+{
+    g_host_copy.store(mode <= GG_HOST_COPY_DEVICE ? mode : GG_HOST_COPY_AUTO);
+}
+
+extern "C" uint32_t gg_host_copy_mode(void)
+{
+    uint32_t m = g_host_copy.load();
+    if (m == 0xffffffffu)
+    {
+        const char *e = getenv("GG_HOST_COPY");
+        m = GG_HOST_COPY_AUTO;
+        if (e && !strcmp(e, "staged")) m = GG_HOST_COPY_STAGED;
+        if (e && !strcmp(e, "driver")) m = GG_HOST_COPY_DRIVER;
+        if (e && !strcmp(e, "device")) m = GG_HOST_COPY_DEVICE;
+        g_host_copy.store(m);
+    }
+    return m;
+}
+
 gg_status gg_copy_h2d(void *dst, const void *src, size_t bytes, cudaStream_t s)
 {
-    if (bytes < ((size_t)4 << 20) || host_pinned(src))
+    uint32_t mode = gg_host_copy_mode();
+    if (mode == GG_HOST_COPY_AUTO) mode = host_page_tables() ? GG_HOST_COPY_DRIVER : GG_HOST_COPY_STAGED;
+    if (bytes < ((size_t)4 << 20) || mode == GG_HOST_COPY_DRIVER || host_pinned(src))
     {
         GG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+        return GG_OK;
+    }
+    if (mode == GG_HOST_COPY_DEVICE && host_page_tables() && (((uintptr_t)src | (uintptr_t)dst) & 15) == 0)
+    {
+        const size_t n16 = bytes / 16, tail = bytes - n16 * 16;
+        k_copy_from_host<<<gg_sm_count() * 2, 1024, 0, s>>>((const uint4 *)src, (uint4 *)dst, n16);
+        GG_CUDA(cudaGetLastError());
+        if (tail)
+            GG_CUDA(cudaMemcpyAsync((unsigned char *)dst + n16 * 16, (const unsigned char *)src + n16 * 16, tail,
+                                    cudaMemcpyHostToDevice, s));
         return GG_OK;
     }
     std::lock_guard<std::mutex> lock(g_stage_mu);
@@ -359,12 +590,22 @@ gg_status gg_copy_h2d(void *dst, const void *src, size_t bytes, cudaStream_t s)
     return GG_OK;
 }
 
+void gg_host_dst_prepare(void *dst, size_t bytes)
+{
+    if (dst && bytes >= ((size_t)4 << 20) && host_page_tables() && !host_pinned(dst)) touch_pages(dst, bytes);
+}
+
 gg_status gg_copy_d2h(void *dst, const void *src, size_t bytes, cudaStream_t s)
 {
     /* a copy to pageable memory blocks the host until the stream's earlier
      * work is done: wait for that work with the bounded poll first */
-    if (!host_pinned(dst)) GG_CHECK(gg_wait(s));
-    if (bytes < ((size_t)4 << 20) || host_pinned(dst))
+    const bool pinned = host_pinned(dst);
+    if (!pinned)
+    {
+        gg_host_dst_prepare(dst, bytes);
+        GG_CHECK(gg_wait(s));
+    }
+    if (bytes < ((size_t)4 << 20) || pinned || host_page_tables())
     {
         GG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
         return gg_wait(s);
@@ -725,9 +966,9 @@ extern "C" gg_status gg_graph_extend(gg_graph *g, const struct GraphCSR *graph, 
     return map_arrays(g, graph, what, gg_stream(g, stream));
 }
 
-static void free_tiles(gg_graph *g, gg_tiles &t)
+static void free_tiles(gg_graph *g, gg_tiles &t, bool idle)
 {
-    gg_dev_free(g, t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2));
+    dev_release(g, t.coord, ((size_t)t.ntiles + 1) * sizeof(uint2), idle);
     t = gg_tiles();
 }
 
@@ -735,30 +976,34 @@ extern "C" gg_status gg_graph_unmap(gg_graph *g)
 {
     if (!g) return GG_OK;
     if (g->own_stream) cudaStreamSynchronize(g->own_stream);
+    /* once for all the blocks below (work of calls on callers' streams
+     * included); if it fails, each block is freed on its own */
+    const bool idle = cudaDeviceSynchronize() == cudaSuccess;
+    if (!idle) cudaGetLastError();
     const size_t off_bytes = ((size_t)g->V + 1) * 4, edge_alloc = ((size_t)g->E + GG_EDGE_PAD) * 4;
     if (g->owns_arrays)
     {
-        gg_dev_free(g, g->out_off, off_bytes);
-        gg_dev_free(g, g->out_adj, edge_alloc);
-        gg_dev_free(g, g->out_w, edge_alloc);
-        gg_dev_free(g, g->in_off, off_bytes);
-        gg_dev_free(g, g->in_adj, edge_alloc);
-        gg_dev_free(g, g->in_w, edge_alloc);
-        gg_dev_free(g, g->out_deg, (size_t)g->V * 4 + 16);
+        dev_release(g, g->out_off, off_bytes, idle);
+        dev_release(g, g->out_adj, edge_alloc, idle);
+        dev_release(g, g->out_w, edge_alloc, idle);
+        dev_release(g, g->in_off, off_bytes, idle);
+        dev_release(g, g->in_adj, edge_alloc, idle);
+        dev_release(g, g->in_w, edge_alloc, idle);
+        dev_release(g, g->out_deg, (size_t)g->V * 4 + 16, idle);
     }
     for (int i = 0; i < 3; i++)
     {
-        gg_dev_free(g, g->in_w16[i], edge_alloc);
-        gg_dev_free(g, g->out_w16[i], edge_alloc);
+        dev_release(g, g->in_w16[i], edge_alloc, idle);
+        dev_release(g, g->out_w16[i], edge_alloc, idle);
     }
-    free_tiles(g, g->in_tiles);
-    free_tiles(g, g->out_tiles);
-    free_tiles(g, g->ppr_tiles);
-    gg_dev_free(g, g->hot_adj, ((size_t)g->E + GG_EDGE_PAD) * 4);
-    gg_dev_free(g, g->hot_list, (size_t)GG_HOT_ENTRIES * 4);
-    free_tiles(g, g->hot_tiles);
-    for (auto &b : g->work) gg_dev_free(g, b.ptr, b.bytes);
-    gg_dev_free(g, g->graphs.coord, g->graphs.bytes);
+    free_tiles(g, g->in_tiles, idle);
+    free_tiles(g, g->out_tiles, idle);
+    free_tiles(g, g->ppr_tiles, idle);
+    dev_release(g, g->hot_adj, ((size_t)g->E + GG_EDGE_PAD) * 4, idle);
+    dev_release(g, g->hot_list, (size_t)GG_HOT_ENTRIES * 4, idle);
+    free_tiles(g, g->hot_tiles, idle);
+    for (auto &b : g->work) dev_release(g, b.ptr, b.bytes, idle);
+    dev_release(g, g->graphs.coord, g->graphs.bytes, idle);
     if (g->pinned) cudaFreeHost(g->pinned);
     if (g->pr_exec) cudaGraphExecDestroy(g->pr_exec);
     for (uint32_t i = 0; i < g->ev_count; i++) cudaEventDestroy(g->ev_pool[i]);

@@ -26,6 +26,53 @@ static struct { struct GraphCSR *graph; gg_graph *g; } g_resident[MAX_RESIDENT];
 #define MAX_PINNED 256
 static void *g_pinned[MAX_PINNED];
 
+#define HOST_CACHE_SLOTS 8
+#define HOST_CACHE_MIN ((size_t)1 << 20)
+#define HOST_CACHE_MAX ((size_t)1 << 30)
+static pthread_mutex_t g_host_cache_lock = PTHREAD_MUTEX_INITIALIZER;
+static struct { void *p; size_t bytes; } g_host_cache[HOST_CACHE_SLOTS];
+static size_t g_host_cache_bytes = 0;
+
+void *gg_host_array_take(size_t bytes)
+{
+    if (bytes >= HOST_CACHE_MIN)
+    {
+        pthread_mutex_lock(&g_host_cache_lock);
+        for (int i = 0; i < HOST_CACHE_SLOTS; i++)
+            if (g_host_cache[i].p && g_host_cache[i].bytes == bytes)
+            {
+                void *p = g_host_cache[i].p;
+                g_host_cache[i].p = NULL;
+                g_host_cache_bytes -= bytes;
+                pthread_mutex_unlock(&g_host_cache_lock);
+                return p;
+            }
+        pthread_mutex_unlock(&g_host_cache_lock);
+    }
+    return malloc(bytes);
+}
+
+void gg_host_array_give(void *p, size_t bytes)
+{
+    if (!p) return;
+    if (bytes >= HOST_CACHE_MIN && bytes <= HOST_CACHE_MAX)
+    {
+        pthread_mutex_lock(&g_host_cache_lock);
+        if (g_host_cache_bytes + bytes <= HOST_CACHE_MAX)
+            for (int i = 0; i < HOST_CACHE_SLOTS; i++)
+                if (!g_host_cache[i].p)
+                {
+                    g_host_cache[i].p = p;
+                    g_host_cache[i].bytes = bytes;
+                    g_host_cache_bytes += bytes;
+                    pthread_mutex_unlock(&g_host_cache_lock);
+                    return;
+                }
+        pthread_mutex_unlock(&g_host_cache_lock);
+    }
+    free(p);
+}
+
 double gg_seconds(void)
 {
     struct timespec ts;

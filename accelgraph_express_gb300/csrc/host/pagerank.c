@@ -12,7 +12,10 @@
 #include "pageRank.h"
 #include "gg_host.h"
 
-struct PageRankStats *newPageRankStatsGraphCSR(struct GraphCSR *graph)
+/* stats with realRanks[v] = v; pageRanks set to base_pr when fill_ranks
+ * (the GPU result overwrites them otherwise).  The arrays are recycled
+ * between calls (gg_host_array_take); the fill runs on all host threads. */
+static struct PageRankStats *stats_new(struct GraphCSR *graph, int fill_ranks)
 {
     struct PageRankStats *s = (struct PageRankStats *)calloc(1, sizeof(struct PageRankStats));
     if (!s) return NULL;
@@ -20,29 +23,32 @@ struct PageRankStats *newPageRankStatsGraphCSR(struct GraphCSR *graph)
     s->damp = Damp;
     s->base_pr = 1.0f - s->damp;
     s->num_vertices = V;
-    s->realRanks = (uint32_t *)malloc((size_t)V * sizeof(uint32_t) + 16);
-    s->pageRanks = (float *)malloc((size_t)V * sizeof(float) + 16);
+    s->realRanks = (uint32_t *)gg_host_array_take((size_t)V * sizeof(uint32_t) + 16);
+    s->pageRanks = (float *)gg_host_array_take((size_t)V * sizeof(float) + 16);
     if (!s->realRanks || !s->pageRanks)
     {
         freePageRankStats(s);
         return NULL;
     }
-    /* first touch of the fresh pages on all host threads */
     const float base = s->base_pr;
+    float *pr = s->pageRanks;
+    uint32_t *rr = s->realRanks;
 #pragma omp parallel for schedule(static)
     for (uint32_t v = 0; v < V; v++)
     {
-        s->pageRanks[v] = base;
-        s->realRanks[v] = v;
+        if (fill_ranks) pr[v] = base;
+        rr[v] = v;
     }
     return s;
 }
 
+struct PageRankStats *newPageRankStatsGraphCSR(struct GraphCSR *graph) { return stats_new(graph, 1); }
+
 void freePageRankStats(struct PageRankStats *s)
 {
     if (!s) return;
-    free(s->realRanks);
-    free(s->pageRanks);
+    gg_host_array_give(s->realRanks, (size_t)s->num_vertices * sizeof(uint32_t) + 16);
+    gg_host_array_give(s->pageRanks, (size_t)s->num_vertices * sizeof(float) + 16);
     free(s);
 }
 
@@ -60,7 +66,7 @@ static struct PageRankStats *pagerank_run(struct Arguments *arguments, struct Gr
 {
     if (!arguments || !graph) return NULL;
     const GraphGpuOptions *o = gpu_options();
-    struct PageRankStats *stats = newPageRankStatsGraphCSR(graph);
+    struct PageRankStats *stats = stats_new(graph, 0);
     if (!stats) return NULL;
     const double t0 = gg_seconds();
     uint32_t what;

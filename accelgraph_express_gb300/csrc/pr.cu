@@ -1237,7 +1237,9 @@ gg_status pagerank_impl(gg_graph *g, const gg_pr_params *p, float *ranks, gg_pr_
     std::vector<IterRec> h(iters + 2);
     double sum = 0.0;
     /* a bounded wait first: a copy to pageable memory would block until the
-     * iterations end, however long that is */
+     * iterations end, however long that is; the rank destination's pages are
+     * made resident while the iterations run */
+    if (ranks && V) gg_host_dst_prepare(ranks, (size_t)V * 4);
     GG_CHECK(gg_wait(R.s));
     GG_CUDA(cudaMemcpyAsync(h.data(), rec, ((size_t)iters + 2) * sizeof(IterRec), cudaMemcpyDeviceToHost, R.s));
     GG_CUDA(cudaMemcpyAsync(&sum, sum_v, sizeof(double), cudaMemcpyDeviceToHost, R.s));

@@ -362,8 +362,11 @@ def main():
     barrier()
     t0 = time.perf_counter()
     e2e_steps = max(3, min(a.steps, 20))
+    call_ms = []
     for _ in range(e2e_steps):
+        tc = time.perf_counter()
         dropin_call()
+        call_ms.append((time.perf_counter() - tc) * 1e3)
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e_value = world * E * ITERS * e2e_steps / e2e_s / 1e9
     h2d = 4 * V + 4 + 4 * E + 4 * V  # CSC edges_idx (+ E sentinel), CSC neighbour ids, out-degree
@@ -383,7 +386,8 @@ def main():
                      "traffic": traffic, "kernel": kernel, "alg_bytes_per_launch": alg,
                      "launch_ms": per_launch_ms, "peak_source": peak_kind, "iteration": iteration},
         "e2e": {"value": e2e_value, "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": e2e_steps, "call": "pageRankGraphCSR + freePageRankStats (ctypes, no Python copies)"},
+                "steps": e2e_steps, "call": "pageRankGraphCSR + freePageRankStats (ctypes, no Python copies)",
+                "ms_per_call": {"min": min(call_ms), "median": statistics.median(call_ms), "max": max(call_ms)}},
         "gpu_launches": launches,
         "clocks": clk,
     }
@@ -967,11 +971,18 @@ def csr_build_extras(gg, torch, peak, scale=24, edge_factor=16):
             got = dg.download(weights=False)
             dg.free()
         del src, dst
-        h = C.c_void_p()
-        t0 = time.perf_counter()
-        gg._check(L.gg_graph_build(el, what, None, C.byref(h)), "gg_graph_build")
-        e2e_s = time.perf_counter() - t0
-        L.gg_graph_unmap(h)
+        # from the host edge list (pageable), the upload inside: the default
+        # route, then each route of gg_set_host_copy_mode
+        routes = {}
+        for name in ("auto", "staged", "driver", "device"):
+            gg.set_host_copy_mode(name)
+            h = C.c_void_p()
+            t0 = time.perf_counter()
+            gg._check(L.gg_graph_build(el, what, None, C.byref(h)), "gg_graph_build")
+            routes[name] = (time.perf_counter() - t0) * 1e3
+            L.gg_graph_unmap(h)
+        gg.set_host_copy_mode("auto")
+        e2e_s = routes["auto"] / 1e3
         t0 = time.perf_counter()
         host = gg.Graph(L.graphCSRFromEdgeList(el))
         host_s = time.perf_counter() - t0
@@ -984,6 +995,7 @@ def csr_build_extras(gg, torch, peak, scale=24, edge_factor=16):
     alg, passes = csr_radix_bytes(V, E)
     return {"graph": f"R-MAT-{scale} edge list, V={V}, E={E}", "device_ms": dev_ms,
             "device_gedges_s": E / (dev_ms / 1e3) / 1e9, "e2e_from_host_ms": e2e_s * 1e3,
+            "e2e_from_host_ms_by_copy_route": routes,
             "host_build_ms": host_s * 1e3, "host_cores": os.cpu_count() or 1,
             "radix_passes_per_direction": passes, "moved_bytes": alg,
             "hbm_frac": alg / (dev_ms / 1e3) / 1e9 / peak, "arrays_equal_host_build": bool(equal)}

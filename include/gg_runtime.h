@@ -78,6 +78,26 @@ void gg_set_wait_timeout_ms(uint32_t ms);
  * that path: at a few microseconds the barriers give up before the other
  * blocks arrive. */
 void gg_set_barrier_limit_us(uint32_t us);
+/* How copies from pageable host memory (4 MB and more) reach HBM:
+ *   GG_HOST_COPY_AUTO    the default: GG_HOST_COPY_DRIVER where the device
+ *                        uses the host's page tables (Grace hosts), else
+ *                        GG_HOST_COPY_STAGED;
+ *   GG_HOST_COPY_STAGED  32 MB chunks through two page-locked buffers, each
+ *                        filled by all host threads while the other's DMA runs;
+ *   GG_HOST_COPY_DRIVER  one cudaMemcpyAsync from the pageable memory;
+ *   GG_HOST_COPY_DEVICE  a kernel reads the pageable memory in place (only
+ *                        where the device uses the host's page tables and
+ *                        source and destination are 16-byte aligned, else
+ *                        staged).
+ * Env GG_HOST_COPY (auto / staged / driver / device) sets the initial mode.
+ * Copies to pageable memory use the driver's copy where the device uses the
+ * host's page tables, else staging. */
+#define GG_HOST_COPY_AUTO 0u
+#define GG_HOST_COPY_STAGED 1u
+#define GG_HOST_COPY_DRIVER 2u
+#define GG_HOST_COPY_DEVICE 3u
+void gg_set_host_copy_mode(uint32_t mode);
+uint32_t gg_host_copy_mode(void);
 
 /* Copy the arrays selected by `what` to HBM.  Offsets are padded so that
  * every array starts on a 256-byte boundary.  The host graph is only read. */
@@ -127,6 +147,13 @@ gg_status gg_graph_download(const gg_graph *g, uint32_t *out_idx, uint32_t *out_
                             uint32_t *in_adj, float *in_w, float *max_weight);
 /* Bytes of device memory held by the mapping (graph + work buffers). */
 size_t gg_graph_device_bytes(const gg_graph *g);
+/* Device memory the library has freed is kept for reuse (a mapping made
+ * and dropped per call then pays no cudaMalloc / cudaFree), up to
+ * GG_DEVICE_CACHE_MB (default 16384) MB; an allocation that fails empties
+ * the cache first.  trim hands every cached block back to CUDA; bytes is
+ * what the cache holds now. */
+void gg_device_cache_trim(void);
+size_t gg_device_cache_bytes(void);
 
 /* ---- PageRank --------------------------------------------------------------- */
 

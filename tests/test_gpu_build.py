@@ -113,16 +113,59 @@ def test_device_build_rejects_bad_ids(gpu):
         gpu.DeviceGraph.build(s, d, num_vertices=5)
 
 
-def test_staged_copies_of_pageable_buffers(gpu, orc):
-    """Pageable host buffers above 4 MB go through page-locked staging in
-    32 MB chunks: an 80 MB edge list uploaded by gg_graph_build (three
-    chunks) and 33.5 MB of BFS distances copied back into a numpy array (two
-    chunks) arrive intact."""
+@pytest.mark.parametrize("route,misaligned", [("staged", False), ("driver", False), ("device", False),
+                                              ("device", True)])
+def test_copies_of_pageable_buffers(gpu, orc, route, misaligned):
+    """Pageable host buffers above 4 MB, by each route of
+    gg_set_host_copy_mode: page-locked staging in 32 MB chunks, the driver's
+    pageable copy, and a kernel reading the source in place where the GPU
+    uses the host's page tables (16-byte aligned sources only: the bytes past
+    the last full 16 go by a small copy; an unaligned source is staged).  An
+    80 MB edge list whose size is not a multiple of 16 bytes, uploaded by
+    gg_graph_build (aligned, and 4 bytes off alignment), and 33.5 MB of BFS
+    distances copied back into a numpy array arrive intact."""
+    gpu.set_host_copy_mode(route)
+    try:
+        _pageable_case(gpu, orc, misaligned)
+    finally:
+        gpu.set_host_copy_mode("auto")
+
+
+def _pageable_case(gpu, orc, misaligned):
+    import ctypes as C
+
     rng = np.random.default_rng(12)
-    V, E = 1 << 23, 20_000_000
+    V, E = 1 << 23, 20_000_001
     s = rng.integers(0, V, E).astype(np.uint32)
     d = rng.integers(0, V, E).astype(np.uint32)
-    dg = gpu.DeviceGraph.build(s, d, num_vertices=V, what=gpu.MAP_OUT | gpu.MAP_IN)
+    if misaligned:
+        # the edge list's arrays (64-byte aligned, 64 bytes of slack) seen
+        # from 4 bytes in; the original pointers are put back before freeing
+        L = gpu.lib()
+        el = gpu.Graph._edge_list(s, d, num_vertices=V)
+        e = el.contents
+        names = ("edges_array_src", "edges_array_dest")
+        ptype = type(e.edges_array_src)
+        # the addresses, not the field objects (those share the struct's memory)
+        keep = [C.cast(getattr(e, n), C.c_void_p).value for n in names]
+        try:
+            for name, arr in (("edges_array_src", s), ("edges_array_dest", d)):
+                addr = C.cast(getattr(e, name), C.c_void_p).value + 4
+                assert addr % 16
+                C.memmove(addr, arr.ctypes.data, E * 4)
+                setattr(e, name, C.cast(C.c_void_p(addr), type(getattr(e, name))))
+            dg = gpu.DeviceGraph.__new__(gpu.DeviceGraph)
+            dg.h = C.c_void_p()
+            st = L.gg_graph_build(el, gpu.MAP_OUT | gpu.MAP_IN, None, C.byref(dg.h))
+            assert st == 0, L.gg_last_error().decode()
+            dg.graph = gpu._Shape(V, E)
+        finally:
+            for n, addr in zip(names, keep):
+                setattr(e, n, C.cast(C.c_void_p(addr), ptype))
+            assert [C.cast(getattr(e, n), C.c_void_p).value for n in names] == keep
+            L.freeEdgeList(el)
+    else:
+        dg = gpu.DeviceGraph.build(s, d, num_vertices=V, what=gpu.MAP_OUT | gpu.MAP_IN)
     got = dg.download(weights=False)
     host = gpu.Graph.from_edges(s, d, num_vertices=V).arrays()
     for k in ("out_off", "out_adj", "in_off", "in_adj"):
