@@ -569,10 +569,15 @@ __device__ __forceinline__ void warp_push(const uint32_t *__restrict__ off, cons
  * blocks of one group do not queue behind the arrivals or the other groups
  * at one L2 slice).  Two levels: blocks arrive at their group's counter, the
  * last of a group at the root, and the last at the root releases every
- * group.  A wait gives up after limit_ns (globaltimer) and sets *err; the
- * block then reports false and the caller leaves, so the other blocks give
- * up at their next barrier and the launch ends with *err set, the context
- * intact.  Bytes 0..511 of ctl are the caller's.
+ * group.  The counters only grow (barrier `gen` completes a group at
+ * (gen + 1) * group size arrivals and the root at (gen + 1) * groups), so
+ * no arrival waits for a counter to be reset.  Ordering: each block's
+ * writes are fenced before it arrives, the last arrivers fence before
+ * passing on, and every block fences after it is released.  A wait gives up
+ * after limit_ns (globaltimer) and sets *err; the block then reports false
+ * and the caller leaves, so the other blocks give up at their next barrier
+ * and the launch ends with *err set, the context intact.  Bytes 0..511 of
+ * ctl are the caller's.
  */
 constexpr unsigned int GG_BAR_GROUPS = 16;
 
@@ -599,13 +604,11 @@ __device__ __forceinline__ bool grid_barrier(char *ctl, unsigned int *err, unsig
         const unsigned int target = gen + 1;
         bool released = false, ok = true;
         __threadfence();
-        if (atomicAdd(count, 1u) == gsize - 1)
+        if (atomicAdd(count, 1u) == target * gsize - 1)
         {
-            atomicExch(count, 0u);
             __threadfence();
-            if (atomicAdd(root, 1u) == G - 1)
+            if (atomicAdd(root, 1u) == target * G - 1)
             {
-                atomicExch(root, 0u);
                 __threadfence();
                 for (unsigned int k = 0; k < G; k++) atomicExch((unsigned int *)(ctl + 4096 + 128 * k), target);
                 released = true;
