@@ -12,13 +12,16 @@
  * Layout: contributions vertex-major, [V][KP] with KP = K rounded up to 16,
  * 32 or 64, stored in FP32 or BF16 and summed in FP32.  At KP = 64 BF16 one
  * vertex's contributions are one 128-byte line, so every edge of the CSC
- * gathers one full line.  A group of KP/2 lanes owns a merge-path tile and
- * walks it edge by edge, each lane summing two vectors; a batch of edges'
- * lines is in flight while the previous ones are summed.  Rows are finished
- * where they end: rank = teleport + d * sum (the teleport row comes through a
- * per-vertex seed index), contribution = rank / outdeg; FP32 ranks are only
- * written by the last iteration.  A row spanning tiles leaves its partial
- * sum in per-tile slots (the tile where it began or that it crosses: `tail`;
+ * gathers one full line.  A group of KP/4 lanes owns a merge-path tile and
+ * walks it edge by edge, each lane summing four vectors from one 8-byte
+ * (BF16) or 16-byte (FP32) load; several groups share a warp, and a batch of
+ * edges' rows is in flight while the previous ones are summed.  Rows are
+ * finished where they end: rank = teleport + d * sum (the teleport row comes
+ * through a per-vertex seed index), contribution = rank * (1 / outdeg) with
+ * the reciprocal computed once per vertex (within an ulp of the division:
+ * the division, 4 per lane per row end, had made the row ends the bulk of
+ * the work); FP32 ranks are only written by the last iteration.  A row
+ * spanning tiles leaves its partial sum in per-tile slots (the tile where it began or that it crosses: `tail`;
  * the tile where it ends: `head`) and k_ppr_fixup adds them in tile order, so
  * every vector's result is deterministic and independent of the vectors
  * batched with it.
@@ -39,58 +42,182 @@ using namespace gg;
 
 constexpr uint32_t NO_SEED = 0xffffffffu;
 
-/* two stored values per lane */
-template <class CT> struct PairIO;
-template <> struct PairIO<float>
+/* VPL stored values per lane, read in one access of 4, 8 or 16 bytes */
+template <class CT, int VPL> struct VecIO;
+template <int VPL> struct Bf16IO
 {
-    typedef float2 Raw;
-    static __device__ __forceinline__ Raw load(const float *p)
+    static constexpr int W = VPL / 2; /* 32-bit words per lane */
+    struct Raw
     {
-        float2 v;
-        asm volatile("ld.global.nc.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
-        return v;
-    }
-    /* through L2 only: contributions rewritten inside the persistent launch */
-    static __device__ __forceinline__ Raw load_cg(const float *p)
-    {
-        float2 v;
-        asm volatile("ld.global.cg.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
-        return v;
-    }
-    static __device__ __forceinline__ float2 unpack(Raw r) { return r; }
-    static __device__ __forceinline__ void store(float *p, float a, float b)
-    {
-        *reinterpret_cast<float2 *>(p) = make_float2(a, b);
-    }
-};
-template <> struct PairIO<__nv_bfloat16>
-{
-    typedef uint32_t Raw;
+        uint32_t w[W];
+    };
     static __device__ __forceinline__ Raw load(const __nv_bfloat16 *p)
     {
-        return ldg_val(reinterpret_cast<const uint32_t *>(p));
+        Raw r;
+        if constexpr (W == 4)
+            asm volatile("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"
+                         : "=r"(r.w[0]), "=r"(r.w[1]), "=r"(r.w[2]), "=r"(r.w[3]) : "l"(p));
+        else if constexpr (W == 2)
+            asm volatile("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(r.w[0]), "=r"(r.w[1]) : "l"(p));
+        else
+            asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(r.w[0]) : "l"(p));
+        return r;
     }
+    /* through L2 only: contributions rewritten inside the persistent launch */
     static __device__ __forceinline__ Raw load_cg(const __nv_bfloat16 *p)
     {
-        uint32_t v;
-        asm volatile("ld.global.cg.u32 %0, [%1];" : "=r"(v) : "l"(p));
-        return v;
+        Raw r;
+        if constexpr (W == 4)
+            asm volatile("ld.global.cg.v4.u32 {%0, %1, %2, %3}, [%4];"
+                         : "=r"(r.w[0]), "=r"(r.w[1]), "=r"(r.w[2]), "=r"(r.w[3]) : "l"(p));
+        else if constexpr (W == 2)
+            asm volatile("ld.global.cg.v2.u32 {%0, %1}, [%2];" : "=r"(r.w[0]), "=r"(r.w[1]) : "l"(p));
+        else
+            asm volatile("ld.global.cg.u32 %0, [%1];" : "=r"(r.w[0]) : "l"(p));
+        return r;
     }
-    /* element 2i is the low half of the word (little-endian), BF16 -> FP32 is exact */
-    static __device__ __forceinline__ float2 unpack(Raw r)
+    /* element 2i is the low half of word i (little-endian); BF16 -> FP32 is exact */
+    static __device__ __forceinline__ void add(float *acc, const Raw &r)
     {
-        return make_float2(__uint_as_float(r << 16), __uint_as_float(r & 0xffff0000u));
+#pragma unroll
+        for (int i = 0; i < W; i++)
+        {
+            acc[2 * i] += __uint_as_float(r.w[i] << 16);
+            acc[2 * i + 1] += __uint_as_float(r.w[i] & 0xffff0000u);
+        }
     }
-    static __device__ __forceinline__ void store(__nv_bfloat16 *p, float a, float b)
+    static __device__ __forceinline__ void store(__nv_bfloat16 *p, const float *c)
     {
-        *reinterpret_cast<__nv_bfloat162 *>(p) = __floats2bfloat162_rn(a, b);
+        uint32_t w[W];
+#pragma unroll
+        for (int i = 0; i < W; i++)
+        {
+            const __nv_bfloat162 h = __floats2bfloat162_rn(c[2 * i], c[2 * i + 1]);
+            w[i] = *reinterpret_cast<const uint32_t *>(&h);
+        }
+        if constexpr (W == 4)
+            *reinterpret_cast<uint4 *>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+        else if constexpr (W == 2)
+            *reinterpret_cast<uint2 *>(p) = make_uint2(w[0], w[1]);
+        else
+            *reinterpret_cast<uint32_t *>(p) = w[0];
     }
 };
+template <int VPL> struct F32IO
+{
+    struct Raw
+    {
+        float v[VPL];
+    };
+    static __device__ __forceinline__ Raw load(const float *p)
+    {
+        Raw r;
+        if constexpr (VPL == 4)
+            asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+                         : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3]) : "l"(p));
+        else
+            asm volatile("ld.global.nc.v2.f32 {%0, %1}, [%2];" : "=f"(r.v[0]), "=f"(r.v[1]) : "l"(p));
+        return r;
+    }
+    static __device__ __forceinline__ Raw load_cg(const float *p)
+    {
+        Raw r;
+        if constexpr (VPL == 4)
+            asm volatile("ld.global.cg.v4.f32 {%0, %1, %2, %3}, [%4];"
+                         : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3]) : "l"(p));
+        else
+            asm volatile("ld.global.cg.v2.f32 {%0, %1}, [%2];" : "=f"(r.v[0]), "=f"(r.v[1]) : "l"(p));
+        return r;
+    }
+    static __device__ __forceinline__ void add(float *acc, const Raw &r)
+    {
+#pragma unroll
+        for (int i = 0; i < VPL; i++) acc[i] += r.v[i];
+    }
+    static __device__ __forceinline__ void store(float *p, const float *c)
+    {
+        if constexpr (VPL == 4)
+            *reinterpret_cast<float4 *>(p) = make_float4(c[0], c[1], c[2], c[3]);
+        else
+            *reinterpret_cast<float2 *>(p) = make_float2(c[0], c[1]);
+    }
+};
+template <int V> struct VecIO<__nv_bfloat16, V> : Bf16IO<V>
+{
+    static constexpr int VPL = V;
+};
+template <int V> struct VecIO<float, V> : F32IO<V>
+{
+    static constexpr int VPL = V;
+};
+
+/* values per lane of the PPR gather: 4 (one 8-byte BF16 or 16-byte FP32
+ * access), fewer for narrow rows so that a lane group spans 2+ lanes.
+ * Measured at K = 64 on R-MAT-22 (BF16 / FP32 GTEPS, 20 iterations): 4 / 4
+ * values per lane 2,249 / 1,856; 8 / 4 with batches of 4 edges 2,032 /
+ * 1,879 (8 with batches of 8: 1,510, too many registers); 2 / 2, the
+ * warp-per-edge layout, 2,037 / 1,330 */
+#ifndef PPR_VPL_BF16
+#define PPR_VPL_BF16 4
+#endif
+#ifndef PPR_VPL_F32
+#define PPR_VPL_F32 4
+#endif
+template <class CT, int KP> constexpr int ppr_vpl()
+{
+    return sizeof(CT) == 2 ? (KP / PPR_VPL_BF16 >= 2 ? PPR_VPL_BF16 : KP / 2)
+                           : (KP / PPR_VPL_F32 >= 2 ? PPR_VPL_F32 : KP / 2);
+}
+template <class CT, int KP> using PprIO = VecIO<CT, ppr_vpl<CT, KP>()>;
+
+/* VPL consecutive floats (aligned to 4 * min(VPL, 4) bytes) */
+template <int VPL>
+__device__ __forceinline__ void load_f32(const float *p, float *v)
+{
+    if constexpr (VPL % 4 == 0)
+    {
+#pragma unroll
+        for (int i = 0; i < VPL; i += 4)
+        {
+            const float4 t = *reinterpret_cast<const float4 *>(p + i);
+            v[i] = t.x;
+            v[i + 1] = t.y;
+            v[i + 2] = t.z;
+            v[i + 3] = t.w;
+        }
+    }
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < VPL; i += 2)
+        {
+            const float2 t = *reinterpret_cast<const float2 *>(p + i);
+            v[i] = t.x;
+            v[i + 1] = t.y;
+        }
+    }
+}
+template <int VPL>
+__device__ __forceinline__ void store_f32(float *p, const float *v)
+{
+    if constexpr (VPL % 4 == 0)
+    {
+#pragma unroll
+        for (int i = 0; i < VPL; i += 4)
+            *reinterpret_cast<float4 *>(p + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+    }
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < VPL; i += 2) *reinterpret_cast<float2 *>(p + i) = make_float2(v[i], v[i + 1]);
+    }
+}
 
 template <class CT>
 struct PprArgs
 {
-    const uint32_t *off, *adj, *outdeg, *seed_idx;
+    const uint32_t *off, *adj, *seed_idx;
+    const float *inv_deg; /* 1 / out-degree, 0 for out-degree 0 */
     const uint2 *coord;
     uint32_t ntiles, V, E;
     uint32_t tile_log2; /* merge items per tile, a power of two (512 by default, the tuned size otherwise) */
@@ -105,71 +232,90 @@ struct PprArgs
     float damp;
 };
 
+/* what changes from one iteration to the next: the contributions read and
+ * written, and the vectors whose ranks this iteration writes (kept apart
+ * from PprArgs so that the persistent kernel reads PprArgs from its
+ * parameter space instead of copying it into registers) */
+template <class CT>
+struct PprIter
+{
+    const CT *cin;
+    CT *cout;
+    unsigned long long rank_mask;
+};
+
 /* the stores of a row end in an iteration where some vectors write their
  * ranks or retire (rare: kept out of line so the unrolled edge loop, which
  * inlines the row end at every edge of a batch, stays small; inlined, it
  * cost the K = 64 gather 20% on R-MAT-22) */
-template <class CT>
+template <int KP, class CT>
 __device__ __noinline__ void ppr_store_masked(CT *cout, float *rank, unsigned long long rank_mask,
-                                              unsigned long long zero_mask, size_t o, float r0, float r1, float c0,
-                                              float c1, uint32_t gl)
+                                              unsigned long long zero_mask, size_t o, const float *r, float *c,
+                                              uint32_t gl)
 {
-    const uint32_t zero = (uint32_t)(zero_mask >> (2 * gl)) & 3u;
-    if (zero & 1u) c0 = 0.0f;
-    if (zero & 2u) c1 = 0.0f;
-    PairIO<CT>::store(cout + o, c0, c1);
-    const uint32_t want = (uint32_t)(rank_mask >> (2 * gl)) & 3u;
-    if (want == 3u)
-        *reinterpret_cast<float2 *>(rank + o) = make_float2(r0, r1);
-    else if (want == 1u)
-        rank[o] = r0;
-    else if (want == 2u)
-        rank[o + 1] = r1;
+    constexpr int VPL = PprIO<CT, KP>::VPL;
+    const uint32_t zero = (uint32_t)(zero_mask >> (VPL * gl)) & ((1u << VPL) - 1u);
+    const uint32_t want = (uint32_t)(rank_mask >> (VPL * gl)) & ((1u << VPL) - 1u);
+#pragma unroll
+    for (int k = 0; k < VPL; k++)
+        if (zero >> k & 1u) c[k] = 0.0f;
+    PprIO<CT, KP>::store(cout + o, c);
+    if (want == (1u << VPL) - 1u)
+        store_f32<VPL>(rank + o, r);
+    else
+#pragma unroll
+        for (int k = 0; k < VPL; k++)
+            if (want >> k & 1u) rank[o + k] = r[k];
 }
 
-/* rank and contribution of row r from its (two-vector) sum.  RS: values per
- * vertex row of cin / cout / rank / tele -- KP, or 64 when only the first KP
- * of wider rows are run (the server's continuous batch) */
+/* rank and contribution of row r from its sums (VPL vectors of this lane):
+ * contribution = rank * (1 / out-degree), the reciprocal computed once per
+ * vertex (within an ulp of rank / out-degree; 0 without out-edges).
+ * RS: values per vertex row of cin / cout / rank / tele -- KP, or 64 when
+ * only the first KP of wider rows are run (the server's continuous batch) */
 template <int KP, int RS, class CT>
-__device__ __forceinline__ void ppr_finish(const PprArgs<CT> &a, uint32_t r, float s0, float s1, uint32_t si,
-                                           uint32_t deg, uint32_t gl)
+__device__ __forceinline__ void ppr_finish(const PprArgs<CT> &a, const PprIter<CT> &it, uint32_t r, const float *s,
+                                           uint32_t si, float inv, uint32_t gl)
 {
-    float r0 = __fmul_rn(a.damp, s0), r1 = __fmul_rn(a.damp, s1);
+    constexpr int VPL = PprIO<CT, KP>::VPL;
+    float rr[VPL], c[VPL];
+#pragma unroll
+    for (int k = 0; k < VPL; k++) rr[k] = __fmul_rn(a.damp, s[k]);
     if (si != NO_SEED)
     {
-        const float2 t = *reinterpret_cast<const float2 *>(a.tele + (size_t)si * RS + 2 * gl);
-        r0 = __fadd_rn(t.x, r0);
-        r1 = __fadd_rn(t.y, r1);
+        float t[VPL];
+        load_f32<VPL>(a.tele + (size_t)si * RS + VPL * gl, t);
+#pragma unroll
+        for (int k = 0; k < VPL; k++) rr[k] = __fadd_rn(t[k], rr[k]);
     }
-    float c0 = 0.0f, c1 = 0.0f;
-    if (deg)
-    {
-        const float fd = __uint2float_rn(deg);
-        c0 = __fdiv_rn(r0, fd);
-        c1 = __fdiv_rn(r1, fd);
-    }
-    const size_t o = (size_t)r * RS + 2 * gl;
-    if ((a.rank_mask | a.zero_mask) == 0ull)
-        PairIO<CT>::store(a.cout + o, c0, c1);
+#pragma unroll
+    for (int k = 0; k < VPL; k++) c[k] = __fmul_rn(rr[k], inv);
+    const size_t o = (size_t)r * RS + VPL * gl;
+    if ((it.rank_mask | a.zero_mask) == 0ull)
+        PprIO<CT, KP>::store(it.cout + o, c);
     else
-        ppr_store_masked<CT>(a.cout, a.rank, a.rank_mask, a.zero_mask, o, r0, r1, c0, c1, gl);
+        ppr_store_masked<KP, CT>(it.cout, a.rank, it.rank_mask, a.zero_mask, o, rr, c, gl);
 }
 
-template <int KP>
-__device__ __forceinline__ void ppr_slot(float *slots, uint32_t tile, float s0, float s1, uint32_t gl)
+template <int KP, int VPL>
+__device__ __forceinline__ void ppr_slot(float *slots, uint32_t tile, const float *s, uint32_t gl)
 {
-    *reinterpret_cast<float2 *>(slots + (size_t)tile * KP + 2 * gl) = make_float2(s0, s1);
+    store_f32<VPL>(slots + (size_t)tile * KP + VPL * gl, s);
 }
 
-/* one group of KP/2 lanes per tile; U edges' lines in flight per batch;
- * COHERENT: contributions read through L2 only (they are rewritten inside
- * the launch by the persistent kernel; the read-only path may keep stale
- * lines from an earlier iteration) */
+/* one group of KP/VPL lanes per tile, each lane VPL vectors with one
+ * 16-byte access per edge; U edges' rows in flight per batch (one id per
+ * lane); COHERENT: contributions read through L2 only (they are rewritten
+ * inside the launch by the persistent kernel; the read-only path may keep
+ * stale lines from an earlier iteration) */
 template <int KP, int RS, class CT, int U, bool COHERENT>
-__device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
+__device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a, const PprIter<CT> &it)
 {
-    constexpr uint32_t LPE = KP / 2;
+    typedef PprIO<CT, KP> IO;
+    constexpr uint32_t VPL = IO::VPL;
+    constexpr uint32_t LPE = KP / VPL;
     static_assert(U <= (int)LPE, "one id load per batch");
+    static_assert(LPE >= 1 && LPE <= 32 && (32 % LPE) == 0, "lane groups tile the warp");
     const uint32_t lane = threadIdx.x & 31, gl = lane % LPE;
     const unsigned gmask = LPE == 32 ? 0xffffffffu : (((1u << LPE) - 1u) << (lane - gl));
     const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) / LPE;
@@ -178,19 +324,20 @@ __device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
     {
         const uint2 c0 = a.coord[tile], c1 = a.coord[tile + 1];
         const uint32_t i0 = c0.x, j0 = c0.y, i1 = c1.x, j1 = c1.y;
-        /* rows rb .. rb+LPE-1, one per lane: end offset, seed index, out-degree */
-        uint32_t rb = i0, w_end = 0, w_seed = NO_SEED, w_deg = 0;
+        /* rows rb .. rb+LPE-1, one per lane: end offset, seed index, 1 / out-degree */
+        uint32_t rb = i0, w_end = 0, w_seed = NO_SEED;
+        float w_inv = 0.0f;
         auto fetch = [&](uint32_t base) {
             rb = base;
             const uint32_t row = base + gl;
             w_end = a.E;
             w_seed = NO_SEED;
-            w_deg = 0;
+            w_inv = 0.0f;
             if (row < a.V)
             {
                 w_end = a.off[row + 1];
                 w_seed = a.seed_idx[row];
-                w_deg = a.outdeg[row];
+                w_inv = a.inv_deg[row];
             }
         };
         fetch(i0);
@@ -198,18 +345,20 @@ __device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
         const uint32_t start0 = i0 < a.V ? a.off[i0] : a.E;
         uint32_t r = i0;
         uint32_t re = __shfl_sync(gmask, w_end, 0, LPE);
-        float s0 = 0.0f, s1 = 0.0f;
+        float acc[VPL];
+#pragma unroll
+        for (uint32_t k = 0; k < VPL; k++) acc[k] = 0.0f;
         /* finish row r (it ends in this tile) and move to r+1 */
         auto next_row = [&]() {
             const uint32_t k = r - rb;
             const uint32_t si = __shfl_sync(gmask, w_seed, k, LPE);
-            const uint32_t deg = __shfl_sync(gmask, w_deg, k, LPE);
+            const float inv = __shfl_sync(gmask, w_inv, k, LPE);
             if (r == i0 && start0 < j0)
-                ppr_slot<KP>(a.head, tile, s0, s1, gl);
+                ppr_slot<KP, VPL>(a.head, tile, acc, gl);
             else
-                ppr_finish<KP, RS, CT>(a, r, s0, s1, si, deg, gl);
-            s0 = 0.0f;
-            s1 = 0.0f;
+                ppr_finish<KP, RS, CT>(a, it, r, acc, si, inv, gl);
+#pragma unroll
+            for (uint32_t q = 0; q < VPL; q++) acc[q] = 0.0f;
             r++;
             if (r - rb >= LPE) fetch(r);
             re = __shfl_sync(gmask, w_end, r - rb, LPE);
@@ -221,14 +370,14 @@ __device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
         for (uint32_t e = j0; e < j1; e += U)
         {
             const uint32_t nb = min((uint32_t)U, j1 - e);
-            typename PairIO<CT>::Raw v[U];
+            typename IO::Raw v[U];
 #pragma unroll
             for (int i = 0; i < U; i++)
             {
                 const uint32_t u = __shfl_sync(gmask, myid, i, LPE);
                 if ((uint32_t)i < nb)
-                    v[i] = COHERENT ? PairIO<CT>::load_cg(a.cin + (size_t)u * RS + 2 * gl)
-                                    : PairIO<CT>::load(a.cin + (size_t)u * RS + 2 * gl);
+                    v[i] = COHERENT ? IO::load_cg(it.cin + (size_t)u * RS + VPL * gl)
+                                    : IO::load(it.cin + (size_t)u * RS + VPL * gl);
             }
             const uint32_t en = e + U;
             myid = 0;
@@ -240,9 +389,7 @@ __device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
                 {
                     /* rows ending before this edge, zero-degree rows included */
                     while (e + i >= re) next_row();
-                    const float2 f = PairIO<CT>::unpack(v[i]);
-                    s0 += f.x;
-                    s1 += f.y;
+                    IO::add(acc, v[i]);
                 }
             }
         }
@@ -252,7 +399,7 @@ __device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
         if (i1 < a.V && j1 > j0)
         {
             const uint32_t o = a.off[i1];
-            if (o < j1) ppr_slot<KP>(a.tail, tile, s0, s1, gl);
+            if (o < j1) ppr_slot<KP, VPL>(a.tail, tile, acc, gl);
         }
     }
 }
@@ -260,16 +407,17 @@ __device__ __forceinline__ void ppr_gather_tiles(const PprArgs<CT> &a)
 template <int KP, int RS, class CT, int U>
 __global__ void __launch_bounds__(256) k_ppr_pull(PprArgs<CT> a)
 {
-    ppr_gather_tiles<KP, RS, CT, U, false>(a);
+    ppr_gather_tiles<KP, RS, CT, U, false>(a, PprIter<CT>{a.cin, a.cout, a.rank_mask});
 }
 
 /* finish the rows spanning tiles: the row that begins in tile t and is
  * still open at t's end (row coord[t+1].x) sums tail[t], the tails of the
  * tiles it crosses and the head of the tile where it ends, in tile order */
 template <int KP, int RS, class CT>
-__device__ __forceinline__ void ppr_fixup_tiles(const PprArgs<CT> &a)
+__device__ __forceinline__ void ppr_fixup_tiles(const PprArgs<CT> &a, const PprIter<CT> &it)
 {
-    constexpr uint32_t LPE = KP / 2, B = 8;
+    constexpr uint32_t VPL = PprIO<CT, KP>::VPL;
+    constexpr uint32_t LPE = KP / VPL, B = 32 / VPL; /* tails in flight per lane: 32 floats */
     const uint32_t lane = threadIdx.x & 31, gl = lane % LPE;
     const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) / LPE;
     const uint32_t ngroups = (gridDim.x * blockDim.x) / LPE;
@@ -280,32 +428,32 @@ __device__ __forceinline__ void ppr_fixup_tiles(const PprArgs<CT> &a)
         if ((((uint64_t)r + a.off[r]) >> a.tile_log2) != t) continue;
         /* the tile of the row's end item */
         const uint32_t t_last = (uint32_t)(((uint64_t)r + a.off[r + 1]) >> a.tile_log2);
-        float2 tot = *reinterpret_cast<const float2 *>(a.tail + (size_t)t * KP + 2 * gl);
+        float tot[VPL];
+        load_f32<VPL>(a.tail + (size_t)t * KP + VPL * gl, tot);
         for (uint32_t m = t + 1; m < t_last; m += B)
         {
-            float2 v[B];
+            float v[B][VPL];
 #pragma unroll
             for (uint32_t i = 0; i < B; i++)
-                if (m + i < t_last) v[i] = *reinterpret_cast<const float2 *>(a.tail + (size_t)(m + i) * KP + 2 * gl);
+                if (m + i < t_last) load_f32<VPL>(a.tail + (size_t)(m + i) * KP + VPL * gl, v[i]);
 #pragma unroll
             for (uint32_t i = 0; i < B; i++)
                 if (m + i < t_last)
-                {
-                    tot.x += v[i].x;
-                    tot.y += v[i].y;
-                }
+#pragma unroll
+                    for (uint32_t k = 0; k < VPL; k++) tot[k] += v[i][k];
         }
-        const float2 h = *reinterpret_cast<const float2 *>(a.head + (size_t)t_last * KP + 2 * gl);
-        tot.x += h.x;
-        tot.y += h.y;
-        ppr_finish<KP, RS, CT>(a, r, tot.x, tot.y, a.seed_idx[r], a.outdeg[r], gl);
+        float h[VPL];
+        load_f32<VPL>(a.head + (size_t)t_last * KP + VPL * gl, h);
+#pragma unroll
+        for (uint32_t k = 0; k < VPL; k++) tot[k] += h[k];
+        ppr_finish<KP, RS, CT>(a, it, r, tot, a.seed_idx[r], a.inv_deg[r], gl);
     }
 }
 
 template <int KP, int RS, class CT>
 __global__ void __launch_bounds__(256) k_ppr_fixup(PprArgs<CT> a)
 {
-    ppr_fixup_tiles<KP, RS, CT>(a);
+    ppr_fixup_tiles<KP, RS, CT>(a, PprIter<CT>{a.cin, a.cout, a.rank_mask});
 }
 
 /* every iteration in one cooperative launch: gather, grid barrier, fix-up
@@ -322,27 +470,45 @@ struct PprLoop
     unsigned long long limit_ns;
 };
 
-/* as many resident CTAs as the per-iteration gather gets (FP32: 3, BF16: 4
- * per SM) */
-template <class CT> constexpr int ppr_persist_ctas() { return sizeof(CT) == 2 ? 4 : 3; }
+/* resident CTAs of the persistent kernel: its gather, fix-up and barrier
+ * take ~120 registers per thread without spills, so 2 CTAs of 256 per SM
+ * (3, with spills, measured the same) */
+#ifndef PPR_PERSIST_CTAS
+#define PPR_PERSIST_CTAS 2
+#endif
+template <class CT> constexpr int ppr_persist_ctas() { return PPR_PERSIST_CTAS; }
+
+/* edges per batch (rows in flight per lane group), at most one per lane of
+ * the group: 6 for BF16, 4 for FP32 measured best (BF16 4 / 6 / 8: 2,204 /
+ * 2,249 / 2,232 GTEPS; FP32 4 / 6 / 8: 1,856 / 1,515 / 1,555) */
+#ifndef PPR_UMAX_BF16
+#define PPR_UMAX_BF16 6
+#endif
+#ifndef PPR_UMAX_F32
+#define PPR_UMAX_F32 4
+#endif
+
+template <int KP, class CT> constexpr int ppr_batch()
+{
+    constexpr int umax = sizeof(CT) == 2 ? PPR_UMAX_BF16 : PPR_UMAX_F32;
+    return (KP / PprIO<CT, KP>::VPL) < umax ? (KP / PprIO<CT, KP>::VPL) : umax;
+}
 
 template <int KP, class CT, int U>
-__global__ void __launch_bounds__(256, ppr_persist_ctas<CT>()) k_ppr_persist(PprArgs<CT> a, PprLoop<CT> L)
+__global__ void __launch_bounds__(256, ppr_persist_ctas<CT>()) k_ppr_persist(const __grid_constant__ PprArgs<CT> a,
+                                                                             const __grid_constant__ PprLoop<CT> L)
 {
     unsigned int gen = 0;
-    for (uint32_t it = 0; it < L.iterations; it++)
+    for (uint32_t i = 0; i < L.iterations; i++)
     {
-        a.cin = (it & 1) ? L.cb1 : L.cb0;
-        a.cout = (it & 1) ? L.cb0 : L.cb1;
-        a.rank_mask = it + 1 == L.iterations ? ~0ull : 0ull;
-        ppr_gather_tiles<KP, KP, CT, U, true>(a);
+        const PprIter<CT> it{(i & 1) ? L.cb1 : L.cb0, (i & 1) ? L.cb0 : L.cb1, i + 1 == L.iterations ? ~0ull : 0ull};
+        ppr_gather_tiles<KP, KP, CT, U, true>(a, it);
         if (!grid_barrier(L.ctl, L.err, L.limit_ns, gen)) return;
-        ppr_fixup_tiles<KP, KP, CT>(a);
-        if (it + 1 < L.iterations && !grid_barrier(L.ctl, L.err, L.limit_ns, gen)) return;
+        ppr_fixup_tiles<KP, KP, CT>(a, it);
+        if (i + 1 < L.iterations && !grid_barrier(L.ctl, L.err, L.limit_ns, gen)) return;
     }
 }
 
-/* contributions of the seed vertices at iteration 0 (the rest is zero) */
 /* contributions of the seed vertices at iteration 0 (the rest is zero), and
  * their seed indices; rows of rs values, of which vectors in `fresh` are
  * written (all of them for gg_ppr; the newly admitted slots for the
@@ -370,15 +536,30 @@ __global__ void k_ppr_seed_init(const uint32_t *__restrict__ seed_vertex, uint32
             c1 = __fdiv_rn(r.y, fd);
         }
         CT *dst = cin + (size_t)v * rs + 2 * gl;
-        if (pair == 3u)
-            PairIO<CT>::store(dst, c0, c1);
-        else
-        {
-            /* one of the pair: the other column belongs to a running vector */
-            if (pair & 1u) dst[0] = from_f32<CT>(c0);
-            if (pair & 2u) dst[1] = from_f32<CT>(c1);
-        }
+        /* only the fresh columns: the others belong to running vectors */
+        if (pair & 1u) dst[0] = from_f32<CT>(c0);
+        if (pair & 2u) dst[1] = from_f32<CT>(c1);
     }
+}
+
+/* inv[v] = 1 / out-degree (correctly rounded), 0 without out-edges */
+__global__ void k_ppr_inv_deg(const uint32_t *__restrict__ outdeg, uint32_t V, float *inv)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    {
+        const uint32_t d = outdeg[v];
+        inv[v] = d ? __frcp_rn(__uint2float_rn(d)) : 0.0f;
+    }
+}
+
+gg_status ppr_inv_deg(gg_graph *g, cudaStream_t s, const float **out)
+{
+    void *inv;
+    GG_CHECK(gg_work(g, 15, (size_t)g->V * 4 + 16, &inv));
+    k_ppr_inv_deg<<<gg_sm_count() * 4, 256, 0, s>>>(g->out_deg, g->V, (float *)inv);
+    GG_CUDA(cudaGetLastError());
+    *out = (const float *)inv;
+    return GG_OK;
 }
 
 template <class K>
@@ -402,8 +583,8 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
                   const float *d_tele, uint32_t *d_seed_idx, float *d_rank, cudaStream_t s, gg_ppr_result &res,
                   std::vector<cudaEvent_t> &evs, void **ctl_out)
 {
-    constexpr int LPE = KP / 2;
-    constexpr int U = LPE < 16 ? LPE : 16;
+    constexpr int LPE = KP / PprIO<CT, KP>::VPL;
+    constexpr int U = ppr_batch<KP, CT>();
     const uint32_t V = g->V;
     gg_tiles &t = g->ppr_tiles;
     const uint32_t tile = g->ppr_tile;
@@ -433,7 +614,9 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
     res.launches++;
 
     PprArgs<CT> a;
-    a.off = g->in_off; a.adj = g->in_adj; a.outdeg = g->out_deg; a.seed_idx = d_seed_idx;
+    a.off = g->in_off; a.adj = g->in_adj; a.seed_idx = d_seed_idx;
+    GG_CHECK(ppr_inv_deg(g, s, &a.inv_deg));
+    res.launches++;
     a.coord = t.coord; a.ntiles = t.ntiles; a.V = V; a.E = g->E; a.tile_log2 = (uint32_t)__builtin_ctz(tile);
     a.rank = d_rank; a.rank_mask = 0; a.zero_mask = 0;
     a.tele = d_tele; a.damp = p->damp;
@@ -504,11 +687,14 @@ namespace {
 template <int KP, class CT>
 gg_status round_run(gg_graph *g, const gg_ppr_round_args &r, cudaStream_t s)
 {
-    constexpr int LPE = KP / 2;
-    constexpr int U = LPE < 16 ? LPE : 16;
+    constexpr int LPE = KP / PprIO<CT, KP>::VPL;
+    constexpr int U = ppr_batch<KP, CT>();
     gg_tiles &t = g->ppr_tiles;
     PprArgs<CT> a;
-    a.off = g->in_off; a.adj = g->in_adj; a.outdeg = g->out_deg; a.seed_idx = r.seed_idx;
+    a.off = g->in_off; a.adj = g->in_adj; a.seed_idx = r.seed_idx;
+    void *inv;
+    GG_CHECK(gg_work(g, 15, (size_t)g->V * 4 + 16, &inv)); /* filled by gg_ppr_round_prepare */
+    a.inv_deg = (const float *)inv;
     a.coord = t.coord; a.ntiles = t.ntiles; a.V = g->V; a.E = g->E;
     a.tile_log2 = (uint32_t)__builtin_ctz(g->ppr_tiles_items);
     a.cin = (const CT *)r.cin; a.cout = (CT *)r.cout; a.rank = r.rank;
@@ -552,6 +738,8 @@ gg_status gg_ppr_round_prepare(gg_graph *g, uint32_t rs, int bf16, void **cb0, v
     GG_CHECK(gg_work(g, 18, (size_t)t.ntiles * rs * sizeof(float) * 2, (void **)slots));
     GG_CUDA(cudaMemsetAsync(*cb0, 0, cb, s));
     GG_CUDA(cudaMemsetAsync(*cb1, 0, cb, s));
+    const float *inv;
+    GG_CHECK(ppr_inv_deg(g, s, &inv));
     return GG_OK;
 }
 

@@ -149,7 +149,9 @@ def test_ppr_persistent_launch_equals_per_iteration_launches(gpu, rg):
     for storage in ("f32", "bf16"):
         one, r1 = dg.ppr(sets, iterations=ITERS, storage=storage)
         many, r2 = dg.ppr(sets, iterations=ITERS, storage=storage, profile=True)
-        assert r1["persistent"] == 1 and r1["launches"] <= 3
+        # seed contributions, 1 / out-degree, the persistent launch (and the
+        # tile coordinates on a mapping's first call)
+        assert r1["persistent"] == 1 and r1["launches"] <= 4
         assert r2["persistent"] == 0 and r2["gather_launches"] == ITERS
         np.testing.assert_array_equal(one, many)
     dg.free()
