@@ -33,7 +33,7 @@ const GraphGpuOptions *gpu_options(void);
 double gg_seconds(void);
 
 /* Large host arrays of the stats structs, recycled: a freed array of at
- * least 1 MiB is kept (up to 8 arrays, 1 GiB in all) and handed out again
+ * least 64 KiB is kept (up to 8 arrays, 1 GiB in all) and handed out again
  * for a request of the same size, so a drop-in call repeated on one graph
  * does not fault in fresh pages for its result arrays every time.  take
  * returns memory as malloc does (contents undefined); give takes memory from

@@ -27,7 +27,7 @@ static struct { struct GraphCSR *graph; gg_graph *g; } g_resident[MAX_RESIDENT];
 static void *g_pinned[MAX_PINNED];
 
 #define HOST_CACHE_SLOTS 8
-#define HOST_CACHE_MIN ((size_t)1 << 20)
+#define HOST_CACHE_MIN ((size_t)64 << 10)
 #define HOST_CACHE_MAX ((size_t)1 << 30)
 static pthread_mutex_t g_host_cache_lock = PTHREAD_MUTEX_INITIALIZER;
 static struct { void *p; size_t bytes; } g_host_cache[HOST_CACHE_SLOTS];

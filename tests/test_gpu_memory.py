@@ -69,7 +69,7 @@ def test_cached_blocks_serve_a_different_graph(gpu, orc):
 
 def test_stats_arrays_recycled_and_initialised(gpu):
     L = gpu.lib()
-    g = gpu.Graph.rmat(18, 16)   # V = 262144: 1 MiB arrays, recycled
+    g = gpu.Graph.rmat(18, 16)   # V = 262144: 1 MiB arrays (recycled from 64 KiB)
     args = gpu.default_arguments(iterations=5, epsilon=0.0)
     gpu.set_gpu_options(storage="f32", device=0, keep_resident=False, verbose=False)
     s1 = L.pageRankGraphCSR(C.byref(args), g.ptr)
