@@ -223,7 +223,12 @@ struct CachedBlock
 };
 std::mutex g_cache_mu;
 std::vector<CachedBlock> g_cache;
-std::unordered_map<void *, size_t> g_live; /* block -> its allocated size */
+struct LiveBlock
+{
+    size_t bytes;
+    int device;
+};
+std::unordered_map<void *, LiveBlock> g_live; /* block -> its allocated size and device */
 size_t g_cache_bytes = 0;
 uint64_t g_cache_seq = 0;
 
@@ -252,26 +257,26 @@ void cache_evict_oldest()
     g_cache.pop_back();
 }
 
-/* a freed block into the cache (the device is idle), or back to CUDA */
+/* a freed block into the cache (its device is idle), or back to CUDA */
 void cache_put(void *p, size_t fallback_bytes)
 {
     std::lock_guard<std::mutex> lock(g_cache_mu);
     size_t bytes = fallback_bytes;
+    int dev = -1;
     auto it = g_live.find(p);
     if (it != g_live.end())
     {
-        bytes = it->second;
+        bytes = it->second.bytes;
+        dev = it->second.device;
         g_live.erase(it);
     }
     const size_t limit = cache_limit();
-    if (bytes > limit)
+    if (bytes > limit || dev < 0)
     {
         cudaFree(p);
         return;
     }
     while (!g_cache.empty() && g_cache_bytes + bytes > limit) cache_evict_oldest();
-    int dev = 0;
-    cudaGetDevice(&dev);
     g_cache.push_back(CachedBlock{p, bytes, dev, ++g_cache_seq});
     g_cache_bytes += bytes;
 }
@@ -327,7 +332,7 @@ gg_status gg_dev_alloc(gg_graph *g, void **p, size_t bytes)
         if (best < g_cache.size())
         {
             *p = g_cache[best].ptr;
-            g_live[*p] = g_cache[best].bytes;
+            g_live[*p] = LiveBlock{g_cache[best].bytes, dev};
             g_cache_bytes -= g_cache[best].bytes;
             g_cache[best] = g_cache.back();
             g_cache.pop_back();
@@ -349,7 +354,7 @@ gg_status gg_dev_alloc(gg_graph *g, void **p, size_t bytes)
     }
     {
         std::lock_guard<std::mutex> lock(g_cache_mu);
-        g_live[*p] = need;
+        g_live[*p] = LiveBlock{need, dev};
     }
     g->device_bytes += need;
     return GG_OK;
@@ -975,6 +980,11 @@ static void free_tiles(gg_graph *g, gg_tiles &t, bool idle)
 extern "C" gg_status gg_graph_unmap(gg_graph *g)
 {
     if (!g) return GG_OK;
+    /* the mapping's device is current while its blocks are released (the
+     * caller's current device is restored at the end) */
+    int caller_dev = -1;
+    if (cudaGetDevice(&caller_dev) != cudaSuccess) cudaGetLastError();
+    if (caller_dev != g->device) cudaSetDevice(g->device);
     if (g->own_stream) cudaStreamSynchronize(g->own_stream);
     /* once for all the blocks below (work of calls on callers' streams
      * included); if it fails, each block is freed on its own */
@@ -1011,7 +1021,9 @@ extern "C" gg_status gg_graph_unmap(gg_graph *g)
     if (g->ev_begin) cudaEventDestroy(g->ev_begin);
     if (g->ev_end) cudaEventDestroy(g->ev_end);
     if (g->own_stream) cudaStreamDestroy(g->own_stream);
+    const int dev = g->device;
     delete g;
+    if (caller_dev >= 0 && caller_dev != dev) cudaSetDevice(caller_dev);
     return GG_OK;
 }
 
