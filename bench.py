@@ -358,7 +358,8 @@ def main():
             raise gg.GgError(f"pageRankGraphCSR failed: {L.gg_last_error().decode()}")
         L.freePageRankStats(st)
 
-    dropin_call()
+    for _ in range(max(3, a.warmup)):
+        dropin_call()
     barrier()
     t0 = time.perf_counter()
     e2e_steps = max(3, min(a.steps, 20))
