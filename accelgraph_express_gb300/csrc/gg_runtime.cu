@@ -438,19 +438,20 @@ gg_status gg_wait(cudaStream_t s)
 /* ---- copies between HBM and pageable host memory -------------------------
  * Copies from pageable memory take one of three routes
  * (gg_set_host_copy_mode).  Measured on a GB300 with a Grace host, a 2.1 GB
- * pageable edge list built into a CSR (upload included) in a long-running
- * process: the driver's own pageable copy 30.6-31.3 ms; a kernel reading
- * the source in place through the host's page tables 29.7 ms once the
- * driver had touched those pages, but 197-240 ms as the process's first
- * access to them; through two page-locked 32 MB buffers, each filled by all
- * host threads while the other's DMA runs, 42-45 ms; page-locking the
- * source in place for one DMA (cudaHostRegister) 133 ms.  So where the GPU
- * uses the host's page tables (cudaDevAttrPageableMemoryAccessUsesHostPage-
- * Tables: Grace hosts) the default is the driver's copy, elsewhere the
- * staging, whose rate does not depend on how the host backs the pages.
- * Copies to pageable memory where the GPU uses the host's page tables are
- * the driver's copy (~190 GB/s once the pages are resident:
- * gg_host_dst_prepare makes them so), else go through the staging buffers. */
+ * pageable edge list built into a CSR (upload included) inside a
+ * long-running process, each route timed on the same list: through two
+ * page-locked 32 MB buffers, each filled by all host threads while the
+ * other's DMA runs, 42-45 ms every time; the driver's own pageable copy, or
+ * a kernel reading the source in place through the host's page tables
+ * (cudaDevAttrPageableMemoryAccessUsesHostPageTables), 30-31 ms once the
+ * buffer had been copied before, but 197-357 ms when the direct route was
+ * the first to read that buffer; page-locking the source in place for one
+ * DMA (cudaHostRegister) 133 ms.  A caller's graph is typically uploaded
+ * once, so the staging, whose rate does not depend on the state of the
+ * host pages, is the default.  Copies to pageable memory where the GPU uses
+ * the host's page tables are the driver's copy (~190 GB/s once the pages
+ * are resident: gg_host_dst_prepare makes them so), else go through the
+ * staging buffers. */
 namespace {
 int g_host_pt_device = -1;
 std::atomic<int> g_host_pt{-1};
@@ -555,7 +556,7 @@ extern "C" uint32_t gg_host_copy_mode(void)
 gg_status gg_copy_h2d(void *dst, const void *src, size_t bytes, cudaStream_t s)
 {
     uint32_t mode = gg_host_copy_mode();
-    if (mode == GG_HOST_COPY_AUTO) mode = host_page_tables() ? GG_HOST_COPY_DRIVER : GG_HOST_COPY_STAGED;
+    if (mode == GG_HOST_COPY_AUTO) mode = GG_HOST_COPY_STAGED;
     if (bytes < ((size_t)4 << 20) || mode == GG_HOST_COPY_DRIVER || host_pinned(src))
     {
         GG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));

@@ -79,9 +79,10 @@ void gg_set_wait_timeout_ms(uint32_t ms);
  * blocks arrive. */
 void gg_set_barrier_limit_us(uint32_t us);
 /* How copies from pageable host memory (4 MB and more) reach HBM:
- *   GG_HOST_COPY_AUTO    the default: GG_HOST_COPY_DRIVER where the device
- *                        uses the host's page tables (Grace hosts), else
- *                        GG_HOST_COPY_STAGED;
+ *   GG_HOST_COPY_AUTO    the default: GG_HOST_COPY_STAGED (the direct routes
+ *                        are faster once a buffer has been copied, but the
+ *                        first direct copy of a buffer was several times
+ *                        slower on a Grace host);
  *   GG_HOST_COPY_STAGED  32 MB chunks through two page-locked buffers, each
  *                        filled by all host threads while the other's DMA runs;
  *   GG_HOST_COPY_DRIVER  one cudaMemcpyAsync from the pageable memory;
