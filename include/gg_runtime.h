@@ -176,7 +176,7 @@ typedef struct gg_pr_params
     double epsilon;
     float damp;               /* 0.85f in the reference */
     uint32_t profile;         /* 1: time every gather launch with CUDA events */
-    uint32_t flags;           /* GG_PR_CUDA_GRAPH, GG_PR_HOT_OFF, GG_PR_HOT_ON */
+    uint32_t flags;           /* GG_PR_CUDA_GRAPH, GG_PR_HOT_OFF, GG_PR_HOT_ON, GG_PR_BATCH_UNION */
 } gg_pr_params;
 
 /* Run the whole call (initialisation, every iteration, normalisation) as
