@@ -79,6 +79,16 @@ template <class T> __device__ __forceinline__ T warp_sum(T v)
     return v;
 }
 
+/* Programmatic dependent launch: a kernel launched with
+ * cudaLaunchAttributeProgrammaticStreamSerialization (gg_launch_pdl) may be
+ * launched while the kernel before it on the stream still runs; it calls
+ * pdl_wait before its first access to memory that kernel writes, which
+ * returns once that kernel has completed and its writes are visible (at
+ * once for a kernel launched without the attribute).  pdl_trigger lets the
+ * next such kernel launch before this one has ended. */
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 /* Block-wide sum of (double, uint32) pairs; the result is valid in thread 0. */
 template <int NT>
 __device__ __forceinline__ void block_sum2(double &a, uint32_t &b)

@@ -167,6 +167,26 @@ gg_status gg_cuda_fail(cudaError_t e, const char *what);
         if (s_ != GG_OK) return s_;                                     \
     } while (0)
 
+/* a kernel launch that may begin while the previous kernel on the stream
+ * still runs (programmatic dependent launch): the kernel must call
+ * pdl_wait() (gg_device.cuh) before it touches that kernel's output */
+template <typename... KArgs, typename... Args>
+inline cudaError_t gg_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                 Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 /* device memory helpers (account into g->device_bytes) */
 gg_status gg_dev_alloc(gg_graph *g, void **p, size_t bytes);
 void gg_dev_free(gg_graph *g, void *p, size_t bytes);

@@ -251,11 +251,13 @@ __global__ void __launch_bounds__(GG_HOT_WARPS * 32, 1)
 {
     typedef typename Fmt<K>::CT CT;
     extern __shared__ __align__(16) unsigned char gg_dyn[];
+    pdl_wait();
     if (it > 0 && rec[it - 1].active == 0u) return;
     CT *s_hot = reinterpret_cast<CT *>(gg_dyn + hot_stage_bytes<K>(blockDim.x >> 5));
     for (uint32_t i = threadIdx.x; i < hot_n; i += blockDim.x) s_hot[i] = cin[hot_list[i]];
     __syncthreads();
     warp_pull_sums_dyn<GG_HOT_IPT>(gg_dyn, off, hot_adj, V, coord, ntiles, sums, PrGatherHot<K>{cin, s_hot});
+    pdl_trigger();
 }
 
 /* grid of k_pr_pull_hot<K> with `warps` warps: one CTA per SM, the
@@ -299,8 +301,10 @@ __global__ void __launch_bounds__(GG_TILE_NT) k_pr_pull(const uint32_t *__restri
                                                         uint32_t ntiles, uint32_t V, typename Fmt<K>::Acc *sums,
                                                         PrGather<K> op, const IterRec *rec, uint32_t it)
 {
+    pdl_wait();
     if (it > 0 && rec[it - 1].active == 0u) return;
     warp_pull_sums<GG_TILE_IPT, GG_TILE_WARPS>(off, adj, V, coord, ntiles, sums, op);
+    pdl_trigger();
 }
 
 /* ---- init, quantise, finalise --------------------------------------------------- */
@@ -345,6 +349,7 @@ __global__ void k_quantize(const float *__restrict__ cf, QT *__restrict__ q, uin
 /* final normalisation and sum (pageRank.c:1080-1085) */
 __global__ void k_pr_finalize(float *__restrict__ rank, uint32_t V, int divide, double *sum)
 {
+    pdl_wait();
     double s = 0.0;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
     {
@@ -457,6 +462,7 @@ __global__ void __launch_bounds__(GG_TILE_NT) k_pr_push_q(const uint32_t *__rest
 template <int K>
 __global__ void k_pr_update(PrCommon c, typename Fmt<K>::Acc *sums, typename Fmt<K>::CT *cout, float *cf)
 {
+    pdl_wait();
     if (c.skip()) return;
     double err = 0.0;
     uint32_t act = 0, tmax = 0;
@@ -498,6 +504,7 @@ __global__ void k_pr_update(PrCommon c, typename Fmt<K>::Acc *sums, typename Fmt
     if constexpr (Fmt<K>::quant) block_max_bits<256>(tmax, &c.rec[c.it + 1].maxbits);
     block_sum2<256>(err, act);
     if (threadIdx.x == 0) c.reduce(err, act);
+    pdl_trigger();
 }
 
 /* ---- BF16 / FP16 storage with the FP32 correction pass ------------------------- */
@@ -570,6 +577,7 @@ template <int K>
 __global__ void k_pr_update_delta(PrCommon c, float init, float *__restrict__ dsum, float *__restrict__ S,
                                   float *__restrict__ chat, typename Fmt<K>::CT *__restrict__ qout)
 {
+    pdl_wait();
     if (c.skip()) return;
     double err = 0.0;
     uint32_t act = 0, tmax = 0;
@@ -825,22 +833,52 @@ gg_status run_pull(Run &R, IterRec *rec, float *rank, uint32_t iters, float base
         const uint32_t hw = R.shape.hot_warps;
         if constexpr (sizeof(Acc) == 4)
             if (R.use_hot && g->hot_cap == hot_entries<K>()) hg = hot_grid<K>(g->hot_tiles.ntiles, hw);
+        /* gather and update as programmatic dependent launches (each kernel
+         * waits for the one before it; its launch overlaps that kernel's
+         * tail), except when they are timed one by one */
+        const bool pdl = !R.p->profile;
         if (hg)
-            k_pr_pull_hot<K><<<hg, hw * 32, hot_smem_bytes<K>(hw), R.s>>>(
-                g->in_off, g->hot_adj, g->hot_tiles.coord, g->hot_tiles.ntiles, V, (Acc *)sums, cin, g->hot_list,
-                g->hot_n, rec, it);
+        {
+            if (pdl)
+                GG_CUDA(gg_launch_pdl(k_pr_pull_hot<K>, dim3(hg), dim3(hw * 32), hot_smem_bytes<K>(hw), R.s, g->in_off,
+                                      g->hot_adj, g->hot_tiles.coord, g->hot_tiles.ntiles, V, (Acc *)sums, cin,
+                                      g->hot_list, g->hot_n, (const IterRec *)rec, it));
+            else
+                k_pr_pull_hot<K><<<hg, hw * 32, hot_smem_bytes<K>(hw), R.s>>>(
+                    g->in_off, g->hot_adj, g->hot_tiles.coord, g->hot_tiles.ntiles, V, (Acc *)sums, cin, g->hot_list,
+                    g->hot_n, rec, it);
+        }
         else
-            k_pr_pull<K><<<gg_persistent_grid((const void *)k_pr_pull<K>, t->ntiles, (int)R.shape.ctas), GG_TILE_NT, 0,
-                           R.s>>>(g->in_off, g->in_adj, t->coord, t->ntiles, V, (Acc *)sums, PrGather<K>{cin}, rec, it);
+        {
+            const int pg = gg_persistent_grid((const void *)k_pr_pull<K>, t->ntiles, (int)R.shape.ctas);
+            if (pdl)
+                GG_CUDA(gg_launch_pdl(k_pr_pull<K>, dim3(pg), dim3(GG_TILE_NT), 0, R.s, g->in_off, g->in_adj, t->coord,
+                                      t->ntiles, V, (Acc *)sums, PrGather<K>{cin}, (const IterRec *)rec, it));
+            else
+                k_pr_pull<K><<<pg, GG_TILE_NT, 0, R.s>>>(g->in_off, g->in_adj, t->coord, t->ntiles, V, (Acc *)sums,
+                                                        PrGather<K>{cin}, rec, it);
+        }
         GG_CHECK(timed_end(R));
         PrCommon c;
         c.rank = rank; c.outdeg = g->out_deg; c.V = V; c.base = base; c.damp = R.p->damp;
         c.eps_f = R.eps_f; c.eps_fl = R.eps_fl; c.rec = rec; c.it = it;
         if constexpr (delta)
-            k_pr_update_delta<K><<<grid_v(V), 256, 0, R.s>>>(c, init, (float *)sums, (float *)Sb, (float *)chb,
-                                                             cb[(it + 1) & 1]);
+        {
+            if (pdl)
+                GG_CUDA(gg_launch_pdl(k_pr_update_delta<K>, dim3(grid_v(V)), dim3(256), 0, R.s, c, init, (float *)sums,
+                                      (float *)Sb, (float *)chb, cb[(it + 1) & 1]));
+            else
+                k_pr_update_delta<K><<<grid_v(V), 256, 0, R.s>>>(c, init, (float *)sums, (float *)Sb, (float *)chb,
+                                                                 cb[(it + 1) & 1]);
+        }
         else
-            k_pr_update<K><<<grid_v(V), 256, 0, R.s>>>(c, (Acc *)sums, cb[(it + 1) & 1], (float *)cf);
+        {
+            if (pdl)
+                GG_CUDA(gg_launch_pdl(k_pr_update<K>, dim3(grid_v(V)), dim3(256), 0, R.s, c, (Acc *)sums,
+                                      cb[(it + 1) & 1], (float *)cf));
+            else
+                k_pr_update<K><<<grid_v(V), 256, 0, R.s>>>(c, (Acc *)sums, cb[(it + 1) & 1], (float *)cf);
+        }
         R.launches += 2;
         R.gather_launches++;
     }
@@ -1033,7 +1071,8 @@ gg_status pagerank_enqueue(Run &R, const gg_pr_params *p, IterRec *rec, float *r
         if (ngraphs)
             k_pr_finalize_seg<<<grid_v(V), 256, 0, R.s>>>(rank, V, voff, ngraphs, (double *)sum_v);
         else
-            k_pr_finalize<<<grid_v(V), 256, 0, R.s>>>(rank, V, p->init_one_over_n ? 0 : 1, (double *)sum_v);
+            GG_CUDA(gg_launch_pdl(k_pr_finalize, dim3(grid_v(V)), dim3(256), 0, R.s, rank, V,
+                                  p->init_one_over_n ? 0 : 1, (double *)sum_v));
         R.launches++;
         GG_CUDA(cudaGetLastError());
     }
