@@ -241,6 +241,24 @@ def test_gpu_calls_fail_loudly_without_device(gg):
     assert gg.lib().graphGpuLastError() != 0
 
 
+def test_host_copy_mode_and_device_cache_controls(gg):
+    """The copy-route setting round-trips, an unknown route falls back to
+    auto, and the device-block cache controls work before any device
+    memory was allocated (an empty cache, nothing to trim)."""
+    L = gg.lib()
+    before = L.gg_host_copy_mode()
+    try:
+        for name, value in gg.HOST_COPY.items():
+            gg.set_host_copy_mode(name)
+            assert L.gg_host_copy_mode() == value, name
+        L.gg_set_host_copy_mode(99)
+        assert L.gg_host_copy_mode() == gg.HOST_COPY["auto"]
+    finally:
+        L.gg_set_host_copy_mode(before)
+    gg.device_cache_trim()
+    assert gg.device_cache_bytes() == 0
+
+
 def test_rmat_batch_is_union_of_single_graphs(gg):
     """generateRMATBatchEdgeList: block i of the union is exactly the R-MAT
     graph of scale scales[i] and seed seed0 + i, renumbered from vertex_off[i]."""
