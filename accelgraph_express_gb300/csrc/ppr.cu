@@ -151,22 +151,18 @@ template <int V> struct VecIO<float, V> : F32IO<V>
     static constexpr int VPL = V;
 };
 
-/* values per lane of the PPR gather: 4 (one 8-byte BF16 or 16-byte FP32
- * access), fewer for narrow rows so that a lane group spans 2+ lanes.
- * Measured at K = 64 on R-MAT-22 (BF16 / FP32 GTEPS, 20 iterations): 4 / 4
- * values per lane 2,249 / 1,856; 8 / 4 with batches of 4 edges 2,032 /
- * 1,879 (8 with batches of 8: 1,510, too many registers); 2 / 2, the
- * warp-per-edge layout, 2,037 / 1,330 */
-#ifndef PPR_VPL_BF16
-#define PPR_VPL_BF16 4
-#endif
-#ifndef PPR_VPL_F32
-#define PPR_VPL_F32 4
-#endif
+/* values per lane of the PPR gather and edges per batch (rows in flight
+ * per lane group, at most one per lane of the group), by storage and row
+ * width KP, as measured on R-MAT-22 (20 iterations, GTEPS, BF16 / FP32):
+ *   KP = 64: 4 per lane (one 8- or 16-byte load), batches of 6 / 4:
+ *            2,249 / 1,856 (2 per lane: 2,037 / 1,330; 8 BF16 per lane
+ *            with batches of 4: 2,032, of 8: 1,510)
+ *   KP = 32: BF16 2 per lane, batches of 8: 1,427 (4 per lane: 1,406);
+ *            FP32 4 per lane, batches of 4: 1,281 (2 per lane: 1,253)
+ *   KP = 16: 2 per lane, batches of 8: 908 / 782 (4 per lane: 712 / 671) */
 template <class CT, int KP> constexpr int ppr_vpl()
 {
-    return sizeof(CT) == 2 ? (KP / PPR_VPL_BF16 >= 2 ? PPR_VPL_BF16 : KP / 2)
-                           : (KP / PPR_VPL_F32 >= 2 ? PPR_VPL_F32 : KP / 2);
+    return (KP == 16 || (sizeof(CT) == 2 && KP == 32)) ? 2 : 4;
 }
 template <class CT, int KP> using PprIO = VecIO<CT, ppr_vpl<CT, KP>()>;
 
@@ -473,25 +469,13 @@ struct PprLoop
 /* resident CTAs of the persistent kernel: its gather, fix-up and barrier
  * take ~120 registers per thread without spills, so 2 CTAs of 256 per SM
  * (3, with spills, measured the same) */
-#ifndef PPR_PERSIST_CTAS
-#define PPR_PERSIST_CTAS 2
-#endif
-template <class CT> constexpr int ppr_persist_ctas() { return PPR_PERSIST_CTAS; }
-
-/* edges per batch (rows in flight per lane group), at most one per lane of
- * the group: 6 for BF16, 4 for FP32 measured best (BF16 4 / 6 / 8: 2,204 /
- * 2,249 / 2,232 GTEPS; FP32 4 / 6 / 8: 1,856 / 1,515 / 1,555) */
-#ifndef PPR_UMAX_BF16
-#define PPR_UMAX_BF16 6
-#endif
-#ifndef PPR_UMAX_F32
-#define PPR_UMAX_F32 4
-#endif
+template <class CT> constexpr int ppr_persist_ctas() { return 2; }
 
 template <int KP, class CT> constexpr int ppr_batch()
 {
-    constexpr int umax = sizeof(CT) == 2 ? PPR_UMAX_BF16 : PPR_UMAX_F32;
-    return (KP / PprIO<CT, KP>::VPL) < umax ? (KP / PprIO<CT, KP>::VPL) : umax;
+    constexpr int lpe = KP / ppr_vpl<CT, KP>();
+    constexpr int umax = ppr_vpl<CT, KP>() == 2 ? 8 : (sizeof(CT) == 2 ? 6 : 4);
+    return lpe < umax ? lpe : umax;
 }
 
 template <int KP, class CT, int U>
