@@ -12,6 +12,7 @@
 
 #include <omp.h>
 #include <unistd.h>
+#include <sys/mman.h>
 
 #include <atomic>
 #include <cmath>
@@ -596,9 +597,26 @@ gg_status gg_copy_h2d(void *dst, const void *src, size_t bytes, cudaStream_t s)
     return GG_OK;
 }
 
+/* the pages at both ends of [p, p + n) are resident (a recycled array:
+ * then the whole range is taken to be, and nothing needs touching) */
+static bool ends_resident(const void *p, size_t n)
+{
+    static const size_t pg = [] {
+        const long v = sysconf(_SC_PAGESIZE);
+        return v > 0 ? (size_t)v : (size_t)4096;
+    }();
+    for (const uintptr_t a : {(uintptr_t)p, (uintptr_t)p + n - 1})
+    {
+        unsigned char in = 0;
+        if (mincore((void *)(a / pg * pg), pg, &in) != 0 || !(in & 1)) return false;
+    }
+    return true;
+}
+
 void gg_host_dst_prepare(void *dst, size_t bytes)
 {
-    if (dst && bytes >= ((size_t)4 << 20) && host_page_tables() && !host_pinned(dst)) touch_pages(dst, bytes);
+    if (dst && bytes >= ((size_t)4 << 20) && host_page_tables() && !host_pinned(dst) && !ends_resident(dst, bytes))
+        touch_pages(dst, bytes);
 }
 
 gg_status gg_copy_d2h(void *dst, const void *src, size_t bytes, cudaStream_t s)

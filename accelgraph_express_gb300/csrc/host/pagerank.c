@@ -5,6 +5,7 @@
  * variant through gg_pagerank, copies the ranks into stats->pageRanks and
  * fills iterations / error_total / time_total like the reference's loop.
  */
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -12,10 +13,36 @@
 #include "pageRank.h"
 #include "gg_host.h"
 
+/* realRanks[v] = v, filled on a helper thread while the GPU runs: the
+ * drop-in call then holds no parallel region of the host threads (on a host
+ * shared with other jobs one preempted thread would stall such a region) */
+struct IdentityFill
+{
+    uint32_t *rr;
+    uint32_t V;
+    pthread_t th;
+    int started;
+};
+
+static void *identity_fill(void *p)
+{
+    struct IdentityFill *f = (struct IdentityFill *)p;
+    for (uint32_t v = 0; v < f->V; v++) f->rr[v] = v;
+    return NULL;
+}
+
+static void identity_join(struct IdentityFill *f)
+{
+    if (f->started) pthread_join(f->th, NULL);
+    f->started = 0;
+}
+
 /* stats with realRanks[v] = v; pageRanks set to base_pr when fill_ranks
  * (the GPU result overwrites them otherwise).  The arrays are recycled
- * between calls (gg_host_array_take); the fill runs on all host threads. */
-static struct PageRankStats *stats_new(struct GraphCSR *graph, int fill_ranks)
+ * between calls (gg_host_array_take).  With `fill` the identity is written
+ * by a helper thread (join it with identity_join before the stats are
+ * used); otherwise the fill runs on all host threads. */
+static struct PageRankStats *stats_new(struct GraphCSR *graph, int fill_ranks, struct IdentityFill *fill)
 {
     struct PageRankStats *s = (struct PageRankStats *)calloc(1, sizeof(struct PageRankStats));
     if (!s) return NULL;
@@ -33,6 +60,13 @@ static struct PageRankStats *stats_new(struct GraphCSR *graph, int fill_ranks)
     const float base = s->base_pr;
     float *pr = s->pageRanks;
     uint32_t *rr = s->realRanks;
+    if (fill && !fill_ranks)
+    {
+        fill->rr = rr;
+        fill->V = V;
+        fill->started = pthread_create(&fill->th, NULL, identity_fill, fill) == 0;
+        if (fill->started) return s;
+    }
 #pragma omp parallel for schedule(static)
     for (uint32_t v = 0; v < V; v++)
     {
@@ -42,7 +76,7 @@ static struct PageRankStats *stats_new(struct GraphCSR *graph, int fill_ranks)
     return s;
 }
 
-struct PageRankStats *newPageRankStatsGraphCSR(struct GraphCSR *graph) { return stats_new(graph, 1); }
+struct PageRankStats *newPageRankStatsGraphCSR(struct GraphCSR *graph) { return stats_new(graph, 1, NULL); }
 
 void freePageRankStats(struct PageRankStats *s)
 {
@@ -66,7 +100,9 @@ static struct PageRankStats *pagerank_run(struct Arguments *arguments, struct Gr
 {
     if (!arguments || !graph) return NULL;
     const GraphGpuOptions *o = gpu_options();
-    struct PageRankStats *stats = stats_new(graph, 0);
+    struct IdentityFill fill;
+    memset(&fill, 0, sizeof(fill));
+    struct PageRankStats *stats = stats_new(graph, 0, &fill);
     if (!stats) return NULL;
     const double t0 = gg_seconds();
     uint32_t what;
@@ -79,6 +115,7 @@ static struct PageRankStats *pagerank_run(struct Arguments *arguments, struct Gr
     gg_graph *g = gpu_acquire(graph, what, 0);
     if (!g)
     {
+        identity_join(&fill);
         freePageRankStats(stats);
         return NULL;
     }
@@ -92,6 +129,7 @@ static struct PageRankStats *pagerank_run(struct Arguments *arguments, struct Gr
     gg_pr_result r;
     gg_status st = gg_pagerank(g, &p, stats->pageRanks, &r, NULL);
     gpu_release_call(graph, g);
+    identity_join(&fill);
     if (st != GG_OK)
     {
         gpu_report(mode_name(mode), st);
