@@ -824,8 +824,7 @@ gg_status do_search(Bfs &B, const gg_bfs_params *p)
     a.src = p->source;
     a.alpha = p->alpha ? p->alpha : 15;
     a.beta = p->beta ? p->beta : 18;
-    int per_sm = 0;
-    GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bfs_do, 256, 0));
+    int per_sm = gg_occupancy((const void *)k_bfs_do, 256, 0);
     if (per_sm < 1) return gg_fail(GG_ERR_CUDA, "k_bfs_do cannot be resident");
     if (per_sm > 8) per_sm = 8;
     void *args[] = {&a};

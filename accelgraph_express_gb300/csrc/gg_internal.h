@@ -260,6 +260,10 @@ int gg_sm_count();
  * sets the kernel's shared-memory carve-out to just hold them, so the rest
  * of each SM's combined L1/shared array caches the gathered values. */
 int gg_persistent_grid(const void *kernel, uint32_t ntiles, int ctas_per_sm = 0);
+/* resident blocks per SM of `kernel` at this block size and dynamic shared
+ * memory (cudaOccupancyMaxActiveBlocksPerMultiprocessor, remembered; 0 on
+ * failure); for kernels whose attributes do not change between launches */
+int gg_occupancy(const void *kernel, int threads, size_t smem);
 
 /* Resident CTAs per SM of the pull gathers.  Measured on GB300 for R-MAT
  * scale 22-24 PageRank and SpMV pulls: fewer CTAs leave more L1 for the hot

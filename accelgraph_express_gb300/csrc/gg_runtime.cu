@@ -82,6 +82,38 @@ unsigned long long gg_barrier_limit_ns() { return g_barrier_limit_ns.load(); }
 
 int gg_sm_count() { return g_sm_count > 0 ? g_sm_count : 152; }
 
+int gg_occupancy(const void *kernel, int threads, size_t smem)
+{
+    /* a host-side computation of a few microseconds, asked per launch by
+     * the single-launch kernels: kept per (kernel, block, shared memory,
+     * device) */
+    struct Entry
+    {
+        const void *kernel;
+        int threads;
+        size_t smem;
+        int device, bps;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) cudaGetLastError();
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (const Entry &e : cache)
+            if (e.kernel == kernel && e.threads == threads && e.smem == smem && e.device == dev) return e.bps;
+    }
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, threads, smem) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return 0;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    cache.push_back(Entry{kernel, threads, smem, dev, bps});
+    return bps;
+}
+
 int gg_persistent_grid(const void *kernel, uint32_t ntiles, int ctas_per_sm)
 {
     /* per (kernel, requested CTAs per SM): the resident CTAs per SM and the
@@ -422,18 +454,34 @@ static gg_status wait_event(cudaEvent_t ev)
 gg_status gg_wait(cudaStream_t s)
 {
     /* Bounded host wait: poll an event instead of blocking forever like the
-     * reference's waitAFU loop. */
-    cudaEvent_t ev;
-    GG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    cudaError_t e = cudaEventRecord(ev, s);
+     * reference's waitAFU loop.  One event per host thread and device is
+     * kept (creating one per wait cost microseconds on every call); one that
+     * no longer records (its context was reset) is made again. */
+    constexpr int MAXDEV = 16;
+    thread_local cudaEvent_t t_ev[MAXDEV] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAXDEV)
+    {
+        cudaGetLastError();
+        cudaEvent_t ev;
+        GG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        cudaError_t e = cudaEventRecord(ev, s);
+        const gg_status st = e == cudaSuccess ? wait_event(ev) : gg_cuda_fail(e, "cudaEventRecord");
+        cudaEventDestroy(ev);
+        return st;
+    }
+    cudaEvent_t &ev = t_ev[dev];
+    cudaError_t e = cudaErrorInvalidResourceHandle;
+    if (ev) e = cudaEventRecord(ev, s);
     if (e != cudaSuccess)
     {
-        cudaEventDestroy(ev);
-        return gg_cuda_fail(e, "cudaEventRecord");
+        cudaGetLastError();
+        ev = nullptr;
+        GG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        e = cudaEventRecord(ev, s);
+        if (e != cudaSuccess) return gg_cuda_fail(e, "cudaEventRecord");
     }
-    const gg_status st = wait_event(ev);
-    cudaEventDestroy(ev);
-    return st;
+    return wait_event(ev);
 }
 
 /* ---- copies between HBM and pageable host memory -------------------------

@@ -549,12 +549,8 @@ gg_status ppr_inv_deg(gg_graph *g, cudaStream_t s, const float **out)
 template <class K>
 int occupancy_grid(K kernel, int threads, size_t work_groups, int lanes_per_group)
 {
-    int bps = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, threads, 0) != cudaSuccess || bps < 1)
-    {
-        cudaGetLastError();
-        bps = 1;
-    }
+    int bps = gg_occupancy((const void *)kernel, threads, 0);
+    if (bps < 1) bps = 1;
     const size_t groups_per_block = (size_t)threads / lanes_per_group;
     const size_t need = (work_groups + groups_per_block - 1) / groups_per_block;
     const size_t cap = (size_t)gg_sm_count() * bps;
@@ -610,8 +606,7 @@ gg_status run_ppr(gg_graph *g, const gg_ppr_params *p, uint32_t nseedv, const ui
     if (!p->profile)
     {
         /* all iterations in one cooperative launch: every block resident */
-        int per_sm = 0;
-        GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ppr_persist<KP, CT, U>, 256, 0));
+        const int per_sm = gg_occupancy((const void *)k_ppr_persist<KP, CT, U>, 256, 0);
         if (per_sm < 1) return gg_fail(GG_ERR_CUDA, "k_ppr_persist cannot be resident");
         const size_t groups_per_block = 256 / LPE;
         const size_t need = ((size_t)t.ntiles + groups_per_block - 1) / groups_per_block;
