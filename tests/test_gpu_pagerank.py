@@ -183,6 +183,31 @@ def test_pagerank_repeat_is_stable(graphs, dgs):
     assert float(np.abs(a - b).max()) <= 1e-5 * float(a.max())
 
 
+def test_pagerank_dependent_launches_equal_plain_launches(gpu, graphs, dgs):
+    """The pull loop's kernels are programmatic dependent launches (each
+    waits for its predecessor on the device); timed runs (profile) launch
+    them plainly.  The integer-summed formats give bit-identical ranks and
+    iteration counts either way, FP32 the same counts and ranks within
+    rounding, on a graph without the hot-vertex table and on one with it."""
+    big = gpu.Graph.rmat(20, 8)
+    dbig = gpu.DeviceGraph(big, gpu.MAP_IN)
+    try:
+        for d in (dgs["rmat16"], dbig):
+            for mode in ("pull_fx64", "pull_q16", "pull"):
+                a, ra = d.pagerank(mode, iterations=12, epsilon=1e-4)
+                b, rb = d.pagerank(mode, iterations=12, epsilon=1e-4, profile=True)
+                assert ra["iterations"] == rb["iterations"], mode
+                if mode == "pull":
+                    np.testing.assert_allclose(a, b, rtol=1e-5, atol=0)
+                else:
+                    np.testing.assert_array_equal(a, b)
+        _, rh = dbig.pagerank("pull", iterations=2, epsilon=0.0)
+        assert rh["hot_table"] == 1
+    finally:
+        dbig.free()
+        big.free()
+
+
 def test_pagerank_edge_cases(gpu, orc):
     # one vertex, no edges
     g = gpu.Graph.from_edges(np.zeros(0, np.uint32), np.zeros(0, np.uint32), num_vertices=1)
