@@ -67,14 +67,75 @@ __global__ void k_hot_mark(const uint32_t *__restrict__ outdeg, uint32_t V, uint
     }
 }
 
-__global__ void k_hot_encode(const uint32_t *__restrict__ adj, uint32_t E, const uint32_t *__restrict__ slot_of,
-                             uint32_t *__restrict__ out)
+/* ids -> encoded ids.  Every CTA first puts the hot vertices into a Bloom
+ * filter in shared memory (BLOOM_BITS bits, two hashes): an id whose two
+ * bits are not both set is not hot and is copied as it is, and only the
+ * others (the hot ones, ~22% of the edges of R-MAT-24, and rare false
+ * positives) read their slot.  Reading the slot of every id at random had
+ * made the pass ~0.9 ms of L2 requests at R-MAT-24.  The ids stream in
+ * 16-byte loads, four in flight per thread. */
+constexpr uint32_t BLOOM_BITS = 1u << 19; /* 64 KB */
+
+__device__ __forceinline__ uint32_t bloom_h1(uint32_t u) { return (u * 0x9E3779B1u) >> 13; }
+__device__ __forceinline__ uint32_t bloom_h2(uint32_t u) { return (u * 0x85EBCA77u + 0x165667B1u) >> 13; }
+
+__global__ void __launch_bounds__(1024) k_hot_encode(const uint32_t *__restrict__ adj, uint64_t n,
+                                                     const uint32_t *__restrict__ slot_of,
+                                                     const uint32_t *__restrict__ hot_list,
+                                                     const uint32_t *__restrict__ counters, uint32_t H,
+                                                     uint32_t *__restrict__ out)
 {
-    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x)
+    extern __shared__ uint32_t bloom[];
+    for (uint32_t i = threadIdx.x; i < BLOOM_BITS / 32; i += blockDim.x) bloom[i] = 0u;
+    __syncthreads();
+    const uint32_t taken = counters[0] + counters[1];
+    const uint32_t nh = taken < H ? taken : H;
+    for (uint32_t i = threadIdx.x; i < nh; i += blockDim.x)
     {
-        const uint32_t u = adj[e];
-        const uint32_t s = slot_of[u];
-        out[e] = s == NO_SLOT ? u : (GG_HOT_FLAG | s);
+        const uint32_t u = hot_list[i], b1 = bloom_h1(u), b2 = bloom_h2(u);
+        atomicOr(&bloom[b1 >> 5], 1u << (b1 & 31));
+        atomicOr(&bloom[b2 >> 5], 1u << (b2 & 31));
+    }
+    __syncthreads();
+    auto enc = [&](uint32_t u) -> uint32_t {
+        const uint32_t b1 = bloom_h1(u), b2 = bloom_h2(u);
+        if (!((bloom[b1 >> 5] >> (b1 & 31)) & (bloom[b2 >> 5] >> (b2 & 31)) & 1u)) return u;
+        const uint32_t sl = slot_of[u];
+        return sl == NO_SLOT ? u : (GG_HOT_FLAG | sl);
+    };
+    const uint64_t nv = n / 4, stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint4 *a4 = reinterpret_cast<const uint4 *>(adj);
+    uint4 *o4 = reinterpret_cast<uint4 *>(out);
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < nv; i += 4 * stride)
+    {
+        uint4 v[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[k] = __ldcs(a4 + i + k * stride);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+        {
+            v[k].x = enc(v[k].x);
+            v[k].y = enc(v[k].y);
+            v[k].z = enc(v[k].z);
+            v[k].w = enc(v[k].w);
+            o4[i + k * stride] = v[k];
+        }
+    }
+    for (; i < nv; i += stride)
+    {
+        uint4 v = __ldcs(a4 + i);
+        v.x = enc(v.x);
+        v.y = enc(v.y);
+        v.z = enc(v.z);
+        v.w = enc(v.w);
+        o4[i] = v;
+    }
+    /* the last n % 4 ids */
+    if (blockIdx.x == 0 && threadIdx.x < n - nv * 4)
+    {
+        const uint64_t e = nv * 4 + threadIdx.x;
+        out[e] = enc(adj[e]);
     }
 }
 
@@ -125,7 +186,11 @@ gg_status gg_hot_prepare(gg_graph *g, cudaStream_t s, uint32_t cap)
     if (!g->hot_list) GG_CHECK(gg_dev_alloc(g, (void **)&g->hot_list, (size_t)GG_HOT_ENTRIES * 4));
     if (!g->hot_adj) GG_CHECK(gg_dev_alloc(g, (void **)&g->hot_adj, ((size_t)E + GG_EDGE_PAD) * 4));
     k_hot_mark<<<grid, 256, 0, s>>>(g->out_deg, V, T, above, H, (uint32_t *)slot_of, g->hot_list, (uint32_t *)cnt);
-    k_hot_encode<<<grid, 256, 0, s>>>(g->in_adj, E, (const uint32_t *)slot_of, g->hot_adj);
+    /* one CTA of 1024 threads per SM (60 registers a thread); adj and out are
+     * whole allocations, 16-byte aligned for the vector loads */
+    GG_CUDA(cudaFuncSetAttribute(k_hot_encode, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(BLOOM_BITS / 8)));
+    k_hot_encode<<<gg_sm_count(), 1024, BLOOM_BITS / 8, s>>>(g->in_adj, (uint64_t)E, (const uint32_t *)slot_of,
+                                                              g->hot_list, (const uint32_t *)cnt, H, g->hot_adj);
     GG_CUDA(cudaGetLastError());
     std::vector<uint32_t> c(4);
     GG_CHECK(gg_wait(s));
