@@ -471,7 +471,31 @@ __global__ void k_pr_update(PrCommon c, typename Fmt<K>::Acc *sums, typename Fmt
     typename Fmt<K>::Acc *__restrict__ sv = sums;
     float *__restrict__ rank = c.rank;
     const uint32_t *__restrict__ outdeg = c.outdeg;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < c.V; v += gridDim.x * blockDim.x)
+    uint32_t v0 = 0;
+    if constexpr (K == K_F32)
+    {
+        /* FP32: two adjacent vertices per step in 8-byte loads and stores
+         * (more loads in flight; every array is a whole allocation), the
+         * same arithmetic per vertex as the loop below */
+        const uint32_t P = c.V >> 1;
+        for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x)
+        {
+            const float2 s = reinterpret_cast<const float2 *>(sv)[p];
+            const float2 pr = reinterpret_cast<const float2 *>(rank)[p];
+            const uint2 d = reinterpret_cast<const uint2 *>(outdeg)[p];
+            if (s.x != 0.0f || s.y != 0.0f) reinterpret_cast<float2 *>(sv)[p] = make_float2(0.0f, 0.0f);
+            const float2 nr = make_float2(next_rank<K>(c.base, c.damp, s.x, 0.0f), next_rank<K>(c.base, c.damp, s.y, 0.0f));
+            reinterpret_cast<float2 *>(rank)[p] = nr;
+            const float e0 = fabsf(__fsub_rn(nr.x, pr.x)), e1 = fabsf(__fsub_rn(nr.y, pr.y));
+            err += (double)e0;
+            err += (double)e1;
+            act += (e0 >= c.eps_f) + (e1 >= c.eps_f);
+            reinterpret_cast<float2 *>(cout)[p] = make_float2(encode<K>(contrib_of(nr.x, d.x), d.x),
+                                                              encode<K>(contrib_of(nr.y, d.y), d.y));
+        }
+        v0 = P * 2;
+    }
+    for (uint32_t v = v0 + blockIdx.x * blockDim.x + threadIdx.x; v < c.V; v += gridDim.x * blockDim.x)
     {
         const typename Fmt<K>::Acc s = sv[v];
         const float pr = rank[v];
@@ -573,43 +597,98 @@ __global__ void k_pr_init_delta(float *__restrict__ rank, const uint32_t *__rest
  * delta is round16(contrib' - chat): what one iteration's rounding lost is
  * sent in the next, so the ranks carry only the rounding of the last delta,
  * which shrinks as the iteration converges. */
+/* one vertex of the correction pass from its loaded values: returns the new
+ * running sum in s, the rank in nr, the stored-so-far value in ch and the
+ * stored 16-bit delta in q */
+template <int K>
+struct DeltaStep
+{
+    typedef typename Fmt<K>::CT CT;
+    float base, damp, init, in_inv, eps_f;
+    int k;
+    bool first;
+    double err;
+    uint32_t act, tmax;
+    __device__ __forceinline__ void operator()(float ds, float &s, float &ch, uint32_t deg, float &nr, CT &q)
+    {
+        const float s_old = s;
+        s = __fadd_rn(s_old, __fmul_rn(ds, in_inv));
+        /* the rank the previous pass wrote, recomputed from its sum (the same
+         * two roundings), so the rank array is only written: a store to a
+         * sector whose read is still in flight stalls */
+        const float pr = first ? init : __fadd_rn(base, __fmul_rn(damp, s_old));
+        nr = __fadd_rn(base, __fmul_rn(damp, s));
+        const float e = fabsf(__fsub_rn(nr, pr));
+        err += (double)e;
+        if (e >= eps_f) act++;
+        const float d = __fsub_rn(contrib_of(nr, deg), ch);
+        ch = __fadd_rn(ch, store_delta<K>(d, k, &q));
+        tmax = max(tmax, __float_as_uint(fabsf(d)));
+    }
+};
+
+template <class CT> struct Pair16;
+template <> struct Pair16<__nv_bfloat16> { typedef __nv_bfloat162 T; static __device__ __forceinline__ T make(__nv_bfloat16 a, __nv_bfloat16 b) { return __halves2bfloat162(a, b); } };
+template <> struct Pair16<__half> { typedef __half2 T; static __device__ __forceinline__ T make(__half a, __half b) { return __halves2half2(a, b); } };
+
+/* The FP32 correction pass: the vertex update (pageRank.c:1055-1069, fused
+ * with the contribution pass :1026-1033) for 16-bit storage.  dsum[v] is
+ * the gathered (pull) or scattered (push) sum of the in-neighbours' stored
+ * deltas; S[v] is the FP32 sum of everything gathered so far (the sum of
+ * the in-neighbours' stored contributions), chat[v] the FP32 value of
+ * everything v has stored so far.  rank' = 0.15 + 0.85 * S, the next stored
+ * delta is round16(contrib' - chat): what one iteration's rounding lost is
+ * sent in the next, so the ranks carry only the rounding of the last delta,
+ * which shrinks as the iteration converges.
+ * A thread takes two adjacent vertices per step (8-byte loads and stores of
+ * every FP32 array, one 4-byte store of the two deltas): the pass moves 34 B
+ * per vertex over six arrays, and one vertex per step left too few loads in
+ * flight to cover DRAM latency.  Every array is a whole allocation (8-byte
+ * aligned); an odd last vertex is taken on its own. */
 template <int K>
 __global__ void k_pr_update_delta(PrCommon c, float init, float *__restrict__ dsum, float *__restrict__ S,
                                   float *__restrict__ chat, typename Fmt<K>::CT *__restrict__ qout)
 {
+    typedef typename Fmt<K>::CT CT;
     pdl_wait();
     if (c.skip()) return;
-    double err = 0.0;
-    uint32_t act = 0, tmax = 0;
-    const float in_inv = c.rec[c.it].qinv;
-    const int k = K == K_F16 ? f16_scale_exp(c.rec[c.it].maxbits) : 0;
+    DeltaStep<K> st{c.base, c.damp, init, c.rec[c.it].qinv, c.eps_f,
+                    K == K_F16 ? f16_scale_exp(c.rec[c.it].maxbits) : 0, c.it == 0, 0.0, 0u, 0u};
     float *__restrict__ rank = c.rank;
     const uint32_t *__restrict__ outdeg = c.outdeg;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < c.V; v += gridDim.x * blockDim.x)
+    const uint32_t P = c.V >> 1, stride = gridDim.x * blockDim.x;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += stride)
     {
+        const float2 ds = reinterpret_cast<const float2 *>(dsum)[p];
+        float2 s = reinterpret_cast<const float2 *>(S)[p];
+        float2 ch = reinterpret_cast<const float2 *>(chat)[p];
+        const uint2 deg = reinterpret_cast<const uint2 *>(outdeg)[p];
+        if (ds.x != 0.0f || ds.y != 0.0f) reinterpret_cast<float2 *>(dsum)[p] = make_float2(0.0f, 0.0f);
+        float2 nr;
+        CT q0, q1;
+        st(ds.x, s.x, ch.x, deg.x, nr.x, q0);
+        st(ds.y, s.y, ch.y, deg.y, nr.y, q1);
+        reinterpret_cast<float2 *>(S)[p] = s;
+        reinterpret_cast<float2 *>(rank)[p] = nr;
+        reinterpret_cast<float2 *>(chat)[p] = ch;
+        reinterpret_cast<typename Pair16<CT>::T *>(qout)[p] = Pair16<CT>::make(q0, q1);
+    }
+    if ((c.V & 1u) && blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        const uint32_t v = c.V - 1;
         const float ds = dsum[v];
         clear_after_read(&dsum[v], ds);
-        const float s_old = S[v];
-        const float s = __fadd_rn(s_old, __fmul_rn(ds, in_inv));
+        float s = S[v], ch = chat[v], nr;
+        st(ds, s, ch, outdeg[v], nr, qout[v]);
         S[v] = s;
-        /* the rank the previous pass wrote, recomputed from its sum (the same
-         * two roundings), so the rank array is only written: a store to a
-         * sector whose read is still in flight stalls */
-        const float pr = c.it == 0 ? init : __fadd_rn(c.base, __fmul_rn(c.damp, s_old));
-        const float nr = __fadd_rn(c.base, __fmul_rn(c.damp, s));
         rank[v] = nr;
-        const float e = fabsf(__fsub_rn(nr, pr));
-        err += (double)e;
-        if (e >= c.eps_f) act++;
-        const float ch = chat[v];
-        const float d = __fsub_rn(contrib_of(nr, outdeg[v]), ch);
-        chat[v] = __fadd_rn(ch, store_delta<K>(d, k, &qout[v]));
-        tmax = max(tmax, __float_as_uint(fabsf(d)));
+        chat[v] = ch;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) c.rec[c.it + 1].qinv = pow2f(-k);
-    block_max_bits<256>(tmax, &c.rec[c.it + 1].maxbits);
-    block_sum2<256>(err, act);
-    if (threadIdx.x == 0) c.reduce(err, act);
+    if (blockIdx.x == 0 && threadIdx.x == 0) c.rec[c.it + 1].qinv = pow2f(-st.k);
+    block_max_bits<256>(st.tmax, &c.rec[c.it + 1].maxbits);
+    block_sum2<256>(st.err, st.act);
+    if (threadIdx.x == 0) c.reduce(st.err, st.act);
+    pdl_trigger();
 }
 
 /* ---- data-driven variants (pageRank.c:2810-3300) -------------------------------- */
