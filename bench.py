@@ -1038,6 +1038,9 @@ def spmv_extras(gg, graph, V, E, sptr, torch, peak):
     o = O.Csr.from_arrays(V, E, out_off, v["out_adj"], in_off, v["in_adj"], v["out_w"], v["in_w"])
     out = {}
     x0 = None
+    # the autotuner's gather shape for this mapping (FP32 timings; both
+    # storages then run in it), as the PageRank legs do
+    tune = dg.autotune(gg.TUNE_SPMV, storage="f32", reps=3, stream=sptr).get("spmv")
     for storage, s in [("f32", 4), ("bf16", 2)]:
         dg.spmv("pull", storage=storage, iterations=2, copy_out=False, stream=sptr)
         torch.cuda.synchronize()
@@ -1059,7 +1062,8 @@ def spmv_extras(gg, graph, V, E, sptr, torch, peak):
             "gteps": E * ITERS / (ms / 1e3) / 1e9, "launch_ms": kms / reps,
             "hbm_frac": alg / (kms / reps / 1e3) / 1e9 / peak,
             "l1_relative": float(np.abs(y - exact).sum() / np.abs(exact).sum()),
-            "linf_relative": float(np.abs(y - exact).max() / np.abs(exact).max())}
+            "linf_relative": float(np.abs(y - exact).max() / np.abs(exact).max()),
+            "gather_shape": tune}
     dg.free()
     return out
 
